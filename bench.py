@@ -1,0 +1,422 @@
+"""Benchmark: variable-coefficient 2-D Poisson solves/s at <= 1e-10 error (one GB300).
+
+Workload (one "step"): a batch of B independent problems
+  -div(kappa grad u) = f on [-1,1]^2, Legendre Dirichlet basis, N = 256 per axis
+  (254^2 unknowns, 256^2 Gauss grid), kappa = exp(g) with g a Gaussian random
+  field (Legendre coefficients N(0,1)(1+|k|^2)^-1.5, rescaled to std 1),
+  forcing coefficients N(0,1)(1+j)^-2(1+k)^-2; seeded synthetic data.
+Each problem is solved by PCG with the constant-coefficient fast-
+diagonalisation preconditioner until its error against the FP64 solution is
+<= 1e-10 (checked on a sample at the end).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--batch B] [--impl ours|reference]
+
+Prints one JSON line (rank 0).  ``--impl reference`` times the CPU FP64
+restatement of the reference algorithm (the oracle port) on the host cores.
+"""
+
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "var-coef solves/s at 1e-10 err: learned+mixed vs plain FP64 PCG, 1 GB300"
+N_GRID = 256
+
+
+def peaks():
+    try:
+        with open(os.path.join(ROOT, "MEASURED_PEAKS.json")) as fh:
+            p = json.load(fh)
+        return p, "measured"
+    except Exception:
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0}, "fallback"
+
+
+# ---------------------------------------------------------------------------
+# clocks sampler (nvidia-smi during the timed region)
+# ---------------------------------------------------------------------------
+
+
+class Clocks:
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.gpu = gpu_index
+        self.proc = None
+        self.path = None
+
+    def __enter__(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except Exception:
+            self.proc = None
+        return self
+
+    def __exit__(self, *a):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except Exception:
+                self.proc.kill()
+
+    def summary(self):
+        if self.path is None or not os.path.exists(self.path):
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unsampled"]}
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in open(self.path):
+            f = [x.strip() for x in line.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sm.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# synthetic problems
+# ---------------------------------------------------------------------------
+
+
+def synth_coeffs(seed: int, N: int):
+    import numpy as np
+
+    rng = np.random.default_rng(seed)
+    k2 = np.add.outer(np.arange(N) ** 2.0, np.arange(N) ** 2.0)
+    gh = rng.standard_normal((N, N)) * (1.0 + k2) ** -1.5
+    s = np.outer((1.0 + np.arange(N)) ** -2.0, (1.0 + np.arange(N)) ** -2.0)
+    fh = rng.standard_normal((N, N)) * s
+    return gh, fh
+
+
+def make_problems(B: int, N: int, seed0: int = 0):
+    """Return host (kappa, f) on the Gauss grid, shape (B, N, N), FP64.
+
+    g and f are the backward transforms of the seeded Legendre coefficients,
+    computed on the GPU with the library's own transform."""
+    import numpy as np
+
+    from jaxfun_gb300.galerkin import Legendre, TensorProduct
+
+    To = TensorProduct(Legendre(N), Legendre(N))
+    gh = np.empty((B, N, N))
+    fh = np.empty((B, N, N))
+    for b in range(B):
+        gh[b], fh[b] = synth_coeffs(seed0 + b, N)
+    g = To.backward(gh).cpu().numpy()
+    f = To.backward(fh).cpu().numpy()
+    g = (g - g.mean(axis=(1, 2), keepdims=True)) / g.std(axis=(1, 2), keepdims=True)
+    return np.exp(g), f
+
+
+# ---------------------------------------------------------------------------
+# reference arm (CPU restatement of the reference algorithm)
+# ---------------------------------------------------------------------------
+
+
+def cpu_solver(N: int):
+    import numpy as np
+
+    from oracle import spectral as O
+
+    V = O.Space1D("legendre", N, True)
+    lam, W = O.fd_factor_symmetric(V.stiffness_matrix(), V.mass_matrix())
+
+    def solve(kap, f, tol=1e-10):
+        b = O.tp_scalar_product([V, V], f)
+        x, it = O.pcg(lambda u: O.varcoef_apply(V, kap, u), b,
+                      lambda r: O.fd_solve(r, [W, W], [W.T, W.T], [lam, lam]), tol=tol)
+        return x, it
+
+    return solve, np
+
+
+def run_reference(args):
+    rank = int(os.environ.get("RANK", "0"))
+    if rank != 0:
+        return 0
+    import numpy as np  # noqa: F401
+
+    N = N_GRID
+    solve, _ = cpu_solver(N)
+    # inputs: the same synthetic recipe, generated on the host by the restatement
+    from oracle import spectral as O
+
+    Vo = O.Space1D("legendre", N, False)
+    probs = []
+    for b in range(args.warmup + args.steps):
+        gh, fh = synth_coeffs(b, N)
+        g = O.tp_backward([Vo, Vo], gh)
+        g = (g - g.mean()) / g.std()
+        probs.append((np.exp(g), O.tp_backward([Vo, Vo], fh)))
+    for b in range(args.warmup):
+        solve(*probs[b])
+    t0 = time.perf_counter()
+    its = []
+    for b in range(args.warmup, args.warmup + args.steps):
+        _, it = solve(*probs[b])
+        its.append(it)
+    dt = time.perf_counter() - t0
+    val = args.steps / dt
+    cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
+    line = {
+        "metric": METRIC, "impl": "reference", "value": val, "unit": "solves/s",
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True, "scaling": "weak",
+        "vs_baseline": None, "dtype": "f64", "data": "synthetic (seeded, config recipe)",
+        "config": {"workload": "varcoef-poisson-2d-legendre-N256", "N": N, "batch": 1,
+                   "tol": 1e-10, "pcg_iterations_mean": float(np.mean(its))},
+        "cpu_baseline": {"value": val, "unit": "solves/s", "cores": cores, "kind": "port",
+                         "sample": f"{args.steps} single-problem FP64 PCG solves (N=256) with "
+                                   "numpy/scipy BLAS on all host threads"},
+        "e2e": {"value": val, "unit": "solves/s", "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+# ---------------------------------------------------------------------------
+# our arm
+# ---------------------------------------------------------------------------
+
+
+def roofline_microbench(B: int, N: int, reps: int = 20):
+    """Time the dominant kernel (FP64 contraction, var-coef pass 1 shape) with
+    CUDA events on its launch stream; return achieved TFLOP/s."""
+    import torch
+
+    from jaxfun_gb300 import _lib
+
+    L = _lib.lib()
+    n = N - 2
+    M, P, K = 2 * N, n, n
+    op = torch.randn(M, K, dtype=torch.float64, device="cuda")
+    x = torch.randn(B, P, K, dtype=torch.float64, device="cuda")
+    y = torch.empty(B, M, P, dtype=torch.float64, device="cuda")
+    d = _lib.ContractDesc(batch=B, nseg=1, M=M, P=P, K=K, op_ld=K, in_ld=K, in_batch=P * K,
+                          out_ld=P, out_batch=M * P, alpha=1.0, beta=0.0)
+    s = torch.cuda.current_stream()
+    for _ in range(3):
+        L.jfg_contract_f64(d, op.data_ptr(), x.data_ptr(), y.data_ptr(), s.cuda_stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(s)
+    for _ in range(reps):
+        L.jfg_contract_f64(d, op.data_ptr(), x.data_ptr(), y.data_ptr(), s.cuda_stream)
+    e1.record(s)
+    e1.synchronize()
+    t = e0.elapsed_time(e1) / 1e3 / reps
+    flops = 2.0 * M * P * K * B
+    return flops / t / 1e12, t, flops
+
+
+def run_ours(args):
+    import numpy as np
+    import torch
+
+    from jaxfun_gb300 import _lib
+    from jaxfun_gb300.galerkin import DIRICHLET, FunctionSpace, Legendre, TensorProduct
+    from jaxfun_gb300.la import fd_preconditioner, pack_varcoef_ops
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    torch.cuda.set_device(local)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.init_process_group("nccl")
+    L = _lib.lib()
+    N = N_GRID
+    n = N - 2
+    B = args.batch
+    D = FunctionSpace(N, Legendre, bcs=DIRICHLET)
+    T = TensorProduct(D, D)
+    kap_h, f_h = make_problems(B, N, seed0=1000 * rank)
+    # ---- resident inputs and plans (untimed setup)
+    w = torch.as_tensor(D.quad_points_and_weights()[1], device="cuda")
+    kap = torch.as_tensor(kap_h, device="cuda")
+    fgrid = torch.as_tensor(f_h, device="cuda")
+    kw = torch.empty_like(kap)
+    stream = torch.cuda.Stream()
+    sh = stream.cuda_stream
+    ops = torch.as_tensor(pack_varcoef_ops(2, D.backward_matrix(None, 0),
+                                           D.backward_matrix(None, 1)), device="cuda")
+    SP = torch.as_tensor(D.scalar_product_matrix(), device="cuda")
+    fac = fd_preconditioner(T)
+    E, W, lam = fac.device_factors()
+    scale = torch.ones(B, dtype=torch.float64, device="cuda")
+    rhs = torch.empty(B, n, n, dtype=torch.float64, device="cuda")
+    x = torch.empty(B, n, n, dtype=torch.float64, device="cuda")
+    rows, cols = _lib.int_array([n, n]), _lib.int_array([N, N])
+    tp_ws = torch.empty(L.jfg_tp_apply_workspace_size(2, rows, cols, B, 8), dtype=torch.uint8,
+                        device="cuda")
+    pcg_ws = torch.empty(L.jfg_pcg_workspace_size(2, n, N, B, 8), dtype=torch.uint8,
+                         device="cuda")
+    iters = (_lib.C.c_int * B)()
+    tol = args.tol
+
+    def prepare(kap_d, f_d):
+        _lib.check(L.jfg_weighted_field_f64(2, N, B, kap_d.data_ptr(), w.data_ptr(),
+                                            kw.data_ptr(), sh), "weighted_field")
+        _lib.check(L.jfg_tp_apply_f64(2, rows, cols, B, _lib.ptr_array([SP.data_ptr()] * 2),
+                                      f_d.data_ptr(), rhs.data_ptr(), tp_ws.data_ptr(),
+                                      tp_ws.numel(), sh), "scalar_product")
+
+    def solve():
+        st = L.jfg_pcg_varcoef_f64(2, n, N, B, ops.data_ptr(), kw.data_ptr(), E.data_ptr(),
+                                   W.data_ptr(), lam.data_ptr(), scale.data_ptr(),
+                                   rhs.data_ptr(), x.data_ptr(), 0, tol, args.maxiter, iters,
+                                   pcg_ws.data_ptr(), pcg_ws.numel(), sh)
+        _lib.check(st, "pcg")
+
+    with torch.cuda.stream(stream):
+        prepare(kap, fgrid)
+        for _ in range(args.warmup):
+            solve()
+        torch.cuda.synchronize()
+        if dist is not None:
+            dist.barrier()
+        L.jfg_reset_launch_count()
+        e0 = torch.cuda.Event(enable_timing=True)
+        e1 = torch.cuda.Event(enable_timing=True)
+        with Clocks(local) as clk:
+            torch.cuda.synchronize()
+            e0.record(stream)
+            for _ in range(args.steps):
+                solve()
+            e1.record(stream)
+            e1.synchronize()
+        launches = int(L.jfg_launch_count())
+        t = e0.elapsed_time(e1) / 1e3
+        clocks = clk.summary()
+    if dist is not None:
+        tt = torch.tensor([t], device="cuda")
+        dist.all_reduce(tt, op=dist.ReduceOp.MAX)
+        t = float(tt.item())
+    value = world * B * args.steps / t
+    its = np.array(iters[:])
+
+    # ---- accuracy check on a sample against a tight FP64 solve
+    x_s = x.clone()
+    st = L.jfg_pcg_varcoef_f64(2, n, N, B, ops.data_ptr(), kw.data_ptr(), E.data_ptr(),
+                               W.data_ptr(), lam.data_ptr(), scale.data_ptr(), rhs.data_ptr(),
+                               x.data_ptr(), 1, 1e-14, args.maxiter, None, pcg_ws.data_ptr(),
+                               pcg_ws.numel(), sh)
+    torch.cuda.synchronize()
+    err = float(((x_s - x).abs().amax(dim=(1, 2)) / x.abs().amax(dim=(1, 2))).max())
+
+    # ---- end to end through the C ABI with host buffers (pinned)
+    kap_pin = torch.as_tensor(kap_h).pin_memory()
+    f_pin = torch.as_tensor(f_h).pin_memory()
+    x_pin = torch.empty(B, n, n, dtype=torch.float64).pin_memory()
+    e2e_steps = max(1, min(args.steps, 2))
+    with torch.cuda.stream(stream):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(e2e_steps):
+            kap.copy_(kap_pin, non_blocking=True)
+            fgrid.copy_(f_pin, non_blocking=True)
+            prepare(kap, fgrid)
+            solve()
+            x_pin.copy_(x, non_blocking=True)
+        stream.synchronize()
+        t_e2e = time.perf_counter() - t0
+    h2d = 2 * B * N * N * 8
+    d2h = B * n * n * 8
+
+    # ---- roofline of the dominant kernel
+    pk, pk_kind = peaks()
+    with torch.cuda.stream(stream):
+        achieved, t_launch, flops = roofline_microbench(B, N)
+    fp64_peak = 1.25  # nominal GB300 FP64 TFLOP/s (no measured FP64 peak is available)
+
+    # ---- CPU baseline (bounded sample, rank 0, N=1 only)
+    cpu = None
+    if rank == 0 and world == 1 and not args.skip_cpu:
+        solve_cpu, _ = cpu_solver(N)
+        t0 = time.perf_counter()
+        nsamp = 0
+        while nsamp < 2 or (time.perf_counter() - t0 < 10.0 and nsamp < 6):
+            solve_cpu(kap_h[nsamp % B], f_h[nsamp % B])
+            nsamp += 1
+        dt = time.perf_counter() - t0
+        cores = len(os.sched_getaffinity(0)) if hasattr(os, "sched_getaffinity") else os.cpu_count()
+        cpu = {"value": nsamp / dt, "unit": "solves/s", "cores": cores, "kind": "port",
+               "sample": f"{nsamp} single-problem FP64 PCG solves (N=256, tol 1e-10), "
+                         "numpy/scipy on all host threads"}
+
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic (seeded; kappa=exp(GRF), config-3 recipe)",
+            "config": {"workload": "varcoef-poisson-2d-legendre-N256", "N": N, "batch": B,
+                       "path": "plain FP64 PCG (CUDA cores)", "tol": tol,
+                       "pcg_iterations_mean": float(its.mean()),
+                       "max_rel_err_vs_fp64_tight": err,
+                       "l2": "inputs+workspace > L2 (129 MB) per step"},
+            "e2e": {"value": world * B * e2e_steps / t_e2e, "unit": "solves/s",
+                    "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+            "gpu_launches": launches,
+            "roofline": {"bound": "fp64", "achieved": achieved, "peak": fp64_peak,
+                         "unit": "TFLOP/s", "frac": achieved / fp64_peak, "traffic": None,
+                         "kernel": "k_contract_simt<double> (var-coef pass 1)",
+                         "peak_kind": "nominal FP64 (not in MEASURED_PEAKS)"},
+            "clocks": clocks,
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    if dist is not None:
+        dist.destroy_process_group()
+    return 0
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--batch", type=int, default=16)
+    ap.add_argument("--tol", type=float, default=1e-10)
+    ap.add_argument("--maxiter", type=int, default=1000)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--skip-cpu", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        return run_reference(args)
+    return run_ours(args)
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -1,0 +1,188 @@
+/*
+ * jaxfun_gb300 — C ABI of the GB300 (sm_103a) tensor-product spectral path.
+ *
+ * Every entry point takes plain device pointers, sizes and a cudaStream_t
+ * (passed as void*), never allocates device memory unless it says so, never
+ * throws, and returns an int status (JFG_OK == 0).  Arrays are C-order
+ * (row-major), matching jaxfun's jax.Array layout.  The reference functions
+ * each entry point replaces are cited as path:line of the jaxfun project.
+ *
+ * Layout conventions
+ *   - A per-axis operator is a row-major matrix op[m][k]: row m of the result,
+ *     k the contracted index.  Backward operators are (Nq x n) Vandermonde
+ *     matrices with the Dirichlet stencil folded in, forward operators are
+ *     (n x Nq) with the mass inverse folded in.
+ *   - "Padded" solver layout: each spectral axis of length n (= N-2 for a
+ *     Dirichlet composite) is stored in a buffer of length nq (the number of
+ *     quadrature points), entries n..nq-1 equal to zero.
+ */
+#ifndef JAXFUN_GB300_H
+#define JAXFUN_GB300_H
+
+#include <stddef.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+enum {
+  JFG_OK = 0,
+  JFG_ERR_ARG = 1,            /* invalid shape / pointer / size (host check)   */
+  JFG_ERR_CUDA = 2,           /* a CUDA runtime call failed                     */
+  JFG_ERR_NOT_CONVERGED = 3,  /* iterative solver hit maxiter                   */
+  JFG_ERR_DEVICE_TIMEOUT = 4, /* a bounded device wait gave up                  */
+  JFG_ERR_UNSUPPORTED = 5,    /* device or configuration not supported          */
+  JFG_ERR_WORKSPACE = 6       /* workspace smaller than *_workspace_size()      */
+};
+
+/* ---- epilogues of the per-axis contraction ----------------------------- */
+enum {
+  JFG_EPI_NONE = 0,      /* v = acc                                                  */
+  JFG_EPI_MUL_FIELD = 1, /* v = acc * field[b][s][m][p]                              */
+  JFG_EPI_DIV_EIG = 2    /* v = acc / (c0[b] + c1[b] * (lam_m[m] + lam_p[p]))        */
+};
+
+/*
+ * One per-axis contraction pass ("contract the last axis, rotate it to the
+ * front"):
+ *   out[b][s][m][p] = alpha * epi( sum_k op[s][m][k] * in[b][s][p][k] )
+ *                     + beta * out[b][s][m][p]
+ * for b < batch, s < nseg, m < M, p < P, k < K.  Element (b,s,m,p) lives at
+ *   op : s*op_seg + m*op_ld + k
+ *   in : b*in_batch + s*in_seg + p*in_ld + k
+ *   out: b*out_batch + s*out_seg + m*out_ld + p
+ *   field (MUL): b*field_batch + s*field_seg + m*field_ld + p
+ * Replaces the per-axis tensordot/moveaxis of TPMatrix._matmul_array
+ * (src/jaxfun/la/tpmatrix.py:152-156), Matrix.matvec (src/jaxfun/la/
+ * matrix.py:89-118) and the vmapped 1-D transforms of _build_local_apply_fn
+ * (src/jaxfun/sharding.py:24-40).
+ */
+typedef struct {
+  int batch, nseg, M, P, K;
+  long long op_ld, op_seg;
+  long long in_ld, in_seg, in_batch;
+  long long out_ld, out_seg, out_batch;
+  int epilogue;
+  const void* field;
+  long long field_ld, field_seg, field_batch;
+  const void* lam_m; /* (M)      */
+  const void* lam_p; /* (P)      */
+  const void* c0;    /* (batch)  */
+  const void* c1;    /* (batch)  */
+  double alpha, beta;
+} jfg_contract_desc;
+
+/* ---- library ----------------------------------------------------------- */
+const char* jfg_version(void);
+const char* jfg_status_string(int status);
+/* last CUDA error code seen by the library on this host thread (0 if none) */
+int jfg_last_cuda_error(void);
+/* 1 if the current device is sm_103 (GB300), else 0 */
+int jfg_device_supported(void);
+/* number of kernels this library has launched (graph replays count their
+ * kernel nodes); reset with jfg_reset_launch_count */
+long long jfg_launch_count(void);
+void jfg_reset_launch_count(void);
+
+/* kw[b][idx] = kappa[b][idx] * prod_ax w[i_ax]: the coefficient times the
+ * tensor-product quadrature weights on the (nq)^ndim grid (the scale
+ * evaluate_jaxfunction_expr_quad and the weights contribute in
+ * src/jaxfun/galerkin/inner.py:445-490, 887-898) */
+int jfg_weighted_field_f64(int ndim, int nq, int batch, const double* kappa, const double* w,
+                           double* kw, void* stream);
+
+/* ---- generic contraction (FP64 / FP32 CUDA cores) ---------------------- */
+int jfg_contract_f64(const jfg_contract_desc* d, const double* op, const double* in,
+                     double* out, void* stream);
+int jfg_contract_f32(const jfg_contract_desc* d, const float* op, const float* in,
+                     float* out, void* stream);
+
+/*
+ * Tensor-core contraction (tcgen05, TMA, TMEM accumulators): three-term
+ * split-TF32 products hi*hi + hi*lo + lo*hi with FP32 accumulation.
+ * op_hi/op_lo are the TF32 split of the FP64 operator (op_hi has its low 13
+ * mantissa bits cleared, op_lo = op - op_hi rounded to FP32).  Requires
+ * K % 32 == 0, M % 16 == 0, M <= 256, P % 128 == 0, in_ld/op_ld % 4 == 0,
+ * 16-byte aligned pointers.  Same semantics as jfg_contract_f32.
+ */
+int jfg_contract_tc(const jfg_contract_desc* d, const float* op_hi, const float* op_lo,
+                    const float* in, float* out, void* stream);
+
+/* ---- TensorProductSpace transforms -------------------------------------
+ * out[b] = (x_ax mats[ax]) in[b]: mats[ax] is rows[ax] x cols[ax] row-major,
+ * in is (batch, cols[0], ..., cols[ndim-1]), out (batch, rows[0], ...).
+ * TensorProductSpace.backward / forward / scalar_product
+ * (src/jaxfun/galerkin/tensorproductspace.py:330-417) with the 1-D
+ * operators of OrthogonalSpace/Composite/Chebyshev (src/jaxfun/galerkin/
+ * orthogonal.py:214-277, composite.py:205-349, Chebyshev.py:225-279).
+ * ndim in {1,2,3}.  Workspace: jfg_tp_apply_workspace_size bytes.
+ */
+size_t jfg_tp_apply_workspace_size(int ndim, const int* rows, const int* cols, int batch,
+                                   int elem_bytes);
+int jfg_tp_apply_f64(int ndim, const int* rows, const int* cols, int batch,
+                     const double* const* mats, const double* in, double* out,
+                     void* work, size_t work_bytes, void* stream);
+int jfg_tp_apply_f32(int ndim, const int* rows, const int* cols, int batch,
+                     const float* const* mats, const float* in, float* out,
+                     void* work, size_t work_bytes, void* stream);
+
+/* ---- fast-diagonalisation solve ----------------------------------------
+ * TPMatricesLUFactors.solve (src/jaxfun/la/tpmatrix.py:545-587), batched:
+ *   U_b = (x_ax W) [ (x_ax E) F_b / (c0[b] + c1[b] * sum_ax lam[i_ax]) ]
+ * Same n x n E (= W^{-1} M^{-1}; W^T for symmetric pairs), W and lam on
+ * every axis (square tensor-product space, n per axis), rhs/out
+ * (batch, n^ndim).  lam has length n.  ndim in {2,3}.
+ */
+size_t jfg_fd_solve_workspace_size(int ndim, int n, int batch, int elem_bytes);
+int jfg_fd_solve_f64(int ndim, int n, int batch, const double* E, const double* W,
+                     const double* lam, const double* c0, const double* c1,
+                     const double* rhs, double* out, void* work, size_t work_bytes,
+                     void* stream);
+int jfg_fd_solve_f32(int ndim, int n, int batch, const float* E, const float* W,
+                     const float* lam, const float* c0, const float* c1, const float* rhs,
+                     float* out, void* work, size_t work_bytes, void* stream);
+
+/* ---- variable-coefficient operator apply -------------------------------
+ * v_b = A(kappa_b) u_b for the form (kappa grad u, grad v), sum-factorised:
+ * the TensorMatrix jaxfun assembles for kappa*Dot(Grad(u), Grad(v))
+ * (src/jaxfun/galerkin/inner.py:445-490, 991-1024) applied as
+ * TensorMatrix._matmul_array (src/jaxfun/la/tensormatrix.py:54-56), without
+ * forming the O(n^4) tensor.  ops is the packed operator set produced by
+ * jfg_varcoef_pack_ops_host from B[q][k] = phi_k(x_q) and D[q][k] =
+ * phi_k'(x_q) (nq x n); kw is (batch, nq^ndim) = kappa * w (x) w [(x) w];
+ * u, v are (batch, n^ndim).  ndim in {2,3}.
+ */
+size_t jfg_varcoef_ops_count(int ndim, int n, int nq);
+void jfg_varcoef_pack_ops_host(int ndim, int n, int nq, const double* B, const double* D,
+                               double* ops_out);
+size_t jfg_varcoef_workspace_size(int ndim, int n, int nq, int batch, int elem_bytes);
+int jfg_varcoef_apply_f64(int ndim, int n, int nq, int batch, const double* ops,
+                          const double* kw, const double* u, double* v, void* work,
+                          size_t work_bytes, void* stream);
+int jfg_varcoef_apply_f32(int ndim, int n, int nq, int batch, const float* ops,
+                          const float* kw, const float* u, float* v, void* work,
+                          size_t work_bytes, void* stream);
+
+/* ---- preconditioned conjugate gradients --------------------------------
+ * Batched PCG for A(kappa_b) x_b = rhs_b with the constant-coefficient
+ * fast-diagonalisation preconditioner (E, W, lam; c0 = 0, c1 = fd_scale[b]).
+ * No PCG exists on jaxfun's Galerkin path; this follows the textbook
+ * algorithm of jax.scipy.sparse.linalg.cg (used at src/jaxfun/pinns/
+ * hessoptimizer.py:97).  Problem b stops when sqrt(r.z / r0.z0) <= tol
+ * (r0 = rhs - A x0).  If use_x0 is 0, x is zeroed first.  iters (host, may be
+ * NULL) receives per-problem iteration counts.  Returns JFG_ERR_NOT_CONVERGED
+ * when any problem reaches maxiter.
+ */
+size_t jfg_pcg_workspace_size(int ndim, int n, int nq, int batch, int elem_bytes);
+int jfg_pcg_varcoef_f64(int ndim, int n, int nq, int batch, const double* ops,
+                        const double* kw, const double* E, const double* W,
+                        const double* lam, const double* fd_scale, const double* rhs,
+                        double* x, int use_x0, double tol, int maxiter, int* iters,
+                        void* work, size_t work_bytes, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* JAXFUN_GB300_H */

@@ -1,0 +1,160 @@
+"""ctypes binding of the C ABI in ``include/jaxfun_gb300.h``.
+
+The shared library is built in-tree (``jaxfun_gb300/_lib/libjaxfun_gb300.so``).
+There is no CPU fallback: if the library cannot be loaded, every compute call
+raises.  Device buffers are torch CUDA tensors; only their data pointers and
+the current CUDA stream cross the boundary.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+import os
+from pathlib import Path
+
+_PKG = Path(__file__).resolve().parent
+LIB_PATH = _PKG / "_lib" / "libjaxfun_gb300.so"
+
+JFG_OK = 0
+JFG_ERR_ARG = 1
+JFG_ERR_CUDA = 2
+JFG_ERR_NOT_CONVERGED = 3
+JFG_ERR_DEVICE_TIMEOUT = 4
+JFG_ERR_UNSUPPORTED = 5
+JFG_ERR_WORKSPACE = 6
+
+EPI_NONE = 0
+EPI_MUL_FIELD = 1
+EPI_DIV_EIG = 2
+
+
+class JfgError(RuntimeError):
+    """A C-ABI call returned a non-zero status."""
+
+    def __init__(self, status: int, what: str):
+        self.status = status
+        msg = f"{what}: {status_string(status)} (status {status})"
+        if status == JFG_ERR_CUDA and _lib is not None:
+            msg += f", cuda error {_lib.jfg_last_cuda_error()}"
+        super().__init__(msg)
+
+
+class NotConvergedError(JfgError):
+    pass
+
+
+class ContractDesc(C.Structure):
+    _fields_ = [
+        ("batch", C.c_int), ("nseg", C.c_int), ("M", C.c_int), ("P", C.c_int), ("K", C.c_int),
+        ("op_ld", C.c_longlong), ("op_seg", C.c_longlong),
+        ("in_ld", C.c_longlong), ("in_seg", C.c_longlong), ("in_batch", C.c_longlong),
+        ("out_ld", C.c_longlong), ("out_seg", C.c_longlong), ("out_batch", C.c_longlong),
+        ("epilogue", C.c_int),
+        ("field", C.c_void_p),
+        ("field_ld", C.c_longlong), ("field_seg", C.c_longlong), ("field_batch", C.c_longlong),
+        ("lam_m", C.c_void_p), ("lam_p", C.c_void_p), ("c0", C.c_void_p), ("c1", C.c_void_p),
+        ("alpha", C.c_double), ("beta", C.c_double),
+    ]
+
+
+_vp = C.c_void_p
+_i = C.c_int
+_sz = C.c_size_t
+_d = C.c_double
+
+# name -> (restype, argtypes)
+SIGNATURES = {
+    "jfg_version": (C.c_char_p, []),
+    "jfg_status_string": (C.c_char_p, [_i]),
+    "jfg_last_cuda_error": (_i, []),
+    "jfg_device_supported": (_i, []),
+    "jfg_launch_count": (C.c_longlong, []),
+    "jfg_reset_launch_count": (None, []),
+    "jfg_weighted_field_f64": (_i, [_i, _i, _i, _vp, _vp, _vp, _vp]),
+    "jfg_contract_f64": (_i, [C.POINTER(ContractDesc), _vp, _vp, _vp, _vp]),
+    "jfg_contract_f32": (_i, [C.POINTER(ContractDesc), _vp, _vp, _vp, _vp]),
+    "jfg_contract_tc": (_i, [C.POINTER(ContractDesc), _vp, _vp, _vp, _vp, _vp]),
+    "jfg_tp_apply_workspace_size": (_sz, [_i, C.POINTER(_i), C.POINTER(_i), _i, _i]),
+    "jfg_tp_apply_f64": (_i, [_i, C.POINTER(_i), C.POINTER(_i), _i, C.POINTER(_vp), _vp, _vp,
+                              _vp, _sz, _vp]),
+    "jfg_tp_apply_f32": (_i, [_i, C.POINTER(_i), C.POINTER(_i), _i, C.POINTER(_vp), _vp, _vp,
+                              _vp, _sz, _vp]),
+    "jfg_fd_solve_workspace_size": (_sz, [_i, _i, _i, _i]),
+    "jfg_fd_solve_f64": (_i, [_i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
+    "jfg_fd_solve_f32": (_i, [_i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
+    "jfg_varcoef_ops_count": (_sz, [_i, _i, _i]),
+    "jfg_varcoef_pack_ops_host": (None, [_i, _i, _i, _vp, _vp, _vp]),
+    "jfg_varcoef_workspace_size": (_sz, [_i, _i, _i, _i, _i]),
+    "jfg_varcoef_apply_f64": (_i, [_i, _i, _i, _i, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
+    "jfg_varcoef_apply_f32": (_i, [_i, _i, _i, _i, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
+    "jfg_pcg_workspace_size": (_sz, [_i, _i, _i, _i, _i]),
+    "jfg_pcg_varcoef_f64": (_i, [_i, _i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i,
+                                 _d, _i, C.POINTER(_i), _vp, _sz, _vp]),
+}
+
+_lib: C.CDLL | None = None
+
+
+def load(build_if_missing: bool = True) -> C.CDLL:
+    """Load the shared library (building it first if absent and nvcc exists)."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists() and build_if_missing:
+        from .build import build
+
+        build()
+    if not LIB_PATH.exists():
+        raise RuntimeError(
+            f"jaxfun_gb300 CUDA library not found at {LIB_PATH}; run jaxfun_gb300.build.build()"
+        )
+    lib = C.CDLL(os.fspath(LIB_PATH))
+    for name, (res, args) in SIGNATURES.items():
+        fn = getattr(lib, name, None)
+        if fn is None:
+            continue
+        fn.restype = res
+        fn.argtypes = args
+    _lib = lib
+    return lib
+
+
+def lib() -> C.CDLL:
+    return load()
+
+
+def status_string(s: int) -> str:
+    if _lib is None:
+        return str(s)
+    return _lib.jfg_status_string(s).decode()
+
+
+def check(status: int, what: str) -> None:
+    if status == JFG_OK:
+        return
+    if status == JFG_ERR_NOT_CONVERGED:
+        raise NotConvergedError(status, what)
+    raise JfgError(status, what)
+
+
+def ptr(t) -> int | None:
+    """Device pointer of a torch tensor (None passes NULL)."""
+    if t is None:
+        return None
+    return t.data_ptr()
+
+
+def stream_handle(stream=None) -> int:
+    import torch
+
+    s = torch.cuda.current_stream() if stream is None else stream
+    return s.cuda_stream
+
+
+def int_array(vals):
+    arr = (C.c_int * len(vals))(*[int(v) for v in vals])
+    return arr
+
+
+def ptr_array(ptrs):
+    return (C.c_void_p * len(ptrs))(*ptrs)

@@ -1,0 +1,168 @@
+// Per-axis contraction on the CUDA cores (FP64 DFMA and FP32 FFMA).
+//
+// out[b][s][m][p] = alpha * epi(sum_k op[s][m][k] * in[b][s][p][k]) + beta * out[b][s][m][p]
+//
+// This is the plain-precision path: FP64 is the parity path (<= 1e-12 against
+// the FP64 oracle) and the FP64 residual of iterative refinement.  GB300's
+// FP64 rate is ~1.2 TFLOP/s (about 2 DFMA/clk/SM), so a 64x64 register-tiled
+// kernel is DFMA-bound long before it is memory-bound.
+#include <stdio.h>
+
+#include "jfg_internal.cuh"
+
+namespace jfg {
+
+namespace {
+
+constexpr int TM = 64;   // rows of the operator per CTA
+constexpr int TP = 64;   // columns (p) per CTA
+constexpr int TK = 16;   // contraction step
+constexpr int NT = 256;  // threads: 16 x 16, each 4 x 4 outputs
+
+template <typename T, int EPI>
+__global__ void __launch_bounds__(NT)
+    k_contract_simt(const jfg_contract_desc d, const T* __restrict__ op,
+                    const T* __restrict__ in, T* __restrict__ out) {
+  __shared__ T As[TK][TM + 4];
+  __shared__ T Bs[TK][TP + 4];
+
+  const int bz = blockIdx.z;
+  const int b = bz / d.nseg;
+  const int s = bz - b * d.nseg;
+  const int m0 = blockIdx.y * TM;
+  const int p0 = blockIdx.x * TP;
+  const T* opS = op + (long long)s * d.op_seg;
+  const T* inS = in + (long long)b * d.in_batch + (long long)s * d.in_seg;
+
+  const int tid = threadIdx.x;
+  const int tx = tid & 15;
+  const int ty = tid >> 4;
+
+  T acc[4][4];
+#pragma unroll
+  for (int i = 0; i < 4; ++i)
+#pragma unroll
+    for (int j = 0; j < 4; ++j) acc[i][j] = T(0);
+
+  for (int k0 = 0; k0 < d.K; k0 += TK) {
+#pragma unroll
+    for (int i = 0; i < (TM * TK) / NT; ++i) {
+      const int idx = tid + i * NT;
+      const int r = idx / TK;
+      const int kk = idx % TK;
+      const int m = m0 + r, k = k0 + kk;
+      As[kk][r] = (m < d.M && k < d.K) ? opS[(long long)m * d.op_ld + k] : T(0);
+      const int p = p0 + r;
+      Bs[kk][r] = (p < d.P && k < d.K) ? inS[(long long)p * d.in_ld + k] : T(0);
+    }
+    __syncthreads();
+#pragma unroll
+    for (int kk = 0; kk < TK; ++kk) {
+      T a[4], bb[4];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) a[i] = As[kk][ty * 4 + i];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) bb[j] = Bs[kk][tx * 4 + j];
+#pragma unroll
+      for (int i = 0; i < 4; ++i)
+#pragma unroll
+        for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], bb[j], acc[i][j]);
+    }
+    __syncthreads();
+  }
+
+  T* outS = out + (long long)b * d.out_batch + (long long)s * d.out_seg;
+  const T alpha = T(d.alpha);
+  const T beta = T(d.beta);
+#pragma unroll
+  for (int i = 0; i < 4; ++i) {
+    const int m = m0 + ty * 4 + i;
+    if (m >= d.M) continue;
+    T denom_m = T(0), c0 = T(0), c1 = T(1);
+    if (EPI == JFG_EPI_DIV_EIG) {
+      denom_m = ((const T*)d.lam_m)[m];
+      c0 = d.c0 ? ((const T*)d.c0)[b] : T(0);
+      c1 = d.c1 ? ((const T*)d.c1)[b] : T(1);
+    }
+#pragma unroll
+    for (int j = 0; j < 4; ++j) {
+      const int p = p0 + tx * 4 + j;
+      if (p >= d.P) continue;
+      T v = acc[i][j];
+      if (EPI == JFG_EPI_MUL_FIELD) {
+        const T* f = (const T*)d.field;
+        v *= f[(long long)b * d.field_batch + (long long)s * d.field_seg +
+               (long long)m * d.field_ld + p];
+      } else if (EPI == JFG_EPI_DIV_EIG) {
+        v = v / (c0 + c1 * (denom_m + ((const T*)d.lam_p)[p]));
+      }
+      T* o = outS + (long long)m * d.out_ld + p;
+      v = alpha * v;
+      if (beta != T(0)) v += beta * *o;
+      *o = v;
+    }
+  }
+}
+
+template <typename T>
+int launch_simt(const jfg_contract_desc& d, const T* op, const T* in, T* out,
+                cudaStream_t st) {
+  JFG_TRY(validate_desc(d));
+  if (!op || !in || !out) return JFG_ERR_ARG;
+  if (d.batch == 0 || d.M == 0 || d.P == 0) return JFG_OK;
+  const long long gz = (long long)d.batch * d.nseg;
+  if (gz > 65535) return JFG_ERR_ARG;
+  dim3 grid((d.P + TP - 1) / TP, (d.M + TM - 1) / TM, (unsigned)gz);
+  if (grid.y > 65535) return JFG_ERR_ARG;
+  switch (d.epilogue) {
+    case JFG_EPI_NONE:
+      k_contract_simt<T, JFG_EPI_NONE><<<grid, NT, 0, st>>>(d, op, in, out);
+      break;
+    case JFG_EPI_MUL_FIELD:
+      k_contract_simt<T, JFG_EPI_MUL_FIELD><<<grid, NT, 0, st>>>(d, op, in, out);
+      break;
+    case JFG_EPI_DIV_EIG:
+      k_contract_simt<T, JFG_EPI_DIV_EIG><<<grid, NT, 0, st>>>(d, op, in, out);
+      break;
+    default:
+      return JFG_ERR_ARG;
+  }
+  JFG_CHECK_LAUNCH();
+  count_launches(1);
+  return JFG_OK;
+}
+
+}  // namespace
+
+int validate_desc(const jfg_contract_desc& d) {
+  if (d.batch < 0 || d.nseg < 1 || d.M < 0 || d.P < 0 || d.K < 1) return JFG_ERR_ARG;
+  if (d.op_ld < d.K || d.in_ld < d.K || d.out_ld < d.P) return JFG_ERR_ARG;
+  if (d.epilogue == JFG_EPI_MUL_FIELD && (!d.field || d.field_ld < d.P)) return JFG_ERR_ARG;
+  if (d.epilogue == JFG_EPI_DIV_EIG && (!d.lam_m || !d.lam_p)) return JFG_ERR_ARG;
+  if (d.epilogue < 0 || d.epilogue > 2) return JFG_ERR_ARG;
+  return JFG_OK;
+}
+
+int contract_f64(const jfg_contract_desc& d, const double* op, const double* in, double* out,
+                 cudaStream_t st) {
+  return launch_simt<double>(d, op, in, out, st);
+}
+
+int contract_f32(const jfg_contract_desc& d, const float* op, const float* in, float* out,
+                 cudaStream_t st) {
+  return launch_simt<float>(d, op, in, out, st);
+}
+
+}  // namespace jfg
+
+extern "C" int jfg_contract_f64(const jfg_contract_desc* d, const double* op, const double* in,
+                                double* out, void* stream) {
+  if (!d) return JFG_ERR_ARG;
+  return jfg::contract_f64(*d, op, in, out, (cudaStream_t)stream);
+}
+
+extern "C" int jfg_contract_f32(const jfg_contract_desc* d, const float* op, const float* in,
+                                float* out, void* stream) {
+  if (!d) return JFG_ERR_ARG;
+  return jfg::contract_f32(*d, op, in, out, (cudaStream_t)stream);
+}

@@ -1,0 +1,121 @@
+// Internal helpers shared by the jaxfun_gb300 CUDA translation units.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "jaxfun_gb300.h"
+
+namespace jfg {
+
+// Last CUDA error observed on this host thread (reported by jfg_last_cuda_error).
+void set_last_cuda_error(cudaError_t e);
+
+// Kernel-launch accounting (jfg_launch_count): every launch site adds its
+// launches; while a stream is being captured into a graph nothing is counted
+// and each graph replay adds its kernel-node count instead.
+void count_launches(long long n);
+void set_capturing(bool on);
+
+#define JFG_CUDA_TRY(expr)                              \
+  do {                                                  \
+    cudaError_t _e = (expr);                            \
+    if (_e != cudaSuccess) {                            \
+      ::jfg::set_last_cuda_error(_e);                   \
+      return JFG_ERR_CUDA;                              \
+    }                                                   \
+  } while (0)
+
+#define JFG_CHECK_LAUNCH()                              \
+  do {                                                  \
+    cudaError_t _e = cudaGetLastError();                \
+    if (_e != cudaSuccess) {                            \
+      ::jfg::set_last_cuda_error(_e);                   \
+      return JFG_ERR_CUDA;                              \
+    }                                                   \
+  } while (0)
+
+// after a <<<>>> launch: check it and count it
+#define JFG_LAUNCHED()                                  \
+  do {                                                  \
+    JFG_CHECK_LAUNCH();                                 \
+    ::jfg::count_launches(1);                           \
+  } while (0)
+
+#define JFG_TRY(expr)                                   \
+  do {                                                  \
+    int _s = (expr);                                    \
+    if (_s != JFG_OK) return _s;                        \
+  } while (0)
+
+// A contraction operator: hi part (always) and, for the split-TF32 tensor-core
+// path, the lo part with the same layout.
+template <typename T>
+struct OpRef {
+  const T* hi;
+  const T* lo;
+  OpRef offset(long long o) const { return OpRef{hi + o, lo ? lo + o : nullptr}; }
+};
+
+// Dispatch of one contraction pass to an engine.
+enum class Engine { F64, F32, TC };
+
+int contract_f64(const jfg_contract_desc& d, const double* op, const double* in, double* out,
+                 cudaStream_t st);
+int contract_f32(const jfg_contract_desc& d, const float* op, const float* in, float* out,
+                 cudaStream_t st);
+int contract_tc(const jfg_contract_desc& d, const float* op_hi, const float* op_lo,
+                const float* in, float* out, cudaStream_t st);
+
+inline int contract(Engine e, const jfg_contract_desc& d, OpRef<double> op, const double* in,
+                    double* out, cudaStream_t st) {
+  (void)e;
+  return contract_f64(d, op.hi, in, out, st);
+}
+inline int contract(Engine e, const jfg_contract_desc& d, OpRef<float> op, const float* in,
+                    float* out, cudaStream_t st) {
+  if (e == Engine::TC) return contract_tc(d, op.hi, op.lo, in, out, st);
+  return contract_f32(d, op.hi, in, out, st);
+}
+
+// A zero-initialised descriptor for a single-segment pass with no epilogue.
+inline jfg_contract_desc make_desc(int batch, int M, int P, int K) {
+  jfg_contract_desc d = {};
+  d.batch = batch;
+  d.nseg = 1;
+  d.M = M;
+  d.P = P;
+  d.K = K;
+  d.op_ld = K;
+  d.in_ld = K;
+  d.in_batch = (long long)P * K;
+  d.out_ld = P;
+  d.out_batch = (long long)M * P;
+  d.epilogue = JFG_EPI_NONE;
+  d.alpha = 1.0;
+  d.beta = 0.0;
+  return d;
+}
+
+int validate_desc(const jfg_contract_desc& d);
+
+// Higher-level sequences (ops.cu), shared by the FP64, FP32 and tensor-core paths.
+template <typename T>
+int tp_apply(Engine e, int ndim, const int* rows, const int* cols, int batch,
+             const OpRef<T>* mats, const T* in, T* out, void* work, size_t work_bytes,
+             cudaStream_t st);
+template <typename T>
+int fd_solve(Engine e, int ndim, int n, int batch, OpRef<T> E, OpRef<T> W, const T* lam,
+             const T* c0, const T* c1, const T* rhs, T* out, void* work, size_t work_bytes,
+             cudaStream_t st);
+template <typename T>
+int varcoef_apply(Engine e, int ndim, int n, int nq, int batch, OpRef<T> ops, const T* kw,
+                  const T* u, T* v, void* work, size_t work_bytes, cudaStream_t st);
+
+size_t tp_apply_ws(int ndim, const int* rows, const int* cols, int batch, int eb);
+size_t fd_ws(int ndim, int n, int batch, int eb);
+size_t varcoef_ws(int ndim, int n, int nq, int batch, int eb);
+
+inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+}  // namespace jfg

@@ -1,0 +1,405 @@
+// Pass sequences of the tensor-product operations on top of the per-axis
+// contraction: separable transforms, fast-diagonalisation solve and the
+// sum-factorised variable-coefficient operator.  The same sequences run on
+// the FP64 / FP32 CUDA-core engines and on the split-TF32 tensor-core engine.
+//
+// Every pass contracts the LAST axis of its input and writes the result axis
+// FIRST ("rotate"), so a d-dimensional field returns to its original axis
+// order after d passes and every pass is the same strided GEMM shape with the
+// contracted index contiguous in memory.
+#include "jfg_internal.cuh"
+
+namespace jfg {
+
+// ---------------------------------------------------------------------------
+// separable transforms: out = (x_ax mats[ax]) in
+// ---------------------------------------------------------------------------
+
+size_t tp_apply_ws(int ndim, const int* rows, const int* cols, int batch, int eb) {
+  if (ndim < 1 || ndim > 3) return 0;
+  int shape[3];
+  int order[3];
+  for (int i = 0; i < ndim; ++i) shape[i] = cols[i], order[i] = i;
+  size_t mx = 0;
+  for (int t = 0; t < ndim - 1; ++t) {
+    const int ax = order[ndim - 1];
+    for (int i = ndim - 1; i > 0; --i) shape[i] = shape[i - 1], order[i] = order[i - 1];
+    shape[0] = rows[ax];
+    order[0] = ax;
+    size_t sz = (size_t)batch;
+    for (int i = 0; i < ndim; ++i) sz *= (size_t)shape[i];
+    if (sz > mx) mx = sz;
+  }
+  return 2 * align_up(mx * eb, 256);
+}
+
+template <typename T>
+int tp_apply(Engine e, int ndim, const int* rows, const int* cols, int batch,
+             const OpRef<T>* mats, const T* in, T* out, void* work, size_t work_bytes,
+             cudaStream_t st) {
+  if (ndim < 1 || ndim > 3 || !rows || !cols || !mats || !in || !out || batch < 0)
+    return JFG_ERR_ARG;
+  for (int i = 0; i < ndim; ++i)
+    if (rows[i] < 1 || cols[i] < 1 || !mats[i].hi) return JFG_ERR_ARG;
+  const size_t need = tp_apply_ws(ndim, rows, cols, batch, (int)sizeof(T));
+  if (ndim > 1 && (!work || work_bytes < need)) return JFG_ERR_WORKSPACE;
+  T* buf[2] = {(T*)work, (T*)((char*)work + need / 2)};
+
+  int shape[3], order[3];
+  for (int i = 0; i < ndim; ++i) shape[i] = cols[i], order[i] = i;
+  const T* src = in;
+  for (int t = 0; t < ndim; ++t) {
+    const int ax = order[ndim - 1];
+    const int K = shape[ndim - 1];
+    long long P = 1;
+    for (int i = 0; i < ndim - 1; ++i) P *= shape[i];
+    const int M = rows[ax];
+    T* dst = (t == ndim - 1) ? out : buf[t & 1];
+    jfg_contract_desc d = make_desc(batch, M, (int)P, K);
+    JFG_TRY(contract(e, d, mats[ax], src, dst, st));
+    for (int i = ndim - 1; i > 0; --i) shape[i] = shape[i - 1], order[i] = order[i - 1];
+    shape[0] = M;
+    order[0] = ax;
+    src = dst;
+  }
+  return JFG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// fast diagonalisation: U = (x W) [(x E) F / (c0 + c1 * sum lam)]
+// ---------------------------------------------------------------------------
+
+template <typename T>
+__global__ void k_lam_sum2(const T* __restrict__ lam, int n, T* __restrict__ out) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i < n * n) out[i] = lam[i / n] + lam[i % n];
+}
+
+size_t fd_ws(int ndim, int n, int batch, int eb) {
+  size_t field = (size_t)batch;
+  for (int i = 0; i < ndim; ++i) field *= (size_t)n;
+  return 2 * align_up(field * eb, 256) + align_up((size_t)n * n * eb, 256);
+}
+
+template <typename T>
+int fd_solve(Engine e, int ndim, int n, int batch, OpRef<T> E, OpRef<T> W, const T* lam,
+             const T* c0, const T* c1, const T* rhs, T* out, void* work, size_t work_bytes,
+             cudaStream_t st) {
+  if ((ndim != 2 && ndim != 3) || n < 1 || batch < 0 || !E.hi || !W.hi || !lam || !rhs ||
+      !out)
+    return JFG_ERR_ARG;
+  const size_t need = fd_ws(ndim, n, batch, (int)sizeof(T));
+  if (!work || work_bytes < need) return JFG_ERR_WORKSPACE;
+  size_t field = (size_t)batch;
+  for (int i = 0; i < ndim; ++i) field *= (size_t)n;
+  const size_t fb = align_up(field * sizeof(T), 256);
+  T* buf[2] = {(T*)work, (T*)((char*)work + fb)};
+  T* lam_p = (T*)((char*)work + 2 * fb);
+  if (batch == 0) return JFG_OK;
+  if (ndim == 3) {
+    k_lam_sum2<T><<<(n * n + 255) / 256, 256, 0, st>>>(lam, n, lam_p);
+    JFG_CHECK_LAUNCH();
+    count_launches(1);
+  }
+  long long P = (long long)n * (ndim == 3 ? n : 1);
+  const T* src = rhs;
+  int b = 0;
+  for (int t = 0; t < 2 * ndim; ++t) {
+    jfg_contract_desc d = make_desc(batch, n, (int)P, n);
+    if (t == ndim - 1) {
+      d.epilogue = JFG_EPI_DIV_EIG;
+      d.lam_m = lam;
+      d.lam_p = (ndim == 3) ? lam_p : lam;
+      d.c0 = c0;
+      d.c1 = c1;
+    }
+    T* dst = (t == 2 * ndim - 1) ? out : buf[b];
+    JFG_TRY(contract(e, d, t < ndim ? E : W, src, dst, st));
+    src = dst;
+    b ^= 1;
+  }
+  return JFG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// variable-coefficient operator (kappa grad u, grad v), sum-factorised
+// ---------------------------------------------------------------------------
+//
+// Packed operators (units of n*nq elements), B[q][k] = phi_k(x_q), D = phi_k':
+//   2-D: [B;D] (2nq x n) | D, B (nq x n) | B^T, D^T (n x nq) | [D^T | B^T] (n x 2nq)
+//   3-D: [B;D] (2nq x n) | D, B, B (nq x n) | B^T, B^T, D^T (n x nq)
+
+size_t varcoef_ws(int ndim, int n, int nq, int batch, int eb) {
+  size_t a, b;
+  if (ndim == 2) {
+    a = (size_t)2 * n * nq;
+    b = (size_t)2 * nq * nq;
+  } else {
+    a = (size_t)3 * nq * nq * nq;
+    b = (size_t)3 * nq * nq * n;
+  }
+  return align_up(a * batch * eb, 256) + align_up(b * batch * eb, 256);
+}
+
+template <typename T>
+int varcoef_apply(Engine e, int ndim, int n, int nq, int batch, OpRef<T> ops, const T* kw,
+                  const T* u, T* v, void* work, size_t work_bytes, cudaStream_t st) {
+  if ((ndim != 2 && ndim != 3) || n < 1 || nq < 1 || batch < 0 || !ops.hi || !kw || !u || !v)
+    return JFG_ERR_ARG;
+  const size_t need = varcoef_ws(ndim, n, nq, batch, (int)sizeof(T));
+  if (!work || work_bytes < need) return JFG_ERR_WORKSPACE;
+  if (batch == 0) return JFG_OK;
+  const long long nn = (long long)n * nq;
+  const size_t a_elems = ndim == 2 ? (size_t)2 * n * nq : (size_t)3 * nq * nq * nq;
+  T* bufA = (T*)work;
+  T* bufB = (T*)((char*)work + align_up(a_elems * batch * sizeof(T), 256));
+
+  if (ndim == 2) {
+    // 1: T[b][r][j] = sum_l [B;D][r][l] U[b][j][l]            (M=2nq, P=n, K=n)
+    jfg_contract_desc d1 = make_desc(batch, 2 * nq, n, n);
+    JFG_TRY(contract(e, d1, ops, u, bufA, st));
+    // 2: G[b][s][p][q] = kw[b][p][q] * sum_j {D,B}[p][j] T[b][s][q][j]
+    jfg_contract_desc d2 = make_desc(batch, nq, nq, n);
+    d2.nseg = 2;
+    d2.op_seg = nn;
+    d2.in_seg = nn;
+    d2.in_batch = 2 * nn;
+    d2.out_seg = (long long)nq * nq;
+    d2.out_batch = 2LL * nq * nq;
+    d2.epilogue = JFG_EPI_MUL_FIELD;
+    d2.field = kw;
+    d2.field_ld = nq;
+    d2.field_seg = 0;
+    d2.field_batch = (long long)nq * nq;
+    JFG_TRY(contract(e, d2, ops.offset(2 * nn), bufA, bufB, st));
+    // 3: H[b][k][s][p] = sum_q {B^T,D^T}[k][q] G[b][s][p][q]   (M=n, P=nq, K=nq)
+    jfg_contract_desc d3 = make_desc(batch, n, nq, nq);
+    d3.nseg = 2;
+    d3.op_seg = nn;
+    d3.in_seg = (long long)nq * nq;
+    d3.in_batch = 2LL * nq * nq;
+    d3.out_ld = 2LL * nq;
+    d3.out_seg = nq;
+    d3.out_batch = 2 * nn;
+    JFG_TRY(contract(e, d3, ops.offset(4 * nn), bufB, bufA, st));
+    // 4: V[b][i][k] = sum_{s,p} [D^T|B^T][i][(s,p)] H[b][k][(s,p)]   (M=n, P=n, K=2nq)
+    jfg_contract_desc d4 = make_desc(batch, n, n, 2 * nq);
+    JFG_TRY(contract(e, d4, ops.offset(6 * nn), bufA, v, st));
+    return JFG_OK;
+  }
+
+  // ---- 3-D ----
+  const long long n2 = (long long)n * n, q2 = (long long)nq * nq;
+  const OpRef<T> BD = ops;                   // [B;D]  (2nq x n)
+  const OpRef<T> Q3 = ops.offset(2 * nn);    // D, B, B
+  const OpRef<T> Q4 = ops.offset(5 * nn);    // B^T, B^T, D^T
+  // 1: T1[b][(s2,q2)][(i0,i1)] = sum_i2 [B;D] U                 (M=2nq, P=n^2, K=n)
+  jfg_contract_desc d1 = make_desc(batch, 2 * nq, (int)n2, n);
+  JFG_TRY(contract(e, d1, BD, u, bufA, st));
+  // 2a: s2=0 rows with [B;D]: T2[b][(c,q1)][(q2,i0)], c in {0,1}  (M=2nq, P=nq*n, K=n)
+  jfg_contract_desc d2 = make_desc(batch, 2 * nq, (int)nn, n);
+  d2.in_batch = 2 * nq * n2;
+  d2.out_batch = 3 * q2 * n;
+  JFG_TRY(contract(e, d2, BD, bufA, bufB, st));
+  // 2b: s2=1 rows with B -> c = 2
+  jfg_contract_desc d2b = d2;
+  d2b.M = nq;
+  JFG_TRY(contract(e, d2b, BD, bufA + nq * n2, bufB + 2 * q2 * n, st));
+  // 3: G[b][c][p0][(q1,q2)] = kw * sum_i0 {D,B,B}[p0][i0] T2[b][c][(q1,q2)][i0]
+  jfg_contract_desc d3 = make_desc(batch, nq, (int)q2, n);
+  d3.nseg = 3;
+  d3.op_seg = nn;
+  d3.in_seg = q2 * n;
+  d3.in_batch = 3 * q2 * n;
+  d3.out_seg = q2 * nq;
+  d3.out_batch = 3 * q2 * nq;
+  d3.epilogue = JFG_EPI_MUL_FIELD;
+  d3.field = kw;
+  d3.field_ld = q2;
+  d3.field_seg = 0;
+  d3.field_batch = q2 * nq;
+  JFG_TRY(contract(e, d3, Q3, bufB, bufA, st));
+  // 4: H1[b][c][k2][(p0,q1)] = sum_q2 {B^T,B^T,D^T}[k2][q2] G     (M=n, P=nq^2, K=nq)
+  jfg_contract_desc d4 = make_desc(batch, n, (int)q2, nq);
+  d4.nseg = 3;
+  d4.op_seg = nn;
+  d4.in_seg = q2 * nq;
+  d4.in_batch = 3 * q2 * nq;
+  d4.out_seg = q2 * n;
+  d4.out_batch = 3 * q2 * n;
+  JFG_TRY(contract(e, d4, Q4, bufA, bufB, st));
+  // 5: H2a = B^T (c=0), H2b = D^T (c=1) + B^T (c=2)      (M=n, P=n*nq, K=nq)
+  T* H2a = bufA;
+  T* H2b = bufA + (size_t)batch * n2 * nq;
+  jfg_contract_desc d5 = make_desc(batch, n, (int)nn, nq);
+  d5.in_batch = 3 * q2 * n;
+  JFG_TRY(contract(e, d5, Q4, bufB, H2a, st));
+  JFG_TRY(contract(e, d5, Q4.offset(2 * nn), bufB + q2 * n, H2b, st));
+  d5.beta = 1.0;
+  JFG_TRY(contract(e, d5, Q4, bufB + 2 * q2 * n, H2b, st));
+  // 6: V = D^T (x) on H2a + B^T (x) on H2b                 (M=n, P=n^2, K=nq)
+  jfg_contract_desc d6 = make_desc(batch, n, (int)n2, nq);
+  JFG_TRY(contract(e, d6, Q4.offset(2 * nn), H2a, v, st));
+  d6.beta = 1.0;
+  JFG_TRY(contract(e, d6, Q4, H2b, v, st));
+  return JFG_OK;
+}
+
+template <typename T>
+__global__ void k_weighted_field(int ndim, int nq, long long total, const T* __restrict__ kappa,
+                                 const T* __restrict__ w, T* __restrict__ kw) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+       i += (long long)gridDim.x * blockDim.x) {
+    long long r = i;
+    T s = T(1);
+    for (int a = 0; a < ndim; ++a) {
+      s *= w[r % nq];
+      r /= nq;
+    }
+    kw[i] = kappa[i] * s;
+  }
+}
+
+template int tp_apply<double>(Engine, int, const int*, const int*, int, const OpRef<double>*,
+                              const double*, double*, void*, size_t, cudaStream_t);
+template int tp_apply<float>(Engine, int, const int*, const int*, int, const OpRef<float>*,
+                             const float*, float*, void*, size_t, cudaStream_t);
+template int fd_solve<double>(Engine, int, int, int, OpRef<double>, OpRef<double>,
+                              const double*, const double*, const double*, const double*,
+                              double*, void*, size_t, cudaStream_t);
+template int fd_solve<float>(Engine, int, int, int, OpRef<float>, OpRef<float>, const float*,
+                             const float*, const float*, const float*, float*, void*, size_t,
+                             cudaStream_t);
+template int varcoef_apply<double>(Engine, int, int, int, int, OpRef<double>, const double*,
+                                   const double*, double*, void*, size_t, cudaStream_t);
+template int varcoef_apply<float>(Engine, int, int, int, int, OpRef<float>, const float*,
+                                  const float*, float*, void*, size_t, cudaStream_t);
+
+}  // namespace jfg
+
+// ---------------------------------------------------------------------------
+// C ABI
+// ---------------------------------------------------------------------------
+
+using jfg::Engine;
+using jfg::OpRef;
+
+extern "C" int jfg_weighted_field_f64(int ndim, int nq, int batch, const double* kappa,
+                                      const double* w, double* kw, void* stream) {
+  if (ndim < 1 || ndim > 3 || nq < 1 || batch < 0 || !kappa || !w || !kw) return JFG_ERR_ARG;
+  long long total = batch;
+  for (int i = 0; i < ndim; ++i) total *= nq;
+  if (total == 0) return JFG_OK;
+  long long blocks = (total + 255) / 256;
+  if (blocks > 4096) blocks = 4096;
+  jfg::k_weighted_field<double><<<(int)blocks, 256, 0, (cudaStream_t)stream>>>(ndim, nq, total,
+                                                                               kappa, w, kw);
+  JFG_CHECK_LAUNCH();
+  jfg::count_launches(1);
+  return JFG_OK;
+}
+
+extern "C" size_t jfg_tp_apply_workspace_size(int ndim, const int* rows, const int* cols,
+                                              int batch, int elem_bytes) {
+  if (!rows || !cols) return 0;
+  return jfg::tp_apply_ws(ndim, rows, cols, batch, elem_bytes);
+}
+
+extern "C" int jfg_tp_apply_f64(int ndim, const int* rows, const int* cols, int batch,
+                                const double* const* mats, const double* in, double* out,
+                                void* work, size_t work_bytes, void* stream) {
+  if (!mats || ndim < 1 || ndim > 3) return JFG_ERR_ARG;
+  OpRef<double> m[3];
+  for (int i = 0; i < ndim; ++i) m[i] = OpRef<double>{mats[i], nullptr};
+  return jfg::tp_apply<double>(Engine::F64, ndim, rows, cols, batch, m, in, out, work,
+                               work_bytes, (cudaStream_t)stream);
+}
+
+extern "C" int jfg_tp_apply_f32(int ndim, const int* rows, const int* cols, int batch,
+                                const float* const* mats, const float* in, float* out,
+                                void* work, size_t work_bytes, void* stream) {
+  if (!mats || ndim < 1 || ndim > 3) return JFG_ERR_ARG;
+  OpRef<float> m[3];
+  for (int i = 0; i < ndim; ++i) m[i] = OpRef<float>{mats[i], nullptr};
+  return jfg::tp_apply<float>(Engine::F32, ndim, rows, cols, batch, m, in, out, work,
+                              work_bytes, (cudaStream_t)stream);
+}
+
+extern "C" size_t jfg_fd_solve_workspace_size(int ndim, int n, int batch, int elem_bytes) {
+  return jfg::fd_ws(ndim, n, batch, elem_bytes);
+}
+
+extern "C" int jfg_fd_solve_f64(int ndim, int n, int batch, const double* E, const double* W,
+                                const double* lam, const double* c0, const double* c1,
+                                const double* rhs, double* out, void* work, size_t work_bytes,
+                                void* stream) {
+  return jfg::fd_solve<double>(Engine::F64, ndim, n, batch, OpRef<double>{E, nullptr},
+                               OpRef<double>{W, nullptr}, lam, c0, c1, rhs, out, work,
+                               work_bytes, (cudaStream_t)stream);
+}
+
+extern "C" int jfg_fd_solve_f32(int ndim, int n, int batch, const float* E, const float* W,
+                                const float* lam, const float* c0, const float* c1,
+                                const float* rhs, float* out, void* work, size_t work_bytes,
+                                void* stream) {
+  return jfg::fd_solve<float>(Engine::F32, ndim, n, batch, OpRef<float>{E, nullptr},
+                              OpRef<float>{W, nullptr}, lam, c0, c1, rhs, out, work,
+                              work_bytes, (cudaStream_t)stream);
+}
+
+extern "C" size_t jfg_varcoef_ops_count(int ndim, int n, int nq) {
+  (void)ndim;
+  return (size_t)8 * n * nq;
+}
+
+extern "C" void jfg_varcoef_pack_ops_host(int ndim, int n, int nq, const double* B,
+                                          const double* D, double* o) {
+  const size_t nn = (size_t)n * nq;
+  // [B;D]
+  for (int q = 0; q < nq; ++q)
+    for (int k = 0; k < n; ++k) {
+      o[(size_t)q * n + k] = B[(size_t)q * n + k];
+      o[nn + (size_t)q * n + k] = D[(size_t)q * n + k];
+    }
+  if (ndim == 2) {
+    for (int q = 0; q < nq; ++q)
+      for (int k = 0; k < n; ++k) {
+        o[2 * nn + (size_t)q * n + k] = D[(size_t)q * n + k];
+        o[3 * nn + (size_t)q * n + k] = B[(size_t)q * n + k];
+        o[4 * nn + (size_t)k * nq + q] = B[(size_t)q * n + k];
+        o[5 * nn + (size_t)k * nq + q] = D[(size_t)q * n + k];
+        o[6 * nn + (size_t)k * 2 * nq + q] = D[(size_t)q * n + k];
+        o[6 * nn + (size_t)k * 2 * nq + nq + q] = B[(size_t)q * n + k];
+      }
+  } else {
+    for (int q = 0; q < nq; ++q)
+      for (int k = 0; k < n; ++k) {
+        o[2 * nn + (size_t)q * n + k] = D[(size_t)q * n + k];
+        o[3 * nn + (size_t)q * n + k] = B[(size_t)q * n + k];
+        o[4 * nn + (size_t)q * n + k] = B[(size_t)q * n + k];
+        o[5 * nn + (size_t)k * nq + q] = B[(size_t)q * n + k];
+        o[6 * nn + (size_t)k * nq + q] = B[(size_t)q * n + k];
+        o[7 * nn + (size_t)k * nq + q] = D[(size_t)q * n + k];
+      }
+  }
+}
+
+extern "C" size_t jfg_varcoef_workspace_size(int ndim, int n, int nq, int batch,
+                                             int elem_bytes) {
+  return jfg::varcoef_ws(ndim, n, nq, batch, elem_bytes);
+}
+
+extern "C" int jfg_varcoef_apply_f64(int ndim, int n, int nq, int batch, const double* ops,
+                                     const double* kw, const double* u, double* v, void* work,
+                                     size_t work_bytes, void* stream) {
+  return jfg::varcoef_apply<double>(Engine::F64, ndim, n, nq, batch,
+                                    OpRef<double>{ops, nullptr}, kw, u, v, work, work_bytes,
+                                    (cudaStream_t)stream);
+}
+
+extern "C" int jfg_varcoef_apply_f32(int ndim, int n, int nq, int batch, const float* ops,
+                                     const float* kw, const float* u, float* v, void* work,
+                                     size_t work_bytes, void* stream) {
+  return jfg::varcoef_apply<float>(Engine::F32, ndim, n, nq, batch, OpRef<float>{ops, nullptr},
+                                   kw, u, v, work, work_bytes, (cudaStream_t)stream);
+}

@@ -1,0 +1,337 @@
+// Batched preconditioned conjugate gradients for the variable-coefficient
+// operator with the constant-coefficient fast-diagonalisation preconditioner.
+//
+// Every problem of the batch runs in lock-step; per-problem scalars live on
+// the device as block partial sums (warp-shuffle reductions), so no kernel
+// waits on the host.  A problem that has converged keeps alpha = 0 from then
+// on.  Chunks of iterations are captured once into a CUDA graph and replayed;
+// the host reads one counter (problems still active) per chunk.
+#include <math.h>
+#include <string.h>
+
+#include "jfg_internal.cuh"
+#include "pcg_internal.cuh"
+
+namespace jfg {
+
+namespace {
+
+constexpr int NB = 16;    // partial sums per problem
+constexpr int DOT_T = 256;
+
+template <typename T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+template <typename T>
+__device__ __forceinline__ T block_sum(T v) {
+  __shared__ T red[32];
+  v = warp_sum(v);
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) red[w] = v;
+  __syncthreads();
+  const int nw = blockDim.x >> 5;
+  v = (threadIdx.x < nw) ? red[threadIdx.x] : T(0);
+  if (w == 0) v = warp_sum(v);
+  __syncthreads();
+  return v;  // valid in thread 0
+}
+
+// part[b*NB + j] = sum over chunk j of x[b]*y[b]
+template <typename T>
+__global__ void __launch_bounds__(DOT_T)
+    k_dot_part(const T* __restrict__ x, const T* __restrict__ y, long long N,
+               T* __restrict__ part) {
+  const int b = blockIdx.y, j = blockIdx.x;
+  const long long chunk = (N + NB - 1) / NB;
+  const long long lo = j * chunk, hi = min(N, lo + chunk);
+  const T* xb = x + (long long)b * N;
+  const T* yb = y + (long long)b * N;
+  T s = T(0);
+  for (long long i = lo + threadIdx.x; i < hi; i += DOT_T) s += xb[i] * yb[i];
+  s = block_sum(s);
+  if (threadIdx.x == 0) part[b * NB + j] = s;
+}
+
+template <typename T>
+__device__ __forceinline__ T sum_part(const T* part, int b) {
+  T s = T(0);
+#pragma unroll
+  for (int j = 0; j < NB; ++j) s += part[b * NB + j];
+  return s;
+}
+
+template <typename T>
+__device__ __forceinline__ bool is_active(T rz, T rz0, double tol) {
+  return rz0 > T(0) && rz > T(0) && (double)rz > tol * tol * (double)rz0;
+}
+
+// x += alpha p ; r -= alpha q ; alpha = rz / (p.q) while active
+template <typename T>
+__global__ void k_update_xr(T* __restrict__ x, T* __restrict__ r, const T* __restrict__ p,
+                            const T* __restrict__ q, long long N, const T* __restrict__ pq_part,
+                            const T* __restrict__ rz_prev, const T* __restrict__ rz0,
+                            double tol) {
+  const int b = blockIdx.y;
+  const T rz = sum_part(rz_prev, b);
+  if (!is_active(rz, rz0[b], tol)) return;
+  const T pq = sum_part(pq_part, b);
+  const T alpha = rz / pq;
+  const long long off = (long long)b * N;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N;
+       i += (long long)gridDim.x * blockDim.x) {
+    x[off + i] += alpha * p[off + i];
+    r[off + i] -= alpha * q[off + i];
+  }
+}
+
+// p = z + beta p ; beta = rz_new / rz_prev while active; counts iterations
+template <typename T>
+__global__ void k_update_p(T* __restrict__ p, const T* __restrict__ z, long long N,
+                           const T* __restrict__ rz_new_part, const T* __restrict__ rz_prev_part,
+                           const T* __restrict__ rz0, double tol, int* __restrict__ iters,
+                           int* __restrict__ nactive) {
+  const int b = blockIdx.y;
+  const T rzp = sum_part(rz_prev_part, b);
+  if (!is_active(rzp, rz0[b], tol)) return;
+  const T rzn = sum_part(rz_new_part, b);
+  const T beta = rzn / rzp;
+  const long long off = (long long)b * N;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N;
+       i += (long long)gridDim.x * blockDim.x)
+    p[off + i] = z[off + i] + beta * p[off + i];
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    iters[b] += 1;
+    if (is_active(rzn, rz0[b], tol)) atomicAdd(nactive, 1);
+  }
+}
+
+template <typename T>
+__global__ void k_set_rz0(const T* __restrict__ part, T* __restrict__ rz0, int batch) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b < batch) rz0[b] = sum_part(part, b);
+}
+
+// y = a - y  (r = rhs - A x)
+template <typename T>
+__global__ void k_sub_from(const T* __restrict__ a, T* __restrict__ y, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    y[i] = a[i] - y[i];
+}
+
+inline int vec_blocks(long long N) {
+  long long b = (N + 255) / 256;
+  if (b > 64) b = 64;
+  return (int)(b < 1 ? 1 : b);
+}
+
+}  // namespace
+
+// ---------------------------------------------------------------------------
+
+template <typename T>
+size_t pcg_ws(int ndim, int n, int nq, int batch) {
+  long long N = 1;
+  for (int i = 0; i < ndim; ++i) N *= n;
+  const size_t vec = align_up((size_t)N * batch * sizeof(T), 256);
+  const size_t scal = align_up((size_t)batch * NB * sizeof(T), 256);
+  const size_t small = align_up((size_t)batch * sizeof(T), 256) +
+                       align_up((size_t)batch * sizeof(int), 256) + 256;
+  size_t inner = varcoef_ws(ndim, n, nq, batch, sizeof(T));
+  const size_t f = fd_ws(ndim, n, batch, sizeof(T));
+  if (f > inner) inner = f;
+  return 4 * vec + 3 * scal + small + inner;
+}
+
+template size_t pcg_ws<double>(int, int, int, int);
+template size_t pcg_ws<float>(int, int, int, int);
+
+template <typename T>
+int pcg_run(const PcgProblem<T>& pb, T* x, int use_x0, double tol, int maxiter, int* iters_host,
+            void* work, size_t work_bytes, cudaStream_t st) {
+  const int ndim = pb.ndim, n = pb.n, nq = pb.nq, batch = pb.batch;
+  if ((ndim != 2 && ndim != 3) || n < 1 || nq < n || batch < 1 || !pb.rhs || !x ||
+      !(tol > 0.0) || maxiter < 0)
+    return JFG_ERR_ARG;
+  const size_t need = pcg_ws<T>(ndim, n, nq, batch);
+  if (!work || work_bytes < need) return JFG_ERR_WORKSPACE;
+  long long N = 1;
+  for (int i = 0; i < ndim; ++i) N *= n;
+  const size_t vec = align_up((size_t)N * batch * sizeof(T), 256);
+  const size_t scal = align_up((size_t)batch * NB * sizeof(T), 256);
+  char* w = (char*)work;
+  T* r = (T*)w;
+  T* z = (T*)(w + vec);
+  T* p = (T*)(w + 2 * vec);
+  T* q = (T*)(w + 3 * vec);
+  T* pq_part = (T*)(w + 4 * vec);
+  T* rz_part[2] = {(T*)(w + 4 * vec + scal), (T*)(w + 4 * vec + 2 * scal)};
+  char* sm = w + 4 * vec + 3 * scal;
+  T* rz0 = (T*)sm;
+  int* iters = (int*)(sm + align_up((size_t)batch * sizeof(T), 256));
+  int* nactive = (int*)(sm + align_up((size_t)batch * sizeof(T), 256) +
+                        align_up((size_t)batch * sizeof(int), 256));
+  void* inner = w + 4 * vec + 3 * scal + align_up((size_t)batch * sizeof(T), 256) +
+                align_up((size_t)batch * sizeof(int), 256) + 256;
+  const size_t inner_bytes = work_bytes - (size_t)((char*)inner - w);
+
+  auto applyA = [&](const T* in, T* out) -> int {
+    return varcoef_apply<T>(pb.engine, ndim, n, nq, batch, pb.ops, pb.kw, in, out, inner,
+                            inner_bytes, st);
+  };
+  auto applyM = [&](const T* in, T* out) -> int {
+    return fd_solve<T>(pb.engine, ndim, n, batch, pb.E, pb.W, pb.lam, nullptr, pb.fd_scale, in,
+                       out, inner, inner_bytes, st);
+  };
+
+  const int vb = vec_blocks(N);
+  const dim3 vgrid(vb, batch);
+  const dim3 dgrid(NB, batch);
+  const long long total = N * batch;
+
+  // ---- setup: r = rhs - A x (or x = 0, r = rhs); z = M^-1 r; p = z
+  JFG_CUDA_TRY(cudaMemsetAsync(iters, 0, sizeof(int) * batch, st));
+  if (use_x0) {
+    JFG_TRY(applyA(x, r));
+    k_sub_from<T><<<vec_blocks(total), 256, 0, st>>>(pb.rhs, r, total);
+    JFG_LAUNCHED();
+  } else {
+    JFG_CUDA_TRY(cudaMemsetAsync(x, 0, sizeof(T) * total, st));
+    JFG_CUDA_TRY(cudaMemcpyAsync(r, pb.rhs, sizeof(T) * total, cudaMemcpyDeviceToDevice, st));
+  }
+  JFG_TRY(applyM(r, z));
+  JFG_CUDA_TRY(cudaMemcpyAsync(p, z, sizeof(T) * total, cudaMemcpyDeviceToDevice, st));
+  k_dot_part<T><<<dgrid, DOT_T, 0, st>>>(r, z, N, rz_part[1]);
+  JFG_LAUNCHED();
+  k_set_rz0<T><<<(batch + 127) / 128, 128, 0, st>>>(rz_part[1], rz0, batch);
+  JFG_LAUNCHED();
+
+  auto iteration = [&](int it, bool reset_counter) -> int {
+    const int prev = (it + 1) & 1, cur = it & 1;
+    JFG_TRY(applyA(p, q));
+    k_dot_part<T><<<dgrid, DOT_T, 0, st>>>(p, q, N, pq_part);
+    JFG_LAUNCHED();
+    k_update_xr<T><<<vgrid, 256, 0, st>>>(x, r, p, q, N, pq_part, rz_part[prev], rz0, tol);
+    JFG_LAUNCHED();
+    JFG_TRY(applyM(r, z));
+    k_dot_part<T><<<dgrid, DOT_T, 0, st>>>(r, z, N, rz_part[cur]);
+    JFG_LAUNCHED();
+    if (reset_counter) JFG_CUDA_TRY(cudaMemsetAsync(nactive, 0, sizeof(int), st));
+    k_update_p<T><<<vgrid, 256, 0, st>>>(p, z, N, rz_part[cur], rz_part[prev], rz0, tol, iters,
+                                         nactive);
+    JFG_LAUNCHED();
+    return JFG_OK;
+  };
+
+  // ---- iterate in chunks of CH iterations (CH even: the partial-sum
+  // ping-pong then lines up with the captured graph)
+  const int CH = 10;
+  const bool use_graph = (st != 0) && (maxiter >= CH);
+  cudaGraphExec_t exec = nullptr;
+  long long graph_kernels = 0;
+  if (use_graph) {
+    cudaGraph_t graph = nullptr;
+    JFG_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
+    set_capturing(true);
+    int s = JFG_OK;
+    for (int i = 0; i < CH && s == JFG_OK; ++i) s = iteration(i, i == CH - 1);
+    set_capturing(false);
+    cudaError_t ec = cudaStreamEndCapture(st, &graph);
+    if (s != JFG_OK) {
+      if (graph) cudaGraphDestroy(graph);
+      return s;
+    }
+    JFG_CUDA_TRY(ec);
+    size_t nn = 0;
+    cudaGraphGetNodes(graph, nullptr, &nn);
+    if (nn > 0) {
+      cudaGraphNode_t nodes[4096];
+      if (nn > 4096) nn = 4096;
+      cudaGraphGetNodes(graph, nodes, &nn);
+      for (size_t i = 0; i < nn; ++i) {
+        cudaGraphNodeType t;
+        if (cudaGraphNodeGetType(nodes[i], &t) == cudaSuccess && t == cudaGraphNodeTypeKernel)
+          ++graph_kernels;
+      }
+    }
+    cudaError_t ei = cudaGraphInstantiate(&exec, graph, 0);
+    cudaGraphDestroy(graph);
+    JFG_CUDA_TRY(ei);
+  }
+  int done_iters = 0;
+  int status = JFG_OK;
+  int h_active = 1;
+  while (done_iters < maxiter) {
+    if (use_graph && maxiter - done_iters >= CH) {
+      cudaError_t e = cudaGraphLaunch(exec, st);
+      if (e != cudaSuccess) {
+        set_last_cuda_error(e);
+        status = JFG_ERR_CUDA;
+        break;
+      }
+      count_launches(graph_kernels);
+      done_iters += CH;
+    } else {
+      const int todo = (maxiter - done_iters < CH) ? maxiter - done_iters : CH;
+      for (int i = 0; i < todo && status == JFG_OK; ++i)
+        status = iteration(done_iters + i, i == todo - 1);
+      if (status != JFG_OK) break;
+      done_iters += todo;
+    }
+    cudaError_t e = cudaMemcpyAsync(&h_active, nactive, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) {
+      set_last_cuda_error(e);
+      status = JFG_ERR_CUDA;
+      break;
+    }
+    if (h_active == 0) break;
+  }
+  if (exec) cudaGraphExecDestroy(exec);
+  if (status != JFG_OK) return status;
+  if (iters_host) {
+    JFG_CUDA_TRY(cudaMemcpyAsync(iters_host, iters, sizeof(int) * batch,
+                                 cudaMemcpyDeviceToHost, st));
+    JFG_CUDA_TRY(cudaStreamSynchronize(st));
+  }
+  return h_active == 0 ? JFG_OK : JFG_ERR_NOT_CONVERGED;
+}
+
+template int pcg_run<double>(const PcgProblem<double>&, double*, int, double, int, int*, void*,
+                             size_t, cudaStream_t);
+template int pcg_run<float>(const PcgProblem<float>&, float*, int, double, int, int*, void*,
+                            size_t, cudaStream_t);
+
+}  // namespace jfg
+
+extern "C" size_t jfg_pcg_workspace_size(int ndim, int n, int nq, int batch, int elem_bytes) {
+  if (elem_bytes == 8) return jfg::pcg_ws<double>(ndim, n, nq, batch);
+  return jfg::pcg_ws<float>(ndim, n, nq, batch);
+}
+
+extern "C" int jfg_pcg_varcoef_f64(int ndim, int n, int nq, int batch, const double* ops,
+                                   const double* kw, const double* E, const double* W,
+                                   const double* lam, const double* fd_scale, const double* rhs,
+                                   double* x, int use_x0, double tol, int maxiter, int* iters,
+                                   void* work, size_t work_bytes, void* stream) {
+  if (!ops || !kw || !E || !W || !lam) return JFG_ERR_ARG;
+  jfg::PcgProblem<double> pb;
+  pb.engine = jfg::Engine::F64;
+  pb.ndim = ndim;
+  pb.n = n;
+  pb.nq = nq;
+  pb.batch = batch;
+  pb.ops = jfg::OpRef<double>{ops, nullptr};
+  pb.kw = kw;
+  pb.E = jfg::OpRef<double>{E, nullptr};
+  pb.W = jfg::OpRef<double>{W, nullptr};
+  pb.lam = lam;
+  pb.fd_scale = fd_scale;
+  pb.rhs = rhs;
+  return jfg::pcg_run<double>(pb, x, use_x0, tol, maxiter, iters, work, work_bytes,
+                              (cudaStream_t)stream);
+}

@@ -1,0 +1,28 @@
+// Internal PCG problem description shared by the plain and mixed solvers.
+#pragma once
+
+#include "jfg_internal.cuh"
+
+namespace jfg {
+
+template <typename T>
+struct PcgProblem {
+  Engine engine = Engine::F64;
+  int ndim = 2, n = 0, nq = 0, batch = 0;
+  OpRef<T> ops{nullptr, nullptr};  // packed variable-coefficient operators
+  const T* kw = nullptr;           // (batch, nq^ndim) kappa * quadrature weights
+  OpRef<T> E{nullptr, nullptr};    // fast-diagonalisation forward (n x n)
+  OpRef<T> W{nullptr, nullptr};    // fast-diagonalisation backward (n x n)
+  const T* lam = nullptr;          // (n)
+  const T* fd_scale = nullptr;     // (batch) constant kappa of the preconditioner
+  const T* rhs = nullptr;          // (batch, n^ndim)
+};
+
+template <typename T>
+size_t pcg_ws(int ndim, int n, int nq, int batch);
+
+template <typename T>
+int pcg_run(const PcgProblem<T>& pb, T* x, int use_x0, double tol, int maxiter,
+            int* iters_host, void* work, size_t work_bytes, cudaStream_t st);
+
+}  // namespace jfg

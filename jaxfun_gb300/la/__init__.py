@@ -1,0 +1,17 @@
+"""Linear algebra on the GPU path (mirrors jaxfun.la)."""
+
+from .tpmatrix import (  # noqa: F401
+    SolverNotApplicable,
+    TPMatrices,
+    TPMatricesLUFactors,
+    TPMatrix,
+    fd_eig,
+    tpmats_lu_factor,
+)
+from .varcoef import (  # noqa: F401
+    VarCoefMatrix,
+    fd_preconditioner,
+    pack_varcoef_ops,
+    pcg,
+    poisson_tpmatrices,
+)

@@ -1,0 +1,134 @@
+"""Variable-coefficient operator (kappa grad u, grad v) and batched PCG.
+
+jaxfun assembles ``inner(kappa*Dot(Grad(u), Grad(v)))`` with a non-separable
+kappa into a dense 4-index ``TensorMatrix`` A[i,k,j,l] (src/jaxfun/galerkin/
+inner.py:445-490, 991-1024; 2-D only, O(n^4) memory) and applies it with
+``einsum("ikjl,kl->ij")`` (src/jaxfun/la/tensormatrix.py:54-56).
+``VarCoefMatrix`` is the same operator applied matrix-free and
+sum-factorised on the GPU in 2-D and 3-D: contract the coefficients to the
+gradient on the quadrature grid, multiply by kappa * w (x) w, contract back.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from .. import _lib
+from ..device import as_device, workspace
+from ..galerkin.tensorproductspace import TensorProductSpace
+from .tpmatrix import TPMatrices, TPMatrix, tpmats_lu_factor
+
+
+def pack_varcoef_ops(ndim: int, B: np.ndarray, D: np.ndarray) -> np.ndarray:
+    """Packed operator set for ``jfg_varcoef_apply_*`` (host, FP64)."""
+    nq, n = B.shape
+    L = _lib.lib()
+    out = np.empty(L.jfg_varcoef_ops_count(ndim, n, nq), dtype=np.float64)
+    Bc = np.ascontiguousarray(B, dtype=np.float64)
+    Dc = np.ascontiguousarray(D, dtype=np.float64)
+    L.jfg_varcoef_pack_ops_host(ndim, n, nq, Bc.ctypes.data, Dc.ctypes.data, out.ctypes.data)
+    return out
+
+
+class VarCoefMatrix:
+    """A(kappa) for (kappa grad u, grad v) on a square tensor-product space.
+
+    ``kappa`` is the coefficient sampled on the quadrature grid, shape
+    ``(*batch, nq, ..., nq)``; ``A @ u`` applies it to coefficient arrays of shape
+    ``(*batch, n, ..., n)`` — the ``TensorMatrix.__matmul__`` call surface.
+    """
+
+    def __init__(self, T: TensorProductSpace, kappa):
+        s0 = T.basespaces[0]
+        if any(s != s0 for s in T.basespaces):
+            raise ValueError("VarCoefMatrix needs the same 1-D space on every axis")
+        self.T = T
+        self.ndim = len(T)
+        self.n = s0.dim
+        self.nq = s0.num_quad_points
+        kappa = as_device(kappa)
+        if tuple(kappa.shape[kappa.ndim - self.ndim :]) != (self.nq,) * self.ndim:
+            raise ValueError("kappa must be sampled on the quadrature grid")
+        self.batch_shape = tuple(kappa.shape[: kappa.ndim - self.ndim])
+        W = as_device(T.weights())
+        self.kw = (kappa * W).contiguous()
+        B = s0.backward_matrix(None, 0)
+        D = s0.backward_matrix(None, 1)
+        self.ops_host = pack_varcoef_ops(self.ndim, B, D)
+        self.ops = as_device(self.ops_host)
+        self.kappa_mean = kappa.reshape(kappa.shape[: kappa.ndim - self.ndim] + (-1,)).mean(-1)
+
+    @property
+    def batch(self) -> int:
+        return int(np.prod(self.batch_shape)) if self.batch_shape else 1
+
+    def __matmul__(self, u) -> torch.Tensor:
+        u = as_device(u)
+        shp = self.batch_shape + (self.n,) * self.ndim
+        if tuple(u.shape) != shp:
+            raise ValueError(f"u shape {tuple(u.shape)} != {shp}")
+        v = torch.empty_like(u)
+        L = _lib.lib()
+        ws = workspace(L.jfg_varcoef_workspace_size(self.ndim, self.n, self.nq, self.batch, 8))
+        st = L.jfg_varcoef_apply_f64(self.ndim, self.n, self.nq, self.batch, self.ops.data_ptr(),
+                                     self.kw.data_ptr(), u.data_ptr(), v.data_ptr(),
+                                     ws.data_ptr(), ws.numel(), _lib.stream_handle())
+        _lib.check(st, "jfg_varcoef_apply_f64")
+        return v
+
+    __call__ = __matmul__
+
+
+def stiffness_mass(T: TensorProductSpace):
+    """(K, M) of the first axis' space: K = (grad-like) stiffness, M = mass."""
+    s = T.basespaces[0]
+    return s.stiffness_matrix(), s.mass_matrix()
+
+
+def poisson_tpmatrices(T: TensorProductSpace, alpha2: float = 0.0) -> TPMatrices:
+    """alpha^2 M (x) M + K (x) M + M (x) K (+ 3-D analogue): the TPMatrices that
+    ``inner(alpha**2*u*v - v*Div(Grad(u)))`` yields (inner.py:520-562, 749-763)."""
+    K, M = stiffness_mass(T)
+    nd = len(T)
+    terms = []
+    if alpha2 != 0.0:
+        terms.append(TPMatrix([M] * nd, alpha2))
+    for ax in range(nd):
+        mats = [M] * nd
+        mats[ax] = K
+        terms.append(TPMatrix(mats, 1.0))
+    return TPMatrices(terms)
+
+
+def fd_preconditioner(T: TensorProductSpace):
+    """Constant-coefficient (kappa = 1) fast-diagonalisation factors."""
+    return tpmats_lu_factor(poisson_tpmatrices(T).tpmats)
+
+
+def pcg(A: VarCoefMatrix, b, M=None, x0=None, tol: float = 1e-10, maxiter: int = 2000,
+        scale=None):
+    """Batched FP64 PCG on the GPU: one C-ABI call (``jfg_pcg_varcoef_f64``).
+
+    Returns (x, iters) with per-problem iteration counts.  Each problem stops
+    when sqrt(r.z / r0.z0) <= tol.  ``M`` are fast-diagonalisation factors
+    (default: the constant-kappa Poisson factors); ``scale`` the per-problem
+    preconditioner constant (default mean kappa; PCG is invariant to it).
+    """
+    if M is None:
+        M = fd_preconditioner(A.T)
+    b = as_device(b)
+    x = torch.zeros_like(b) if x0 is None else as_device(x0).clone()
+    E, W, lam = M.device_factors()
+    sc = A.kappa_mean.reshape(-1) if scale is None else as_device(scale).reshape(-1)
+    sc = sc.contiguous()
+    L = _lib.lib()
+    ws = workspace(L.jfg_pcg_workspace_size(A.ndim, A.n, A.nq, A.batch, 8))
+    iters = (_lib.C.c_int * A.batch)()
+    st = L.jfg_pcg_varcoef_f64(A.ndim, A.n, A.nq, A.batch, A.ops.data_ptr(), A.kw.data_ptr(),
+                               E.data_ptr(), W.data_ptr(), lam.data_ptr(), sc.data_ptr(),
+                               b.data_ptr(), x.data_ptr(), 0 if x0 is None else 1, float(tol),
+                               int(maxiter), iters, ws.data_ptr(), ws.numel(),
+                               _lib.stream_handle())
+    _lib.check(st, "jfg_pcg_varcoef_f64")
+    return x, np.array(iters[:], dtype=np.int64)

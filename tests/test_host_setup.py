@@ -1,0 +1,88 @@
+"""Product host setup (FP64 operators) against the oracle; C-ABI library load (CPU only)."""
+
+import re
+from pathlib import Path
+
+import numpy as np
+import pytest
+
+from jaxfun_gb300.galerkin import DIRICHLET, Chebyshev, FunctionSpace, Legendre
+from jaxfun_gb300.la import fd_eig
+from oracle import spectral as O
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+@pytest.mark.parametrize("N", [5, 16, 64, 257])
+def test_gauss_legendre_matches_oracle(N):
+    from jaxfun_gb300.galerkin import legendre_gauss
+
+    x, w = legendre_gauss(N)
+    xo, wo = O.legendre_gauss(N)
+    assert np.abs(x - xo).max() < 4e-16 and np.abs(w - wo).max() < 1e-15
+
+
+@pytest.mark.parametrize("space,fam", [(Legendre, "legendre"), (Chebyshev, "chebyshev")])
+@pytest.mark.parametrize("bcs", [None, DIRICHLET])
+def test_operators_match_oracle(space, fam, bcs):
+    N = 12
+    V = FunctionSpace(N, space, bcs=bcs)
+    Vo = O.Space1D(fam, N, bcs is not None)
+    c = np.random.default_rng(0).standard_normal(V.dim)
+    assert np.abs(V.backward_matrix() @ c - Vo.backward(c)).max() < 1e-13
+    u = Vo.backward(c)
+    assert np.abs(V.forward_matrix() @ u - Vo.forward(u)).max() < 1e-13
+    assert np.abs(V.scalar_product_matrix() @ u - Vo.scalar_product(u)).max() < 1e-13
+    assert np.abs(V.mass_matrix() - Vo.mass_matrix()).max() < 1e-14
+    if bcs is not None:
+        assert np.abs(V.stiffness_matrix() - Vo.stiffness_matrix()).max() < 1e-9
+
+
+def test_fd_eig_chebyshev_reconstructs():
+    V = FunctionSpace(40, Chebyshev, bcs=DIRICHLET)
+    K, M = V.stiffness_matrix(), V.mass_matrix()
+    lam, W, E = fd_eig(K, M)
+    assert np.all(lam > 0)
+    assert np.abs(E @ M @ W - np.eye(38)).max() < 1e-9
+    assert np.abs(E @ K @ W - np.diag(lam)).max() < 1e-9 * lam.max()
+
+
+def _header_symbols():
+    txt = (ROOT / "include" / "jaxfun_gb300.h").read_text()
+    return sorted(set(re.findall(r"\b(jfg_[a-z0-9_]+)\s*\(", txt)))
+
+
+def test_library_exports_every_header_symbol(lib):
+    syms = _header_symbols()
+    assert len(syms) > 10
+    missing = [s for s in syms if not hasattr(lib, s)]
+    assert not missing, missing
+
+
+def test_host_side_argument_checks(lib):
+    from jaxfun_gb300 import _lib
+
+    assert lib.jfg_version().startswith(b"jaxfun_gb300")
+    assert lib.jfg_status_string(_lib.JFG_ERR_ARG) == b"invalid argument"
+    # NULL descriptor / bad shapes are rejected before any CUDA call
+    assert lib.jfg_contract_f64(None, None, None, None, None) == _lib.JFG_ERR_ARG
+    d = _lib.ContractDesc(batch=1, nseg=1, M=4, P=4, K=0)
+    assert lib.jfg_contract_f64(d, None, None, None, None) == _lib.JFG_ERR_ARG
+    d = _lib.ContractDesc(batch=1, nseg=1, M=4, P=4, K=4, op_ld=2, in_ld=4, out_ld=4)
+    assert lib.jfg_contract_f32(d, None, None, None, None) == _lib.JFG_ERR_ARG
+    rows = _lib.int_array([4, 4])
+    assert lib.jfg_tp_apply_f64(4, rows, rows, 1, None, None, None, None, 0, None) == _lib.JFG_ERR_ARG
+    assert lib.jfg_fd_solve_workspace_size(2, 8, 3, 8) > 0
+
+
+def test_varcoef_pack_layout(lib):
+    from jaxfun_gb300.la import pack_varcoef_ops
+
+    rng = np.random.default_rng(0)
+    B, D = rng.standard_normal((6, 4)), rng.standard_normal((6, 4))
+    p = pack_varcoef_ops(2, B, D)
+    nn = 24
+    assert np.array_equal(p[:nn].reshape(6, 4), B)
+    assert np.array_equal(p[nn:2 * nn].reshape(6, 4), D)
+    assert np.array_equal(p[4 * nn:5 * nn].reshape(4, 6), B.T)
+    assert np.array_equal(p[6 * nn:].reshape(4, 12), np.hstack([D.T, B.T]))
