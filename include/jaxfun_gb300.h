@@ -108,6 +108,12 @@ int jfg_contract_f32(const jfg_contract_desc* d, const float* op, const float* i
  */
 int jfg_contract_tc(const jfg_contract_desc* d, const float* op_hi, const float* op_lo,
                     const float* in, float* out, void* stream);
+/* Split n FP64 values into TF32 hi (round to nearest) and FP32 lo = x - hi
+ * (host arrays), the operator format jfg_contract_tc expects. */
+void jfg_split_tf32_host(size_t n, const double* src, float* hi, float* lo);
+/* Reads and clears the device status word the tensor-core kernels set when a
+ * bounded wait expires (JFG_OK or JFG_ERR_DEVICE_TIMEOUT); synchronous. */
+int jfg_device_status(void);
 
 /* ---- TensorProductSpace transforms -------------------------------------
  * out[b] = (x_ax mats[ax]) in[b]: mats[ax] is rows[ax] x cols[ax] row-major,

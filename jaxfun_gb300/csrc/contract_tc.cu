@@ -1,16 +1,498 @@
-// Placeholder replaced by the tcgen05 kernel.
+// Per-axis contraction on the 5th-generation tensor cores (sm_103a):
+// TMA -> shared memory -> tcgen05.mma (kind::tf32) -> TMEM -> epilogue.
+//
+//   out[b][s][m][p] = alpha * epi( sum_k op[s][m][k] * in[b][s][p][k] ) + beta * out
+//
+// Precision: three-term split TF32.  Each FP32 input x is split exactly into
+// hi = x with its low 13 mantissa bits cleared (a TF32 value) and lo = x - hi;
+// the operator is pre-split the same way on the host.  The tensor cores then
+// accumulate hi*hi + hi*lo + lo*hi in FP32, which gives FP32-level accuracy
+// (about 2^-22 relative per product) at three TF32 MMAs per block.
+//
+// CTA tile: 128 rows of p (the MMA M dimension, one TMEM lane per row) by up
+// to 256 operator rows m (the MMA N dimension, one TMEM column each), K in
+// blocks of 32 FP32 (128 B rows, 128-byte swizzle).  Warp roles:
+//   warp 0     TMA producer (one thread)
+//   warp 1     TMEM allocator and MMA issuer (one thread)
+//   warps 2-5  split the staged input tile into hi/lo, then run the epilogue
+//              (tcgen05.ld 32 lanes x 16 columns per warp quarter)
+// Every mbarrier wait is bounded by a global-timer budget; on expiry the
+// kernel records JFG_ERR_DEVICE_TIMEOUT in a device status word, drains its own
+// TMA copies (bounded), frees its TMEM and returns.
+#include <cuda.h>
+#include <stdio.h>
+#include <string.h>
+
 #include "jfg_internal.cuh"
 
 namespace jfg {
+
+__device__ int g_tc_status = 0;
+
+namespace {
+
+constexpr int TILE_P = 128;
+constexpr int KB = 32;                     // FP32 elements per K block (128 B)
+constexpr int NTHREADS = 192;
+constexpr uint32_t XBYTES = TILE_P * KB * 4;  // 16 KB
+constexpr unsigned long long WAIT_NS = 2000000000ull;  // 2 s budget per wait
+
+struct TcParams {
+  jfg_contract_desc d;
+  int Mtile;       // padded operator rows per CTA (multiple of 16, <= 256)
+  int stages;
+  int tmem_cols;
+  int seg_in_map;  // 1 if the input map has a segment dimension
+  int bat_in_map;  // 1 if the input map has a batch dimension
+  int seg_op_map;  // 1 if the operator maps have a segment dimension
+};
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ unsigned long long gtimer() {
+  unsigned long long t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint64_t* bar, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(smem_u32(bar)), "r"(count));
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint64_t* bar, uint32_t bytes) {
+  asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(smem_u32(bar)),
+               "r"(bytes)
+               : "memory");
+}
+
+__device__ __forceinline__ void mbar_arrive(uint64_t* bar) {
+  asm volatile("mbarrier.arrive.shared::cta.b64 _, [%0];" ::"r"(smem_u32(bar)) : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try(uint64_t* bar, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred P1;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 P1, [%1], %2;\n\t"
+      "selp.b32 %0, 1, 0, P1;\n\t}"
+      : "=r"(ok)
+      : "r"(smem_u32(bar)), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Bounded wait: false (and the status word set) if the budget runs out.
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+  if (mbar_try(bar, parity)) return true;
+  const unsigned long long t0 = gtimer();
+  while (true) {
+    for (int i = 0; i < 256; ++i)
+      if (mbar_try(bar, parity)) return true;
+    if (gtimer() - t0 > WAIT_NS) {
+      atomicExch(&g_tc_status, JFG_ERR_DEVICE_TIMEOUT);
+      return false;
+    }
+  }
+}
+
+__device__ __forceinline__ void tma_load_3d(void* dst, const CUtensorMap* map, uint64_t* bar,
+                                            int c0, int c1, int c2) {
+  asm volatile(
+      "cp.async.bulk.tensor.3d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%3, %4, %5}], [%2];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(smem_u32(bar)), "r"(c0), "r"(c1), "r"(c2)
+      : "memory");
+}
+
+__device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, uint64_t* bar,
+                                            int c0, int c1, int c2, int c3) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.shared::cluster.global.mbarrier::complete_tx::bytes"
+      " [%0], [%1, {%3, %4, %5, %6}], [%2];" ::"r"(smem_u32(dst)),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(smem_u32(bar)), "r"(c0), "r"(c1), "r"(c2),
+      "r"(c3)
+      : "memory");
+}
+
+// Shared-memory matrix descriptor: K-major operand, 128-byte swizzle, 8-row
+// core-matrix groups 1024 B apart.
+__device__ __forceinline__ uint64_t sdesc(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);  // start address
+  d |= (uint64_t)1 << 16;                     // leading byte offset (unused, SW128 K-major)
+  d |= (uint64_t)(1024 >> 4) << 32;           // stride byte offset
+  d |= (uint64_t)1 << 46;                     // descriptor version
+  d |= (uint64_t)2 << 61;                     // SWIZZLE_128B
+  return d;
+}
+
+// Instruction descriptor: kind::tf32, D = F32, A = B = TF32, both K-major.
+__host__ __device__ constexpr uint32_t idesc_tf32(int M, int N) {
+  return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) |
+         ((uint32_t)(M >> 4) << 24);
+}
+
+__device__ __forceinline__ void mma_tf32(uint32_t tmem, uint64_t a, uint64_t b, uint32_t idesc,
+                                         uint32_t accum) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], %1, %2, %3, p;\n\t}" ::"r"(tmem),
+      "l"(a), "l"(b), "r"(idesc), "r"(accum));
+}
+
+__device__ __forceinline__ void mma_commit(uint64_t* bar) {
+  asm volatile(
+      "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
+          smem_u32(bar))
+      : "memory");
+}
+
+__device__ __forceinline__ void tmem_ld16(uint32_t taddr, float* v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 "
+      "{%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]),
+        "=r"(r[7]), "=r"(r[8]), "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]),
+        "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+__device__ __forceinline__ float tf32_hi(float x) {
+  return __uint_as_float(__float_as_uint(x) & 0xFFFFE000u);
+}
+
+template <int EPI>
+__global__ void __launch_bounds__(NTHREADS, 1)
+    k_contract_tc(const __grid_constant__ CUtensorMap tmX, const __grid_constant__ CUtensorMap tmOh,
+                  const __grid_constant__ CUtensorMap tmOl, const __grid_constant__ TcParams prm,
+                  float* __restrict__ out) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  const jfg_contract_desc& d = prm.d;
+  const int Mt = prm.Mtile;
+  const int S = prm.stages;
+  const uint32_t obytes = (uint32_t)Mt * KB * 4;
+  const uint32_t stage_bytes = 2 * XBYTES + 2 * obytes;
+  uint64_t* bars = (uint64_t*)(smem + (size_t)S * stage_bytes);
+  uint64_t* full = bars;
+  uint64_t* conv = bars + S;
+  uint64_t* empty = bars + 2 * S;
+  uint64_t* accum = bars + 3 * S;
+  uint32_t* tmem_slot = (uint32_t*)(bars + 3 * S + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int p0 = blockIdx.x * TILE_P;
+  const int bs = blockIdx.y;
+  const int b = bs / d.nseg;
+  const int s = bs - b * d.nseg;
+  const int m0 = blockIdx.z * 256;
+  const int nkb = (d.K + KB - 1) / KB;
+
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < S; ++i) {
+      mbar_init(&full[i], 1);
+      mbar_init(&conv[i], 4);
+      mbar_init(&empty[i], 1);
+    }
+    mbar_init(accum, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     smem_u32(tmem_slot)),
+                 "r"(prm.tmem_cols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+
+  auto Xh = [&](int st) { return smem + (size_t)st * stage_bytes; };
+  auto Xl = [&](int st) { return smem + (size_t)st * stage_bytes + XBYTES; };
+  auto Oh = [&](int st) { return smem + (size_t)st * stage_bytes + 2 * XBYTES; };
+  auto Ol = [&](int st) { return smem + (size_t)st * stage_bytes + 2 * XBYTES + obytes; };
+
+  if (warp == 0) {
+    if (lane == 0) {
+      const int cs = prm.seg_in_map ? s : 0;
+      const int cb = prm.bat_in_map ? b : 0;
+      const int os = prm.seg_op_map ? s : 0;
+      int issued = 0;
+      for (int kb = 0; kb < nkb; ++kb) {
+        const int st = kb % S;
+        const uint32_t u = (uint32_t)(kb / S);
+        if (kb >= S && !mbar_wait(&empty[st], (u & 1u) ^ 1u)) break;
+        mbar_expect_tx(&full[st], XBYTES + 2 * obytes);
+        tma_load_4d(Xh(st), &tmX, &full[st], kb * KB, p0, cs, cb);
+        tma_load_3d(Oh(st), &tmOh, &full[st], kb * KB, m0, os);
+        tma_load_3d(Ol(st), &tmOl, &full[st], kb * KB, m0, os);
+        issued = kb + 1;
+      }
+      // drain: the most recent use of every stage must have landed before exit
+      for (int kb = (issued > S ? issued - S : 0); kb < issued; ++kb)
+        mbar_wait(&full[kb % S], (uint32_t)(kb / S) & 1u);
+    }
+  } else if (warp == 1) {
+    if (lane == 0) {
+      const uint32_t idesc = idesc_tf32(TILE_P, Mt);
+      bool ok = true;
+      for (int kb = 0; kb < nkb; ++kb) {
+        const int st = kb % S;
+        if (!mbar_wait(&conv[st], (uint32_t)(kb / S) & 1u)) {
+          ok = false;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t xh = smem_u32(Xh(st)), xl = smem_u32(Xl(st));
+        const uint32_t oh = smem_u32(Oh(st)), ol = smem_u32(Ol(st));
+#pragma unroll
+        for (int kk = 0; kk < KB / 8; ++kk) {
+          const uint32_t off = kk * 32;  // 8 TF32 = 32 B per MMA
+          mma_tf32(tmem, sdesc(xh + off), sdesc(oh + off), idesc, (kb | kk) ? 1u : 0u);
+          mma_tf32(tmem, sdesc(xh + off), sdesc(ol + off), idesc, 1u);
+          mma_tf32(tmem, sdesc(xl + off), sdesc(oh + off), idesc, 1u);
+        }
+        mma_commit(&empty[st]);
+      }
+      if (ok) mma_commit(accum);
+    }
+  } else {
+    // ---- split the staged input tile into TF32 hi (in place) and lo
+    const int ct = threadIdx.x - 64;  // 0..127
+    bool ok = true;
+    for (int kb = 0; kb < nkb; ++kb) {
+      const int st = kb % S;
+      if (!mbar_wait(&full[st], (uint32_t)(kb / S) & 1u)) {
+        ok = false;
+        break;
+      }
+      float4* xh = (float4*)Xh(st);
+      float4* xl = (float4*)Xl(st);
+#pragma unroll
+      for (int i = 0; i < (int)(XBYTES / 16 / 128); ++i) {
+        const int idx = ct + i * 128;
+        float4 v = xh[idx];
+        float4 h = make_float4(tf32_hi(v.x), tf32_hi(v.y), tf32_hi(v.z), tf32_hi(v.w));
+        xh[idx] = h;
+        xl[idx] = make_float4(v.x - h.x, v.y - h.y, v.z - h.z, v.w - h.w);
+      }
+      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&conv[st]);
+    }
+    // ---- epilogue: TMEM -> registers -> global
+    if (ok && mbar_wait(accum, 0)) {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const int q = warp & 3;  // TMEM lane quarter this warp may access
+      const int row = 32 * q + lane;
+      const int p = p0 + row;
+      float* outS = out + (long long)b * d.out_batch + (long long)s * d.out_seg;
+      const float alpha = (float)d.alpha, beta = (float)d.beta;
+      float c0 = 0.f, c1 = 1.f, lp = 0.f;
+      if (EPI == JFG_EPI_DIV_EIG) {
+        c0 = d.c0 ? ((const float*)d.c0)[b] : 0.f;
+        c1 = d.c1 ? ((const float*)d.c1)[b] : 1.f;
+        lp = (p < d.P) ? ((const float*)d.lam_p)[p] : 0.f;
+      }
+      const float* fld = nullptr;
+      if (EPI == JFG_EPI_MUL_FIELD)
+        fld = (const float*)d.field + (long long)b * d.field_batch + (long long)s * d.field_seg;
+      for (int c = 0; c < Mt / 16; ++c) {
+        float v[16];
+        tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(c * 16), v);
+        if (p < d.P) {
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            const int m = m0 + c * 16 + j;
+            if (m < d.M) {
+              float r = v[j];
+              if (EPI == JFG_EPI_MUL_FIELD) {
+                r *= fld[(long long)m * d.field_ld + p];
+              } else if (EPI == JFG_EPI_DIV_EIG) {
+                r = r / (c0 + c1 * (((const float*)d.lam_m)[m] + lp));
+              }
+              float* o = outS + (long long)m * d.out_ld + p;
+              r *= alpha;
+              if (beta != 0.f) r += beta * *o;
+              *o = r;
+            }
+          }
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 1) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(prm.tmem_cols)
+                 : "memory");
+  }
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+
+typedef CUresult (*EncodeTiledFn)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*,
+                                  const cuuint64_t*, const cuuint64_t*, const cuuint32_t*,
+                                  const cuuint32_t*, CUtensorMapInterleave, CUtensorMapSwizzle,
+                                  CUtensorMapL2promotion, CUtensorMapFloatOOBfill);
+
+EncodeTiledFn encode_fn() {
+  static EncodeTiledFn fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (EncodeTiledFn)p;
+  }
+  return fn;
+}
+
+int make_map(CUtensorMap* map, const float* base, int rank, const cuuint64_t* dims,
+             const cuuint64_t* strides_bytes, const cuuint32_t* box) {
+  EncodeTiledFn fn = encode_fn();
+  if (!fn) return JFG_ERR_UNSUPPORTED;
+  cuuint32_t estr[5] = {1, 1, 1, 1, 1};
+  CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, (cuuint32_t)rank, (void*)base, dims,
+                  strides_bytes, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                  CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? JFG_OK : JFG_ERR_ARG;
+}
+
+template <int EPI>
+int setup_kernel_attr(size_t smem) {
+  static size_t set = 0;
+  if (set < smem) {
+    JFG_CUDA_TRY(cudaFuncSetAttribute(k_contract_tc<EPI>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
+    set = smem;
+  }
+  return JFG_OK;
+}
+
+}  // namespace
+
 int contract_tc(const jfg_contract_desc& d, const float* op_hi, const float* op_lo,
                 const float* in, float* out, cudaStream_t st) {
-  (void)d; (void)op_hi; (void)op_lo; (void)in; (void)out; (void)st;
-  return JFG_ERR_UNSUPPORTED;
+  JFG_TRY(validate_desc(d));
+  if (!op_hi || !op_lo || !in || !out) return JFG_ERR_ARG;
+  if (d.batch == 0 || d.M == 0 || d.P == 0) return JFG_OK;
+  // TMA: 16-byte aligned bases and strides
+  auto al16 = [](const void* p) { return ((uintptr_t)p & 15u) == 0; };
+  if (!al16(op_hi) || !al16(op_lo) || !al16(in)) return JFG_ERR_ARG;
+  if ((d.op_ld & 3) || (d.in_ld & 3) || (d.op_seg & 3) || (d.in_seg & 3) || (d.in_batch & 3))
+    return JFG_ERR_ARG;
+  const long long gy = (long long)d.batch * d.nseg;
+  if (gy > 65535) return JFG_ERR_ARG;
+
+  const int mchunks = (d.M + 255) / 256;
+  const int Mfull = d.M > 256 ? 256 : d.M;
+  const int Mt = (Mfull + 15) / 16 * 16;
+  int cols = 32;
+  while (cols < Mt) cols <<= 1;
+  const size_t stage = 2 * (size_t)XBYTES + 2 * (size_t)Mt * KB * 4;
+  int stages = (int)((220 * 1024) / stage);
+  if (stages > 4) stages = 4;
+  if (stages < 2) return JFG_ERR_UNSUPPORTED;
+  const size_t smem = 1024 + stages * stage + (3 * stages + 1) * 8 + 16;
+
+  TcParams prm;
+  prm.d = d;
+  prm.Mtile = Mt;
+  prm.stages = stages;
+  prm.tmem_cols = cols;
+  prm.seg_in_map = (d.nseg > 1 && d.in_seg != 0) ? 1 : 0;
+  prm.bat_in_map = (d.batch > 1 && d.in_batch != 0) ? 1 : 0;
+  prm.seg_op_map = (d.nseg > 1 && d.op_seg != 0) ? 1 : 0;
+
+  CUtensorMap mx, moh, mol;
+  {
+    cuuint64_t dims[4] = {(cuuint64_t)d.K, (cuuint64_t)d.P,
+                          (cuuint64_t)(prm.seg_in_map ? d.nseg : 1),
+                          (cuuint64_t)(prm.bat_in_map ? d.batch : 1)};
+    cuuint64_t str[3] = {(cuuint64_t)d.in_ld * 4,
+                         (cuuint64_t)(prm.seg_in_map ? d.in_seg : d.in_ld * d.P) * 4,
+                         (cuuint64_t)(prm.bat_in_map ? d.in_batch : d.in_ld * d.P) * 4};
+    cuuint32_t box[4] = {KB, TILE_P, 1, 1};
+    JFG_TRY(make_map(&mx, in, 4, dims, str, box));
+  }
+  {
+    cuuint64_t dims[3] = {(cuuint64_t)d.K, (cuuint64_t)d.M,
+                          (cuuint64_t)(prm.seg_op_map ? d.nseg : 1)};
+    cuuint64_t str[2] = {(cuuint64_t)d.op_ld * 4,
+                         (cuuint64_t)(prm.seg_op_map ? d.op_seg : d.op_ld * d.M) * 4};
+    cuuint32_t box[3] = {KB, (cuuint32_t)Mt, 1};
+    JFG_TRY(make_map(&moh, op_hi, 3, dims, str, box));
+    JFG_TRY(make_map(&mol, op_lo, 3, dims, str, box));
+  }
+  dim3 grid((d.P + TILE_P - 1) / TILE_P, (unsigned)gy, (unsigned)mchunks);
+  switch (d.epilogue) {
+    case JFG_EPI_NONE:
+      JFG_TRY(setup_kernel_attr<JFG_EPI_NONE>(smem));
+      k_contract_tc<JFG_EPI_NONE><<<grid, NTHREADS, smem, st>>>(mx, moh, mol, prm, out);
+      break;
+    case JFG_EPI_MUL_FIELD:
+      JFG_TRY(setup_kernel_attr<JFG_EPI_MUL_FIELD>(smem));
+      k_contract_tc<JFG_EPI_MUL_FIELD><<<grid, NTHREADS, smem, st>>>(mx, moh, mol, prm, out);
+      break;
+    case JFG_EPI_DIV_EIG:
+      JFG_TRY(setup_kernel_attr<JFG_EPI_DIV_EIG>(smem));
+      k_contract_tc<JFG_EPI_DIV_EIG><<<grid, NTHREADS, smem, st>>>(mx, moh, mol, prm, out);
+      break;
+    default:
+      return JFG_ERR_ARG;
+  }
+  JFG_LAUNCHED();
+  return JFG_OK;
 }
+
+int tc_status_take(int* status) {
+  int zero = 0;
+  JFG_CUDA_TRY(cudaMemcpyFromSymbol(status, g_tc_status, sizeof(int)));
+  JFG_CUDA_TRY(cudaMemcpyToSymbol(g_tc_status, &zero, sizeof(int)));
+  return JFG_OK;
+}
+
 }  // namespace jfg
 
 extern "C" int jfg_contract_tc(const jfg_contract_desc* d, const float* op_hi,
                                const float* op_lo, const float* in, float* out, void* stream) {
   if (!d) return JFG_ERR_ARG;
   return jfg::contract_tc(*d, op_hi, op_lo, in, out, (cudaStream_t)stream);
+}
+
+extern "C" int jfg_device_status(void) {
+  int s = 0;
+  int r = jfg::tc_status_take(&s);
+  return r != JFG_OK ? r : s;
+}
+
+extern "C" void jfg_split_tf32_host(size_t n, const double* src, float* hi, float* lo) {
+  for (size_t i = 0; i < n; ++i) {
+    const float f = (float)src[i];
+    uint32_t u;
+    memcpy(&u, &f, 4);
+    // round-to-nearest onto the TF32 grid (10 explicit mantissa bits)
+    uint32_t r = (u + 0x1000u) & 0xFFFFE000u;
+    float h;
+    memcpy(&h, &r, 4);
+    if (!(h == h) || (h - h != 0.0f)) h = f;  // keep inf/nan as is
+    hi[i] = h;
+    lo[i] = (float)(src[i] - (double)h);
+  }
 }

@@ -1,0 +1,104 @@
+"""Tensor-core (tcgen05, split-TF32) contraction against an FP64 reference of the
+same FP32 inputs.  Tolerance: 2e-6 relative to the output's max magnitude
+(three-term split TF32 with FP32 accumulation)."""
+
+import numpy as np
+import pytest
+import torch
+
+from jaxfun_gb300 import _lib
+
+pytestmark = pytest.mark.gpu
+TC_TOL = 2e-6
+
+
+def split(op64):
+    L = _lib.lib()
+    a = np.ascontiguousarray(op64, dtype=np.float64)
+    hi = np.empty(a.shape, dtype=np.float32)
+    lo = np.empty(a.shape, dtype=np.float32)
+    L.jfg_split_tf32_host(a.size, a.ctypes.data, hi.ctypes.data, lo.ctypes.data)
+    return hi, lo
+
+
+def run_tc(op64, x32, out0=None, epi=0, field=None, lam_m=None, lam_p=None, c0=None, c1=None,
+           alpha=1.0, beta=0.0):
+    L = _lib.lib()
+    S, M, K = op64.shape
+    B, S2, P, K2 = x32.shape
+    assert S2 == S and K2 == K
+    hi, lo = split(op64)
+    dev = lambda a: torch.as_tensor(np.ascontiguousarray(a), device="cuda")  # noqa: E731
+    t_hi, t_lo, t_x = dev(hi), dev(lo), dev(x32)
+    out = dev(out0.astype(np.float32)) if out0 is not None else torch.zeros(
+        B, S, M, P, dtype=torch.float32, device="cuda")
+    d = _lib.ContractDesc(batch=B, nseg=S, M=M, P=P, K=K, op_ld=K, op_seg=M * K, in_ld=K,
+                          in_seg=P * K, in_batch=S * P * K, out_ld=P, out_seg=M * P,
+                          out_batch=S * M * P, epilogue=epi, alpha=alpha, beta=beta)
+    keep = []
+    if epi == 1:
+        f = dev(field.astype(np.float32))
+        keep.append(f)
+        d.field, d.field_ld, d.field_seg, d.field_batch = f.data_ptr(), P, M * P, S * M * P
+    if epi == 2:
+        ts = [dev(a.astype(np.float32)) for a in (lam_m, lam_p, c0, c1)]
+        keep += ts
+        d.lam_m, d.lam_p, d.c0, d.c1 = (t.data_ptr() for t in ts)
+    st = L.jfg_contract_tc(d, t_hi.data_ptr(), t_lo.data_ptr(), t_x.data_ptr(), out.data_ptr(),
+                           _lib.stream_handle())
+    assert st == 0, _lib.status_string(st)
+    torch.cuda.synchronize()
+    assert L.jfg_device_status() == 0
+    return out.cpu().numpy().astype(np.float64)
+
+
+def rel(a, b):
+    return np.abs(a - b).max() / np.abs(b).max()
+
+
+@pytest.mark.parametrize("B,S,M,P,K", [
+    (1, 1, 256, 128, 32),
+    (2, 1, 256, 256, 256),
+    (1, 2, 128, 300, 96),
+    (3, 1, 48, 130, 64),
+    (1, 1, 512, 256, 128),
+    (1, 1, 254, 129, 256),
+    (2, 3, 16, 128, 40),
+])
+def test_tc_matches_fp64(B, S, M, P, K):
+    rng = np.random.default_rng(M + P + K)
+    op = rng.standard_normal((S, M, K))
+    x = rng.standard_normal((B, S, P, K)).astype(np.float32)
+    ref = np.einsum("smk,bspk->bsmp", op, x.astype(np.float64))
+    out = run_tc(op, x)
+    assert rel(out, ref) < TC_TOL
+
+
+def test_tc_epilogues():
+    rng = np.random.default_rng(5)
+    B, S, M, P, K = 2, 2, 64, 256, 64
+    op = rng.standard_normal((S, M, K))
+    x = rng.standard_normal((B, S, P, K)).astype(np.float32)
+    ref = np.einsum("smk,bspk->bsmp", op, x.astype(np.float64))
+    fld = rng.uniform(0.5, 2, (B, S, M, P)).astype(np.float32)
+    out0 = rng.standard_normal((B, S, M, P)).astype(np.float32)
+    out = run_tc(op, x, out0=out0, epi=1, field=fld, alpha=0.5, beta=2.0)
+    want = 0.5 * ref * fld + 2.0 * out0
+    assert rel(out, want) < TC_TOL
+    lam_m, lam_p = rng.uniform(1, 2, M), rng.uniform(1, 2, P)
+    c0, c1 = rng.uniform(0, 1, B), rng.uniform(1, 2, B)
+    out = run_tc(op, x, epi=2, lam_m=lam_m, lam_p=lam_p, c0=c0, c1=c1)
+    den = (c0[:, None, None, None].astype(np.float32).astype(np.float64)
+           + c1[:, None, None, None].astype(np.float32) * (lam_m.astype(np.float32)[None, None, :, None]
+                                                           + lam_p.astype(np.float32)[None, None, None, :]))
+    assert rel(out, ref / den) < TC_TOL
+
+
+def test_tc_rejects_misaligned_strides():
+    L = _lib.lib()
+    x = torch.zeros(1024, dtype=torch.float32, device="cuda")
+    d = _lib.ContractDesc(batch=1, nseg=1, M=16, P=16, K=30, op_ld=30, in_ld=30, in_batch=480,
+                          out_ld=16, out_batch=256, alpha=1.0)
+    st = L.jfg_contract_tc(d, x.data_ptr(), x.data_ptr(), x.data_ptr(), x.data_ptr(),
+                           _lib.stream_handle())
+    assert st == _lib.JFG_ERR_ARG
