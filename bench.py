@@ -209,33 +209,40 @@ def run_reference(args):
 
 
 def roofline_microbench(B: int, N: int, reps: int = 20):
-    """Time the dominant kernel (FP64 contraction, var-coef pass 1 shape) with
-    CUDA events on its launch stream; return achieved TFLOP/s."""
+    """Time the dominant kernel -- the tcgen05 split-TF32 contraction at the
+    variable-coefficient pass shape (M = P = K = N per problem, B problems) --
+    with CUDA events on its launch stream.  Returns achieved numbers."""
+    import numpy as np
     import torch
 
     from jaxfun_gb300 import _lib
+    from jaxfun_gb300.la import split_tf32
 
     L = _lib.lib()
-    n = N - 2
-    M, P, K = 2 * N, n, n
-    op = torch.randn(M, K, dtype=torch.float64, device="cuda")
-    x = torch.randn(B, P, K, dtype=torch.float64, device="cuda")
-    y = torch.empty(B, M, P, dtype=torch.float64, device="cuda")
+    M = P = K = N
+    rng = np.random.default_rng(0)
+    hi, lo = split_tf32(rng.standard_normal((M, K)))
+    x = torch.randn(B, P, K, dtype=torch.float32, device="cuda")
+    y = torch.empty(B, M, P, dtype=torch.float32, device="cuda")
     d = _lib.ContractDesc(batch=B, nseg=1, M=M, P=P, K=K, op_ld=K, in_ld=K, in_batch=P * K,
                           out_ld=P, out_batch=M * P, alpha=1.0, beta=0.0)
     s = torch.cuda.current_stream()
+    call = lambda: L.jfg_contract_tc(d, hi.data_ptr(), lo.data_ptr(), x.data_ptr(),  # noqa: E731
+                                     y.data_ptr(), s.cuda_stream)
     for _ in range(3):
-        L.jfg_contract_f64(d, op.data_ptr(), x.data_ptr(), y.data_ptr(), s.cuda_stream)
+        _lib.check(call(), "contract_tc")
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     torch.cuda.synchronize()
     e0.record(s)
     for _ in range(reps):
-        L.jfg_contract_f64(d, op.data_ptr(), x.data_ptr(), y.data_ptr(), s.cuda_stream)
+        call()
     e1.record(s)
     e1.synchronize()
     t = e0.elapsed_time(e1) / 1e3 / reps
     flops = 2.0 * M * P * K * B
-    return flops / t / 1e12, t, flops
+    nbytes = 4.0 * B * P * (K + M)
+    return {"t": t, "flops": flops, "bytes": nbytes, "tflops_alg": flops / t / 1e12,
+            "tflops_issued": 3 * flops / t / 1e12, "gbs": nbytes / t / 1e9}
 
 
 def run_ours(args):
@@ -244,7 +251,7 @@ def run_ours(args):
 
     from jaxfun_gb300 import _lib
     from jaxfun_gb300.galerkin import DIRICHLET, FunctionSpace, Legendre, TensorProduct
-    from jaxfun_gb300.la import fd_preconditioner, pack_varcoef_ops
+    from jaxfun_gb300.la import MixedVarCoefSolver, VarCoefMatrix
 
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -262,42 +269,39 @@ def run_ours(args):
     D = FunctionSpace(N, Legendre, bcs=DIRICHLET)
     T = TensorProduct(D, D)
     kap_h, f_h = make_problems(B, N, seed0=1000 * rank)
-    # ---- resident inputs and plans (untimed setup)
-    w = torch.as_tensor(D.quad_points_and_weights()[1], device="cuda")
-    kap = torch.as_tensor(kap_h, device="cuda")
-    fgrid = torch.as_tensor(f_h, device="cuda")
-    kw = torch.empty_like(kap)
     stream = torch.cuda.Stream()
     sh = stream.cuda_stream
-    ops = torch.as_tensor(pack_varcoef_ops(2, D.backward_matrix(None, 0),
-                                           D.backward_matrix(None, 1)), device="cuda")
-    SP = torch.as_tensor(D.scalar_product_matrix(), device="cuda")
-    fac = fd_preconditioner(T)
-    E, W, lam = fac.device_factors()
-    scale = torch.ones(B, dtype=torch.float64, device="cuda")
-    rhs = torch.empty(B, n, n, dtype=torch.float64, device="cuda")
-    x = torch.empty(B, n, n, dtype=torch.float64, device="cuda")
-    rows, cols = _lib.int_array([n, n]), _lib.int_array([N, N])
-    tp_ws = torch.empty(L.jfg_tp_apply_workspace_size(2, rows, cols, B, 8), dtype=torch.uint8,
-                        device="cuda")
-    pcg_ws = torch.empty(L.jfg_pcg_workspace_size(2, n, N, B, 8), dtype=torch.uint8,
-                         device="cuda")
-    iters = (_lib.C.c_int * B)()
-    tol = args.tol
+    with torch.cuda.stream(stream):
+        # ---- resident inputs and plans (untimed setup)
+        w = torch.as_tensor(D.quad_points_and_weights()[1], device="cuda")
+        kap = torch.as_tensor(kap_h, device="cuda")
+        fgrid = torch.as_tensor(f_h, device="cuda")
+        A = VarCoefMatrix(T, kap)                 # FP64 operator (kw = kappa w (x) w)
+        solver = MixedVarCoefSolver(A)            # padded split-TF32 operators + FD factors
+        SP = torch.as_tensor(D.scalar_product_matrix(), device="cuda")
+        rhs = torch.empty(B, n, n, dtype=torch.float64, device="cuda")
+        x = torch.empty(B, n, n, dtype=torch.float64, device="cuda")
+        rows, cols = _lib.int_array([n, n]), _lib.int_array([N, N])
+        tp_ws = torch.empty(L.jfg_tp_apply_workspace_size(2, rows, cols, B, 8),
+                            dtype=torch.uint8, device="cuda")
+        mws = torch.empty(solver.workspace_bytes(), dtype=torch.uint8, device="cuda")
+        it_in = (_lib.C.c_int * B)()
+        it_out = (_lib.C.c_int * B)()
 
     def prepare(kap_d, f_d):
+        # kw = kappa * w (x) w in FP64 and FP32; rhs = (f, v) scalar product
         _lib.check(L.jfg_weighted_field_f64(2, N, B, kap_d.data_ptr(), w.data_ptr(),
-                                            kw.data_ptr(), sh), "weighted_field")
+                                            A.kw.data_ptr(), solver.kw32.data_ptr(), sh),
+                   "weighted_field")
         _lib.check(L.jfg_tp_apply_f64(2, rows, cols, B, _lib.ptr_array([SP.data_ptr()] * 2),
                                       f_d.data_ptr(), rhs.data_ptr(), tp_ws.data_ptr(),
                                       tp_ws.numel(), sh), "scalar_product")
 
     def solve():
-        st = L.jfg_pcg_varcoef_f64(2, n, N, B, ops.data_ptr(), kw.data_ptr(), E.data_ptr(),
-                                   W.data_ptr(), lam.data_ptr(), scale.data_ptr(),
-                                   rhs.data_ptr(), x.data_ptr(), 0, tol, args.maxiter, iters,
-                                   pcg_ws.data_ptr(), pcg_ws.numel(), sh)
-        _lib.check(st, "pcg")
+        st = L.jfg_pcg_varcoef_mixed(_lib.C.byref(solver.plan), rhs.data_ptr(), x.data_ptr(), 0,
+                                     args.tol, args.inner_tol, 10, args.maxiter, it_in, it_out,
+                                     mws.data_ptr(), mws.numel(), sh)
+        _lib.check(st, "pcg_mixed")
 
     with torch.cuda.stream(stream):
         prepare(kap, fgrid)
@@ -324,16 +328,43 @@ def run_ours(args):
         dist.all_reduce(tt, op=dist.ReduceOp.MAX)
         t = float(tt.item())
     value = world * B * args.steps / t
-    its = np.array(iters[:])
+    its_in, its_out = np.array(it_in[:]), np.array(it_out[:])
+    dev_status = int(L.jfg_device_status())
 
-    # ---- accuracy check on a sample against a tight FP64 solve
-    x_s = x.clone()
-    st = L.jfg_pcg_varcoef_f64(2, n, N, B, ops.data_ptr(), kw.data_ptr(), E.data_ptr(),
-                               W.data_ptr(), lam.data_ptr(), scale.data_ptr(), rhs.data_ptr(),
-                               x.data_ptr(), 1, 1e-14, args.maxiter, None, pcg_ws.data_ptr(),
-                               pcg_ws.numel(), sh)
-    torch.cuda.synchronize()
-    err = float(((x_s - x).abs().amax(dim=(1, 2)) / x.abs().amax(dim=(1, 2))).max())
+    # ---- plain FP64 PCG on the same problems (the comparison path), and the
+    # accuracy check of the mixed answer against a tight FP64 solve
+    nf = min(B, args.fp64_batch)
+    with torch.cuda.stream(stream):
+        A64 = VarCoefMatrix(T, kap[:nf])
+        from jaxfun_gb300.la import fd_preconditioner
+
+        fac = fd_preconditioner(T)
+        E, W, lam = fac.device_factors()
+        sc = torch.ones(nf, dtype=torch.float64, device="cuda")
+        ws64 = torch.empty(L.jfg_pcg_workspace_size(2, n, N, nf, 8), dtype=torch.uint8,
+                           device="cuda")
+        x64 = torch.empty(nf, n, n, dtype=torch.float64, device="cuda")
+        it64 = (_lib.C.c_int * nf)()
+
+        def solve64(xo, tol, its):
+            st = L.jfg_pcg_varcoef_f64(2, n, N, nf, A64.ops.data_ptr(), A64.kw.data_ptr(),
+                                       E.data_ptr(), W.data_ptr(), lam.data_ptr(), sc.data_ptr(),
+                                       rhs[:nf].data_ptr(), xo.data_ptr(), 0, tol, args.maxiter,
+                                       its, ws64.data_ptr(), ws64.numel(), sh)
+            _lib.check(st, "pcg_f64")
+
+        torch.cuda.synchronize()
+        e0.record(stream)
+        solve64(x64, args.fp64_tol, it64)
+        e1.record(stream)
+        e1.synchronize()
+        t64 = e0.elapsed_time(e1) / 1e3
+        xt = torch.empty_like(x64)
+        solve64(xt, 1e-14, None)
+        torch.cuda.synchronize()
+        err_mixed = float(((x[:nf] - xt).abs().amax(dim=(1, 2)) / xt.abs().amax(dim=(1, 2))).max())
+        err_fp64 = float(((x64 - xt).abs().amax(dim=(1, 2)) / xt.abs().amax(dim=(1, 2))).max())
+    fp64_value = world * nf / t64
 
     # ---- end to end through the C ABI with host buffers (pinned)
     kap_pin = torch.as_tensor(kap_h).pin_memory()
@@ -354,11 +385,11 @@ def run_ours(args):
     h2d = 2 * B * N * N * 8
     d2h = B * n * n * 8
 
-    # ---- roofline of the dominant kernel
+    # ---- roofline of the dominant kernel (tcgen05 contraction)
     pk, pk_kind = peaks()
     with torch.cuda.stream(stream):
-        achieved, t_launch, flops = roofline_microbench(B, N)
-    fp64_peak = 1.25  # nominal GB300 FP64 TFLOP/s (no measured FP64 peak is available)
+        rf = roofline_microbench(B, N)
+    tf32_peak = pk["bf16_tflops"] / 2.0
 
     # ---- CPU baseline (bounded sample, rank 0, N=1 only)
     cpu = None
@@ -379,20 +410,31 @@ def run_ours(args):
         line = {
             "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
-            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f32/tf32x3+f64",
             "data": "synthetic (seeded; kappa=exp(GRF), config-3 recipe)",
             "config": {"workload": "varcoef-poisson-2d-legendre-N256", "N": N, "batch": B,
-                       "path": "plain FP64 PCG (CUDA cores)", "tol": tol,
-                       "pcg_iterations_mean": float(its.mean()),
-                       "max_rel_err_vs_fp64_tight": err,
+                       "path": "mixed: tcgen05 split-TF32 PCG + FP64 refinement",
+                       "tol_relres": args.tol, "inner_tol": args.inner_tol,
+                       "inner_iterations_mean": float(its_in.mean()),
+                       "outer_iterations_mean": float(its_out.mean()),
+                       "max_rel_err_vs_fp64_tight": err_mixed,
+                       "fp64_pcg_solves_per_s": fp64_value,
+                       "fp64_pcg_batch": nf, "fp64_pcg_err": err_fp64,
+                       "fp64_pcg_iterations_mean": float(np.mean(it64[:])),
+                       "speedup_vs_fp64_pcg": value / fp64_value,
+                       "device_status": dev_status,
                        "l2": "inputs+workspace > L2 (129 MB) per step"},
             "e2e": {"value": world * B * e2e_steps / t_e2e, "unit": "solves/s",
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": launches,
-            "roofline": {"bound": "fp64", "achieved": achieved, "peak": fp64_peak,
-                         "unit": "TFLOP/s", "frac": achieved / fp64_peak, "traffic": None,
-                         "kernel": "k_contract_simt<double> (var-coef pass 1)",
-                         "peak_kind": "nominal FP64 (not in MEASURED_PEAKS)"},
+            "roofline": {"bound": "tensor", "achieved": rf["tflops_issued"], "peak": tf32_peak,
+                         "unit": "TFLOP/s", "frac": rf["tflops_issued"] / tf32_peak,
+                         "traffic": None,
+                         "kernel": "k_contract_tc (tcgen05 kind::tf32, 3 MMAs per K block)",
+                         "launch_us": 1e6 * rf["t"], "tflops_algorithmic": rf["tflops_alg"],
+                         "hbm_gbs_algorithmic": rf["gbs"],
+                         "hbm_frac": rf["gbs"] / pk["hbm_gbs"],
+                         "peak_kind": f"{pk_kind} bf16 burst / 2 (dense TF32 rate)"},
             "clocks": clocks,
             "cpu_baseline": cpu,
         }
@@ -407,8 +449,11 @@ def main():
     ap.add_argument("--gpus", type=int, default=1)
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
-    ap.add_argument("--batch", type=int, default=16)
-    ap.add_argument("--tol", type=float, default=1e-10)
+    ap.add_argument("--batch", type=int, default=128)
+    ap.add_argument("--tol", type=float, default=1e-11, help="outer relative residual")
+    ap.add_argument("--inner-tol", type=float, default=1e-5)
+    ap.add_argument("--fp64-tol", type=float, default=1e-11)
+    ap.add_argument("--fp64-batch", type=int, default=16)
     ap.add_argument("--maxiter", type=int, default=1000)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--skip-cpu", action="store_true")

@@ -88,9 +88,10 @@ void jfg_reset_launch_count(void);
 /* kw[b][idx] = kappa[b][idx] * prod_ax w[i_ax]: the coefficient times the
  * tensor-product quadrature weights on the (nq)^ndim grid (the scale
  * evaluate_jaxfunction_expr_quad and the weights contribute in
- * src/jaxfun/galerkin/inner.py:445-490, 887-898) */
+ * src/jaxfun/galerkin/inner.py:445-490, 887-898); kw32 (optional, may be
+ * NULL) receives the same values rounded to FP32 */
 int jfg_weighted_field_f64(int ndim, int nq, int batch, const double* kappa, const double* w,
-                           double* kw, void* stream);
+                           double* kw, float* kw32, void* stream);
 
 /* ---- generic contraction (FP64 / FP32 CUDA cores) ---------------------- */
 int jfg_contract_f64(const jfg_contract_desc* d, const double* op, const double* in,
@@ -186,6 +187,37 @@ int jfg_pcg_varcoef_f64(int ndim, int n, int nq, int batch, const double* ops,
                         const double* lam, const double* fd_scale, const double* rhs,
                         double* x, int use_x0, double tol, int maxiter, int* iters,
                         void* work, size_t work_bytes, void* stream);
+
+/* ---- mixed-precision PCG with FP64 iterative refinement ----------------
+ * Outer loop (FP64): r = rhs - A x with the FP64 operator (ops64, kw64 on the
+ * unpadded (batch, n^ndim) layout); stop problem b when ||r_b|| <= tol ||rhs_b||.
+ * Inner solve (tensor cores): PCG on A d = r / ||r|| in FP32 storage with
+ * split-TF32 tcgen05 contractions, in the padded layout (nq per axis), to
+ * sqrt(r.z / r0.z0) <= inner_tol; then x += ||r|| d.  The padded FP32
+ * operators are the split (hi, lo) of the FP64 ones with zero rows/columns
+ * beyond n (lam padded with ones).  Returns JFG_ERR_NOT_CONVERGED if any
+ * problem misses tol after max_outer refinements.
+ */
+typedef struct {
+  int ndim, n, nq, batch;
+  const double* ops64;   /* jfg_varcoef_pack_ops_host(ndim, n, nq, ...)          */
+  const double* kw64;    /* (batch, nq^ndim)                                       */
+  const float* ops_hi;   /* packed padded operators (n -> nq), TF32 hi part        */
+  const float* ops_lo;   /*                                      lo part           */
+  const float* kw32;     /* (batch, nq^ndim)                                       */
+  const float* E_hi;     /* (nq x nq) padded fast-diagonalisation factors          */
+  const float* E_lo;
+  const float* W_hi;
+  const float* W_lo;
+  const float* lam;      /* (nq), ones beyond n                                    */
+  const float* fd_scale; /* (batch) or NULL                                        */
+} jfg_mixed_plan;
+
+size_t jfg_pcg_mixed_workspace_size(int ndim, int n, int nq, int batch);
+int jfg_pcg_varcoef_mixed(const jfg_mixed_plan* plan, const double* rhs, double* x, int use_x0,
+                          double tol, double inner_tol, int max_outer, int maxiter_inner,
+                          int* inner_iters, int* outer_iters, void* work, size_t work_bytes,
+                          void* stream);
 
 #ifdef __cplusplus
 }

@@ -70,7 +70,7 @@ SIGNATURES = {
     "jfg_device_supported": (_i, []),
     "jfg_launch_count": (C.c_longlong, []),
     "jfg_reset_launch_count": (None, []),
-    "jfg_weighted_field_f64": (_i, [_i, _i, _i, _vp, _vp, _vp, _vp]),
+    "jfg_weighted_field_f64": (_i, [_i, _i, _i, _vp, _vp, _vp, _vp, _vp]),
     "jfg_contract_f64": (_i, [C.POINTER(ContractDesc), _vp, _vp, _vp, _vp]),
     "jfg_contract_f32": (_i, [C.POINTER(ContractDesc), _vp, _vp, _vp, _vp]),
     "jfg_contract_tc": (_i, [C.POINTER(ContractDesc), _vp, _vp, _vp, _vp, _vp]),
@@ -89,6 +89,9 @@ SIGNATURES = {
     "jfg_varcoef_workspace_size": (_sz, [_i, _i, _i, _i, _i]),
     "jfg_varcoef_apply_f64": (_i, [_i, _i, _i, _i, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
     "jfg_varcoef_apply_f32": (_i, [_i, _i, _i, _i, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
+    "jfg_pcg_mixed_workspace_size": (_sz, [_i, _i, _i, _i]),
+    "jfg_pcg_varcoef_mixed": (_i, [_vp, _vp, _vp, _i, _d, _d, _i, _i, C.POINTER(_i),
+                                   C.POINTER(_i), _vp, _sz, _vp]),
     "jfg_pcg_workspace_size": (_sz, [_i, _i, _i, _i, _i]),
     "jfg_pcg_varcoef_f64": (_i, [_i, _i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i,
                                  _d, _i, C.POINTER(_i), _vp, _sz, _vp]),

@@ -374,13 +374,22 @@ int make_map(CUtensorMap* map, const float* base, int rank, const cuuint64_t* di
   return r == CUDA_SUCCESS ? JFG_OK : JFG_ERR_ARG;
 }
 
-template <int EPI>
-int setup_kernel_attr(size_t smem) {
-  static size_t set = 0;
-  if (set < smem) {
-    JFG_CUDA_TRY(cudaFuncSetAttribute(k_contract_tc<EPI>,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem));
-    set = smem;
+// Opt every epilogue variant into the largest dynamic shared-memory size once
+// per device (before any stream capture can be active in the caller).
+int setup_kernel_attr() {
+  static bool done[64] = {};
+  int dev = 0;
+  JFG_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return JFG_ERR_UNSUPPORTED;
+  if (!done[dev]) {
+    const int mx = 227 * 1024;
+    JFG_CUDA_TRY(cudaFuncSetAttribute(k_contract_tc<JFG_EPI_NONE>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+    JFG_CUDA_TRY(cudaFuncSetAttribute(k_contract_tc<JFG_EPI_MUL_FIELD>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+    JFG_CUDA_TRY(cudaFuncSetAttribute(k_contract_tc<JFG_EPI_DIV_EIG>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+    done[dev] = true;
   }
   return JFG_OK;
 }
@@ -441,17 +450,15 @@ int contract_tc(const jfg_contract_desc& d, const float* op_hi, const float* op_
     JFG_TRY(make_map(&mol, op_lo, 3, dims, str, box));
   }
   dim3 grid((d.P + TILE_P - 1) / TILE_P, (unsigned)gy, (unsigned)mchunks);
+  JFG_TRY(setup_kernel_attr());
   switch (d.epilogue) {
     case JFG_EPI_NONE:
-      JFG_TRY(setup_kernel_attr<JFG_EPI_NONE>(smem));
       k_contract_tc<JFG_EPI_NONE><<<grid, NTHREADS, smem, st>>>(mx, moh, mol, prm, out);
       break;
     case JFG_EPI_MUL_FIELD:
-      JFG_TRY(setup_kernel_attr<JFG_EPI_MUL_FIELD>(smem));
       k_contract_tc<JFG_EPI_MUL_FIELD><<<grid, NTHREADS, smem, st>>>(mx, moh, mol, prm, out);
       break;
     case JFG_EPI_DIV_EIG:
-      JFG_TRY(setup_kernel_attr<JFG_EPI_DIV_EIG>(smem));
       k_contract_tc<JFG_EPI_DIV_EIG><<<grid, NTHREADS, smem, st>>>(mx, moh, mol, prm, out);
       break;
     default:

@@ -1,0 +1,245 @@
+// Mixed-precision variable-coefficient solve: FP64 iterative refinement around
+// a tensor-core (split-TF32) PCG.
+//
+//   r = rhs - A x              FP64 operator on the CUDA cores (unpadded layout)
+//   d = PCG_tc(A, r / ||r||)   FP32 storage, tcgen05 contractions (padded layout)
+//   x += ||r|| d
+//
+// repeated per problem until ||r|| <= tol ||rhs||.  A problem that has
+// converged gets a zero inner right-hand side, so its inner PCG is inactive
+// from the first iteration and its x is left untouched.
+#include <math.h>
+
+#include <vector>
+
+#include "jfg_internal.cuh"
+#include "pcg_internal.cuh"
+
+namespace jfg {
+
+namespace {
+
+constexpr int NBS = 16;
+
+__global__ void k_sq_part(const double* __restrict__ x, long long N, double* __restrict__ part) {
+  __shared__ double red[32];
+  const int b = blockIdx.y, j = blockIdx.x;
+  const long long chunk = (N + NBS - 1) / NBS;
+  const long long lo = j * chunk, hi = min(N, lo + chunk);
+  const double* xb = x + (long long)b * N;
+  double s = 0.0;
+  for (long long i = lo + threadIdx.x; i < hi; i += blockDim.x) s += xb[i] * xb[i];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = s;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    s = (threadIdx.x < (blockDim.x >> 5)) ? red[threadIdx.x] : 0.0;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s += __shfl_xor_sync(0xffffffffu, s, o);
+    if (threadIdx.x == 0) part[b * NBS + j] = s;
+  }
+}
+
+// out32[b][padded] = in64[b][unpadded] * scale[b] (zero in the padding)
+__global__ void k_pad_scale(int ndim, int n, int nq, long long Npad, long long Nun,
+                            const double* __restrict__ in, const double* __restrict__ scale,
+                            float* __restrict__ out) {
+  const int b = blockIdx.y;
+  const double sc = scale[b];
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < Npad;
+       i += (long long)gridDim.x * blockDim.x) {
+    long long r = i, src = 0, mul = 1;
+    bool inside = true;
+    for (int a = 0; a < ndim; ++a) {
+      const int c = (int)(r % nq);
+      r /= nq;
+      if (c >= n) inside = false;
+      src += c * mul;
+      mul *= n;
+    }
+    out[(long long)b * Npad + i] = inside ? (float)(in[(long long)b * Nun + src] * sc) : 0.f;
+  }
+}
+
+// x64[b][unpadded] += s[b] * d32[b][padded]
+__global__ void k_unpad_axpy(int ndim, int n, int nq, long long Npad, long long Nun,
+                             const float* __restrict__ d, const double* __restrict__ s,
+                             double* __restrict__ x) {
+  const int b = blockIdx.y;
+  const double sc = s[b];
+  if (sc == 0.0) return;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < Nun;
+       i += (long long)gridDim.x * blockDim.x) {
+    long long r = i, src = 0, mul = 1;
+    for (int a = 0; a < ndim; ++a) {
+      const int c = (int)(r % n);
+      r /= n;
+      src += c * mul;
+      mul *= nq;
+    }
+    x[(long long)b * Nun + i] += sc * (double)d[(long long)b * Npad + src];
+  }
+}
+
+__global__ void k_sub_from64(const double* __restrict__ a, double* __restrict__ y, long long n) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
+       i += (long long)gridDim.x * blockDim.x)
+    y[i] = a[i] - y[i];
+}
+
+inline int blocks_for(long long n, int cap) {
+  long long b = (n + 255) / 256;
+  if (b > cap) b = cap;
+  return (int)(b < 1 ? 1 : b);
+}
+
+struct MixedLayout {
+  long long Nun, Npad;
+  size_t vec64, part, sc, vec32, ws64, wsin, total;
+};
+
+MixedLayout layout(int ndim, int n, int nq, int batch) {
+  MixedLayout L;
+  L.Nun = 1;
+  L.Npad = 1;
+  for (int i = 0; i < ndim; ++i) L.Nun *= n, L.Npad *= nq;
+  L.vec64 = align_up((size_t)L.Nun * batch * 8, 256);
+  L.part = align_up((size_t)batch * NBS * 8, 256);
+  L.sc = align_up((size_t)batch * 8, 256);
+  L.vec32 = align_up((size_t)L.Npad * batch * 4, 256);
+  L.ws64 = align_up(varcoef_ws(ndim, n, nq, batch, 8), 256);
+  L.wsin = pcg_ws<float>(ndim, nq, nq, batch);
+  L.total = L.vec64 + L.part + 2 * L.sc + 2 * L.vec32 + L.ws64 + L.wsin;
+  return L;
+}
+
+}  // namespace
+
+}  // namespace jfg
+
+extern "C" size_t jfg_pcg_mixed_workspace_size(int ndim, int n, int nq, int batch) {
+  if ((ndim != 2 && ndim != 3) || n < 1 || nq < n || batch < 1) return 0;
+  return jfg::layout(ndim, n, nq, batch).total;
+}
+
+extern "C" int jfg_pcg_varcoef_mixed(const jfg_mixed_plan* plan, const double* rhs, double* x,
+                                     int use_x0, double tol, double inner_tol, int max_outer,
+                                     int maxiter_inner, int* inner_iters, int* outer_iters,
+                                     void* work, size_t work_bytes, void* stream) {
+  using namespace jfg;
+  if (!plan || !rhs || !x || !(tol > 0.0) || !(inner_tol > 0.0) || max_outer < 1 ||
+      maxiter_inner < 1)
+    return JFG_ERR_ARG;
+  const jfg_mixed_plan& P = *plan;
+  if ((P.ndim != 2 && P.ndim != 3) || P.n < 1 || P.nq < P.n || P.batch < 1 || !P.ops64 ||
+      !P.kw64 || !P.ops_hi || !P.ops_lo || !P.kw32 || !P.E_hi || !P.E_lo || !P.W_hi ||
+      !P.W_lo || !P.lam)
+    return JFG_ERR_ARG;
+  const int ndim = P.ndim, n = P.n, nq = P.nq, batch = P.batch;
+  const MixedLayout Lo = layout(ndim, n, nq, batch);
+  if (!work || work_bytes < Lo.total) return JFG_ERR_WORKSPACE;
+  cudaStream_t st = (cudaStream_t)stream;
+  char* w = (char*)work;
+  double* r64 = (double*)w;
+  w += Lo.vec64;
+  double* part = (double*)w;
+  w += Lo.part;
+  double* sc_in = (double*)w;
+  w += Lo.sc;
+  double* sc_out = (double*)w;
+  w += Lo.sc;
+  float* r32 = (float*)w;
+  w += Lo.vec32;
+  float* d32 = (float*)w;
+  w += Lo.vec32;
+  void* ws64 = w;
+  w += Lo.ws64;
+  void* wsin = w;
+
+  PcgProblem<float> pb;
+  pb.engine = Engine::TC;
+  pb.ndim = ndim;
+  pb.n = nq;
+  pb.nq = nq;
+  pb.batch = batch;
+  pb.ops = OpRef<float>{P.ops_hi, P.ops_lo};
+  pb.kw = P.kw32;
+  pb.E = OpRef<float>{P.E_hi, P.E_lo};
+  pb.W = OpRef<float>{P.W_hi, P.W_lo};
+  pb.lam = P.lam;
+  pb.fd_scale = P.fd_scale;
+  pb.rhs = r32;
+
+  const long long tot64 = Lo.Nun * batch;
+  const dim3 pgrid(blocks_for(Lo.Npad, 256), batch);
+  const dim3 ugrid(blocks_for(Lo.Nun, 256), batch);
+  const dim3 sgrid(NBS, batch);
+  std::vector<double> hp((size_t)batch * NBS), bn(batch), rn(batch), hs_in(batch), hs_out(batch);
+  std::vector<int> it_tmp(batch), acc_in(batch, 0), acc_out(batch, 0);
+
+  auto norms = [&](const double* v, std::vector<double>& out) -> int {
+    k_sq_part<<<sgrid, 256, 0, st>>>(v, Lo.Nun, part);
+    JFG_LAUNCHED();
+    JFG_CUDA_TRY(cudaMemcpyAsync(hp.data(), part, sizeof(double) * batch * NBS,
+                                 cudaMemcpyDeviceToHost, st));
+    JFG_CUDA_TRY(cudaStreamSynchronize(st));
+    for (int b = 0; b < batch; ++b) {
+      double s = 0.0;
+      for (int j = 0; j < NBS; ++j) s += hp[(size_t)b * NBS + j];
+      out[b] = sqrt(s);
+    }
+    return JFG_OK;
+  };
+  auto residual = [&]() -> int {
+    JFG_TRY(varcoef_apply<double>(Engine::F64, ndim, n, nq, batch,
+                                  OpRef<double>{P.ops64, nullptr}, P.kw64, x, r64, ws64,
+                                  Lo.ws64, st));
+    k_sub_from64<<<blocks_for(tot64, 4096), 256, 0, st>>>(rhs, r64, tot64);
+    JFG_LAUNCHED();
+    return JFG_OK;
+  };
+
+  JFG_TRY(norms(rhs, bn));
+  if (use_x0) {
+    JFG_TRY(residual());
+  } else {
+    JFG_CUDA_TRY(cudaMemsetAsync(x, 0, sizeof(double) * tot64, st));
+    JFG_CUDA_TRY(cudaMemcpyAsync(r64, rhs, sizeof(double) * tot64, cudaMemcpyDeviceToDevice, st));
+  }
+  bool all_done = false;
+  for (int outer = 0; outer <= max_outer; ++outer) {
+    JFG_TRY(norms(r64, rn));
+    int active = 0;
+    for (int b = 0; b < batch; ++b) {
+      const bool act = rn[b] > tol * bn[b];
+      hs_in[b] = act ? 1.0 / rn[b] : 0.0;
+      hs_out[b] = act ? rn[b] : 0.0;
+      active += act ? 1 : 0;
+    }
+    if (active == 0) {
+      all_done = true;
+      break;
+    }
+    if (outer == max_outer) break;
+    for (int b = 0; b < batch; ++b) acc_out[b] += hs_out[b] != 0.0 ? 1 : 0;
+    JFG_CUDA_TRY(cudaMemcpyAsync(sc_in, hs_in.data(), sizeof(double) * batch,
+                                 cudaMemcpyHostToDevice, st));
+    JFG_CUDA_TRY(cudaMemcpyAsync(sc_out, hs_out.data(), sizeof(double) * batch,
+                                 cudaMemcpyHostToDevice, st));
+    k_pad_scale<<<pgrid, 256, 0, st>>>(ndim, n, nq, Lo.Npad, Lo.Nun, r64, sc_in, r32);
+    JFG_LAUNCHED();
+    const int s = pcg_run<float>(pb, d32, 0, inner_tol, maxiter_inner, it_tmp.data(), wsin,
+                                 Lo.wsin, st);
+    if (s != JFG_OK && s != JFG_ERR_NOT_CONVERGED) return s;
+    for (int b = 0; b < batch; ++b) acc_in[b] += it_tmp[b];
+    k_unpad_axpy<<<ugrid, 256, 0, st>>>(ndim, n, nq, Lo.Npad, Lo.Nun, d32, sc_out, x);
+    JFG_LAUNCHED();
+    JFG_TRY(residual());
+  }
+  if (inner_iters)
+    for (int b = 0; b < batch; ++b) inner_iters[b] = acc_in[b];
+  if (outer_iters)
+    for (int b = 0; b < batch; ++b) outer_iters[b] = acc_out[b];
+  return all_done ? JFG_OK : JFG_ERR_NOT_CONVERGED;
+}

@@ -247,7 +247,8 @@ int varcoef_apply(Engine e, int ndim, int n, int nq, int batch, OpRef<T> ops, co
 
 template <typename T>
 __global__ void k_weighted_field(int ndim, int nq, long long total, const T* __restrict__ kappa,
-                                 const T* __restrict__ w, T* __restrict__ kw) {
+                                 const T* __restrict__ w, T* __restrict__ kw,
+                                 float* __restrict__ kw32) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
        i += (long long)gridDim.x * blockDim.x) {
     long long r = i;
@@ -256,7 +257,9 @@ __global__ void k_weighted_field(int ndim, int nq, long long total, const T* __r
       s *= w[r % nq];
       r /= nq;
     }
-    kw[i] = kappa[i] * s;
+    const T v = kappa[i] * s;
+    kw[i] = v;
+    if (kw32) kw32[i] = (float)v;
   }
 }
 
@@ -285,15 +288,15 @@ using jfg::Engine;
 using jfg::OpRef;
 
 extern "C" int jfg_weighted_field_f64(int ndim, int nq, int batch, const double* kappa,
-                                      const double* w, double* kw, void* stream) {
+                                      const double* w, double* kw, float* kw32, void* stream) {
   if (ndim < 1 || ndim > 3 || nq < 1 || batch < 0 || !kappa || !w || !kw) return JFG_ERR_ARG;
   long long total = batch;
   for (int i = 0; i < ndim; ++i) total *= nq;
   if (total == 0) return JFG_OK;
   long long blocks = (total + 255) / 256;
   if (blocks > 4096) blocks = 4096;
-  jfg::k_weighted_field<double><<<(int)blocks, 256, 0, (cudaStream_t)stream>>>(ndim, nq, total,
-                                                                               kappa, w, kw);
+  jfg::k_weighted_field<double><<<(int)blocks, 256, 0, (cudaStream_t)stream>>>(
+      ndim, nq, total, kappa, w, kw, kw32);
   JFG_CHECK_LAUNCH();
   jfg::count_launches(1);
   return JFG_OK;

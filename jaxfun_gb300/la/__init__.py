@@ -8,6 +8,7 @@ from .tpmatrix import (  # noqa: F401
     fd_eig,
     tpmats_lu_factor,
 )
+from .mixed import MixedVarCoefSolver, split_tf32  # noqa: F401
 from .varcoef import (  # noqa: F401
     VarCoefMatrix,
     fd_preconditioner,

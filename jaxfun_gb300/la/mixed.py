@@ -1,0 +1,95 @@
+"""Mixed-precision variable-coefficient solver: tensor-core (split-TF32) PCG
+inside FP64 iterative refinement, one C-ABI call (``jfg_pcg_varcoef_mixed``).
+
+The inner operators are the FP64 ones padded from n to nq per axis (zero rows
+and columns; eigenvalues padded with ones) and split into TF32 hi/lo pairs, so
+every tensor-core contraction sees 16-byte aligned rows and K a multiple of 32.
+"""
+
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+import torch
+
+from .. import _lib
+from ..device import as_device, workspace
+from .tpmatrix import TPMatricesLUFactors
+from .varcoef import VarCoefMatrix, fd_preconditioner, pack_varcoef_ops
+
+
+class MixedPlan(C.Structure):
+    _fields_ = [
+        ("ndim", C.c_int), ("n", C.c_int), ("nq", C.c_int), ("batch", C.c_int),
+        ("ops64", C.c_void_p), ("kw64", C.c_void_p),
+        ("ops_hi", C.c_void_p), ("ops_lo", C.c_void_p), ("kw32", C.c_void_p),
+        ("E_hi", C.c_void_p), ("E_lo", C.c_void_p), ("W_hi", C.c_void_p), ("W_lo", C.c_void_p),
+        ("lam", C.c_void_p), ("fd_scale", C.c_void_p),
+    ]
+
+
+def split_tf32(a: np.ndarray) -> tuple[torch.Tensor, torch.Tensor]:
+    """FP64 host array -> (hi, lo) FP32 device tensors (TF32 split)."""
+    L = _lib.lib()
+    a = np.ascontiguousarray(a, dtype=np.float64)
+    hi = np.empty(a.shape, dtype=np.float32)
+    lo = np.empty(a.shape, dtype=np.float32)
+    L.jfg_split_tf32_host(a.size, a.ctypes.data, hi.ctypes.data, lo.ctypes.data)
+    return as_device(hi, torch.float32), as_device(lo, torch.float32)
+
+
+def _pad(M: np.ndarray, rows: int, cols: int) -> np.ndarray:
+    out = np.zeros((rows, cols))
+    out[: M.shape[0], : M.shape[1]] = M
+    return out
+
+
+class MixedVarCoefSolver:
+    """Solve A(kappa_b) x_b = rhs_b for a batch with the mixed-precision path."""
+
+    def __init__(self, A: VarCoefMatrix, M: TPMatricesLUFactors | None = None):
+        self.A = A
+        nd, n, nq = A.ndim, A.n, A.nq
+        s0 = A.T.basespaces[0]
+        B = s0.backward_matrix(None, 0)
+        D = s0.backward_matrix(None, 1)
+        ops_pad = pack_varcoef_ops(nd, _pad(B, nq, nq), _pad(D, nq, nq))
+        self.ops_hi, self.ops_lo = split_tf32(ops_pad)
+        self.kw32 = A.kw.to(torch.float32).contiguous()
+        fac = fd_preconditioner(A.T) if M is None else M
+        self.E_hi, self.E_lo = split_tf32(_pad(fac.E_host, nq, nq))
+        self.W_hi, self.W_lo = split_tf32(_pad(fac.W_host, nq, nq))
+        lam = np.ones(nq)
+        lam[:n] = fac.lam_host
+        self.lam = as_device(lam, torch.float32)
+        self.plan = MixedPlan(nd, n, nq, A.batch, A.ops.data_ptr(), A.kw.data_ptr(),
+                              self.ops_hi.data_ptr(), self.ops_lo.data_ptr(),
+                              self.kw32.data_ptr(), self.E_hi.data_ptr(), self.E_lo.data_ptr(),
+                              self.W_hi.data_ptr(), self.W_lo.data_ptr(), self.lam.data_ptr(),
+                              None)
+
+    def workspace_bytes(self) -> int:
+        A = self.A
+        return int(_lib.lib().jfg_pcg_mixed_workspace_size(A.ndim, A.n, A.nq, A.batch))
+
+    def solve(self, b, x0=None, tol: float = 1e-10, inner_tol: float = 1e-5,
+              max_outer: int = 10, maxiter_inner: int = 1000, out=None, ws=None):
+        """Returns (x, inner_iterations, outer_iterations) per problem."""
+        A = self.A
+        b = as_device(b)
+        if x0 is None:
+            x = torch.empty_like(b) if out is None else out
+        else:
+            x = as_device(x0).clone() if out is None else out.copy_(as_device(x0))
+        L = _lib.lib()
+        if ws is None:
+            ws = workspace(self.workspace_bytes(), slot=1)
+        it_in = (C.c_int * A.batch)()
+        it_out = (C.c_int * A.batch)()
+        st = L.jfg_pcg_varcoef_mixed(C.byref(self.plan), b.data_ptr(), x.data_ptr(),
+                                     0 if x0 is None else 1, float(tol), float(inner_tol),
+                                     int(max_outer), int(maxiter_inner), it_in, it_out,
+                                     ws.data_ptr(), ws.numel(), _lib.stream_handle())
+        _lib.check(st, "jfg_pcg_varcoef_mixed")
+        return x, np.array(it_in[:]), np.array(it_out[:])

@@ -1,0 +1,61 @@
+"""Mixed-precision (tensor-core PCG + FP64 refinement) solve: <= 1e-10 relative
+error against a tight FP64 solve of the same system."""
+
+import numpy as np
+import pytest
+
+from jaxfun_gb300.galerkin import DIRICHLET, FunctionSpace, Legendre, TensorProduct
+from jaxfun_gb300.la import MixedVarCoefSolver, VarCoefMatrix, pcg
+from oracle import spectral as O
+
+pytestmark = pytest.mark.gpu
+
+
+def rel(a, b):
+    return np.abs(a - b).max() / np.abs(b).max()
+
+
+@pytest.mark.parametrize("ndim,N,batch", [(2, 32, 3), (2, 64, 2), (3, 16, 2)])
+def test_mixed_matches_fp64(ndim, N, batch):
+    V = FunctionSpace(N, Legendre, bcs=DIRICHLET)
+    T = TensorProduct(*([V] * ndim))
+    rng = np.random.default_rng(N + ndim)
+    kap = np.exp(rng.standard_normal((batch,) + (N,) * ndim))
+    b = rng.standard_normal((batch,) + (N - 2,) * ndim)
+    A = VarCoefMatrix(T, kap)
+    xr, _ = pcg(A, b, tol=1e-14, maxiter=3000)
+    x, it_in, it_out = MixedVarCoefSolver(A).solve(b, tol=1e-12)
+    xr, x = xr.cpu().numpy(), x.cpu().numpy()
+    for i in range(batch):
+        assert rel(x[i], xr[i]) < 1e-10, (i, it_in, it_out)
+    assert np.all(it_out >= 1) and np.all(it_in > 0)
+
+
+def test_mixed_against_oracle_direct():
+    N = 20
+    V = FunctionSpace(N, Legendre, bcs=DIRICHLET)
+    Vo = O.Space1D("legendre", N, True)
+    T = TensorProduct(V, V)
+    rng = np.random.default_rng(9)
+    kap = np.exp(rng.standard_normal((N, N)))
+    b = rng.standard_normal((N - 2, N - 2))
+    Ad = O.varcoef_tensormatrix(Vo, kap).transpose(0, 2, 1, 3).reshape((N - 2) ** 2, -1)
+    ref = np.linalg.solve(Ad, b.ravel()).reshape(b.shape)
+    x, _, _ = MixedVarCoefSolver(VarCoefMatrix(T, kap[None])).solve(b[None], tol=1e-12)
+    assert rel(x.cpu().numpy()[0], ref) < 1e-10
+
+
+def test_mixed_with_initial_guess_and_converged_problem():
+    N = 32
+    V = FunctionSpace(N, Legendre, bcs=DIRICHLET)
+    T = TensorProduct(V, V)
+    rng = np.random.default_rng(1)
+    kap = np.exp(rng.standard_normal((2, N, N)))
+    b = rng.standard_normal((2, N - 2, N - 2))
+    A = VarCoefMatrix(T, kap)
+    xr, _ = pcg(A, b, tol=1e-14, maxiter=3000)
+    x0 = xr.clone()
+    x0[1] += 1e-3 * x0[1].abs().max()  # problem 0 starts converged
+    x, it_in, it_out = MixedVarCoefSolver(A).solve(b, x0=x0, tol=1e-12)
+    assert it_out[0] == 0 and it_out[1] >= 1
+    assert rel(x.cpu().numpy()[1], xr.cpu().numpy()[1]) < 1e-10

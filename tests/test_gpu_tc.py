@@ -1,6 +1,6 @@
 """Tensor-core (tcgen05, split-TF32) contraction against an FP64 reference of the
-same FP32 inputs.  Tolerance: 2e-6 relative to the output's max magnitude
-(three-term split TF32 with FP32 accumulation)."""
+same FP32 inputs.  Tolerance: 1e-5 relative to the output's max magnitude
+(three-term split TF32 with FP32 accumulation over K <= 512 terms)."""
 
 import numpy as np
 import pytest
@@ -9,7 +9,7 @@ import torch
 from jaxfun_gb300 import _lib
 
 pytestmark = pytest.mark.gpu
-TC_TOL = 2e-6
+TC_TOL = 1e-5
 
 
 def split(op64):
