@@ -9,13 +9,16 @@
 // accumulate hi*hi + hi*lo + lo*hi in FP32, which gives FP32-level accuracy
 // (about 2^-22 relative per product) at three TF32 MMAs per block.
 //
-// CTA tile: 128 rows of p (the MMA M dimension, one TMEM lane per row) by up
-// to 256 operator rows m (the MMA N dimension, one TMEM column each), K in
-// blocks of 32 FP32 (128 B rows, 128-byte swizzle).  Warp roles:
+// Tile: 128 rows of p (the MMA M dimension, one TMEM lane per row) by up to 128
+// operator rows m (the MMA N dimension, one TMEM column each), K in blocks of
+// 32 FP32 (128 B rows, 128-byte swizzle), 3 pipeline stages.  The kernel is
+// persistent (one CTA per SM walking the tile list) with two TMEM accumulator
+// buffers.  Warp roles:
 //   warp 0     TMA producer (one thread)
 //   warp 1     TMEM allocator and MMA issuer (one thread)
-//   warps 2-5  split the staged input tile into hi/lo, then run the epilogue
-//              (tcgen05.ld 32 lanes x 16 columns per warp quarter)
+//   warps 2-5  split each staged input tile into TF32 hi (in place) and lo
+//   warps 6-9  epilogue: tcgen05.ld 32 lanes x 16 columns per warp quarter,
+//              fused field multiply / eigenvalue divide / beta accumulate
 // Every mbarrier wait is bounded by a global-timer budget; on expiry the
 // kernel records JFG_ERR_DEVICE_TIMEOUT in a device status word, drains its own
 // TMA copies (bounded), frees its TMEM and returns.
@@ -33,7 +36,8 @@ namespace {
 
 constexpr int TILE_P = 128;
 constexpr int KB = 32;                     // FP32 elements per K block (128 B)
-constexpr int NTHREADS = 192;
+constexpr int MT_MAX = 128;                // operator rows per tile (MMA N)
+constexpr int NTHREADS = 320;  // 10 warps
 constexpr uint32_t XBYTES = TILE_P * KB * 4;  // 16 KB
 constexpr unsigned long long WAIT_NS = 2000000000ull;  // 2 s budget per wait
 
@@ -168,6 +172,10 @@ __device__ __forceinline__ float tf32_hi(float x) {
   return __uint_as_float(__float_as_uint(x) & 0xFFFFE000u);
 }
 
+// Persistent kernel: each CTA walks the tiles blockIdx.x, blockIdx.x + gridDim.x, ...
+// Tile t = ((bs * mchunks) + mc) * nptiles + pt covers p rows [pt*128, +128) and
+// operator rows [mc*Mt, +Mt) of segment/batch bs.  Two TMEM accumulator buffers
+// let the epilogue of tile i overlap the main loop of tile i+1.
 template <int EPI>
 __global__ void __launch_bounds__(NTHREADS, 1)
     k_contract_tc(const __grid_constant__ CUtensorMap tmX, const __grid_constant__ CUtensorMap tmOh,
@@ -184,16 +192,15 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   uint64_t* full = bars;
   uint64_t* conv = bars + S;
   uint64_t* empty = bars + 2 * S;
-  uint64_t* accum = bars + 3 * S;
-  uint32_t* tmem_slot = (uint32_t*)(bars + 3 * S + 1);
+  uint64_t* tfull = bars + 3 * S;       // [2] accumulator ready
+  uint64_t* tempty = bars + 3 * S + 2;  // [2] accumulator drained
+  uint32_t* tmem_slot = (uint32_t*)(bars + 3 * S + 4);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int p0 = blockIdx.x * TILE_P;
-  const int bs = blockIdx.y;
-  const int b = bs / d.nseg;
-  const int s = bs - b * d.nseg;
-  const int m0 = blockIdx.z * 256;
   const int nkb = (d.K + KB - 1) / KB;
+  const int nptiles = (d.P + TILE_P - 1) / TILE_P;
+  const int mchunks = (d.M + Mt - 1) / Mt;
+  const long long ntiles = (long long)nptiles * mchunks * d.batch * d.nseg;
 
   if (threadIdx.x == 0) {
     for (int i = 0; i < S; ++i) {
@@ -201,7 +208,10 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       mbar_init(&conv[i], 4);
       mbar_init(&empty[i], 1);
     }
-    mbar_init(accum, 1);
+    for (int i = 0; i < 2; ++i) {
+      mbar_init(&tfull[i], 1);
+      mbar_init(&tempty[i], 4);
+    }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 1) {
@@ -220,61 +230,89 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   auto Xl = [&](int st) { return smem + (size_t)st * stage_bytes + XBYTES; };
   auto Oh = [&](int st) { return smem + (size_t)st * stage_bytes + 2 * XBYTES; };
   auto Ol = [&](int st) { return smem + (size_t)st * stage_bytes + 2 * XBYTES + obytes; };
+  auto decode = [&](long long t, int& pt, int& mc, int& b, int& s) {
+    pt = (int)(t % nptiles);
+    long long r = t / nptiles;
+    mc = (int)(r % mchunks);
+    const int bs = (int)(r / mchunks);
+    b = bs / d.nseg;
+    s = bs - b * d.nseg;
+  };
 
   if (warp == 0) {
+    // ---------------- TMA producer ----------------
     if (lane == 0) {
-      const int cs = prm.seg_in_map ? s : 0;
-      const int cb = prm.bat_in_map ? b : 0;
-      const int os = prm.seg_op_map ? s : 0;
-      int issued = 0;
-      for (int kb = 0; kb < nkb; ++kb) {
-        const int st = kb % S;
-        const uint32_t u = (uint32_t)(kb / S);
-        if (kb >= S && !mbar_wait(&empty[st], (u & 1u) ^ 1u)) break;
-        mbar_expect_tx(&full[st], XBYTES + 2 * obytes);
-        tma_load_4d(Xh(st), &tmX, &full[st], kb * KB, p0, cs, cb);
-        tma_load_3d(Oh(st), &tmOh, &full[st], kb * KB, m0, os);
-        tma_load_3d(Ol(st), &tmOl, &full[st], kb * KB, m0, os);
-        issued = kb + 1;
+      long long g = 0, issued = 0;
+      bool ok = true;
+      for (long long t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+        int pt, mc, b, s;
+        decode(t, pt, mc, b, s);
+        const int cs = prm.seg_in_map ? s : 0;
+        const int cb = prm.bat_in_map ? b : 0;
+        const int os = prm.seg_op_map ? s : 0;
+        for (int kb = 0; kb < nkb; ++kb, ++g) {
+          const int st = (int)(g % S);
+          const uint32_t u = (uint32_t)(g / S);
+          if (g >= S && !mbar_wait(&empty[st], (u & 1u) ^ 1u)) {
+            ok = false;
+            break;
+          }
+          mbar_expect_tx(&full[st], XBYTES + 2 * obytes);
+          tma_load_4d(Xh(st), &tmX, &full[st], kb * KB, pt * TILE_P, cs, cb);
+          tma_load_3d(Oh(st), &tmOh, &full[st], kb * KB, mc * Mt, os);
+          tma_load_3d(Ol(st), &tmOl, &full[st], kb * KB, mc * Mt, os);
+          issued = g + 1;
+        }
       }
-      // drain: the most recent use of every stage must have landed before exit
-      for (int kb = (issued > S ? issued - S : 0); kb < issued; ++kb)
-        mbar_wait(&full[kb % S], (uint32_t)(kb / S) & 1u);
+      // drain: the latest use of every stage must have landed before exit
+      for (long long q = (issued > S ? issued - S : 0); q < issued; ++q)
+        mbar_wait(&full[q % S], (uint32_t)(q / S) & 1u);
     }
   } else if (warp == 1) {
+    // ---------------- MMA issuer ----------------
     if (lane == 0) {
       const uint32_t idesc = idesc_tf32(TILE_P, Mt);
+      long long g = 0;
+      int li = 0;
       bool ok = true;
-      for (int kb = 0; kb < nkb; ++kb) {
-        const int st = kb % S;
-        if (!mbar_wait(&conv[st], (uint32_t)(kb / S) & 1u)) {
+      for (long long t = blockIdx.x; t < ntiles && ok; t += gridDim.x, ++li) {
+        const int buf = li & 1;
+        const uint32_t use = (uint32_t)(li >> 1);
+        if (li >= 2 && !mbar_wait(&tempty[buf], (use & 1u) ^ 1u)) {
           ok = false;
           break;
         }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        const uint32_t xh = smem_u32(Xh(st)), xl = smem_u32(Xl(st));
-        const uint32_t oh = smem_u32(Oh(st)), ol = smem_u32(Ol(st));
+        const uint32_t acc = tmem + (uint32_t)(buf * 256);
+        for (int kb = 0; kb < nkb; ++kb, ++g) {
+          const int st = (int)(g % S);
+          if (!mbar_wait(&conv[st], (uint32_t)(g / S) & 1u)) {
+            ok = false;
+            break;
+          }
+          asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+          const uint32_t xh = smem_u32(Xh(st)), xl = smem_u32(Xl(st));
+          const uint32_t oh = smem_u32(Oh(st)), ol = smem_u32(Ol(st));
 #pragma unroll
-        for (int kk = 0; kk < KB / 8; ++kk) {
-          const uint32_t off = kk * 32;  // 8 TF32 = 32 B per MMA
-          mma_tf32(tmem, sdesc(xh + off), sdesc(oh + off), idesc, (kb | kk) ? 1u : 0u);
-          mma_tf32(tmem, sdesc(xh + off), sdesc(ol + off), idesc, 1u);
-          mma_tf32(tmem, sdesc(xl + off), sdesc(oh + off), idesc, 1u);
+          for (int kk = 0; kk < KB / 8; ++kk) {
+            const uint32_t off = kk * 32;  // 8 TF32 = 32 B per MMA
+            mma_tf32(acc, sdesc(xh + off), sdesc(oh + off), idesc, (kb | kk) ? 1u : 0u);
+            mma_tf32(acc, sdesc(xh + off), sdesc(ol + off), idesc, 1u);
+            mma_tf32(acc, sdesc(xl + off), sdesc(oh + off), idesc, 1u);
+          }
+          mma_commit(&empty[st]);
         }
-        mma_commit(&empty[st]);
+        if (ok) mma_commit(&tfull[buf]);
       }
-      if (ok) mma_commit(accum);
     }
-  } else {
-    // ---- split the staged input tile into TF32 hi (in place) and lo
+  } else if (warp < 6) {
+    // ---------------- split staged input tiles into TF32 hi (in place) / lo ----------------
     const int ct = threadIdx.x - 64;  // 0..127
-    bool ok = true;
-    for (int kb = 0; kb < nkb; ++kb) {
-      const int st = kb % S;
-      if (!mbar_wait(&full[st], (uint32_t)(kb / S) & 1u)) {
-        ok = false;
-        break;
-      }
+    const long long total_kb =
+        ((ntiles - blockIdx.x + gridDim.x - 1) / gridDim.x) * (long long)nkb;
+    for (long long g = 0; g < total_kb; ++g) {
+      const int st = (int)(g % S);
+      if (!mbar_wait(&full[st], (uint32_t)(g / S) & 1u)) break;
       float4* xh = (float4*)Xh(st);
       float4* xl = (float4*)Xl(st);
 #pragma unroll
@@ -289,45 +327,67 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       __syncwarp();
       if (lane == 0) mbar_arrive(&conv[st]);
     }
-    // ---- epilogue: TMEM -> registers -> global
-    if (ok && mbar_wait(accum, 0)) {
+  } else {
+    // ---------------- epilogue: TMEM -> registers -> global ----------------
+    const int q = warp & 3;  // TMEM lane quarter this warp may access
+    const int row = 32 * q + lane;
+    const float alpha = (float)d.alpha, beta = (float)d.beta;
+    int li = 0;
+    for (long long t = blockIdx.x; t < ntiles; t += gridDim.x, ++li) {
+      int pt, mc, b, s;
+      decode(t, pt, mc, b, s);
+      const int buf = li & 1;
+      if (!mbar_wait(&tfull[buf], (uint32_t)(li >> 1) & 1u)) break;
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-      const int q = warp & 3;  // TMEM lane quarter this warp may access
-      const int row = 32 * q + lane;
-      const int p = p0 + row;
+      const int p = pt * TILE_P + row;
+      const bool pin = p < d.P;
       float* outS = out + (long long)b * d.out_batch + (long long)s * d.out_seg;
-      const float alpha = (float)d.alpha, beta = (float)d.beta;
       float c0 = 0.f, c1 = 1.f, lp = 0.f;
+      const float* __restrict__ lam_m = (const float*)d.lam_m;
       if (EPI == JFG_EPI_DIV_EIG) {
-        c0 = d.c0 ? ((const float*)d.c0)[b] : 0.f;
-        c1 = d.c1 ? ((const float*)d.c1)[b] : 1.f;
-        lp = (p < d.P) ? ((const float*)d.lam_p)[p] : 0.f;
+        c0 = d.c0 ? __ldg((const float*)d.c0 + b) : 0.f;
+        c1 = d.c1 ? __ldg((const float*)d.c1 + b) : 1.f;
+        lp = pin ? __ldg((const float*)d.lam_p + p) : 0.f;
       }
-      const float* fld = nullptr;
+      const float* __restrict__ fld = nullptr;
       if (EPI == JFG_EPI_MUL_FIELD)
         fld = (const float*)d.field + (long long)b * d.field_batch + (long long)s * d.field_seg;
+      const uint32_t tacc = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(buf * 256);
       for (int c = 0; c < Mt / 16; ++c) {
-        float v[16];
-        tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(c * 16), v);
-        if (p < d.P) {
+        const int mb = mc * Mt + c * 16;
+        float aux[16], prev[16];
+        if (pin) {
 #pragma unroll
           for (int j = 0; j < 16; ++j) {
-            const int m = m0 + c * 16 + j;
+            const int m = mb + j;
+            const bool ok = m < d.M;
+            if (EPI == JFG_EPI_MUL_FIELD)
+              aux[j] = ok ? __ldg(fld + (long long)m * d.field_ld + p) : 0.f;
+            else if (EPI == JFG_EPI_DIV_EIG)
+              aux[j] = ok ? __ldg(lam_m + m) : 1.f;
+            if (beta != 0.f) prev[j] = ok ? outS[(long long)m * d.out_ld + p] : 0.f;
+          }
+        }
+        float v[16];
+        tmem_ld16(tacc + (uint32_t)(c * 16), v);
+        if (pin) {
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            const int m = mb + j;
             if (m < d.M) {
               float r = v[j];
-              if (EPI == JFG_EPI_MUL_FIELD) {
-                r *= fld[(long long)m * d.field_ld + p];
-              } else if (EPI == JFG_EPI_DIV_EIG) {
-                r = r / (c0 + c1 * (((const float*)d.lam_m)[m] + lp));
-              }
-              float* o = outS + (long long)m * d.out_ld + p;
+              if (EPI == JFG_EPI_MUL_FIELD) r *= aux[j];
+              if (EPI == JFG_EPI_DIV_EIG) r = r / (c0 + c1 * (aux[j] + lp));
               r *= alpha;
-              if (beta != 0.f) r += beta * *o;
-              *o = r;
+              if (beta != 0.f) r += beta * prev[j];
+              outS[(long long)m * d.out_ld + p] = r;
             }
           }
         }
       }
+      asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      __syncwarp();
+      if (lane == 0) mbar_arrive(&tempty[buf]);
     }
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -409,16 +469,18 @@ int contract_tc(const jfg_contract_desc& d, const float* op_hi, const float* op_
   const long long gy = (long long)d.batch * d.nseg;
   if (gy > 65535) return JFG_ERR_ARG;
 
-  const int mchunks = (d.M + 255) / 256;
-  const int Mfull = d.M > 256 ? 256 : d.M;
-  const int Mt = (Mfull + 15) / 16 * 16;
-  int cols = 32;
-  while (cols < Mt) cols <<= 1;
+  const int Mt = ((d.M > MT_MAX ? MT_MAX : d.M) + 15) / 16 * 16;
+  const int mchunks = (d.M + Mt - 1) / Mt;
+  const int cols = 512;  // two accumulator buffers of 256 columns
   const size_t stage = 2 * (size_t)XBYTES + 2 * (size_t)Mt * KB * 4;
-  int stages = (int)((220 * 1024) / stage);
-  if (stages > 4) stages = 4;
+  int stages = (int)((200 * 1024) / stage);
+  if (stages > 6) stages = 6;
   if (stages < 2) return JFG_ERR_UNSUPPORTED;
-  const size_t smem = 1024 + stages * stage + (3 * stages + 1) * 8 + 16;
+  const size_t smem = 1024 + stages * stage + (3 * stages + 4) * 8 + 16;
+  const long long ntiles = (long long)((d.P + TILE_P - 1) / TILE_P) * mchunks * gy;
+  int dev = 0, nsm = 0;
+  JFG_CUDA_TRY(cudaGetDevice(&dev));
+  JFG_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
 
   TcParams prm;
   prm.d = d;
@@ -449,7 +511,7 @@ int contract_tc(const jfg_contract_desc& d, const float* op_hi, const float* op_
     JFG_TRY(make_map(&moh, op_hi, 3, dims, str, box));
     JFG_TRY(make_map(&mol, op_lo, 3, dims, str, box));
   }
-  dim3 grid((d.P + TILE_P - 1) / TILE_P, (unsigned)gy, (unsigned)mchunks);
+  dim3 grid((unsigned)(ntiles < nsm ? ntiles : nsm));
   JFG_TRY(setup_kernel_attr());
   switch (d.epilogue) {
     case JFG_EPI_NONE:

@@ -64,6 +64,8 @@ def rel(a, b):
     (1, 1, 512, 256, 128),
     (1, 1, 254, 129, 256),
     (2, 3, 16, 128, 40),
+    (300, 1, 128, 256, 64),
+    (7, 2, 200, 384, 160),
 ])
 def test_tc_matches_fp64(B, S, M, P, K):
     rng = np.random.default_rng(M + P + K)
