@@ -150,6 +150,25 @@ int jfg_fd_solve_f32(int ndim, int n, int batch, const float* E, const float* W,
                      const float* lam, const float* c0, const float* c1, const float* rhs,
                      float* out, void* work, size_t work_bytes, void* stream);
 
+/*
+ * jfg_fd_solve_f64 without a workspace argument: for callers that cannot
+ * allocate device memory where they solve (inside CUDA-graph capture, inside
+ * a host runtime that owns all device memory and offers no workspace, in a
+ * loop that must not block on an allocator).  No counterpart in the
+ * reference.  Scratch comes from a fixed 32 MiB device array inside the
+ * library (jfg_fd_solve_noalloc_max_bytes()); every GPU that loads the library
+ * holds it until exit.  A call whose scratch need (jfg_fd_solve_workspace_size)
+ * exceeds it returns JFG_ERR_WORKSPACE and launches nothing.  All calls share
+ * the array: calls whose kernels overlap on the GPU race; calls ordered on one
+ * stream are safe.  The first call on a device resolves the array's device
+ * address (with that device current); make it outside stream capture.
+ * Allocates nothing (no cudaMalloc/cudaFree, no allocating library call).
+ */
+size_t jfg_fd_solve_noalloc_max_bytes(void);
+int jfg_fd_solve_f64_noalloc(int ndim, int n, int batch, const double* E, const double* W,
+                             const double* lam, const double* c0, const double* c1,
+                             const double* rhs, double* out, void* stream);
+
 /* ---- variable-coefficient operator apply -------------------------------
  * v_b = A(kappa_b) u_b for the form (kappa grad u, grad v), sum-factorised:
  * the TensorMatrix jaxfun assembles for kappa*Dot(Grad(u), Grad(v))
