@@ -450,16 +450,28 @@ def main():
     ap.add_argument("--steps", type=int, default=3)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--batch", type=int, default=128)
-    ap.add_argument("--tol", type=float, default=1e-11, help="outer relative residual")
+    # stopping rules calibrated on seeded problems so that each path ends at
+    # <= 1e-10 max relative error against a tight FP64 solve (checked below)
+    ap.add_argument("--tol", type=float, default=3e-11, help="outer relative residual")
     ap.add_argument("--inner-tol", type=float, default=1e-5)
-    ap.add_argument("--fp64-tol", type=float, default=1e-11)
+    ap.add_argument("--fp64-tol", type=float, default=2e-11)
     ap.add_argument("--fp64-batch", type=int, default=16)
     ap.add_argument("--maxiter", type=int, default=1000)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--kernel-only", action="store_true",
+                    help="time only the dominant kernel (tcgen05 contraction, B problems of "
+                         "256^3) and print its numbers; used for ncu captures")
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.kernel_only:
+        import torch
+
+        torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+        print(json.dumps({"kernel": "k_contract_tc", "batch": args.batch,
+                          **roofline_microbench(args.batch, N_GRID, reps=3)}), flush=True)
+        return 0
     return run_ours(args)
 
 

@@ -17,8 +17,9 @@
 //   warp 0     TMA producer (one thread)
 //   warp 1     TMEM allocator and MMA issuer (one thread)
 //   warps 2-5  split each staged input tile into TF32 hi (in place) and lo
-//   warps 6-9  epilogue: tcgen05.ld 32 lanes x 16 columns per warp quarter,
-//              fused field multiply / eigenvalue divide / beta accumulate
+//   warps 6-13 epilogue: two warps per TMEM lane quarter, tcgen05.ld 32 lanes
+//              x 16 columns, fused field multiply / eigenvalue divide / beta
+//              accumulate
 // Every mbarrier wait is bounded by a global-timer budget; on expiry the
 // kernel records JFG_ERR_DEVICE_TIMEOUT in a device status word, drains its own
 // TMA copies (bounded), frees its TMEM and returns.
@@ -37,7 +38,7 @@ namespace {
 constexpr int TILE_P = 128;
 constexpr int KB = 32;                     // FP32 elements per K block (128 B)
 constexpr int MT_MAX = 128;                // operator rows per tile (MMA N)
-constexpr int NTHREADS = 320;  // 10 warps
+constexpr int NTHREADS = 448;  // 14 warps
 constexpr uint32_t XBYTES = TILE_P * KB * 4;  // 16 KB
 constexpr unsigned long long WAIT_NS = 2000000000ull;  // 2 s budget per wait
 
@@ -176,7 +177,7 @@ __device__ __forceinline__ float tf32_hi(float x) {
 // Tile t = ((bs * mchunks) + mc) * nptiles + pt covers p rows [pt*128, +128) and
 // operator rows [mc*Mt, +Mt) of segment/batch bs.  Two TMEM accumulator buffers
 // let the epilogue of tile i overlap the main loop of tile i+1.
-template <int EPI>
+template <int EPI, bool BETA>
 __global__ void __launch_bounds__(NTHREADS, 1)
     k_contract_tc(const __grid_constant__ CUtensorMap tmX, const __grid_constant__ CUtensorMap tmOh,
                   const __grid_constant__ CUtensorMap tmOl, const __grid_constant__ TcParams prm,
@@ -210,7 +211,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     }
     for (int i = 0; i < 2; ++i) {
       mbar_init(&tfull[i], 1);
-      mbar_init(&tempty[i], 4);
+      mbar_init(&tempty[i], 8);
     }
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
@@ -329,7 +330,11 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     }
   } else {
     // ---------------- epilogue: TMEM -> registers -> global ----------------
+    // Eight warps: two per TMEM lane quarter, each taking every other group
+    // of 32 accumulator columns; field / eigenvalue loads of a group are all
+    // issued before its TMEM load so they are in flight together.
     const int q = warp & 3;  // TMEM lane quarter this warp may access
+    const int half = (warp - 6) >> 2;
     const int row = 32 * q + lane;
     const float alpha = (float)d.alpha, beta = (float)d.beta;
     int li = 0;
@@ -353,33 +358,36 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       if (EPI == JFG_EPI_MUL_FIELD)
         fld = (const float*)d.field + (long long)b * d.field_batch + (long long)s * d.field_seg;
       const uint32_t tacc = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(buf * 256);
-      for (int c = 0; c < Mt / 16; ++c) {
+      for (int c = half * 2; c < Mt / 16; c += 4) {
+        // columns [c*16, c*16+32): two 16-column TMEM loads
         const int mb = mc * Mt + c * 16;
-        float aux[16], prev[16];
+        const int nj = (c + 1 < Mt / 16) ? 32 : 16;
+        float aux[32], prev[32];
         if (pin) {
 #pragma unroll
-          for (int j = 0; j < 16; ++j) {
+          for (int j = 0; j < 32; ++j) {
             const int m = mb + j;
-            const bool ok = m < d.M;
+            const bool ok = j < nj && m < d.M;
             if (EPI == JFG_EPI_MUL_FIELD)
               aux[j] = ok ? __ldg(fld + (long long)m * d.field_ld + p) : 0.f;
             else if (EPI == JFG_EPI_DIV_EIG)
               aux[j] = ok ? __ldg(lam_m + m) : 1.f;
-            if (beta != 0.f) prev[j] = ok ? outS[(long long)m * d.out_ld + p] : 0.f;
+            if (BETA) prev[j] = ok ? outS[(long long)m * d.out_ld + p] : 0.f;
           }
         }
-        float v[16];
+        float v[32];
         tmem_ld16(tacc + (uint32_t)(c * 16), v);
+        if (nj == 32) tmem_ld16(tacc + (uint32_t)(c * 16 + 16), v + 16);
         if (pin) {
 #pragma unroll
-          for (int j = 0; j < 16; ++j) {
+          for (int j = 0; j < 32; ++j) {
             const int m = mb + j;
-            if (m < d.M) {
+            if (j < nj && m < d.M) {
               float r = v[j];
               if (EPI == JFG_EPI_MUL_FIELD) r *= aux[j];
-              if (EPI == JFG_EPI_DIV_EIG) r = r / (c0 + c1 * (aux[j] + lp));
+              if (EPI == JFG_EPI_DIV_EIG) r = __fdividef(r, c0 + c1 * (aux[j] + lp));
               r *= alpha;
-              if (beta != 0.f) r += beta * prev[j];
+              if (BETA) r += beta * prev[j];
               outS[(long long)m * d.out_ld + p] = r;
             }
           }
@@ -443,12 +451,16 @@ int setup_kernel_attr() {
   if (dev < 0 || dev >= 64) return JFG_ERR_UNSUPPORTED;
   if (!done[dev]) {
     const int mx = 227 * 1024;
-    JFG_CUDA_TRY(cudaFuncSetAttribute(k_contract_tc<JFG_EPI_NONE>,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
-    JFG_CUDA_TRY(cudaFuncSetAttribute(k_contract_tc<JFG_EPI_MUL_FIELD>,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
-    JFG_CUDA_TRY(cudaFuncSetAttribute(k_contract_tc<JFG_EPI_DIV_EIG>,
-                                      cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+#define JFG_SET_ATTR(E, B)                                                                 \
+  JFG_CUDA_TRY(cudaFuncSetAttribute(k_contract_tc<E, B>,                                   \
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, mx))
+    JFG_SET_ATTR(JFG_EPI_NONE, false);
+    JFG_SET_ATTR(JFG_EPI_NONE, true);
+    JFG_SET_ATTR(JFG_EPI_MUL_FIELD, false);
+    JFG_SET_ATTR(JFG_EPI_MUL_FIELD, true);
+    JFG_SET_ATTR(JFG_EPI_DIV_EIG, false);
+    JFG_SET_ATTR(JFG_EPI_DIV_EIG, true);
+#undef JFG_SET_ATTR
     done[dev] = true;
   }
   return JFG_OK;
@@ -513,19 +525,28 @@ int contract_tc(const jfg_contract_desc& d, const float* op_hi, const float* op_
   }
   dim3 grid((unsigned)(ntiles < nsm ? ntiles : nsm));
   JFG_TRY(setup_kernel_attr());
+  const bool hb = d.beta != 0.0;
+#define JFG_LAUNCH(E)                                                                      \
+  do {                                                                                     \
+    if (hb)                                                                                \
+      k_contract_tc<E, true><<<grid, NTHREADS, smem, st>>>(mx, moh, mol, prm, out);        \
+    else                                                                                   \
+      k_contract_tc<E, false><<<grid, NTHREADS, smem, st>>>(mx, moh, mol, prm, out);       \
+  } while (0)
   switch (d.epilogue) {
     case JFG_EPI_NONE:
-      k_contract_tc<JFG_EPI_NONE><<<grid, NTHREADS, smem, st>>>(mx, moh, mol, prm, out);
+      JFG_LAUNCH(JFG_EPI_NONE);
       break;
     case JFG_EPI_MUL_FIELD:
-      k_contract_tc<JFG_EPI_MUL_FIELD><<<grid, NTHREADS, smem, st>>>(mx, moh, mol, prm, out);
+      JFG_LAUNCH(JFG_EPI_MUL_FIELD);
       break;
     case JFG_EPI_DIV_EIG:
-      k_contract_tc<JFG_EPI_DIV_EIG><<<grid, NTHREADS, smem, st>>>(mx, moh, mol, prm, out);
+      JFG_LAUNCH(JFG_EPI_DIV_EIG);
       break;
     default:
       return JFG_ERR_ARG;
   }
+#undef JFG_LAUNCH
   JFG_LAUNCHED();
   return JFG_OK;
 }
