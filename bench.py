@@ -245,6 +245,57 @@ def roofline_microbench(B: int, N: int, reps: int = 20):
             "tflops_issued": 3 * flops / t / 1e12, "gbs": nbytes / t / 1e9}
 
 
+def run_transforms(args):
+    """Secondary measurement (not the headline): 16 FP64 fields on the 256^3
+    Chebyshev-Gauss grid, forward + backward round trip, FP64 CUDA-core path vs
+    split-TF32 tensor-core path (FP32 storage); errors vs the FP64 path."""
+    import numpy as np
+    import torch
+
+    from jaxfun_gb300.galerkin import Chebyshev, TensorProduct
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    N, F = args.n_transform, args.fields
+    C = Chebyshev(N)
+    T = TensorProduct(C, C, C)
+    rng = np.random.default_rng(0)
+    i = np.arange(N, dtype=np.float64)
+    s = 1.0 / (1.0 + i[:, None, None] + i[None, :, None] + i[None, None, :]) ** 3
+    c = torch.empty((F, N, N, N), dtype=torch.float64, device="cuda")
+    for k in range(F):
+        c[k] = torch.as_tensor(np.random.default_rng(k).standard_normal((N, N, N)) * s)
+    u = T.backward(c)                       # FP64 grid fields (the inputs)
+    u32 = u.float()
+    res = {}
+    for prec, x in (("f64", u), ("tc", u32)):
+        for _ in range(args.warmup):
+            T.backward(T.forward(x, precision=prec), precision=prec)
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record()
+        for _ in range(args.steps):
+            y = T.backward(T.forward(x, precision=prec), precision=prec)
+        e1.record()
+        e1.synchronize()
+        t = e0.elapsed_time(e1) / 1e3 / args.steps
+        eb = 8 if prec == "f64" else 4
+        nbytes = 6 * 2 * F * N**3 * eb          # 6 passes, each reads and writes one field set
+        flops = 6 * 2.0 * N * F * N**3           # useful contraction FLOPs
+        err = float((y.double() - u).abs().max() / u.abs().max())
+        res[prec] = {"ms": 1e3 * t, "gbs": nbytes / t / 1e9, "tflops_alg": flops / t / 1e12,
+                     "max_rel_err_vs_input": err}
+    pk, kind = peaks()
+    t_roof_tc = max(6 * 2.0 * N * F * N**3 / (pk["bf16_tflops"] / 2 * 1e12),
+                    6 * 2 * F * N**3 * 4 / (pk["hbm_gbs"] * 1e9))
+    line = {"workload": f"chebyshev-3d-N{N}-{F}fields-roundtrip", "unit": "ms per round trip",
+            "f64": res["f64"], "tc": res["tc"],
+            "tc_roofline_ms": 1e3 * t_roof_tc,
+            "tc_roofline_frac": 1e3 * t_roof_tc / res["tc"]["ms"],
+            "roofline_note": f"max(useful FLOP / (bf16 {kind} / 2), FP32 bytes / HBM {kind})"}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -462,9 +513,16 @@ def main():
     ap.add_argument("--kernel-only", action="store_true",
                     help="time only the dominant kernel (tcgen05 contraction, B problems of "
                          "256^3) and print its numbers; used for ncu captures")
+    ap.add_argument("--config", default="varcoef2d", choices=["varcoef2d", "transforms"],
+                    help="varcoef2d: the headline; transforms: batched 3-D Chebyshev "
+                         "round trip (secondary report)")
+    ap.add_argument("--n-transform", type=int, default=256)
+    ap.add_argument("--fields", type=int, default=16)
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.config == "transforms":
+        return run_transforms(args)
     if args.kernel_only:
         import torch
 

@@ -133,6 +133,12 @@ int jfg_tp_apply_f64(int ndim, const int* rows, const int* cols, int batch,
 int jfg_tp_apply_f32(int ndim, const int* rows, const int* cols, int batch,
                      const float* const* mats, const float* in, float* out,
                      void* work, size_t work_bytes, void* stream);
+/* Same transforms on the tensor cores (jfg_contract_tc per pass): operators
+ * given as TF32 (hi, lo) splits, FP32 data; rows/cols % 4 == 0 and 16-byte
+ * aligned buffers (the TMA constraints of jfg_contract_tc). */
+int jfg_tp_apply_tc(int ndim, const int* rows, const int* cols, int batch,
+                    const float* const* mats_hi, const float* const* mats_lo, const float* in,
+                    float* out, void* work, size_t work_bytes, void* stream);
 
 /* ---- fast-diagonalisation solve ----------------------------------------
  * TPMatricesLUFactors.solve (src/jaxfun/la/tpmatrix.py:545-587), batched:

@@ -59,6 +59,45 @@ def tp_apply(mats: list[np.ndarray], x, dtype=torch.float64) -> torch.Tensor:
     return out
 
 
+_SPLIT_CACHE: dict[tuple, tuple] = {}
+
+
+def device_op_split(mat: np.ndarray):
+    """Upload (once) the TF32 (hi, lo) split of a host FP64 operator."""
+    key = (id(mat), mat.shape, torch.cuda.current_device())
+    t = _SPLIT_CACHE.get(key)
+    if t is None:
+        from ..la.mixed import split_tf32
+
+        t = split_tf32(mat) + (mat,)
+        _SPLIT_CACHE[key] = t
+    return t[0], t[1]
+
+
+def tp_apply_tc(mats: list[np.ndarray], x) -> torch.Tensor:
+    """Tensor-core (split-TF32, tcgen05) version of ``tp_apply``: FP32 data."""
+    nd = len(mats)
+    x = as_device(x, torch.float32)
+    cols = [m.shape[1] for m in mats]
+    rows = [m.shape[0] for m in mats]
+    if list(x.shape[x.ndim - nd :]) != cols:
+        raise ValueError(f"trailing shape {tuple(x.shape[x.ndim - nd:])} != {tuple(cols)}")
+    lead = x.shape[: x.ndim - nd]
+    batch = int(np.prod(lead)) if lead else 1
+    out = torch.empty(lead + tuple(rows), dtype=torch.float32, device=x.device)
+    if batch == 0:
+        return out
+    L = _lib.lib()
+    r_a, c_a = _lib.int_array(rows), _lib.int_array(cols)
+    ws = workspace(L.jfg_tp_apply_workspace_size(nd, r_a, c_a, batch, 4))
+    ops = [device_op_split(m) for m in mats]
+    st = L.jfg_tp_apply_tc(nd, r_a, c_a, batch, _lib.ptr_array([o[0].data_ptr() for o in ops]),
+                           _lib.ptr_array([o[1].data_ptr() for o in ops]), x.data_ptr(),
+                           out.data_ptr(), ws.data_ptr(), ws.numel(), _lib.stream_handle())
+    _lib.check(st, "jfg_tp_apply_tc")
+    return out
+
+
 def _apply_1d(mat: np.ndarray, x) -> torch.Tensor:
     return tp_apply([mat], x)
 
@@ -113,23 +152,33 @@ class TensorProductSpace:
         return W
 
     # ---- transforms (tensorproductspace.py:330-417) -------------------------
-    def backward(self, c, N: tuple[int | None, ...] | None = None) -> torch.Tensor:
+    # precision: "f64" (FP64 CUDA cores, parity path) or "tc" (FP32 data,
+    # split-TF32 tcgen05 contractions)
+    def _apply(self, mats, x, precision):
+        if precision == "f64":
+            return tp_apply(mats, x)
+        if precision == "tc":
+            return tp_apply_tc(mats, x)
+        raise ValueError(f"unknown precision {precision!r}")
+
+    def backward(self, c, N: tuple[int | None, ...] | None = None,
+                 precision: str = "f64") -> torch.Tensor:
         mats = [
             s.backward_matrix(None if N is None else N[i]) for i, s in enumerate(self.basespaces)
         ]
-        return tp_apply(mats, c)
+        return self._apply(mats, c, precision)
 
-    def forward(self, u) -> torch.Tensor:
+    def forward(self, u, precision: str = "f64") -> torch.Tensor:
         nd = len(self)
         shp = tuple(u.shape[-nd:])
         mats = [s.forward_matrix(shp[i]) for i, s in enumerate(self.basespaces)]
-        return tp_apply(mats, u)
+        return self._apply(mats, u, precision)
 
-    def scalar_product(self, u) -> torch.Tensor:
+    def scalar_product(self, u, precision: str = "f64") -> torch.Tensor:
         nd = len(self)
         shp = tuple(u.shape[-nd:])
         mats = [s.scalar_product_matrix(shp[i]) for i, s in enumerate(self.basespaces)]
-        return tp_apply(mats, u)
+        return self._apply(mats, u, precision)
 
     def backward_derivative(self, c, k: tuple[int, ...]) -> torch.Tensor:
         """d^k u / dx^k on the quadrature grid (per-axis derivative orders)."""
