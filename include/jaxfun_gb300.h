@@ -213,6 +213,64 @@ int jfg_pcg_varcoef_f64(int ndim, int n, int nq, int batch, const double* ops,
                         double* x, int use_x0, double tol, int maxiter, int* iters,
                         void* work, size_t work_bytes, void* stream);
 
+/* ---- BF16 tensor-core GEMM for the spectral neural operator ------------
+ * D[b][m][n] = alpha * sum_k A[b][m][k] * B[b][n][k]   (BF16 in, FP32 accumulate)
+ * then, in this order: + add[b][m][n] (FP32), + bias[n], * gelu'(gg[b][m][n]),
+ * pre = value (FP32), value = gelu(value) if act == 1.  Outputs (each optional):
+ * d32 (FP32 row-major; atomically added when ksplit > 1 or d32_accumulate),
+ * dbf (BF16 row-major), dtbf (BF16 transposed: dtbf[b][n][m]).  A/B are K-major
+ * with row strides lda/ldb (multiples of 8 elements) and batch strides
+ * (0 = shared).  ksplit > 1 splits K across CTAs (d32 only, no add/bias/act).
+ * tcgen05 kind::f16, 128 x N tiles (N <= 256), TMA 128-byte swizzle.  No
+ * counterpart in the reference (the learned initial guess is new).
+ */
+typedef struct {
+  int batch, M, N, K, ksplit;
+  long long lda, a_batch, ldb, b_batch;
+  float alpha;
+  int act; /* 0 none, 1 GELU */
+  const float* add;
+  long long ld_add, add_batch;
+  const float* bias;
+  const float* gg;
+  long long ld_gg, gg_batch;
+  float* d32;
+  long long ld_d32, d32_batch;
+  int d32_accumulate;
+  float* pre;
+  long long ld_pre, pre_batch;
+  void* dbf;
+  long long ld_dbf, dbf_batch;
+  void* dtbf;
+  long long ld_dtbf, dtbf_batch;
+} jfg_gemm_desc;
+
+int jfg_gemm_bf16(const jfg_gemm_desc* d, const void* A, const void* B, void* stream);
+
+/* ---- spectral neural operator helpers (CUDA cores) ---------------------
+ * Mode mixing of a spectral convolution: for every mode q and sample b,
+ *   out[b][co][q] = sum_ci R[q][co][ci] * x[b][q][ci]        (forward, BF16 out)
+ * backward: dx[b][ci][q] = sum_co R[q][co][ci] * dy[b][q][co]  (BF16 out) and
+ *           dR[q][co][ci] = sum_b dy[b][q][co] * x[b][q][ci]    (FP32, overwritten)
+ * x, dy are FP32 [b][q][c]; R FP32 [q][co][ci]. */
+int jfg_sno_modemix_fwd(int batch, int nmodes, int C, const float* R, const float* x,
+                        void* out_bf16, void* stream);
+int jfg_sno_modemix_bwd(int batch, int nmodes, int C, const float* R, const float* x,
+                        const float* dy, void* dx_bf16, float* dR, void* stream);
+/* colsum[n] (+)= sum_r src[r][n] for BF16 src (rows x n); accumulate 0/1 */
+int jfg_colsum_bf16(long long rows, int n, const void* src, float* out, int accumulate,
+                    void* stream);
+/* Adam (decoupled from torch): p -= lr * mhat / (sqrt(vhat) + eps); optional
+ * BF16 copies of p (row-major, and transposed when rows/cols > 0) */
+int jfg_adam_step(long long n, float* p, const float* g, float* m, float* v, float lr,
+                  float beta1, float beta2, float eps, int step, void* p_bf16,
+                  void* pt_bf16, int rows, int cols, void* stream);
+/* loss partials and dpred for 0.5*mean((pred - target)^2):
+ * pred FP32 (rows, ld_pred) column 0; writes dq BF16 (rows x 16, col 0 used) and
+ * its transpose dqt (16 x rows); loss_out[0] (+)= sum of squares (atomic). */
+int jfg_sno_mse(long long rows, const float* pred, long long ld_pred, const float* target,
+                void* dq_bf16, void* dqt_bf16, float* loss_out, void* stream);
+
 /* ---- mixed-precision PCG with FP64 iterative refinement ----------------
  * Outer loop (FP64): r = rhs - A x with the FP64 operator (ops64, kw64 on the
  * unpadded (batch, n^ndim) layout); stop problem b when ||r_b|| <= tol ||rhs_b||.

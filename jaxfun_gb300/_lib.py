@@ -167,3 +167,34 @@ def int_array(vals):
 
 def ptr_array(ptrs):
     return (C.c_void_p * len(ptrs))(*ptrs)
+
+
+class GemmDesc(C.Structure):
+    """Mirror of jfg_gemm_desc (include/jaxfun_gb300.h)."""
+
+    _fields_ = [
+        ("batch", C.c_int), ("M", C.c_int), ("N", C.c_int), ("K", C.c_int), ("ksplit", C.c_int),
+        ("lda", C.c_longlong), ("a_batch", C.c_longlong),
+        ("ldb", C.c_longlong), ("b_batch", C.c_longlong),
+        ("alpha", C.c_float), ("act", C.c_int),
+        ("add", C.c_void_p), ("ld_add", C.c_longlong), ("add_batch", C.c_longlong),
+        ("bias", C.c_void_p),
+        ("gg", C.c_void_p), ("ld_gg", C.c_longlong), ("gg_batch", C.c_longlong),
+        ("d32", C.c_void_p), ("ld_d32", C.c_longlong), ("d32_batch", C.c_longlong),
+        ("d32_accumulate", C.c_int),
+        ("pre", C.c_void_p), ("ld_pre", C.c_longlong), ("pre_batch", C.c_longlong),
+        ("dbf", C.c_void_p), ("ld_dbf", C.c_longlong), ("dbf_batch", C.c_longlong),
+        ("dtbf", C.c_void_p), ("ld_dtbf", C.c_longlong), ("dtbf_batch", C.c_longlong),
+    ]
+
+
+_ll = C.c_longlong
+_f = C.c_float
+SIGNATURES.update({
+    "jfg_gemm_bf16": (_i, [C.POINTER(GemmDesc), _vp, _vp, _vp]),
+    "jfg_sno_modemix_fwd": (_i, [_i, _i, _i, _vp, _vp, _vp, _vp]),
+    "jfg_sno_modemix_bwd": (_i, [_i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "jfg_colsum_bf16": (_i, [_ll, _i, _vp, _vp, _i, _vp]),
+    "jfg_adam_step": (_i, [_ll, _vp, _vp, _vp, _vp, _f, _f, _f, _f, _i, _vp, _vp, _i, _i, _vp]),
+    "jfg_sno_mse": (_i, [_ll, _vp, _ll, _vp, _vp, _vp, _vp, _vp]),
+})

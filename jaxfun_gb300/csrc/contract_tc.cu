@@ -567,9 +567,12 @@ extern "C" int jfg_contract_tc(const jfg_contract_desc* d, const float* op_hi,
 }
 
 extern "C" int jfg_device_status(void) {
-  int s = 0;
+  int s = 0, g = 0;
   int r = jfg::tc_status_take(&s);
-  return r != JFG_OK ? r : s;
+  if (r != JFG_OK) return r;
+  r = jfg::gemm_status_take(&g);
+  if (r != JFG_OK) return r;
+  return s != JFG_OK ? s : g;
 }
 
 extern "C" void jfg_split_tf32_host(size_t n, const double* src, float* hi, float* lo) {

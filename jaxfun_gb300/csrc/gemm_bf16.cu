@@ -1,0 +1,285 @@
+// BF16 tensor-core GEMM with fused epilogues for the spectral neural operator
+// (training and inference).
+//
+//   D[b][m][n] = alpha * sum_k A[b][m][k] B[b][n][k]      (kind::f16, BF16 in, FP32 TMEM)
+//
+// One CTA computes a 128 x N tile (N <= 256): TMA loads 64-wide K blocks of A
+// and B (128-byte swizzle) into a multi-stage ring, one thread issues
+// tcgen05.mma (4 x K=16 per block) into a TMEM accumulator, four epilogue warps
+// read it back with tcgen05.ld (one TMEM lane quarter each; thread = row m) and
+// apply add / bias / GELU-derivative / GELU, writing any of FP32 row-major
+// (optionally atomically, for split-K), BF16 row-major and BF16 transposed.
+#include <cuda_bf16.h>
+#include <math.h>
+
+#include "tc_common.cuh"
+
+namespace jfg {
+
+__device__ int g_gemm_status = 0;
+
+EncodeTiledFn tensor_map_encoder() {
+  static EncodeTiledFn fn = nullptr;
+  if (!fn) {
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault,
+                                         &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = (EncodeTiledFn)p;
+  }
+  return fn;
+}
+
+namespace {
+
+constexpr int TM = 128;
+constexpr int KBE = 64;  // BF16 elements per K block (128 B)
+constexpr int NTH = 192;
+constexpr uint32_t ABYTES = TM * KBE * 2;  // 16 KB
+
+struct GemmParams {
+  jfg_gemm_desc d;
+  int Nt, stages, tmem_cols, kb_per_split, a_bat, b_bat;
+  int a_perm, b_perm;  // 1: tensor map dims ordered (K, batch, rows)
+};
+
+__device__ __forceinline__ float gelu(float x) {
+  return 0.5f * x * (1.0f + erff(x * 0.70710678118654752f));
+}
+__device__ __forceinline__ float gelu_grad(float x) {
+  return 0.5f * (1.0f + erff(x * 0.70710678118654752f)) +
+         x * 0.39894228040143268f * expf(-0.5f * x * x);
+}
+
+__global__ void __launch_bounds__(NTH, 1)
+    k_gemm_bf16(const __grid_constant__ CUtensorMap tmA, const __grid_constant__ CUtensorMap tmB,
+                const __grid_constant__ GemmParams prm) {
+  extern __shared__ uint8_t smem_raw[];
+  uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
+  const jfg_gemm_desc& d = prm.d;
+  const int Nt = prm.Nt, S = prm.stages;
+  const uint32_t bbytes = (uint32_t)Nt * KBE * 2;
+  const uint32_t stage_bytes = ABYTES + bbytes;
+  uint64_t* full = (uint64_t*)(smem + (size_t)S * stage_bytes);
+  uint64_t* empty = full + S;
+  uint64_t* accum = full + 2 * S;
+  uint32_t* tmem_slot = (uint32_t*)(full + 2 * S + 1);
+
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int m0 = blockIdx.x * TM;
+  const int b = blockIdx.y;
+  const int nkb_all = (d.K + KBE - 1) / KBE;
+  const int kb0 = blockIdx.z * prm.kb_per_split;
+  const int kb1 = min(nkb_all, kb0 + prm.kb_per_split);
+  const int nkb = kb1 > kb0 ? kb1 - kb0 : 0;
+
+  if (threadIdx.x == 0) {
+    for (int i = 0; i < S; ++i) {
+      tc::mbar_init(&full[i], 1);
+      tc::mbar_init(&empty[i], 1);
+    }
+    tc::mbar_init(accum, 1);
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 1) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
+                     tc::smem_u32(tmem_slot)),
+                 "r"(prm.tmem_cols)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+  const uint32_t tmem = *tmem_slot;
+
+  if (warp == 0) {
+    if (lane == 0 && nkb > 0) {
+      int issued = 0;
+      for (int i = 0; i < nkb; ++i) {
+        const int st = i % S;
+        const uint32_t u = (uint32_t)(i / S);
+        if (i >= S && !tc::mbar_wait(&empty[st], (u & 1u) ^ 1u, &g_gemm_status)) break;
+        uint8_t* sa = smem + (size_t)st * stage_bytes;
+        tc::mbar_expect_tx(&full[st], stage_bytes);
+        const int ab = prm.a_bat ? b : 0, bb = prm.b_bat ? b : 0;
+        if (prm.a_perm)
+          tc::tma_load_3d(sa, &tmA, &full[st], (kb0 + i) * KBE, ab, m0);
+        else
+          tc::tma_load_3d(sa, &tmA, &full[st], (kb0 + i) * KBE, m0, ab);
+        if (prm.b_perm)
+          tc::tma_load_3d(sa + ABYTES, &tmB, &full[st], (kb0 + i) * KBE, bb, 0);
+        else
+          tc::tma_load_3d(sa + ABYTES, &tmB, &full[st], (kb0 + i) * KBE, 0, bb);
+        issued = i + 1;
+      }
+      for (int i = (issued > S ? issued - S : 0); i < issued; ++i)
+        tc::mbar_wait(&full[i % S], (uint32_t)(i / S) & 1u, &g_gemm_status);
+    }
+  } else if (warp == 1) {
+    if (lane == 0 && nkb > 0) {
+      const uint32_t idesc = tc::idesc_bf16(TM, Nt);
+      bool ok = true;
+      for (int i = 0; i < nkb; ++i) {
+        const int st = i % S;
+        if (!tc::mbar_wait(&full[st], (uint32_t)(i / S) & 1u, &g_gemm_status)) {
+          ok = false;
+          break;
+        }
+        asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+        const uint32_t sa = tc::smem_u32(smem + (size_t)st * stage_bytes);
+        const uint32_t sb = sa + ABYTES;
+#pragma unroll
+        for (int kk = 0; kk < KBE / 16; ++kk) {
+          const uint32_t off = kk * 32;  // 16 BF16 = 32 B per MMA
+          tc::mma_bf16(tmem, tc::sdesc_sw128(sa + off), tc::sdesc_sw128(sb + off), idesc,
+                       (i | kk) ? 1u : 0u);
+        }
+        tc::mma_commit(&empty[st]);
+      }
+      if (ok) tc::mma_commit(accum);
+    }
+  } else if (nkb > 0) {
+    // ---------------- epilogue ----------------
+    const int q = warp & 3;
+    const int m = m0 + 32 * q + lane;
+    if (tc::mbar_wait(accum, 0, &g_gemm_status)) {
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+      const bool mok = m < d.M;
+      const bool split = prm.kb_per_split < nkb_all || d.d32_accumulate;
+      for (int c = 0; c < Nt / 16; ++c) {
+        float v[16];
+        tc::tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(c * 16), v);
+        if (!mok) continue;
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const int n = c * 16 + j;
+          if (n >= d.N) break;
+          float r = d.alpha * v[j];
+          if (!split) {
+            if (d.add) r += d.add[(long long)b * d.add_batch + (long long)m * d.ld_add + n];
+            if (d.bias) r += d.bias[n];
+            if (d.gg)
+              r *= gelu_grad(d.gg[(long long)b * d.gg_batch + (long long)m * d.ld_gg + n]);
+            if (d.pre) d.pre[(long long)b * d.pre_batch + (long long)m * d.ld_pre + n] = r;
+            if (d.act == 1) r = gelu(r);
+            if (d.d32) d.d32[(long long)b * d.d32_batch + (long long)m * d.ld_d32 + n] = r;
+          } else if (d.d32) {
+            atomicAdd(d.d32 + (long long)b * d.d32_batch + (long long)m * d.ld_d32 + n, r);
+          }
+          if (!split) {
+            const __nv_bfloat16 h = __float2bfloat16(r);
+            if (d.dbf)
+              ((__nv_bfloat16*)d.dbf)[(long long)b * d.dbf_batch + (long long)m * d.ld_dbf + n] = h;
+            if (d.dtbf)
+              ((__nv_bfloat16*)d.dtbf)[(long long)b * d.dtbf_batch + (long long)n * d.ld_dtbf + m] = h;
+          }
+        }
+      }
+    }
+  }
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+  __syncthreads();
+  if (warp == 1) {
+    asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
+                 "r"(prm.tmem_cols)
+                 : "memory");
+  }
+}
+
+// 3-D BF16 tensor map over (K, rows, batch); when the batch stride is smaller
+// than the row stride (samples interleaved inside each row) the dimensions are
+// ordered (K, batch, rows) so that strides increase, with a box of one sample.
+int make_map_bf16(CUtensorMap* map, const void* base, cuuint64_t K, cuuint64_t rows,
+                  cuuint64_t nb, cuuint64_t ld, cuuint64_t bstride, cuuint32_t box_rows,
+                  bool perm) {
+  EncodeTiledFn fn = tensor_map_encoder();
+  if (!fn) return JFG_ERR_UNSUPPORTED;
+  cuuint64_t dims[3] = {K, rows, nb};
+  cuuint64_t str[2] = {ld * 2, bstride * 2};
+  cuuint32_t box[3] = {KBE, box_rows, 1};
+  if (perm) {
+    dims[1] = nb;
+    dims[2] = rows;
+    str[0] = bstride * 2;
+    str[1] = ld * 2;
+    box[1] = 1;
+    box[2] = box_rows;
+  }
+  cuuint32_t estr[3] = {1, 1, 1};
+  CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 3, (void*)base, dims, str, box, estr,
+                  CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  return r == CUDA_SUCCESS ? JFG_OK : JFG_ERR_ARG;
+}
+
+}  // namespace
+
+}  // namespace jfg
+
+extern "C" int jfg_gemm_bf16(const jfg_gemm_desc* dp, const void* A, const void* B,
+                             void* stream) {
+  using namespace jfg;
+  if (!dp || !A || !B) return JFG_ERR_ARG;
+  const jfg_gemm_desc& d = *dp;
+  if (d.batch < 0 || d.M < 0 || d.N < 1 || d.N > 256 || d.K < 1 || d.ksplit < 1 ||
+      d.ksplit > 1024)
+    return JFG_ERR_ARG;
+  if (d.batch == 0 || d.M == 0) return JFG_OK;
+  if ((d.lda & 7) || (d.ldb & 7) || (d.a_batch & 7) || (d.b_batch & 7) || d.lda < d.K ||
+      d.ldb < d.K)
+    return JFG_ERR_ARG;
+  if (((uintptr_t)A & 15) || ((uintptr_t)B & 15)) return JFG_ERR_ARG;
+  if (d.ksplit > 1 && (d.add || d.bias || d.gg || d.act || d.pre || d.dbf || d.dtbf || !d.d32))
+    return JFG_ERR_ARG;
+  if (d.batch > 65535) return JFG_ERR_ARG;
+  GemmParams prm;
+  prm.d = d;
+  prm.Nt = (d.N + 15) / 16 * 16;
+  int cols = 32;
+  while (cols < prm.Nt) cols <<= 1;
+  prm.tmem_cols = cols;
+  const size_t stage = ABYTES + (size_t)prm.Nt * KBE * 2;
+  int stages = (int)((200 * 1024) / stage);
+  if (stages > 6) stages = 6;
+  prm.stages = stages;
+  const int nkb = (d.K + KBE - 1) / KBE;
+  prm.kb_per_split = (nkb + d.ksplit - 1) / d.ksplit;
+  prm.a_bat = (d.batch > 1 && d.a_batch != 0) ? 1 : 0;
+  prm.b_bat = (d.batch > 1 && d.b_batch != 0) ? 1 : 0;
+  const int ksplit = (nkb + prm.kb_per_split - 1) / prm.kb_per_split;
+  prm.a_perm = (prm.a_bat && d.a_batch < d.lda) ? 1 : 0;
+  prm.b_perm = (prm.b_bat && d.b_batch < d.ldb) ? 1 : 0;
+  if ((prm.a_perm && d.a_batch < d.K) || (prm.b_perm && d.b_batch < d.K)) return JFG_ERR_ARG;
+  CUtensorMap ma, mb;
+  JFG_TRY(make_map_bf16(&ma, A, d.K, d.M, prm.a_bat ? d.batch : 1, d.lda,
+                        prm.a_bat ? d.a_batch : d.lda * d.M, TM, prm.a_perm != 0));
+  JFG_TRY(make_map_bf16(&mb, B, d.K, d.N, prm.b_bat ? d.batch : 1, d.ldb,
+                        prm.b_bat ? d.b_batch : d.ldb * d.N, (cuuint32_t)prm.Nt,
+                        prm.b_perm != 0));
+  const size_t smem = 1024 + stages * stage + (2 * stages + 1) * 8 + 16;
+  static bool attr_done[64] = {};
+  int dev = 0;
+  JFG_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return JFG_ERR_UNSUPPORTED;
+  if (!attr_done[dev]) {
+    JFG_CUDA_TRY(cudaFuncSetAttribute(k_gemm_bf16, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                                      227 * 1024));
+    attr_done[dev] = true;
+  }
+  dim3 grid((d.M + TM - 1) / TM, d.batch, ksplit);
+  k_gemm_bf16<<<grid, NTH, smem, (cudaStream_t)stream>>>(ma, mb, prm);
+  JFG_LAUNCHED();
+  return JFG_OK;
+}
+
+namespace jfg {
+int gemm_status_take(int* status) {
+  int zero = 0;
+  JFG_CUDA_TRY(cudaMemcpyFromSymbol(status, g_gemm_status, sizeof(int)));
+  JFG_CUDA_TRY(cudaMemcpyToSymbol(g_gemm_status, &zero, sizeof(int)));
+  return JFG_OK;
+}
+}  // namespace jfg

@@ -112,6 +112,9 @@ template <typename T>
 int varcoef_apply(Engine e, int ndim, int n, int nq, int batch, OpRef<T> ops, const T* kw,
                   const T* u, T* v, void* work, size_t work_bytes, cudaStream_t st);
 
+// Read and clear the device status word of the BF16 GEMM kernel.
+int gemm_status_take(int* status);
+
 size_t tp_apply_ws(int ndim, const int* rows, const int* cols, int batch, int eb);
 size_t fd_ws(int ndim, int n, int batch, int eb);
 size_t varcoef_ws(int ndim, int n, int nq, int batch, int eb);

