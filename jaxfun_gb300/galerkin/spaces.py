@@ -186,7 +186,10 @@ class OrthogonalSpace:
         else:
             D2 = np.where(mask, cols * (cols**2 - rows**2) * np.pi / 2, 0.0)
         S = self.S
-        return -(S @ D2 @ S.T)
+        # "+ 0.0" turns the -0.0 entries of the negated product into +0.0, so
+        # the matrix is bit-identical to the closed forms (diag(4k+6) for
+        # Legendre) and LAPACK picks the same eigenvector signs for it
+        return -(S @ D2 @ S.T) + 0.0
 
     # -- dense per-axis operators (FP64, host) -------------------------------
     @functools.lru_cache(maxsize=16)
