@@ -173,6 +173,36 @@ def relative_l2(model: SNO, data: dict) -> float:
     return float(((pred - T).norm(dim=1) / T.norm(dim=1)).mean())
 
 
+def evaluate_gain(model: SNO, maps: GridMaps, nprob: int = 128, seed: int = 3,
+                  tol: float = 3e-11, inner_tol: float = 1e-5) -> dict:
+    """Mixed-precision solves of held-out problems from a zero start and from the
+    learned guess: iterations, time, and error against a tight FP64 solve."""
+    from ..la import pcg
+
+    data = generate(nprob, seed, maps, keep_fine=True, log=lambda *_: None)
+    kap, f, b, _ = data["fine"][0] if len(data["fine"]) == 1 else [
+        torch.cat([c[i] for c in data["fine"]]) for i in range(4)]
+    A = VarCoefMatrix(maps.T, kap)
+    S = MixedVarCoefSolver(A)
+    xt, _ = pcg(A, b, tol=1e-14, maxiter=3000)
+    out = {}
+    for name in ("zero", "learned"):
+        for rep in range(2):  # second repetition is timed
+            torch.cuda.synchronize()
+            t0 = time.perf_counter()
+            x0 = initial_guess(model, maps, data["X"], data["s"]) if name == "learned" else None
+            x, it_in, it_out = S.solve(b, x0=x0, tol=tol, inner_tol=inner_tol)
+            torch.cuda.synchronize()
+            dt = time.perf_counter() - t0
+        err = float(((x - xt).abs().amax(dim=(1, 2)) / xt.abs().amax(dim=(1, 2))).max())
+        out[name] = {"inner_iterations_mean": float(it_in.mean()),
+                     "outer_iterations_mean": float(it_out.mean()), "ms": 1e3 * dt,
+                     "solves_per_s": nprob / dt, "max_rel_err": err}
+    x0 = initial_guess(model, maps, data["X"], data["s"])
+    out["guess_rel_err_mean"] = float(((x0 - xt).norm(dim=(1, 2)) / xt.norm(dim=(1, 2))).mean())
+    return out
+
+
 def save(model: SNO, path: str, meta: dict | None = None):
     sd = model.state_dict()
     arrs = {k: (v.astype(np.float16) if k.startswith("R") else v.astype(np.float32))
@@ -206,11 +236,15 @@ def main():
         tr = generate(args.train, seed=1, maps=maps)
         te = generate(args.test, seed=2, maps=maps)
         model = SNO(SNOConfig(batch=args.batch), seed=0)
+        t0 = time.perf_counter()
         hist = train(model, tr, args.epochs, lr=args.lr)
+        t_train = time.perf_counter() - t0
         err = relative_l2(model, te)
-    print(json.dumps({"train_loss": hist, "test_rel_l2": err}))
-    save(model, args.out, {"train": args.train, "test": args.test, "epochs": args.epochs,
-                           "test_rel_l2": err, "train_loss": hist})
+        gain = evaluate_gain(model, maps)
+    meta = {"train": args.train, "test": args.test, "epochs": args.epochs, "lr": args.lr,
+            "test_rel_l2": err, "train_loss": hist, "train_seconds": t_train, "gain": gain}
+    print(json.dumps(meta))
+    save(model, args.out, meta)
 
 
 if __name__ == "__main__":
