@@ -294,6 +294,8 @@ typedef struct {
   const float* W_lo;
   const float* lam;      /* (nq), ones beyond n                                    */
   const float* fd_scale; /* (batch) or NULL                                        */
+  const float* ops32;    /* packed padded operators rounded to FP32, or NULL: used for
+                            r -= ||r|| A d once ||r|| <= 1e-4 ||rhs|| (else FP64 r = b - A x) */
 } jfg_mixed_plan;
 
 size_t jfg_pcg_mixed_workspace_size(int ndim, int n, int nq, int batch);
@@ -301,6 +303,15 @@ int jfg_pcg_varcoef_mixed(const jfg_mixed_plan* plan, const double* rhs, double*
                           double tol, double inner_tol, int max_outer, int maxiter_inner,
                           int* inner_iters, int* outer_iters, void* work, size_t work_bytes,
                           void* stream);
+/* The same solve with a learned initial guess (batch, n^ndim) FP64 (may be
+ * NULL): the first inner solve starts from guess / ||rhs|| and keeps it, per
+ * problem, only where its preconditioned residual beats the zero start; the
+ * inner tolerance is then measured relative to the right-hand side.  The
+ * answer is always the converged solve judged by the outer residual. */
+int jfg_pcg_varcoef_mixed_guess(const jfg_mixed_plan* plan, const double* rhs, double* x,
+                                const double* guess, int use_x0, double tol, double inner_tol,
+                                int max_outer, int maxiter_inner, int* inner_iters,
+                                int* outer_iters, void* work, size_t work_bytes, void* stream);
 
 #ifdef __cplusplus
 }

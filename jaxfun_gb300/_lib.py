@@ -96,6 +96,8 @@ SIGNATURES = {
     "jfg_pcg_mixed_workspace_size": (_sz, [_i, _i, _i, _i]),
     "jfg_pcg_varcoef_mixed": (_i, [_vp, _vp, _vp, _i, _d, _d, _i, _i, C.POINTER(_i),
                                    C.POINTER(_i), _vp, _sz, _vp]),
+    "jfg_pcg_varcoef_mixed_guess": (_i, [_vp, _vp, _vp, _vp, _i, _d, _d, _i, _i, C.POINTER(_i),
+                                         C.POINTER(_i), _vp, _sz, _vp]),
     "jfg_pcg_workspace_size": (_sz, [_i, _i, _i, _i, _i]),
     "jfg_pcg_varcoef_f64": (_i, [_i, _i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _i,
                                  _d, _i, C.POINTER(_i), _vp, _sz, _vp]),

@@ -115,6 +115,32 @@ __global__ void k_set_rz0(const T* __restrict__ part, T* __restrict__ rz0, int b
   if (b < batch) rz0[b] = sum_part(part, b);
 }
 
+// Per problem: if the guess residual is not better than the zero start
+// (r.z >= b.M^-1 b), restart from zero: x = 0, r = b, z = M^-1 b.
+template <typename T>
+__global__ void k_judge_guess(T* __restrict__ x, T* __restrict__ r, T* __restrict__ z,
+                              const T* __restrict__ b, const T* __restrict__ zb, long long N,
+                              const T* __restrict__ rz_part, const T* __restrict__ bz_part) {
+  const int bi = blockIdx.y;
+  if (sum_part(rz_part, bi) < sum_part(bz_part, bi)) return;
+  const long long off = (long long)bi * N;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N;
+       i += (long long)gridDim.x * blockDim.x) {
+    x[off + i] = T(0);
+    r[off + i] = b[off + i];
+    z[off + i] = zb[off + i];
+  }
+}
+
+// rz partials of problems that fell back to the zero start become b.M^-1 b
+template <typename T>
+__global__ void k_fix_rz(T* __restrict__ rz_part, const T* __restrict__ bz_part, int batch) {
+  const int bi = blockIdx.x * blockDim.x + threadIdx.x;
+  if (bi >= batch) return;
+  if (sum_part(rz_part, bi) >= sum_part(bz_part, bi))
+    for (int j = 0; j < NB; ++j) rz_part[bi * NB + j] = bz_part[bi * NB + j];
+}
+
 // y = a - y  (r = rhs - A x)
 template <typename T>
 __global__ void k_sub_from(const T* __restrict__ a, T* __restrict__ y, long long n) {
@@ -204,11 +230,26 @@ int pcg_run(const PcgProblem<T>& pb, T* x, int use_x0, double tol, int maxiter, 
     JFG_CUDA_TRY(cudaMemcpyAsync(r, pb.rhs, sizeof(T) * total, cudaMemcpyDeviceToDevice, st));
   }
   JFG_TRY(applyM(r, z));
-  JFG_CUDA_TRY(cudaMemcpyAsync(p, z, sizeof(T) * total, cudaMemcpyDeviceToDevice, st));
   k_dot_part<T><<<dgrid, DOT_T, 0, st>>>(r, z, N, rz_part[1]);
   JFG_LAUNCHED();
-  k_set_rz0<T><<<(batch + 127) / 128, 128, 0, st>>>(rz_part[1], rz0, batch);
-  JFG_LAUNCHED();
+  if (use_x0 && pb.judge_x0) {
+    // Judge the initial guess against the zero start: keep it only where its
+    // preconditioned residual is smaller than that of the right-hand side,
+    // and measure convergence relative to the right-hand side either way.
+    JFG_TRY(applyM(pb.rhs, q));
+    k_dot_part<T><<<dgrid, DOT_T, 0, st>>>(pb.rhs, q, N, pq_part);
+    JFG_LAUNCHED();
+    k_judge_guess<T><<<vgrid, 256, 0, st>>>(x, r, z, pb.rhs, q, N, rz_part[1], pq_part);
+    JFG_LAUNCHED();
+    k_set_rz0<T><<<(batch + 127) / 128, 128, 0, st>>>(pq_part, rz0, batch);
+    JFG_LAUNCHED();
+    k_fix_rz<T><<<(batch + 127) / 128, 128, 0, st>>>(rz_part[1], pq_part, batch);
+    JFG_LAUNCHED();
+  } else {
+    k_set_rz0<T><<<(batch + 127) / 128, 128, 0, st>>>(rz_part[1], rz0, batch);
+    JFG_LAUNCHED();
+  }
+  JFG_CUDA_TRY(cudaMemcpyAsync(p, z, sizeof(T) * total, cudaMemcpyDeviceToDevice, st));
 
   auto iteration = [&](int it, bool reset_counter) -> int {
     const int prev = (it + 1) & 1, cur = it & 1;

@@ -16,6 +16,9 @@ struct PcgProblem {
   const T* lam = nullptr;          // (n)
   const T* fd_scale = nullptr;     // (batch) constant kappa of the preconditioner
   const T* rhs = nullptr;          // (batch, n^ndim)
+  // with an initial guess: keep it per problem only if its preconditioned
+  // residual beats the zero start, and stop relative to the right-hand side
+  bool judge_x0 = false;
 };
 
 template <typename T>

@@ -25,7 +25,7 @@ class MixedPlan(C.Structure):
         ("ops64", C.c_void_p), ("kw64", C.c_void_p),
         ("ops_hi", C.c_void_p), ("ops_lo", C.c_void_p), ("kw32", C.c_void_p),
         ("E_hi", C.c_void_p), ("E_lo", C.c_void_p), ("W_hi", C.c_void_p), ("W_lo", C.c_void_p),
-        ("lam", C.c_void_p), ("fd_scale", C.c_void_p),
+        ("lam", C.c_void_p), ("fd_scale", C.c_void_p), ("ops32", C.c_void_p),
     ]
 
 
@@ -56,6 +56,7 @@ class MixedVarCoefSolver:
         D = s0.backward_matrix(None, 1)
         ops_pad = pack_varcoef_ops(nd, _pad(B, nq, nq), _pad(D, nq, nq))
         self.ops_hi, self.ops_lo = split_tf32(ops_pad)
+        self.ops32 = as_device(ops_pad, torch.float32)
         self.kw32 = A.kw.to(torch.float32).contiguous()
         fac = fd_preconditioner(A.T) if M is None else M
         self.E_hi, self.E_lo = split_tf32(_pad(fac.E_host, nq, nq))
@@ -67,29 +68,35 @@ class MixedVarCoefSolver:
                               self.ops_hi.data_ptr(), self.ops_lo.data_ptr(),
                               self.kw32.data_ptr(), self.E_hi.data_ptr(), self.E_lo.data_ptr(),
                               self.W_hi.data_ptr(), self.W_lo.data_ptr(), self.lam.data_ptr(),
-                              None)
+                              None, self.ops32.data_ptr())
 
     def workspace_bytes(self) -> int:
         A = self.A
         return int(_lib.lib().jfg_pcg_mixed_workspace_size(A.ndim, A.n, A.nq, A.batch))
 
     def solve(self, b, x0=None, tol: float = 1e-10, inner_tol: float = 1e-5,
-              max_outer: int = 10, maxiter_inner: int = 1000, out=None, ws=None):
-        """Returns (x, inner_iterations, outer_iterations) per problem."""
+              max_outer: int = 10, maxiter_inner: int = 1000, out=None, ws=None, guess=None):
+        """Returns (x, inner_iterations, outer_iterations) per problem.
+
+        ``x0``: an FP64 starting iterate (its residual is formed in FP64);
+        ``guess``: a learned initial guess for the first inner solve (judged per
+        problem against the zero start, see jfg_pcg_varcoef_mixed_guess)."""
         A = self.A
         b = as_device(b)
         if x0 is None:
             x = torch.empty_like(b) if out is None else out
         else:
             x = as_device(x0).clone() if out is None else out.copy_(as_device(x0))
+        g = None if guess is None else as_device(guess)
         L = _lib.lib()
         if ws is None:
             ws = workspace(self.workspace_bytes(), slot=1)
         it_in = (C.c_int * A.batch)()
         it_out = (C.c_int * A.batch)()
-        st = L.jfg_pcg_varcoef_mixed(C.byref(self.plan), b.data_ptr(), x.data_ptr(),
-                                     0 if x0 is None else 1, float(tol), float(inner_tol),
-                                     int(max_outer), int(maxiter_inner), it_in, it_out,
-                                     ws.data_ptr(), ws.numel(), _lib.stream_handle())
+        st = L.jfg_pcg_varcoef_mixed_guess(C.byref(self.plan), b.data_ptr(), x.data_ptr(),
+                                           None if g is None else g.data_ptr(),
+                                           0 if x0 is None else 1, float(tol), float(inner_tol),
+                                           int(max_outer), int(maxiter_inner), it_in, it_out,
+                                           ws.data_ptr(), ws.numel(), _lib.stream_handle())
         _lib.check(st, "jfg_pcg_varcoef_mixed")
         return x, np.array(it_in[:]), np.array(it_out[:])

@@ -32,7 +32,7 @@ N_FINE = 256
 class GridMaps:
     """Per-axis FP64 operators between the solver's space and the network grid."""
 
-    def __init__(self, N: int = N_FINE, n: int = 64):
+    def __init__(self, N: int = N_FINE, n: int = 64, guess_modes: int = 32):
         self.N, self.n = N, n
         Lo, lo = Legendre(N), Legendre(n)
         # fine-grid field -> first n Legendre modes -> values on the n-point grid
@@ -41,10 +41,13 @@ class GridMaps:
         # solver coefficients (N-2) -> values on the n-point grid
         self.coef_to_net = D.backward_matrix(n)
         d = FunctionSpace(n, Legendre, bcs=DIRICHLET)
-        # network-grid values -> Dirichlet coefficients (first n-2; the basis
-        # functions phi_k = L_k - L_{k+2} do not depend on N), padded to N-2
+        # network-grid values -> Dirichlet coefficients (the basis functions
+        # phi_k = L_k - L_{k+2} do not depend on N), padded to N-2.  Only the
+        # first guess_modes are kept: the network resolves 32 Legendre modes
+        # per axis and its higher-mode content is noise in the energy norm.
         G = np.zeros((N - 2, n))
-        G[: n - 2] = d.forward_matrix()
+        m = min(guess_modes, n - 2)
+        G[:m] = d.forward_matrix()[:m]
         self.net_to_coef = G
         x = lo.mesh()
         self.X, self.Y = np.meshgrid(x, x, indexing="ij")
@@ -191,7 +194,7 @@ def evaluate_gain(model: SNO, maps: GridMaps, nprob: int = 128, seed: int = 3,
             torch.cuda.synchronize()
             t0 = time.perf_counter()
             x0 = initial_guess(model, maps, data["X"], data["s"]) if name == "learned" else None
-            x, it_in, it_out = S.solve(b, x0=x0, tol=tol, inner_tol=inner_tol)
+            x, it_in, it_out = S.solve(b, guess=x0, tol=tol, inner_tol=inner_tol)
             torch.cuda.synchronize()
             dt = time.perf_counter() - t0
         err = float(((x - xt).abs().amax(dim=(1, 2)) / xt.abs().amax(dim=(1, 2))).max())
