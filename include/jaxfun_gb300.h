@@ -109,6 +109,10 @@ int jfg_contract_f32(const jfg_contract_desc* d, const float* op, const float* i
  */
 int jfg_contract_tc(const jfg_contract_desc* d, const float* op_hi, const float* op_lo,
                     const float* in, float* out, void* stream);
+/* Kernel variant of jfg_contract_tc: 1 (default) keeps the split input tile
+ * (MMA operand A) in TMEM, written by the split warps with tcgen05.st, so the
+ * MMAs read only operand B from shared memory; 0 keeps A in shared memory. */
+int jfg_tc_set_variant(int operand_a_in_tmem);
 /* Split n FP64 values into TF32 hi (round to nearest) and FP32 lo = x - hi
  * (host arrays), the operator format jfg_contract_tc expects. */
 void jfg_split_tf32_host(size_t n, const double* src, float* hi, float* lo);

@@ -75,6 +75,7 @@ SIGNATURES = {
     "jfg_contract_f32": (_i, [C.POINTER(ContractDesc), _vp, _vp, _vp, _vp]),
     "jfg_contract_tc": (_i, [C.POINTER(ContractDesc), _vp, _vp, _vp, _vp, _vp]),
     "jfg_split_tf32_host": (None, [_sz, _vp, _vp, _vp]),
+    "jfg_tc_set_variant": (_i, [_i]),
     "jfg_device_status": (_i, []),
     "jfg_tp_apply_workspace_size": (_sz, [_i, C.POINTER(_i), C.POINTER(_i), _i, _i]),
     "jfg_tp_apply_f64": (_i, [_i, C.POINTER(_i), C.POINTER(_i), _i, C.POINTER(_vp), _vp, _vp,

@@ -33,6 +33,10 @@ namespace jfg {
 
 __device__ int g_tc_status = 0;
 
+// Kernel variant: 1 keeps the split input tile in TMEM (default), 0 in shared
+// memory (jfg_tc_set_variant).
+static int g_operand_a_in_tmem = 1;
+
 namespace {
 
 constexpr int TILE_P = 128;
@@ -50,7 +54,14 @@ struct TcParams {
   int seg_in_map;  // 1 if the input map has a segment dimension
   int bat_in_map;  // 1 if the input map has a batch dimension
   int seg_op_map;  // 1 if the operator maps have a segment dimension
+  int tmem_a;      // 1: split input tile (MMA operand A) kept in TMEM, not shared memory
 };
+
+// TMEM column map when operand A lives in TMEM: accumulator buffers at
+// columns [0, 128) and [128, 256); stage s keeps A hi at 256 + 64 s and A lo
+// at 256 + 64 s + 32 (32 TF32 columns each).
+constexpr int ACC_STRIDE_TA = 128;
+constexpr int A_COL0 = 256;
 
 __device__ __forceinline__ uint32_t smem_u32(const void* p) {
   return (uint32_t)__cvta_generic_to_shared(p);
@@ -148,6 +159,31 @@ __device__ __forceinline__ void mma_tf32(uint32_t tmem, uint64_t a, uint64_t b, 
       "l"(a), "l"(b), "r"(idesc), "r"(accum));
 }
 
+// Same MMA with operand A read from TMEM (128 lanes x 8 TF32 columns).
+__device__ __forceinline__ void mma_tf32_ta(uint32_t tmem, uint32_t a_tmem, uint64_t b,
+                                            uint32_t idesc, uint32_t accum) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::tf32 [%0], [%1], %2, %3, p;\n\t}" ::"r"(tmem),
+      "r"(a_tmem), "l"(b), "r"(idesc), "r"(accum));
+}
+
+// Store 32 consecutive 32-bit columns of this thread's TMEM lane.
+__device__ __forceinline__ void tmem_st32(uint32_t taddr, const uint32_t* v) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x32.b32 [%0], "
+      "{%1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, %16, "
+      "%17, %18, %19, %20, %21, %22, %23, %24, %25, %26, %27, %28, %29, %30, %31, %32};" ::"r"(
+          taddr),
+      "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7]),
+      "r"(v[8]), "r"(v[9]), "r"(v[10]), "r"(v[11]), "r"(v[12]), "r"(v[13]), "r"(v[14]),
+      "r"(v[15]), "r"(v[16]), "r"(v[17]), "r"(v[18]), "r"(v[19]), "r"(v[20]), "r"(v[21]),
+      "r"(v[22]), "r"(v[23]), "r"(v[24]), "r"(v[25]), "r"(v[26]), "r"(v[27]), "r"(v[28]),
+      "r"(v[29]), "r"(v[30]), "r"(v[31])
+      : "memory");
+}
+
 __device__ __forceinline__ void mma_commit(uint64_t* bar) {
   asm volatile(
       "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
@@ -188,7 +224,10 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   const int Mt = prm.Mtile;
   const int S = prm.stages;
   const uint32_t obytes = (uint32_t)Mt * KB * 4;
-  const uint32_t stage_bytes = 2 * XBYTES + 2 * obytes;
+  const bool ta = prm.tmem_a != 0;
+  const uint32_t xbuf = ta ? XBYTES : 2 * XBYTES;  // X tile (+ its lo part when in SMEM)
+  const uint32_t stage_bytes = xbuf + 2 * obytes;
+  const uint32_t acc_stride = ta ? ACC_STRIDE_TA : 256;
   uint64_t* bars = (uint64_t*)(smem + (size_t)S * stage_bytes);
   uint64_t* full = bars;
   uint64_t* conv = bars + S;
@@ -229,8 +268,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 
   auto Xh = [&](int st) { return smem + (size_t)st * stage_bytes; };
   auto Xl = [&](int st) { return smem + (size_t)st * stage_bytes + XBYTES; };
-  auto Oh = [&](int st) { return smem + (size_t)st * stage_bytes + 2 * XBYTES; };
-  auto Ol = [&](int st) { return smem + (size_t)st * stage_bytes + 2 * XBYTES + obytes; };
+  auto Oh = [&](int st) { return smem + (size_t)st * stage_bytes + xbuf; };
+  auto Ol = [&](int st) { return smem + (size_t)st * stage_bytes + xbuf + obytes; };
   auto decode = [&](long long t, int& pt, int& mc, int& b, int& s) {
     pt = (int)(t % nptiles);
     long long r = t / nptiles;
@@ -284,7 +323,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           break;
         }
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-        const uint32_t acc = tmem + (uint32_t)(buf * 256);
+        const uint32_t acc = tmem + (uint32_t)buf * acc_stride;
         for (int kb = 0; kb < nkb; ++kb, ++g) {
           const int st = (int)(g % S);
           if (!mbar_wait(&conv[st], (uint32_t)(g / S) & 1u)) {
@@ -292,14 +331,25 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             break;
           }
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-          const uint32_t xh = smem_u32(Xh(st)), xl = smem_u32(Xl(st));
           const uint32_t oh = smem_u32(Oh(st)), ol = smem_u32(Ol(st));
+          if (ta) {
+            const uint32_t ah = tmem + (uint32_t)(A_COL0 + 64 * st), al = ah + 32;
 #pragma unroll
-          for (int kk = 0; kk < KB / 8; ++kk) {
-            const uint32_t off = kk * 32;  // 8 TF32 = 32 B per MMA
-            mma_tf32(acc, sdesc(xh + off), sdesc(oh + off), idesc, (kb | kk) ? 1u : 0u);
-            mma_tf32(acc, sdesc(xh + off), sdesc(ol + off), idesc, 1u);
-            mma_tf32(acc, sdesc(xl + off), sdesc(oh + off), idesc, 1u);
+            for (int kk = 0; kk < KB / 8; ++kk) {
+              const uint32_t off = kk * 32;  // 8 TF32 = 32 B of B per MMA, 8 A columns
+              mma_tf32_ta(acc, ah + 8 * kk, sdesc(oh + off), idesc, (kb | kk) ? 1u : 0u);
+              mma_tf32_ta(acc, ah + 8 * kk, sdesc(ol + off), idesc, 1u);
+              mma_tf32_ta(acc, al + 8 * kk, sdesc(oh + off), idesc, 1u);
+            }
+          } else {
+            const uint32_t xh = smem_u32(Xh(st)), xl = smem_u32(Xl(st));
+#pragma unroll
+            for (int kk = 0; kk < KB / 8; ++kk) {
+              const uint32_t off = kk * 32;  // 8 TF32 = 32 B per MMA
+              mma_tf32(acc, sdesc(xh + off), sdesc(oh + off), idesc, (kb | kk) ? 1u : 0u);
+              mma_tf32(acc, sdesc(xh + off), sdesc(ol + off), idesc, 1u);
+              mma_tf32(acc, sdesc(xl + off), sdesc(oh + off), idesc, 1u);
+            }
           }
           mma_commit(&empty[st]);
         }
@@ -311,20 +361,46 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     const int ct = threadIdx.x - 64;  // 0..127
     const long long total_kb =
         ((ntiles - blockIdx.x + gridDim.x - 1) / gridDim.x) * (long long)nkb;
+    // TMEM mode: thread = row r of the tile (its warp's lane quarter), reads
+    // its 32 values from the 128-byte-swizzled tile and stores hi / lo into
+    // its TMEM lane with tcgen05.st.
+    const int row = 32 * (warp & 3) + lane;
     for (long long g = 0; g < total_kb; ++g) {
       const int st = (int)(g % S);
       if (!mbar_wait(&full[st], (uint32_t)(g / S) & 1u)) break;
-      float4* xh = (float4*)Xh(st);
-      float4* xl = (float4*)Xl(st);
+      if (ta) {
+        const float4* xr = (const float4*)(Xh(st) + row * 128);
+        uint32_t h[32], l[32];
 #pragma unroll
-      for (int i = 0; i < (int)(XBYTES / 16 / 128); ++i) {
-        const int idx = ct + i * 128;
-        float4 v = xh[idx];
-        float4 h = make_float4(tf32_hi(v.x), tf32_hi(v.y), tf32_hi(v.z), tf32_hi(v.w));
-        xh[idx] = h;
-        xl[idx] = make_float4(v.x - h.x, v.y - h.y, v.z - h.z, v.w - h.w);
+        for (int c = 0; c < 8; ++c) {
+          const float4 v = xr[c ^ (row & 7)];
+          const float hv[4] = {tf32_hi(v.x), tf32_hi(v.y), tf32_hi(v.z), tf32_hi(v.w)};
+          const float vv[4] = {v.x, v.y, v.z, v.w};
+#pragma unroll
+          for (int e = 0; e < 4; ++e) {
+            h[4 * c + e] = __float_as_uint(hv[e]);
+            l[4 * c + e] = __float_as_uint(vv[e] - hv[e]);
+          }
+        }
+        const uint32_t tbase = tmem + ((uint32_t)(32 * (warp & 3)) << 16) +
+                               (uint32_t)(A_COL0 + 64 * st);
+        tmem_st32(tbase, h);
+        tmem_st32(tbase + 32, l);
+        asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+      } else {
+        float4* xh = (float4*)Xh(st);
+        float4* xl = (float4*)Xl(st);
+#pragma unroll
+        for (int i = 0; i < (int)(XBYTES / 16 / 128); ++i) {
+          const int idx = ct + i * 128;
+          float4 v = xh[idx];
+          float4 h = make_float4(tf32_hi(v.x), tf32_hi(v.y), tf32_hi(v.z), tf32_hi(v.w));
+          xh[idx] = h;
+          xl[idx] = make_float4(v.x - h.x, v.y - h.y, v.z - h.z, v.w - h.w);
+        }
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       }
-      asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
       __syncwarp();
       if (lane == 0) mbar_arrive(&conv[st]);
     }
@@ -357,7 +433,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       const float* __restrict__ fld = nullptr;
       if (EPI == JFG_EPI_MUL_FIELD)
         fld = (const float*)d.field + (long long)b * d.field_batch + (long long)s * d.field_seg;
-      const uint32_t tacc = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(buf * 256);
+      const uint32_t tacc = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)buf * acc_stride;
       for (int c = half * 2; c < Mt / 16; c += 4) {
         // columns [c*16, c*16+32): two 16-column TMEM loads
         const int mb = mc * Mt + c * 16;
@@ -483,10 +559,11 @@ int contract_tc(const jfg_contract_desc& d, const float* op_hi, const float* op_
 
   const int Mt = ((d.M > MT_MAX ? MT_MAX : d.M) + 15) / 16 * 16;
   const int mchunks = (d.M + Mt - 1) / Mt;
-  const int cols = 512;  // two accumulator buffers of 256 columns
-  const size_t stage = 2 * (size_t)XBYTES + 2 * (size_t)Mt * KB * 4;
+  const int cols = 512;  // two accumulator buffers (+ operand A stages in TMEM mode)
+  const int ta = g_operand_a_in_tmem;
+  const size_t stage = (ta ? 1 : 2) * (size_t)XBYTES + 2 * (size_t)Mt * KB * 4;
   int stages = (int)((200 * 1024) / stage);
-  if (stages > 6) stages = 6;
+  if (stages > (ta ? 4 : 6)) stages = ta ? 4 : 6;
   if (stages < 2) return JFG_ERR_UNSUPPORTED;
   const size_t smem = 1024 + stages * stage + (3 * stages + 4) * 8 + 16;
   const long long ntiles = (long long)((d.P + TILE_P - 1) / TILE_P) * mchunks * gy;
@@ -502,6 +579,7 @@ int contract_tc(const jfg_contract_desc& d, const float* op_hi, const float* op_
   prm.seg_in_map = (d.nseg > 1 && d.in_seg != 0) ? 1 : 0;
   prm.bat_in_map = (d.batch > 1 && d.in_batch != 0) ? 1 : 0;
   prm.seg_op_map = (d.nseg > 1 && d.op_seg != 0) ? 1 : 0;
+  prm.tmem_a = ta;
 
   CUtensorMap mx, moh, mol;
   {
@@ -564,6 +642,12 @@ extern "C" int jfg_contract_tc(const jfg_contract_desc* d, const float* op_hi,
                                const float* op_lo, const float* in, float* out, void* stream) {
   if (!d) return JFG_ERR_ARG;
   return jfg::contract_tc(*d, op_hi, op_lo, in, out, (cudaStream_t)stream);
+}
+
+extern "C" int jfg_tc_set_variant(int operand_a_in_tmem) {
+  if (operand_a_in_tmem != 0 && operand_a_in_tmem != 1) return JFG_ERR_ARG;
+  jfg::g_operand_a_in_tmem = operand_a_in_tmem;
+  return JFG_OK;
 }
 
 extern "C" int jfg_device_status(void) {

@@ -12,6 +12,14 @@ pytestmark = pytest.mark.gpu
 TC_TOL = 1e-5
 
 
+@pytest.fixture(params=[1, 0], ids=["A-in-TMEM", "A-in-SMEM"], autouse=True)
+def variant(request):
+    L = _lib.lib()
+    assert L.jfg_tc_set_variant(request.param) == 0
+    yield request.param
+    L.jfg_tc_set_variant(1)
+
+
 def split(op64):
     L = _lib.lib()
     a = np.ascontiguousarray(op64, dtype=np.float64)
