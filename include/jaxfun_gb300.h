@@ -160,6 +160,38 @@ int jfg_fd_solve_f32(int ndim, int n, int batch, const float* E, const float* W,
                      const float* lam, const float* c0, const float* c1, const float* rhs,
                      float* out, void* work, size_t work_bytes, void* stream);
 
+/* Tensor-core FD solve (split-TF32 tcgen05 passes, FP32 data): E/W given as
+ * TF32 (hi, lo) pairs; n % 4 == 0 (pad with zero rows/columns and lam = 1). */
+int jfg_fd_solve_tc(int ndim, int n, int batch, const float* E_hi, const float* E_lo,
+                    const float* W_hi, const float* W_lo, const float* lam, const float* c0,
+                    const float* c1, const float* rhs, float* out, void* work,
+                    size_t work_bytes, void* stream);
+
+/* v_b = alpha2[b] (M (x) M) u_b + (K (x) M) u_b + (M (x) K) u_b for 2-D
+ * Dirichlet composites (family 0 Legendre, 1 Chebyshev; n = N - 2 per axis,
+ * u/v (batch, n, n) FP64), computed in O(n^2) per problem from the closed
+ * forms of M = S diag(h) S^T and K = -S D2 S^T (src/jaxfun/galerkin/
+ * composite.py:330-333, Legendre.py:19-33, Chebyshev.py:21-35); with b != NULL
+ * it returns v = b - A u (the FP64 refinement residual).  alpha2 may be NULL. */
+size_t jfg_helmholtz_workspace_size(int n, int batch);
+int jfg_helmholtz_apply_f64(int family, int n, int batch, const double* alpha2, const double* u,
+                            const double* b, double* v, void* work, size_t work_bytes,
+                            void* stream);
+
+/* Mixed-precision batch of equal-size Dirichlet Helmholtz solves: FP64
+ * iterative refinement x += ||r|| FD_tc(r / ||r||), r = b - A x (structured
+ * FP64 apply above), until ||r_b|| <= tol ||b_b||.  The FD correction runs on
+ * the tensor cores in the padded layout (nq >= n, nq % 4 == 0; E/W padded
+ * with zeros, lam32 with ones) with D = alpha2_32[b] + lam_i + lam_j.
+ * refinements (host, may be NULL) receives per-problem correction counts.
+ * Uneven batches are solved group by group (one call per size). */
+size_t jfg_helmholtz_solve_workspace_size(int n, int nq, int batch);
+int jfg_helmholtz_solve_mixed(int family, int n, int nq, int batch, const float* E_hi,
+                              const float* E_lo, const float* W_hi, const float* W_lo,
+                              const float* lam32, const double* alpha2, const float* alpha2_32,
+                              const double* rhs, double* x, double tol, int max_refine,
+                              int* refinements, void* work, size_t work_bytes, void* stream);
+
 /*
  * jfg_fd_solve_f64 without a workspace argument: for callers that cannot
  * allocate device memory where they solve (inside CUDA-graph capture, inside

@@ -87,6 +87,13 @@ SIGNATURES = {
     "jfg_fd_solve_workspace_size": (_sz, [_i, _i, _i, _i]),
     "jfg_fd_solve_f64": (_i, [_i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
     "jfg_fd_solve_f32": (_i, [_i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
+    "jfg_fd_solve_tc": (_i, [_i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz,
+                             _vp]),
+    "jfg_helmholtz_workspace_size": (_sz, [_i, _i]),
+    "jfg_helmholtz_apply_f64": (_i, [_i, _i, _i, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
+    "jfg_helmholtz_solve_workspace_size": (_sz, [_i, _i, _i]),
+    "jfg_helmholtz_solve_mixed": (_i, [_i, _i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
+                                       _vp, _d, _i, C.POINTER(_i), _vp, _sz, _vp]),
     "jfg_fd_solve_noalloc_max_bytes": (_sz, []),
     "jfg_fd_solve_f64_noalloc": (_i, [_i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "jfg_varcoef_ops_count": (_sz, [_i, _i, _i]),

@@ -116,6 +116,45 @@ MixedLayout layout(int ndim, int n, int nq, int batch) {
 
 }  // namespace
 
+// ---- refinement glue shared with the Helmholtz batch solver -------------
+
+int launch_pad_scale(int ndim, int n, int nq, int batch, const double* in, const double* scale,
+                     float* out, cudaStream_t st) {
+  long long Nun = 1, Npad = 1;
+  for (int i = 0; i < ndim; ++i) Nun *= n, Npad *= nq;
+  k_pad_scale<<<dim3(blocks_for(Npad, 256), batch), 256, 0, st>>>(ndim, n, nq, Npad, Nun, in,
+                                                                    scale, out);
+  JFG_LAUNCHED();
+  return JFG_OK;
+}
+
+int launch_unpad_axpy(int ndim, int n, int nq, int batch, const float* d, const double* s,
+                      double* x, double sign, cudaStream_t st) {
+  long long Nun = 1, Npad = 1;
+  for (int i = 0; i < ndim; ++i) Nun *= n, Npad *= nq;
+  k_unpad_axpy<<<dim3(blocks_for(Nun, 256), batch), 256, 0, st>>>(ndim, n, nq, Npad, Nun, d, s,
+                                                                    x, sign);
+  JFG_LAUNCHED();
+  return JFG_OK;
+}
+
+int batch_norms(long long N, int batch, const double* x, double* part_dev,
+                std::vector<double>& norms, cudaStream_t st) {
+  k_sq_part<<<dim3(NBS, batch), 256, 0, st>>>(x, N, part_dev);
+  JFG_LAUNCHED();
+  std::vector<double> hp((size_t)batch * NBS);
+  JFG_CUDA_TRY(cudaMemcpyAsync(hp.data(), part_dev, sizeof(double) * batch * NBS,
+                               cudaMemcpyDeviceToHost, st));
+  JFG_CUDA_TRY(cudaStreamSynchronize(st));
+  norms.assign(batch, 0.0);
+  for (int b = 0; b < batch; ++b) {
+    double s = 0.0;
+    for (int j = 0; j < NBS; ++j) s += hp[(size_t)b * NBS + j];
+    norms[b] = sqrt(s);
+  }
+  return JFG_OK;
+}
+
 }  // namespace jfg
 
 extern "C" size_t jfg_pcg_mixed_workspace_size(int ndim, int n, int nq, int batch) {

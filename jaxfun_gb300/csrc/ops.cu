@@ -364,6 +364,16 @@ extern "C" int jfg_fd_solve_f32(int ndim, int n, int batch, const float* E, cons
                               work_bytes, (cudaStream_t)stream);
 }
 
+extern "C" int jfg_fd_solve_tc(int ndim, int n, int batch, const float* E_hi, const float* E_lo,
+                               const float* W_hi, const float* W_lo, const float* lam,
+                               const float* c0, const float* c1, const float* rhs, float* out,
+                               void* work, size_t work_bytes, void* stream) {
+  if (!E_lo || !W_lo) return JFG_ERR_ARG;
+  return jfg::fd_solve<float>(Engine::TC, ndim, n, batch, OpRef<float>{E_hi, E_lo},
+                              OpRef<float>{W_hi, W_lo}, lam, c0, c1, rhs, out, work, work_bytes,
+                              (cudaStream_t)stream);
+}
+
 extern "C" size_t jfg_varcoef_ops_count(int ndim, int n, int nq) {
   (void)ndim;
   return (size_t)8 * n * nq;

@@ -1,6 +1,8 @@
 // Internal PCG problem description shared by the plain and mixed solvers.
 #pragma once
 
+#include <vector>
+
 #include "jfg_internal.cuh"
 
 namespace jfg {
@@ -23,6 +25,17 @@ struct PcgProblem {
 
 template <typename T>
 size_t pcg_ws(int ndim, int n, int nq, int batch);
+
+// out32 (padded nq per axis) = in64 (n per axis) * scale[b]; zero padding
+int launch_pad_scale(int ndim, int n, int nq, int batch, const double* in, const double* scale,
+                     float* out, cudaStream_t st);
+// x64 (n per axis) += sign * s[b] * d32 (padded); problems with s[b] == 0 untouched
+int launch_unpad_axpy(int ndim, int n, int nq, int batch, const float* d, const double* s,
+                      double* x, double sign, cudaStream_t st);
+// 2-norms of the batch's vectors (length N each); synchronises the stream.
+// part_dev holds batch * 16 doubles.
+int batch_norms(long long N, int batch, const double* x, double* part_dev,
+                std::vector<double>& norms, cudaStream_t st);
 
 template <typename T>
 int pcg_run(const PcgProblem<T>& pb, T* x, int use_x0, double tol, int maxiter,
