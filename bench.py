@@ -296,6 +296,60 @@ def run_transforms(args):
     return 0
 
 
+def run_helmholtz(args):
+    """Secondary measurement (not the headline): 1024 Chebyshev Dirichlet Helmholtz
+    problems, N ~ U{32,48,...,512}, alpha ~ U[0,50], forcing coefficients
+    N(0,1)(1+j)^-2(1+k)^-2; tensor-core FD corrections + FP64 refinement to
+    relative residual tol; error of one problem per size vs the FP64 FD path."""
+    import numpy as np
+    import torch
+
+    from jaxfun_gb300.galerkin import DIRICHLET, Chebyshev, FunctionSpace, TensorProduct
+    from jaxfun_gb300.la import poisson_tpmatrices
+    from jaxfun_gb300.la.helmholtz import UnevenHelmholtzSolver
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    rng = np.random.default_rng(0)
+    nprob = args.nprob
+    sizes = np.arange(32, 513, 16)
+    Ns = rng.choice(sizes, size=nprob)
+    alphas = rng.uniform(0.0, 50.0, size=nprob)
+    rhs = []
+    for N in Ns:
+        C_ = Chebyshev(int(N))
+        To = TensorProduct(C_, C_)
+        D = FunctionSpace(int(N), Chebyshev, bcs=DIRICHLET)
+        T = TensorProduct(D, D)
+        j = np.arange(N)
+        fh = rng.standard_normal((N, N)) * np.outer((1.0 + j) ** -2.0, (1.0 + j) ** -2.0)
+        rhs.append(T.scalar_product(To.backward(fh)))
+    S = UnevenHelmholtzSolver("chebyshev", Ns, alphas)
+    for _ in range(args.warmup):
+        xs, refs = S.solve(rhs, tol=args.tol)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        xs, refs = S.solve(rhs, tol=args.tol)
+    torch.cuda.synchronize()
+    t = (time.perf_counter() - t0) / args.steps
+    errs = {}
+    for g in S.groups:
+        i = int(g.idx[0])
+        D = FunctionSpace(g.N, Chebyshev, bcs=DIRICHLET)
+        fac = poisson_tpmatrices(TensorProduct(D, D), 1.0).lu_factor()
+        ref = fac.solve(rhs[i], c0=alphas[i] ** 2, c1=1.0)
+        errs[g.N] = float((xs[i] - ref).abs().max() / ref.abs().max())
+    n3 = float(np.mean((Ns - 2.0) ** 3))
+    fd_flops = 8.0 * n3 * nprob  # one FD pass of the batch: 4 contractions of 2 n^3
+    line = {"workload": f"helmholtz-chebyshev-uneven-{nprob}x-N32..512", "unit": "solves/s",
+            "solves_per_s": nprob / t, "ms_per_batch": 1e3 * t,
+            "refinements_mean": float(np.mean(refs)), "max_rel_err_vs_fp64_fd": max(errs.values()),
+            "groups": len(S.groups), "fd_pass_gflop": fd_flops / 1e9,
+            "launch_structure": "one tensor-core FD call per size group (31 groups)"}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
 def run_ours(args):
     import numpy as np
     import torch
@@ -554,9 +608,11 @@ def main():
     ap.add_argument("--kernel-only", action="store_true",
                     help="time only the dominant kernel (tcgen05 contraction, B problems of "
                          "256^3) and print its numbers; used for ncu captures")
-    ap.add_argument("--config", default="varcoef2d", choices=["varcoef2d", "transforms"],
+    ap.add_argument("--config", default="varcoef2d",
+                    choices=["varcoef2d", "transforms", "helmholtz"],
                     help="varcoef2d: the headline; transforms: batched 3-D Chebyshev "
-                         "round trip (secondary report)")
+                         "round trip; helmholtz: uneven Helmholtz batch (secondary reports)")
+    ap.add_argument("--nprob", type=int, default=1024)
     ap.add_argument("--n-transform", type=int, default=256)
     ap.add_argument("--fields", type=int, default=16)
     args = ap.parse_args()
@@ -564,6 +620,8 @@ def main():
         return run_reference(args)
     if args.config == "transforms":
         return run_transforms(args)
+    if args.config == "helmholtz":
+        return run_helmholtz(args)
     if args.kernel_only:
         import torch
 
