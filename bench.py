@@ -332,20 +332,89 @@ def run_helmholtz(args):
         xs, refs = S.solve(rhs, tol=args.tol)
     torch.cuda.synchronize()
     t = (time.perf_counter() - t0) / args.steps
-    errs = {}
+    from jaxfun_gb300.la.helmholtz import helmholtz_apply
+
+    errs, res_ours, res_fd = {}, {}, {}
     for g in S.groups:
         i = int(g.idx[0])
         D = FunctionSpace(g.N, Chebyshev, bcs=DIRICHLET)
         fac = poisson_tpmatrices(TensorProduct(D, D), 1.0).lu_factor()
-        ref = fac.solve(rhs[i], c0=alphas[i] ** 2, c1=1.0)
-        errs[g.N] = float((xs[i] - ref).abs().max() / ref.abs().max())
+        b = rhs[i][None]
+        a2 = alphas[i] ** 2
+        # reference: FP64 FD solve, refined in FP64 with the structured residual
+        ref = fac.solve(b, c0=a2, c1=1.0)
+        rr = lambda u: b - helmholtz_apply("chebyshev", g.N, a2, u)  # noqa: E731
+        res_fd[g.N] = float(rr(ref).norm() / b.norm())
+        for _ in range(3):
+            ref = ref + fac.solve(rr(ref), c0=a2, c1=1.0)
+        res_ours[g.N] = float(rr(xs[i][None]).norm() / b.norm())
+        errs[g.N] = float((xs[i] - ref[0]).abs().max() / ref.abs().max())
     n3 = float(np.mean((Ns - 2.0) ** 3))
     fd_flops = 8.0 * n3 * nprob  # one FD pass of the batch: 4 contractions of 2 n^3
     line = {"workload": f"helmholtz-chebyshev-uneven-{nprob}x-N32..512", "unit": "solves/s",
             "solves_per_s": nprob / t, "ms_per_batch": 1e3 * t,
-            "refinements_mean": float(np.mean(refs)), "max_rel_err_vs_fp64_fd": max(errs.values()),
+            "refinements_mean": float(np.mean(refs)),
+            "max_rel_err_vs_fp64_refined_fd": max(errs.values()),
+            "max_relres_ours": max(res_ours.values()),
+            "max_relres_plain_fp64_fd": max(res_fd.values()),
             "groups": len(S.groups), "fd_pass_gflop": fd_flops / 1e9,
             "launch_structure": "one tensor-core FD call per size group (31 groups)"}
+    print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_varcoef3d(args):
+    """Secondary measurement (not the headline): 32 problems -div(kappa grad u) = f
+    on 128^3 Legendre Dirichlet, kappa = exp(g) from the 3-D random-field recipe,
+    mixed-precision solve vs plain FP64 PCG (on a subset), error vs a tight FP64
+    solve."""
+    import numpy as np
+    import torch
+
+    from jaxfun_gb300.galerkin import DIRICHLET, FunctionSpace, Legendre, TensorProduct
+    from jaxfun_gb300.la import MixedVarCoefSolver, VarCoefMatrix, pcg
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    N, B = args.n3d, args.batch3d
+    D = FunctionSpace(N, Legendre, bcs=DIRICHLET)
+    T = TensorProduct(D, D, D)
+    Lo = Legendre(N)
+    To = TensorProduct(Lo, Lo, Lo)
+    gen = torch.Generator(device="cuda").manual_seed(0)
+    k = torch.arange(N, dtype=torch.float64, device="cuda")
+    k2 = k[:, None, None] ** 2 + k[None, :, None] ** 2 + k[None, None, :] ** 2
+    fs = ((1 + k[:, None, None]) * (1 + k[None, :, None]) * (1 + k[None, None, :])) ** -2.0
+    gh = torch.randn((B, N, N, N), generator=gen, dtype=torch.float64, device="cuda") * (1 + k2) ** -1.5
+    fh = torch.randn((B, N, N, N), generator=gen, dtype=torch.float64, device="cuda") * fs
+    g = To.backward(gh)
+    g = (g - g.mean(dim=(1, 2, 3), keepdim=True)) / g.std(dim=(1, 2, 3), keepdim=True)
+    kap = torch.exp(g)
+    b = T.scalar_product(To.backward(fh))
+    A = VarCoefMatrix(T, kap)
+    S = MixedVarCoefSolver(A)
+    for _ in range(args.warmup):
+        x, it_in, it_out = S.solve(b, tol=args.tol)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        x, it_in, it_out = S.solve(b, tol=args.tol)
+    torch.cuda.synchronize()
+    t = (time.perf_counter() - t0) / args.steps
+    nf = min(B, 4)
+    A4 = VarCoefMatrix(T, kap[:nf])
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    x64, it64 = pcg(A4, b[:nf], tol=args.fp64_tol, maxiter=3000)
+    torch.cuda.synchronize()
+    t64 = time.perf_counter() - t0
+    xt, _ = pcg(A4, b[:nf], tol=1e-14, maxiter=4000)
+    err = float(((x[:nf] - xt).abs().amax(dim=(1, 2, 3)) / xt.abs().amax(dim=(1, 2, 3))).max())
+    err64 = float(((x64 - xt).abs().amax(dim=(1, 2, 3)) / xt.abs().amax(dim=(1, 2, 3))).max())
+    line = {"workload": f"varcoef-poisson-3d-legendre-N{N}-batch{B}", "unit": "solves/s",
+            "mixed_solves_per_s": B / t, "mixed_inner_iterations_mean": float(it_in.mean()),
+            "mixed_outer_iterations_mean": float(it_out.mean()), "mixed_max_rel_err": err,
+            "fp64_pcg_solves_per_s": nf / t64, "fp64_pcg_iterations_mean": float(it64.mean()),
+            "fp64_pcg_max_rel_err": err64, "speedup": (B / t) / (nf / t64)}
     print(json.dumps(line), flush=True)
     return 0
 
@@ -609,10 +678,12 @@ def main():
                     help="time only the dominant kernel (tcgen05 contraction, B problems of "
                          "256^3) and print its numbers; used for ncu captures")
     ap.add_argument("--config", default="varcoef2d",
-                    choices=["varcoef2d", "transforms", "helmholtz"],
+                    choices=["varcoef2d", "transforms", "helmholtz", "varcoef3d"],
                     help="varcoef2d: the headline; transforms: batched 3-D Chebyshev "
                          "round trip; helmholtz: uneven Helmholtz batch (secondary reports)")
     ap.add_argument("--nprob", type=int, default=1024)
+    ap.add_argument("--n3d", type=int, default=128)
+    ap.add_argument("--batch3d", type=int, default=32)
     ap.add_argument("--n-transform", type=int, default=256)
     ap.add_argument("--fields", type=int, default=16)
     args = ap.parse_args()
@@ -622,6 +693,8 @@ def main():
         return run_transforms(args)
     if args.config == "helmholtz":
         return run_helmholtz(args)
+    if args.config == "varcoef3d":
+        return run_varcoef3d(args)
     if args.kernel_only:
         import torch
 
