@@ -42,6 +42,7 @@ struct GemmParams {
   jfg_gemm_desc d;
   int Nt, stages, tmem_cols, kb_per_split, a_bat, b_bat;
   int a_perm, b_perm;  // 1: tensor map dims ordered (K, batch, rows)
+  int vec_ok;          // 1: every row-major operand allows 16-byte vector access
 };
 
 __device__ __forceinline__ float gelu(float x) {
@@ -152,6 +153,74 @@ __global__ void __launch_bounds__(NTH, 1)
         float v[16];
         tc::tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(c * 16), v);
         if (!mok) continue;
+        if (!split && c * 16 + 16 <= d.N && prm.vec_ok) {
+          // whole 16-column group of this thread's row: 16-byte vector accesses
+          const int n0 = c * 16;
+          float r[16];
+#pragma unroll
+          for (int j = 0; j < 16; ++j) r[j] = d.alpha * v[j];
+          if (d.add) {
+            const float4* a4 = (const float4*)(d.add + (long long)b * d.add_batch +
+                                                (long long)m * d.ld_add + n0);
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+              const float4 t = a4[j];
+              r[4 * j] += t.x, r[4 * j + 1] += t.y, r[4 * j + 2] += t.z, r[4 * j + 3] += t.w;
+            }
+          }
+          if (d.bias) {
+#pragma unroll
+            for (int j = 0; j < 16; ++j) r[j] += d.bias[n0 + j];
+          }
+          if (d.gg) {
+            const float4* g4 = (const float4*)(d.gg + (long long)b * d.gg_batch +
+                                                (long long)m * d.ld_gg + n0);
+#pragma unroll
+            for (int j = 0; j < 4; ++j) {
+              const float4 t = g4[j];
+              r[4 * j] *= gelu_grad(t.x), r[4 * j + 1] *= gelu_grad(t.y);
+              r[4 * j + 2] *= gelu_grad(t.z), r[4 * j + 3] *= gelu_grad(t.w);
+            }
+          }
+          if (d.pre) {
+            float4* p4 = (float4*)(d.pre + (long long)b * d.pre_batch + (long long)m * d.ld_pre + n0);
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+              p4[j] = make_float4(r[4 * j], r[4 * j + 1], r[4 * j + 2], r[4 * j + 3]);
+          }
+          if (d.act == 1) {
+#pragma unroll
+            for (int j = 0; j < 16; ++j) r[j] = gelu(r[j]);
+          }
+          if (d.d32) {
+            float4* o4 = (float4*)(d.d32 + (long long)b * d.d32_batch + (long long)m * d.ld_d32 + n0);
+#pragma unroll
+            for (int j = 0; j < 4; ++j)
+              o4[j] = make_float4(r[4 * j], r[4 * j + 1], r[4 * j + 2], r[4 * j + 3]);
+          }
+          if (d.dbf || d.dtbf) {
+            __nv_bfloat16 h[16];
+#pragma unroll
+            for (int j = 0; j < 16; ++j) h[j] = __float2bfloat16(r[j]);
+            if (d.dbf) {
+              uint32_t w[8];
+#pragma unroll
+              for (int j = 0; j < 8; ++j)
+                w[j] = (uint32_t)__bfloat16_as_ushort(h[2 * j]) |
+                       ((uint32_t)__bfloat16_as_ushort(h[2 * j + 1]) << 16);
+              uint4* o = (uint4*)((__nv_bfloat16*)d.dbf + (long long)b * d.dbf_batch +
+                                  (long long)m * d.ld_dbf + n0);
+              o[0] = make_uint4(w[0], w[1], w[2], w[3]);
+              o[1] = make_uint4(w[4], w[5], w[6], w[7]);
+            }
+            if (d.dtbf) {
+              __nv_bfloat16* t = (__nv_bfloat16*)d.dtbf + (long long)b * d.dtbf_batch + m;
+#pragma unroll
+              for (int j = 0; j < 16; ++j) t[(long long)(n0 + j) * d.ld_dtbf] = h[j];
+            }
+          }
+          continue;
+        }
 #pragma unroll
         for (int j = 0; j < 16; ++j) {
           const int n = c * 16 + j;
@@ -250,6 +319,17 @@ extern "C" int jfg_gemm_bf16(const jfg_gemm_desc* dp, const void* A, const void*
   prm.a_bat = (d.batch > 1 && d.a_batch != 0) ? 1 : 0;
   prm.b_bat = (d.batch > 1 && d.b_batch != 0) ? 1 : 0;
   const int ksplit = (nkb + prm.kb_per_split - 1) / prm.kb_per_split;
+  {
+    auto f4 = [](const void* p, long long ld, long long bs) {
+      return p == nullptr || ((((uintptr_t)p) & 15) == 0 && (ld & 3) == 0 && (bs & 3) == 0);
+    };
+    auto h8 = [](const void* p, long long ld, long long bs) {
+      return p == nullptr || ((((uintptr_t)p) & 15) == 0 && (ld & 7) == 0 && (bs & 7) == 0);
+    };
+    prm.vec_ok = f4(d.add, d.ld_add, d.add_batch) && f4(d.gg, d.ld_gg, d.gg_batch) &&
+                 f4(d.pre, d.ld_pre, d.pre_batch) && f4(d.d32, d.ld_d32, d.d32_batch) &&
+                 h8(d.dbf, d.ld_dbf, d.dbf_batch);
+  }
   prm.a_perm = (prm.a_bat && d.a_batch < d.lda) ? 1 : 0;
   prm.b_perm = (prm.b_bat && d.b_batch < d.ldb) ? 1 : 0;
   if ((prm.a_perm && d.a_batch < d.K) || (prm.b_perm && d.b_batch < d.K)) return JFG_ERR_ARG;

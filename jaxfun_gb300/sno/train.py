@@ -23,6 +23,7 @@ import numpy as np
 import torch
 
 from ..galerkin import DIRICHLET, FunctionSpace, Legendre, TensorProduct, tp_apply
+from ..galerkin.tensorproductspace import tp_apply_tc
 from ..la import MixedVarCoefSolver, VarCoefMatrix
 from .model import CIN, SNO, SNOConfig
 
@@ -73,8 +74,9 @@ def features(g, f, maps: GridMaps):
     """Network inputs (B*n^2, 16) FP32 and the per-sample forcing scale."""
     B = g.shape[0]
     n = maps.n
-    g64 = tp_apply([maps.to_net, maps.to_net], g)
-    f64 = tp_apply([maps.to_net, maps.to_net], f)
+    # spectral truncation onto the network grid on the tensor cores (FP32 data)
+    g64 = tp_apply_tc([maps.to_net, maps.to_net], g)
+    f64 = tp_apply_tc([maps.to_net, maps.to_net], f)
     s = f64.pow(2).mean(dim=(1, 2)).sqrt().clamp_min(1e-30)
     X = torch.zeros((B, n, n, CIN), dtype=torch.float32, device="cuda")
     X[..., 0] = g64.float()
@@ -164,8 +166,8 @@ def predict(model: SNO, X: torch.Tensor, Bt: int | None = None) -> torch.Tensor:
 
 def initial_guess(model: SNO, maps: GridMaps, X: torch.Tensor, s: torch.Tensor) -> torch.Tensor:
     """Learned initial guess in the solver's coefficient space (B, N-2, N-2) FP64."""
-    u = predict(model, X).double() * s[:, None, None]
-    return tp_apply([maps.net_to_coef, maps.net_to_coef], u)
+    u = predict(model, X) * s[:, None, None].float()
+    return tp_apply_tc([maps.net_to_coef, maps.net_to_coef], u).double()
 
 
 def relative_l2(model: SNO, data: dict) -> float:
