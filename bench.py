@@ -245,6 +245,53 @@ def roofline_microbench(B: int, N: int, reps: int = 20):
             "tflops_issued": 3 * flops / t / 1e12, "gbs": nbytes / t / 1e9}
 
 
+def other_kernel_microbench(which: str, B: int, reps: int = 3):
+    """CUDA-event timing of the BF16 GEMM ('gemm') or the FP64 contraction ('fp64')."""
+    import ctypes
+
+    import torch
+
+    from jaxfun_gb300 import _lib
+
+    L = _lib.lib()
+    s = torch.cuda.current_stream()
+    if which == "gemm":
+        M, N, K, P = 1024, 64, 4096, 4096
+        A = torch.randn(M, K, device="cuda").to(torch.bfloat16)
+        Bm = torch.randn(N, B * P, device="cuda").to(torch.bfloat16)
+        out = torch.empty(B, M, N, device="cuda")
+        d = _lib.GemmDesc(batch=B, M=M, N=N, K=K, ksplit=1, lda=K, a_batch=0, ldb=B * P,
+                          b_batch=P, alpha=1.0, d32=out.data_ptr(), ld_d32=N, d32_batch=M * N)
+        call = lambda: L.jfg_gemm_bf16(ctypes.byref(d), A.data_ptr(), Bm.data_ptr(),  # noqa: E731
+                                       s.cuda_stream)
+        flops = 2.0 * M * N * K * B
+        name = "k_gemm_bf16"
+    else:
+        N_ = N_GRID
+        n = N_ - 2
+        M, P, K = 2 * N_, n, n
+        op = torch.randn(M, K, dtype=torch.float64, device="cuda")
+        x = torch.randn(B, P, K, dtype=torch.float64, device="cuda")
+        y = torch.empty(B, M, P, dtype=torch.float64, device="cuda")
+        d = _lib.ContractDesc(batch=B, nseg=1, M=M, P=P, K=K, op_ld=K, in_ld=K, in_batch=P * K,
+                              out_ld=P, out_batch=M * P, alpha=1.0, beta=0.0)
+        call = lambda: L.jfg_contract_f64(d, op.data_ptr(), x.data_ptr(), y.data_ptr(),  # noqa: E731
+                                          s.cuda_stream)
+        flops = 2.0 * M * P * K * B
+        name = "k_contract_simt<double>"
+    for _ in range(2):
+        _lib.check(call(), name)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    e0.record(s)
+    for _ in range(reps):
+        call()
+    e1.record(s)
+    e1.synchronize()
+    t = e0.elapsed_time(e1) / 1e3 / reps
+    return {"kernel": name, "t": t, "tflops": flops / t / 1e12}
+
+
 def run_transforms(args):
     """Secondary measurement (not the headline): 16 FP64 fields on the 256^3
     Chebyshev-Gauss grid, forward + backward round trip, FP64 CUDA-core path vs
@@ -672,9 +719,13 @@ def main():
     ap.add_argument("--no-learned", action="store_true", help="mixed solve from a zero start")
     ap.add_argument("--weights", default=os.path.join(
         ROOT, "jaxfun_gb300", "sno", "weights", "sno_varcoef2d_N256.npz"))
-    ap.add_argument("--kernel-only", action="store_true",
-                    help="time only the dominant kernel (tcgen05 contraction, B problems of "
-                         "256^3) and print its numbers; used for ncu captures")
+    ap.add_argument("--kernel-only", nargs="?", const="contract", default=None,
+                    choices=["contract", "gemm", "fp64"],
+                    help="time one kernel and print its numbers (used for ncu captures): "
+                         "contract = tcgen05 split-TF32 contraction, B problems of 256^3; "
+                         "gemm = BF16 GEMM of the neural operator's spectral transform "
+                         "(1024 x 64 x 4096 per sample, B samples); fp64 = FP64 CUDA-core "
+                         "contraction at the variable-coefficient pass shape")
     ap.add_argument("--config", default="varcoef2d",
                     choices=["varcoef2d", "transforms", "helmholtz", "varcoef3d"],
                     help="varcoef2d: the headline; transforms: batched 3-D Chebyshev "
@@ -700,8 +751,11 @@ def main():
         import torch
 
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-        print(json.dumps({"kernel": "k_contract_tc", "batch": args.batch,
-                          **roofline_microbench(args.batch, N_GRID, reps=3)}), flush=True)
+        if args.kernel_only == "contract":
+            out = {"kernel": "k_contract_tc", **roofline_microbench(args.batch, N_GRID, reps=3)}
+        else:
+            out = other_kernel_microbench(args.kernel_only, args.batch)
+        print(json.dumps({"batch": args.batch, **out}), flush=True)
         return 0
     return run_ours(args)
 
