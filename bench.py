@@ -32,6 +32,9 @@ sys.path.insert(0, ROOT)
 
 METRIC = "var-coef solves/s at 1e-10 err: learned+mixed vs plain FP64 PCG, 1 GB300"
 N_GRID = 256
+# DRAM bytes (read + write) of one k_contract_tc launch at M = 512, P = K = 256,
+# 128 problems, from ncu (dram__bytes_read.sum + dram__bytes_write.sum).
+TC_TRAFFIC_PER_LAUNCH_B128 = 34.662912e6 + 9.000960e6
 
 
 def peaks():
@@ -208,10 +211,12 @@ def run_reference(args):
 # ---------------------------------------------------------------------------
 
 
-def roofline_microbench(B: int, N: int, reps: int = 20):
+def roofline_microbench(B: int, N: int, reps: int = 20, M: int | None = None):
     """Time the dominant kernel -- the tcgen05 split-TF32 contraction at the
-    variable-coefficient pass shape (M = P = K = N per problem, B problems) --
-    with CUDA events on its launch stream.  Returns achieved numbers."""
+    first variable-coefficient pass shape of the inner solve (stacked [B; D]
+    operator: M = 2N quadrature rows, P = K = N padded coefficients, B problems;
+    M = N gives the preconditioner pass) -- with CUDA events on its launch
+    stream.  Returns achieved numbers; FLOPs count each contraction once."""
     import numpy as np
     import torch
 
@@ -219,7 +224,8 @@ def roofline_microbench(B: int, N: int, reps: int = 20):
     from jaxfun_gb300.la import split_tf32
 
     L = _lib.lib()
-    M = P = K = N
+    P = K = N
+    M = 2 * N if M is None else M
     rng = np.random.default_rng(0)
     hi, lo = split_tf32(rng.standard_normal((M, K)))
     x = torch.randn(B, P, K, dtype=torch.float32, device="cuda")
@@ -241,12 +247,14 @@ def roofline_microbench(B: int, N: int, reps: int = 20):
     t = e0.elapsed_time(e1) / 1e3 / reps
     flops = 2.0 * M * P * K * B
     nbytes = 4.0 * B * P * (K + M)
-    return {"t": t, "flops": flops, "bytes": nbytes, "tflops_alg": flops / t / 1e12,
+    return {"M": M, "P": P, "K": K, "t": t, "flops": flops, "bytes": nbytes,
+            "tflops_alg": flops / t / 1e12,
             "tflops_issued": 3 * flops / t / 1e12, "gbs": nbytes / t / 1e9}
 
 
 def other_kernel_microbench(which: str, B: int, reps: int = 3):
-    """CUDA-event timing of the BF16 GEMM ('gemm') or the FP64 contraction ('fp64')."""
+    """CUDA-event timing of the BF16 GEMM ('gemm'), the FP64 contraction ('fp64') or
+    its double-FP32 counterpart ('df64')."""
     import ctypes
 
     import torch
@@ -275,10 +283,11 @@ def other_kernel_microbench(which: str, B: int, reps: int = 3):
         y = torch.empty(B, M, P, dtype=torch.float64, device="cuda")
         d = _lib.ContractDesc(batch=B, nseg=1, M=M, P=P, K=K, op_ld=K, in_ld=K, in_batch=P * K,
                               out_ld=P, out_batch=M * P, alpha=1.0, beta=0.0)
-        call = lambda: L.jfg_contract_f64(d, op.data_ptr(), x.data_ptr(), y.data_ptr(),  # noqa: E731
-                                          s.cuda_stream)
+        fn = L.jfg_contract_f64 if which == "fp64" else L.jfg_contract_df64
+        call = lambda: fn(d, op.data_ptr(), x.data_ptr(), y.data_ptr(),  # noqa: E731
+                          s.cuda_stream)
         flops = 2.0 * M * P * K * B
-        name = "k_contract_simt<double>"
+        name = "k_contract_simt<double>" if which == "fp64" else "k_contract_df"
     for _ in range(2):
         _lib.check(call(), name)
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -684,12 +693,19 @@ def run_ours(args):
             "e2e": {"value": world * B * e2e_steps / t_e2e, "unit": "solves/s",
                     "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
             "gpu_launches": launches,
-            "roofline": {"bound": "tensor", "achieved": rf["tflops_issued"], "peak": tf32_peak,
-                         "unit": "TFLOP/s", "frac": rf["tflops_issued"] / tf32_peak,
-                         "traffic": None,
+            "roofline": {"bound": "tensor", "achieved": rf["tflops_alg"], "peak": tf32_peak,
+                         "unit": "TFLOP/s", "frac": rf["tflops_alg"] / tf32_peak,
+                         "traffic": (None if TC_TRAFFIC_PER_LAUNCH_B128 is None
+                                     else TC_TRAFFIC_PER_LAUNCH_B128 * B / 128),
+                         "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of "
+                                           "one launch at this shape with 128 problems, scaled "
+                                           "by problems per launch",
                          "kernel": "k_contract_tc (tcgen05 kind::tf32, 3 MMAs per K block)",
-                         "launch_us": 1e6 * rf["t"], "tflops_algorithmic": rf["tflops_alg"],
-                         "hbm_gbs_algorithmic": rf["gbs"],
+                         "launch_shape": {"M": rf["M"], "P": rf["P"], "K": rf["K"], "batch": B},
+                         "launch_us": 1e6 * rf["t"], "flops_per_launch": rf["flops"],
+                         "issued_tflops": rf["tflops_issued"],
+                         "issued_frac": rf["tflops_issued"] / tf32_peak,
+                         "bytes_per_launch": rf["bytes"], "hbm_gbs_algorithmic": rf["gbs"],
                          "hbm_frac": rf["gbs"] / pk["hbm_gbs"],
                          "peak_kind": f"{pk_kind} bf16 burst / 2 (dense TF32 rate)"},
             "clocks": clocks,
@@ -720,12 +736,13 @@ def main():
     ap.add_argument("--weights", default=os.path.join(
         ROOT, "jaxfun_gb300", "sno", "weights", "sno_varcoef2d_N256.npz"))
     ap.add_argument("--kernel-only", nargs="?", const="contract", default=None,
-                    choices=["contract", "gemm", "fp64"],
+                    choices=["contract", "gemm", "fp64", "df64"],
                     help="time one kernel and print its numbers (used for ncu captures): "
                          "contract = tcgen05 split-TF32 contraction, B problems of 256^3; "
                          "gemm = BF16 GEMM of the neural operator's spectral transform "
                          "(1024 x 64 x 4096 per sample, B samples); fp64 = FP64 CUDA-core "
-                         "contraction at the variable-coefficient pass shape")
+                         "contraction at the variable-coefficient pass shape; df64 = the same "
+                         "pass in double-FP32 arithmetic")
     ap.add_argument("--config", default="varcoef2d",
                     choices=["varcoef2d", "transforms", "helmholtz", "varcoef3d"],
                     help="varcoef2d: the headline; transforms: batched 3-D Chebyshev "

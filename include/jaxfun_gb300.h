@@ -71,6 +71,13 @@ typedef struct {
   const void* c0;    /* (batch)  */
   const void* c1;    /* (batch)  */
   double alpha, beta;
+  /* Optional active subset (device pointers; NULL = every problem): only
+   * problems b = batch_list[j], j < *batch_count <= batch, are computed.  The
+   * kernels read *batch_count and the list when they start, so a list that an
+   * earlier kernel on the stream rebuilt (also inside a captured graph) takes
+   * effect without the host.  Entries outside [0, batch) are skipped. */
+  const int* batch_list;
+  const int* batch_count;
 } jfg_contract_desc;
 
 /* ---- library ----------------------------------------------------------- */
@@ -98,6 +105,12 @@ int jfg_contract_f64(const jfg_contract_desc* d, const double* op, const double*
                      double* out, void* stream);
 int jfg_contract_f32(const jfg_contract_desc* d, const float* op, const float* in,
                      float* out, void* stream);
+/* FP64 in/out, computed in double-FP32 arithmetic on the FP32 units: operands
+ * split into hi + lo FP32 pairs, error-free products (FMA) and TwoSum
+ * accumulation, ~2^-46 relative error per product (FP64: 2^-53).  Used for the
+ * refinement residual, where GB300's FP64 rate would dominate. */
+int jfg_contract_df64(const jfg_contract_desc* d, const double* op, const double* in,
+                      double* out, void* stream);
 
 /*
  * Tensor-core contraction (tcgen05, TMA, TMEM accumulators): three-term
@@ -332,6 +345,8 @@ typedef struct {
   const float* fd_scale; /* (batch) or NULL                                        */
   const float* ops32;    /* packed padded operators rounded to FP32, or NULL: used for
                             r -= ||r|| A d once ||r|| <= 1e-4 ||rhs|| (else FP64 r = b - A x) */
+  int residual;          /* arithmetic of r = b - A x: 0 FP64 (DFMA), 1 double-FP32
+                            (jfg_contract_df64 passes)                                */
 } jfg_mixed_plan;
 
 size_t jfg_pcg_mixed_workspace_size(int ndim, int n, int nq, int batch);

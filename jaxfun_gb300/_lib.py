@@ -54,6 +54,7 @@ class ContractDesc(C.Structure):
         ("field_ld", C.c_longlong), ("field_seg", C.c_longlong), ("field_batch", C.c_longlong),
         ("lam_m", C.c_void_p), ("lam_p", C.c_void_p), ("c0", C.c_void_p), ("c1", C.c_void_p),
         ("alpha", C.c_double), ("beta", C.c_double),
+        ("batch_list", C.c_void_p), ("batch_count", C.c_void_p),
     ]
 
 
@@ -73,6 +74,7 @@ SIGNATURES = {
     "jfg_weighted_field_f64": (_i, [_i, _i, _i, _vp, _vp, _vp, _vp, _vp]),
     "jfg_contract_f64": (_i, [C.POINTER(ContractDesc), _vp, _vp, _vp, _vp]),
     "jfg_contract_f32": (_i, [C.POINTER(ContractDesc), _vp, _vp, _vp, _vp]),
+    "jfg_contract_df64": (_i, [C.POINTER(ContractDesc), _vp, _vp, _vp, _vp]),
     "jfg_contract_tc": (_i, [C.POINTER(ContractDesc), _vp, _vp, _vp, _vp, _vp]),
     "jfg_split_tf32_host": (None, [_sz, _vp, _vp, _vp]),
     "jfg_tc_set_variant": (_i, [_i]),

@@ -27,8 +27,11 @@ __global__ void __launch_bounds__(NT)
   __shared__ T Bs[TK][TP + 4];
 
   const int bz = blockIdx.z;
-  const int b = bz / d.nseg;
-  const int s = bz - b * d.nseg;
+  const int slot = bz / d.nseg;
+  const int s = bz - slot * d.nseg;
+  const int b = active_problem(d.batch_list, active_count(d.batch_list, d.batch_count, d.batch),
+                               d.batch, slot);
+  if (b < 0) return;
   const int m0 = blockIdx.y * TM;
   const int p0 = blockIdx.x * TP;
   const T* opS = op + (long long)s * d.op_seg;
@@ -140,6 +143,7 @@ int validate_desc(const jfg_contract_desc& d) {
   if (d.epilogue == JFG_EPI_MUL_FIELD && (!d.field || d.field_ld < d.P)) return JFG_ERR_ARG;
   if (d.epilogue == JFG_EPI_DIV_EIG && (!d.lam_m || !d.lam_p)) return JFG_ERR_ARG;
   if (d.epilogue < 0 || d.epilogue > 2) return JFG_ERR_ARG;
+  if ((d.batch_list == nullptr) != (d.batch_count == nullptr)) return JFG_ERR_ARG;
   return JFG_OK;
 }
 

@@ -240,7 +240,10 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   const int nkb = (d.K + KB - 1) / KB;
   const int nptiles = (d.P + TILE_P - 1) / TILE_P;
   const int mchunks = (d.M + Mt - 1) / Mt;
-  const long long ntiles = (long long)nptiles * mchunks * d.batch * d.nseg;
+  // problems of this launch: the whole batch, or the active list's count
+  const int nb = active_count(d.batch_list, d.batch_count, d.batch);
+  const long long ntiles = (long long)nptiles * mchunks * nb * d.nseg;
+  if ((long long)blockIdx.x >= ntiles) return;  // no tile for this CTA (uniform)
 
   if (threadIdx.x == 0) {
     for (int i = 0; i < S; ++i) {
@@ -270,13 +273,15 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   auto Xl = [&](int st) { return smem + (size_t)st * stage_bytes + XBYTES; };
   auto Oh = [&](int st) { return smem + (size_t)st * stage_bytes + xbuf; };
   auto Ol = [&](int st) { return smem + (size_t)st * stage_bytes + xbuf + obytes; };
+  // b = problem index (-1: an out-of-range list entry, computed but not stored)
   auto decode = [&](long long t, int& pt, int& mc, int& b, int& s) {
     pt = (int)(t % nptiles);
     long long r = t / nptiles;
     mc = (int)(r % mchunks);
     const int bs = (int)(r / mchunks);
-    b = bs / d.nseg;
-    s = bs - b * d.nseg;
+    const int slot = bs / d.nseg;
+    s = bs - slot * d.nseg;
+    b = active_problem(d.batch_list, nb, d.batch, slot);
   };
 
   if (warp == 0) {
@@ -288,7 +293,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         int pt, mc, b, s;
         decode(t, pt, mc, b, s);
         const int cs = prm.seg_in_map ? s : 0;
-        const int cb = prm.bat_in_map ? b : 0;
+        const int cb = (prm.bat_in_map && b > 0) ? b : 0;
         const int os = prm.seg_op_map ? s : 0;
         for (int kb = 0; kb < nkb; ++kb, ++g) {
           const int st = (int)(g % S);
@@ -421,18 +426,19 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       if (!mbar_wait(&tfull[buf], (uint32_t)(li >> 1) & 1u)) break;
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       const int p = pt * TILE_P + row;
-      const bool pin = p < d.P;
-      float* outS = out + (long long)b * d.out_batch + (long long)s * d.out_seg;
+      const bool pin = p < d.P && b >= 0;
+      const int bb = b < 0 ? 0 : b;
+      float* outS = out + (long long)bb * d.out_batch + (long long)s * d.out_seg;
       float c0 = 0.f, c1 = 1.f, lp = 0.f;
       const float* __restrict__ lam_m = (const float*)d.lam_m;
       if (EPI == JFG_EPI_DIV_EIG) {
-        c0 = d.c0 ? __ldg((const float*)d.c0 + b) : 0.f;
-        c1 = d.c1 ? __ldg((const float*)d.c1 + b) : 1.f;
+        c0 = d.c0 ? __ldg((const float*)d.c0 + bb) : 0.f;
+        c1 = d.c1 ? __ldg((const float*)d.c1 + bb) : 1.f;
         lp = pin ? __ldg((const float*)d.lam_p + p) : 0.f;
       }
       const float* __restrict__ fld = nullptr;
       if (EPI == JFG_EPI_MUL_FIELD)
-        fld = (const float*)d.field + (long long)b * d.field_batch + (long long)s * d.field_seg;
+        fld = (const float*)d.field + (long long)bb * d.field_batch + (long long)s * d.field_seg;
       const uint32_t tacc = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)buf * acc_stride;
       for (int c = half * 2; c < Mt / 16; c += 4) {
         // columns [c*16, c*16+32): two 16-column TMEM loads

@@ -58,18 +58,21 @@ struct OpRef {
 };
 
 // Dispatch of one contraction pass to an engine.
-enum class Engine { F64, F32, TC };
+// DF: FP64 data, double-FP32 arithmetic (contract_df.cu).
+enum class Engine { F64, F32, TC, DF };
 
 int contract_f64(const jfg_contract_desc& d, const double* op, const double* in, double* out,
                  cudaStream_t st);
 int contract_f32(const jfg_contract_desc& d, const float* op, const float* in, float* out,
                  cudaStream_t st);
+int contract_df64(const jfg_contract_desc& d, const double* op, const double* in, double* out,
+                  cudaStream_t st);
 int contract_tc(const jfg_contract_desc& d, const float* op_hi, const float* op_lo,
                 const float* in, float* out, cudaStream_t st);
 
 inline int contract(Engine e, const jfg_contract_desc& d, OpRef<double> op, const double* in,
                     double* out, cudaStream_t st) {
-  (void)e;
+  if (e == Engine::DF) return contract_df64(d, op.hi, in, out, st);
   return contract_f64(d, op.hi, in, out, st);
 }
 inline int contract(Engine e, const jfg_contract_desc& d, OpRef<float> op, const float* in,
@@ -78,9 +81,31 @@ inline int contract(Engine e, const jfg_contract_desc& d, OpRef<float> op, const
   return contract_f32(d, op.hi, in, out, st);
 }
 
+// Optional device-side active subset of a batch (jfg_contract_desc.batch_list).
+struct Active {
+  const int* list = nullptr;
+  const int* count = nullptr;
+};
+
+// Problem index of slot j of a (possibly listed) batch, or -1 when the slot is
+// past the active count or the entry is out of range.  n_active is *count
+// (or batch without a list), read once by the caller.
+__device__ __forceinline__ int active_problem(const int* list, int n_active, int batch, int j) {
+  if (j >= n_active) return -1;
+  const int b = list ? list[j] : j;
+  return (b >= 0 && b < batch) ? b : -1;
+}
+__device__ __forceinline__ int active_count(const int* list, const int* count, int batch) {
+  if (!list) return batch;
+  const int c = *count;
+  return c < 0 ? 0 : (c > batch ? batch : c);
+}
+
 // A zero-initialised descriptor for a single-segment pass with no epilogue.
-inline jfg_contract_desc make_desc(int batch, int M, int P, int K) {
+inline jfg_contract_desc make_desc(int batch, int M, int P, int K, Active act = Active()) {
   jfg_contract_desc d = {};
+  d.batch_list = act.list;
+  d.batch_count = act.count;
   d.batch = batch;
   d.nseg = 1;
   d.M = M;
@@ -107,10 +132,11 @@ int tp_apply(Engine e, int ndim, const int* rows, const int* cols, int batch,
 template <typename T>
 int fd_solve(Engine e, int ndim, int n, int batch, OpRef<T> E, OpRef<T> W, const T* lam,
              const T* c0, const T* c1, const T* rhs, T* out, void* work, size_t work_bytes,
-             cudaStream_t st);
+             cudaStream_t st, Active act = Active());
 template <typename T>
 int varcoef_apply(Engine e, int ndim, int n, int nq, int batch, OpRef<T> ops, const T* kw,
-                  const T* u, T* v, void* work, size_t work_bytes, cudaStream_t st);
+                  const T* u, T* v, void* work, size_t work_bytes, cudaStream_t st,
+                  Active act = Active());
 
 // Read and clear the device status word of the BF16 GEMM kernel.
 int gemm_status_take(int* status);

@@ -191,7 +191,7 @@ extern "C" int jfg_pcg_varcoef_mixed_guess(const jfg_mixed_plan* plan, const dou
   const jfg_mixed_plan& P = *plan;
   if ((P.ndim != 2 && P.ndim != 3) || P.n < 1 || P.nq < P.n || P.batch < 1 || !P.ops64 ||
       !P.kw64 || !P.ops_hi || !P.ops_lo || !P.kw32 || !P.E_hi || !P.E_lo || !P.W_hi ||
-      !P.W_lo || !P.lam)
+      !P.W_lo || !P.lam || (P.residual != 0 && P.residual != 1))
     return JFG_ERR_ARG;
   const int ndim = P.ndim, n = P.n, nq = P.nq, batch = P.batch;
   const MixedLayout Lo = layout(ndim, n, nq, batch);
@@ -249,7 +249,8 @@ extern "C" int jfg_pcg_varcoef_mixed_guess(const jfg_mixed_plan* plan, const dou
     return JFG_OK;
   };
   auto residual = [&]() -> int {
-    JFG_TRY(varcoef_apply<double>(Engine::F64, ndim, n, nq, batch,
+    JFG_TRY(varcoef_apply<double>(P.residual == 1 ? Engine::DF : Engine::F64, ndim, n, nq,
+                                  batch,
                                   OpRef<double>{P.ops64, nullptr}, P.kw64, x, r64, ws64,
                                   Lo.ws64, st));
     k_sub_from64<<<blocks_for(tot64, 4096), 256, 0, st>>>(rhs, r64, tot64);

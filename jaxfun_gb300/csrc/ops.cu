@@ -84,7 +84,7 @@ size_t fd_ws(int ndim, int n, int batch, int eb) {
 template <typename T>
 int fd_solve(Engine e, int ndim, int n, int batch, OpRef<T> E, OpRef<T> W, const T* lam,
              const T* c0, const T* c1, const T* rhs, T* out, void* work, size_t work_bytes,
-             cudaStream_t st) {
+             cudaStream_t st, Active act) {
   if ((ndim != 2 && ndim != 3) || n < 1 || batch < 0 || !E.hi || !W.hi || !lam || !rhs ||
       !out)
     return JFG_ERR_ARG;
@@ -105,7 +105,7 @@ int fd_solve(Engine e, int ndim, int n, int batch, OpRef<T> E, OpRef<T> W, const
   const T* src = rhs;
   int b = 0;
   for (int t = 0; t < 2 * ndim; ++t) {
-    jfg_contract_desc d = make_desc(batch, n, (int)P, n);
+    jfg_contract_desc d = make_desc(batch, n, (int)P, n, act);
     if (t == ndim - 1) {
       d.epilogue = JFG_EPI_DIV_EIG;
       d.lam_m = lam;
@@ -143,7 +143,8 @@ size_t varcoef_ws(int ndim, int n, int nq, int batch, int eb) {
 
 template <typename T>
 int varcoef_apply(Engine e, int ndim, int n, int nq, int batch, OpRef<T> ops, const T* kw,
-                  const T* u, T* v, void* work, size_t work_bytes, cudaStream_t st) {
+                  const T* u, T* v, void* work, size_t work_bytes, cudaStream_t st,
+                  Active act) {
   if ((ndim != 2 && ndim != 3) || n < 1 || nq < 1 || batch < 0 || !ops.hi || !kw || !u || !v)
     return JFG_ERR_ARG;
   const size_t need = varcoef_ws(ndim, n, nq, batch, (int)sizeof(T));
@@ -156,10 +157,10 @@ int varcoef_apply(Engine e, int ndim, int n, int nq, int batch, OpRef<T> ops, co
 
   if (ndim == 2) {
     // 1: T[b][r][j] = sum_l [B;D][r][l] U[b][j][l]            (M=2nq, P=n, K=n)
-    jfg_contract_desc d1 = make_desc(batch, 2 * nq, n, n);
+    jfg_contract_desc d1 = make_desc(batch, 2 * nq, n, n, act);
     JFG_TRY(contract(e, d1, ops, u, bufA, st));
     // 2: G[b][s][p][q] = kw[b][p][q] * sum_j {D,B}[p][j] T[b][s][q][j]
-    jfg_contract_desc d2 = make_desc(batch, nq, nq, n);
+    jfg_contract_desc d2 = make_desc(batch, nq, nq, n, act);
     d2.nseg = 2;
     d2.op_seg = nn;
     d2.in_seg = nn;
@@ -173,7 +174,7 @@ int varcoef_apply(Engine e, int ndim, int n, int nq, int batch, OpRef<T> ops, co
     d2.field_batch = (long long)nq * nq;
     JFG_TRY(contract(e, d2, ops.offset(2 * nn), bufA, bufB, st));
     // 3: H[b][k][s][p] = sum_q {B^T,D^T}[k][q] G[b][s][p][q]   (M=n, P=nq, K=nq)
-    jfg_contract_desc d3 = make_desc(batch, n, nq, nq);
+    jfg_contract_desc d3 = make_desc(batch, n, nq, nq, act);
     d3.nseg = 2;
     d3.op_seg = nn;
     d3.in_seg = (long long)nq * nq;
@@ -183,7 +184,7 @@ int varcoef_apply(Engine e, int ndim, int n, int nq, int batch, OpRef<T> ops, co
     d3.out_batch = 2 * nn;
     JFG_TRY(contract(e, d3, ops.offset(4 * nn), bufB, bufA, st));
     // 4: V[b][i][k] = sum_{s,p} [D^T|B^T][i][(s,p)] H[b][k][(s,p)]   (M=n, P=n, K=2nq)
-    jfg_contract_desc d4 = make_desc(batch, n, n, 2 * nq);
+    jfg_contract_desc d4 = make_desc(batch, n, n, 2 * nq, act);
     JFG_TRY(contract(e, d4, ops.offset(6 * nn), bufA, v, st));
     return JFG_OK;
   }
@@ -194,10 +195,10 @@ int varcoef_apply(Engine e, int ndim, int n, int nq, int batch, OpRef<T> ops, co
   const OpRef<T> Q3 = ops.offset(2 * nn);    // D, B, B
   const OpRef<T> Q4 = ops.offset(5 * nn);    // B^T, B^T, D^T
   // 1: T1[b][(s2,q2)][(i0,i1)] = sum_i2 [B;D] U                 (M=2nq, P=n^2, K=n)
-  jfg_contract_desc d1 = make_desc(batch, 2 * nq, (int)n2, n);
+  jfg_contract_desc d1 = make_desc(batch, 2 * nq, (int)n2, n, act);
   JFG_TRY(contract(e, d1, BD, u, bufA, st));
   // 2a: s2=0 rows with [B;D]: T2[b][(c,q1)][(q2,i0)], c in {0,1}  (M=2nq, P=nq*n, K=n)
-  jfg_contract_desc d2 = make_desc(batch, 2 * nq, (int)nn, n);
+  jfg_contract_desc d2 = make_desc(batch, 2 * nq, (int)nn, n, act);
   d2.in_batch = 2 * nq * n2;
   d2.out_batch = 3 * q2 * n;
   JFG_TRY(contract(e, d2, BD, bufA, bufB, st));
@@ -206,7 +207,7 @@ int varcoef_apply(Engine e, int ndim, int n, int nq, int batch, OpRef<T> ops, co
   d2b.M = nq;
   JFG_TRY(contract(e, d2b, BD, bufA + nq * n2, bufB + 2 * q2 * n, st));
   // 3: G[b][c][p0][(q1,q2)] = kw * sum_i0 {D,B,B}[p0][i0] T2[b][c][(q1,q2)][i0]
-  jfg_contract_desc d3 = make_desc(batch, nq, (int)q2, n);
+  jfg_contract_desc d3 = make_desc(batch, nq, (int)q2, n, act);
   d3.nseg = 3;
   d3.op_seg = nn;
   d3.in_seg = q2 * n;
@@ -220,7 +221,7 @@ int varcoef_apply(Engine e, int ndim, int n, int nq, int batch, OpRef<T> ops, co
   d3.field_batch = q2 * nq;
   JFG_TRY(contract(e, d3, Q3, bufB, bufA, st));
   // 4: H1[b][c][k2][(p0,q1)] = sum_q2 {B^T,B^T,D^T}[k2][q2] G     (M=n, P=nq^2, K=nq)
-  jfg_contract_desc d4 = make_desc(batch, n, (int)q2, nq);
+  jfg_contract_desc d4 = make_desc(batch, n, (int)q2, nq, act);
   d4.nseg = 3;
   d4.op_seg = nn;
   d4.in_seg = q2 * nq;
@@ -231,14 +232,14 @@ int varcoef_apply(Engine e, int ndim, int n, int nq, int batch, OpRef<T> ops, co
   // 5: H2a = B^T (c=0), H2b = D^T (c=1) + B^T (c=2)      (M=n, P=n*nq, K=nq)
   T* H2a = bufA;
   T* H2b = bufA + (size_t)batch * n2 * nq;
-  jfg_contract_desc d5 = make_desc(batch, n, (int)nn, nq);
+  jfg_contract_desc d5 = make_desc(batch, n, (int)nn, nq, act);
   d5.in_batch = 3 * q2 * n;
   JFG_TRY(contract(e, d5, Q4, bufB, H2a, st));
   JFG_TRY(contract(e, d5, Q4.offset(2 * nn), bufB + q2 * n, H2b, st));
   d5.beta = 1.0;
   JFG_TRY(contract(e, d5, Q4, bufB + 2 * q2 * n, H2b, st));
   // 6: V = D^T (x) on H2a + B^T (x) on H2b                 (M=n, P=n^2, K=nq)
-  jfg_contract_desc d6 = make_desc(batch, n, (int)n2, nq);
+  jfg_contract_desc d6 = make_desc(batch, n, (int)n2, nq, act);
   JFG_TRY(contract(e, d6, Q4.offset(2 * nn), H2a, v, st));
   d6.beta = 1.0;
   JFG_TRY(contract(e, d6, Q4, H2b, v, st));
@@ -269,14 +270,14 @@ template int tp_apply<float>(Engine, int, const int*, const int*, int, const OpR
                              const float*, float*, void*, size_t, cudaStream_t);
 template int fd_solve<double>(Engine, int, int, int, OpRef<double>, OpRef<double>,
                               const double*, const double*, const double*, const double*,
-                              double*, void*, size_t, cudaStream_t);
+                              double*, void*, size_t, cudaStream_t, Active);
 template int fd_solve<float>(Engine, int, int, int, OpRef<float>, OpRef<float>, const float*,
                              const float*, const float*, const float*, float*, void*, size_t,
-                             cudaStream_t);
+                             cudaStream_t, Active);
 template int varcoef_apply<double>(Engine, int, int, int, int, OpRef<double>, const double*,
-                                   const double*, double*, void*, size_t, cudaStream_t);
+                                   const double*, double*, void*, size_t, cudaStream_t, Active);
 template int varcoef_apply<float>(Engine, int, int, int, int, OpRef<float>, const float*,
-                                  const float*, float*, void*, size_t, cudaStream_t);
+                                  const float*, float*, void*, size_t, cudaStream_t, Active);
 
 }  // namespace jfg
 

@@ -1,11 +1,15 @@
 // Batched preconditioned conjugate gradients for the variable-coefficient
 // operator with the constant-coefficient fast-diagonalisation preconditioner.
 //
-// Every problem of the batch runs in lock-step; per-problem scalars live on
-// the device as block partial sums (warp-shuffle reductions), so no kernel
-// waits on the host.  A problem that has converged keeps alpha = 0 from then
-// on.  Chunks of iterations are captured once into a CUDA graph and replayed;
-// the host reads one counter (problems still active) per chunk.
+// Per-problem scalars live on the device as block partial sums (warp-shuffle
+// reductions), so no kernel waits on the host.  The problems still iterating
+// form a device-side active list, rebuilt after every iteration by a one-block
+// compaction kernel; every kernel of the iteration (the tensor-core or CUDA-core
+// contraction passes included) reads the list when it starts and works on the
+// listed problems only, so a converged problem costs nothing from then on and
+// the batch pays for the mean iteration count, not the maximum.  Chunks of
+// iterations are captured once into a CUDA graph and replayed; the host reads
+// the active count once per chunk.
 #include <math.h>
 #include <string.h>
 
@@ -40,12 +44,14 @@ __device__ __forceinline__ T block_sum(T v) {
   return v;  // valid in thread 0
 }
 
-// part[b*NB + j] = sum over chunk j of x[b]*y[b]
+// part[b*NB + j] = sum over chunk j of x[b]*y[b]  (listed problems, or all)
 template <typename T>
 __global__ void __launch_bounds__(DOT_T)
     k_dot_part(const T* __restrict__ x, const T* __restrict__ y, long long N,
-               T* __restrict__ part) {
-  const int b = blockIdx.y, j = blockIdx.x;
+               T* __restrict__ part, const int* __restrict__ list, const int* count, int batch) {
+  const int b = active_problem(list, active_count(list, count, batch), batch, blockIdx.y);
+  if (b < 0) return;
+  const int j = blockIdx.x;
   const long long chunk = (N + NB - 1) / NB;
   const long long lo = j * chunk, hi = min(N, lo + chunk);
   const T* xb = x + (long long)b * N;
@@ -74,8 +80,10 @@ template <typename T>
 __global__ void k_update_xr(T* __restrict__ x, T* __restrict__ r, const T* __restrict__ p,
                             const T* __restrict__ q, long long N, const T* __restrict__ pq_part,
                             const T* __restrict__ rz_prev, const T* __restrict__ rz0,
-                            double tol) {
-  const int b = blockIdx.y;
+                            double tol, const int* __restrict__ list, const int* count,
+                            int batch) {
+  const int b = active_problem(list, active_count(list, count, batch), batch, blockIdx.y);
+  if (b < 0) return;
   const T rz = sum_part(rz_prev, b);
   if (!is_active(rz, rz0[b], tol)) return;
   const T pq = sum_part(pq_part, b);
@@ -93,8 +101,9 @@ template <typename T>
 __global__ void k_update_p(T* __restrict__ p, const T* __restrict__ z, long long N,
                            const T* __restrict__ rz_new_part, const T* __restrict__ rz_prev_part,
                            const T* __restrict__ rz0, double tol, int* __restrict__ iters,
-                           int* __restrict__ nactive) {
-  const int b = blockIdx.y;
+                           const int* __restrict__ list, const int* count, int batch) {
+  const int b = active_problem(list, active_count(list, count, batch), batch, blockIdx.y);
+  if (b < 0) return;
   const T rzp = sum_part(rz_prev_part, b);
   if (!is_active(rzp, rz0[b], tol)) return;
   const T rzn = sum_part(rz_new_part, b);
@@ -103,10 +112,44 @@ __global__ void k_update_p(T* __restrict__ p, const T* __restrict__ z, long long
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N;
        i += (long long)gridDim.x * blockDim.x)
     p[off + i] = z[off + i] + beta * p[off + i];
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    iters[b] += 1;
-    if (is_active(rzn, rz0[b], tol)) atomicAdd(nactive, 1);
+  if (blockIdx.x == 0 && threadIdx.x == 0) iters[b] += 1;
+}
+
+// Active list: keep the problems whose r.z is still above tol^2 r0.z0.  With
+// init the candidates are 0..batch-1, else the current list (filtered in
+// place: an entry moves only to a lower slot, after its chunk has been read).
+// One block; the order of the problems is kept.
+constexpr int CMP_T = 256;
+template <typename T>
+__global__ void __launch_bounds__(CMP_T)
+    k_compact(const T* __restrict__ rz_part, const T* __restrict__ rz0, double tol,
+              int* __restrict__ list, int* __restrict__ count, int batch, int init) {
+  __shared__ int wcnt[CMP_T / 32];
+  __shared__ int base;
+  const int n = init ? batch : active_count(list, count, batch);
+  if (threadIdx.x == 0) base = 0;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int j0 = 0; j0 < n; j0 += CMP_T) {
+    const int j = j0 + threadIdx.x;
+    int b = -1;
+    if (j < n) b = init ? j : list[j];
+    const bool keep = b >= 0 && b < batch && is_active(sum_part(rz_part, b), rz0[b], tol);
+    const unsigned m = __ballot_sync(0xffffffffu, keep);
+    if (lane == 0) wcnt[w] = __popc(m);
+    __syncthreads();  // every list[j] of this chunk has been read
+    int off = base + __popc(m & ((1u << lane) - 1u));
+    for (int i = 0; i < w; ++i) off += wcnt[i];
+    if (keep) list[off] = b;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int t = 0;
+      for (int i = 0; i < CMP_T / 32; ++i) t += wcnt[i];
+      base += t;
+    }
+    __syncthreads();
   }
+  if (threadIdx.x == 0) *count = base;
 }
 
 template <typename T>
@@ -166,7 +209,7 @@ size_t pcg_ws(int ndim, int n, int nq, int batch) {
   const size_t vec = align_up((size_t)N * batch * sizeof(T), 256);
   const size_t scal = align_up((size_t)batch * NB * sizeof(T), 256);
   const size_t small = align_up((size_t)batch * sizeof(T), 256) +
-                       align_up((size_t)batch * sizeof(int), 256) + 256;
+                       2 * align_up((size_t)batch * sizeof(int), 256) + 256;
   size_t inner = varcoef_ws(ndim, n, nq, batch, sizeof(T));
   const size_t f = fd_ws(ndim, n, batch, sizeof(T));
   if (f > inner) inner = f;
@@ -199,19 +242,20 @@ int pcg_run(const PcgProblem<T>& pb, T* x, int use_x0, double tol, int maxiter, 
   char* sm = w + 4 * vec + 3 * scal;
   T* rz0 = (T*)sm;
   int* iters = (int*)(sm + align_up((size_t)batch * sizeof(T), 256));
-  int* nactive = (int*)(sm + align_up((size_t)batch * sizeof(T), 256) +
-                        align_up((size_t)batch * sizeof(int), 256));
-  void* inner = w + 4 * vec + 3 * scal + align_up((size_t)batch * sizeof(T), 256) +
-                align_up((size_t)batch * sizeof(int), 256) + 256;
+  int* alist = (int*)(sm + align_up((size_t)batch * sizeof(T), 256) +
+                      align_up((size_t)batch * sizeof(int), 256));
+  int* nactive = (int*)((char*)alist + align_up((size_t)batch * sizeof(int), 256));
+  void* inner = (char*)nactive + 256;
   const size_t inner_bytes = work_bytes - (size_t)((char*)inner - w);
 
-  auto applyA = [&](const T* in, T* out) -> int {
+  const Active all, act{alist, nactive};
+  auto applyA = [&](const T* in, T* out, Active a) -> int {
     return varcoef_apply<T>(pb.engine, ndim, n, nq, batch, pb.ops, pb.kw, in, out, inner,
-                            inner_bytes, st);
+                            inner_bytes, st, a);
   };
-  auto applyM = [&](const T* in, T* out) -> int {
+  auto applyM = [&](const T* in, T* out, Active a) -> int {
     return fd_solve<T>(pb.engine, ndim, n, batch, pb.E, pb.W, pb.lam, nullptr, pb.fd_scale, in,
-                       out, inner, inner_bytes, st);
+                       out, inner, inner_bytes, st, a);
   };
 
   const int vb = vec_blocks(N);
@@ -222,22 +266,22 @@ int pcg_run(const PcgProblem<T>& pb, T* x, int use_x0, double tol, int maxiter, 
   // ---- setup: r = rhs - A x (or x = 0, r = rhs); z = M^-1 r; p = z
   JFG_CUDA_TRY(cudaMemsetAsync(iters, 0, sizeof(int) * batch, st));
   if (use_x0) {
-    JFG_TRY(applyA(x, r));
+    JFG_TRY(applyA(x, r, all));
     k_sub_from<T><<<vec_blocks(total), 256, 0, st>>>(pb.rhs, r, total);
     JFG_LAUNCHED();
   } else {
     JFG_CUDA_TRY(cudaMemsetAsync(x, 0, sizeof(T) * total, st));
     JFG_CUDA_TRY(cudaMemcpyAsync(r, pb.rhs, sizeof(T) * total, cudaMemcpyDeviceToDevice, st));
   }
-  JFG_TRY(applyM(r, z));
-  k_dot_part<T><<<dgrid, DOT_T, 0, st>>>(r, z, N, rz_part[1]);
+  JFG_TRY(applyM(r, z, all));
+  k_dot_part<T><<<dgrid, DOT_T, 0, st>>>(r, z, N, rz_part[1], nullptr, nullptr, batch);
   JFG_LAUNCHED();
   if (use_x0 && pb.judge_x0) {
     // Judge the initial guess against the zero start: keep it only where its
     // preconditioned residual is smaller than that of the right-hand side,
     // and measure convergence relative to the right-hand side either way.
-    JFG_TRY(applyM(pb.rhs, q));
-    k_dot_part<T><<<dgrid, DOT_T, 0, st>>>(pb.rhs, q, N, pq_part);
+    JFG_TRY(applyM(pb.rhs, q, all));
+    k_dot_part<T><<<dgrid, DOT_T, 0, st>>>(pb.rhs, q, N, pq_part, nullptr, nullptr, batch);
     JFG_LAUNCHED();
     k_judge_guess<T><<<vgrid, 256, 0, st>>>(x, r, z, pb.rhs, q, N, rz_part[1], pq_part);
     JFG_LAUNCHED();
@@ -250,20 +294,25 @@ int pcg_run(const PcgProblem<T>& pb, T* x, int use_x0, double tol, int maxiter, 
     JFG_LAUNCHED();
   }
   JFG_CUDA_TRY(cudaMemcpyAsync(p, z, sizeof(T) * total, cudaMemcpyDeviceToDevice, st));
+  // the problems that start active (r0.z0 > 0)
+  k_compact<T><<<1, CMP_T, 0, st>>>(rz_part[1], rz0, tol, alist, nactive, batch, 1);
+  JFG_LAUNCHED();
 
-  auto iteration = [&](int it, bool reset_counter) -> int {
+  auto iteration = [&](int it) -> int {
     const int prev = (it + 1) & 1, cur = it & 1;
-    JFG_TRY(applyA(p, q));
-    k_dot_part<T><<<dgrid, DOT_T, 0, st>>>(p, q, N, pq_part);
+    JFG_TRY(applyA(p, q, act));
+    k_dot_part<T><<<dgrid, DOT_T, 0, st>>>(p, q, N, pq_part, alist, nactive, batch);
     JFG_LAUNCHED();
-    k_update_xr<T><<<vgrid, 256, 0, st>>>(x, r, p, q, N, pq_part, rz_part[prev], rz0, tol);
+    k_update_xr<T><<<vgrid, 256, 0, st>>>(x, r, p, q, N, pq_part, rz_part[prev], rz0, tol, alist,
+                                          nactive, batch);
     JFG_LAUNCHED();
-    JFG_TRY(applyM(r, z));
-    k_dot_part<T><<<dgrid, DOT_T, 0, st>>>(r, z, N, rz_part[cur]);
+    JFG_TRY(applyM(r, z, act));
+    k_dot_part<T><<<dgrid, DOT_T, 0, st>>>(r, z, N, rz_part[cur], alist, nactive, batch);
     JFG_LAUNCHED();
-    if (reset_counter) JFG_CUDA_TRY(cudaMemsetAsync(nactive, 0, sizeof(int), st));
     k_update_p<T><<<vgrid, 256, 0, st>>>(p, z, N, rz_part[cur], rz_part[prev], rz0, tol, iters,
-                                         nactive);
+                                         alist, nactive, batch);
+    JFG_LAUNCHED();
+    k_compact<T><<<1, CMP_T, 0, st>>>(rz_part[cur], rz0, tol, alist, nactive, batch, 0);
     JFG_LAUNCHED();
     return JFG_OK;
   };
@@ -279,7 +328,7 @@ int pcg_run(const PcgProblem<T>& pb, T* x, int use_x0, double tol, int maxiter, 
     JFG_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     set_capturing(true);
     int s = JFG_OK;
-    for (int i = 0; i < CH && s == JFG_OK; ++i) s = iteration(i, i == CH - 1);
+    for (int i = 0; i < CH && s == JFG_OK; ++i) s = iteration(i);
     set_capturing(false);
     cudaError_t ec = cudaStreamEndCapture(st, &graph);
     if (s != JFG_OK) {
@@ -319,7 +368,7 @@ int pcg_run(const PcgProblem<T>& pb, T* x, int use_x0, double tol, int maxiter, 
     } else {
       const int todo = (maxiter - done_iters < CH) ? maxiter - done_iters : CH;
       for (int i = 0; i < todo && status == JFG_OK; ++i)
-        status = iteration(done_iters + i, i == todo - 1);
+        status = iteration(done_iters + i);
       if (status != JFG_OK) break;
       done_iters += todo;
     }

@@ -26,6 +26,7 @@ class MixedPlan(C.Structure):
         ("ops_hi", C.c_void_p), ("ops_lo", C.c_void_p), ("kw32", C.c_void_p),
         ("E_hi", C.c_void_p), ("E_lo", C.c_void_p), ("W_hi", C.c_void_p), ("W_lo", C.c_void_p),
         ("lam", C.c_void_p), ("fd_scale", C.c_void_p), ("ops32", C.c_void_p),
+        ("residual", C.c_int),
     ]
 
 
@@ -48,7 +49,12 @@ def _pad(M: np.ndarray, rows: int, cols: int) -> np.ndarray:
 class MixedVarCoefSolver:
     """Solve A(kappa_b) x_b = rhs_b for a batch with the mixed-precision path."""
 
-    def __init__(self, A: VarCoefMatrix, M: TPMatricesLUFactors | None = None):
+    def __init__(self, A: VarCoefMatrix, M: TPMatricesLUFactors | None = None,
+                 residual: str = "df64"):
+        """``residual``: arithmetic of the refinement residual r = b - A x,
+        "df64" (double-FP32 on the FP32 units) or "f64" (FP64 FMAs)."""
+        if residual not in ("df64", "f64"):
+            raise ValueError(f"residual must be 'df64' or 'f64', not {residual!r}")
         self.A = A
         nd, n, nq = A.ndim, A.n, A.nq
         s0 = A.T.basespaces[0]
@@ -68,7 +74,7 @@ class MixedVarCoefSolver:
                               self.ops_hi.data_ptr(), self.ops_lo.data_ptr(),
                               self.kw32.data_ptr(), self.E_hi.data_ptr(), self.E_lo.data_ptr(),
                               self.W_hi.data_ptr(), self.W_lo.data_ptr(), self.lam.data_ptr(),
-                              None, self.ops32.data_ptr())
+                              None, self.ops32.data_ptr(), 1 if residual == "df64" else 0)
 
     def workspace_bytes(self) -> int:
         A = self.A
