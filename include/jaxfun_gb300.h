@@ -126,6 +126,36 @@ int jfg_contract_tc(const jfg_contract_desc* d, const float* op_hi, const float*
  * (MMA operand A) in TMEM, written by the split warps with tcgen05.st, so the
  * MMAs read only operand B from shared memory; 0 keeps A in shared memory. */
 int jfg_tc_set_variant(int operand_a_in_tmem);
+/* Launch configuration of the tensor-core contraction. */
+typedef struct {
+  int operand_a_in_tmem; /* 1: split input tile in TMEM; 0: in shared memory          */
+  int order;             /* grouped launches: 0 groups as given, 1 by operator-tile
+                            work, 2 by total work (largest first)                    */
+  int ctas;              /* persistent CTAs (0: one per SM)                          */
+  int stages;            /* pipeline stages (0: as many as fit, else >= 2)           */
+} jfg_tc_config;
+/*
+ * Grouped tensor-core contraction: ngroups independent contractions (each a
+ * jfg_contract_desc with its own shapes, batch and pointers; one epilogue kind
+ * and beta != 0 either for all or for none) run in ONE persistent launch (per
+ * 40 groups) whose CTAs walk the tiles of all groups -- e.g. the per-axis
+ * passes of many fast-diagonalisation solves of uneven N.  cfg NULL: the
+ * configuration jfg_tc_autotune chose for this signature, else the default.
+ */
+int jfg_contract_tc_grouped(int ngroups, const jfg_contract_desc* descs,
+                            const float* const* op_hi, const float* const* op_lo,
+                            const float* const* in, float* const* out,
+                            const jfg_tc_config* cfg, void* stream);
+/*
+ * Autotuner: times every candidate configuration (operand A in TMEM or shared
+ * memory x group order x pipeline depth) of the grouped contraction on the
+ * given operands with CUDA events (reps launches each; the contraction runs,
+ * so out is written), keeps the fastest for this launch signature (shapes,
+ * batches, epilogue) and returns it with its time.  Not during stream capture.
+ */
+int jfg_tc_autotune(int ngroups, const jfg_contract_desc* descs, const float* const* op_hi,
+                    const float* const* op_lo, const float* const* in, float* const* out,
+                    int reps, jfg_tc_config* best, float* best_ms, void* stream);
 /* Split n FP64 values into TF32 hi (round to nearest) and FP32 lo = x - hi
  * (host arrays), the operator format jfg_contract_tc expects. */
 void jfg_split_tf32_host(size_t n, const double* src, float* hi, float* lo);
@@ -197,13 +227,37 @@ int jfg_helmholtz_apply_f64(int family, int n, int batch, const double* alpha2, 
  * the tensor cores in the padded layout (nq >= n, nq % 4 == 0; E/W padded
  * with zeros, lam32 with ones) with D = alpha2_32[b] + lam_i + lam_j.
  * refinements (host, may be NULL) receives per-problem correction counts.
- * Uneven batches are solved group by group (one call per size). */
+ * (jfg_helmholtz_solve_grouped solves uneven batches in one call.) */
 size_t jfg_helmholtz_solve_workspace_size(int n, int nq, int batch);
 int jfg_helmholtz_solve_mixed(int family, int n, int nq, int batch, const float* E_hi,
                               const float* E_lo, const float* W_hi, const float* W_lo,
                               const float* lam32, const double* alpha2, const float* alpha2_32,
                               const double* rhs, double* x, double tol, int max_refine,
                               int* refinements, void* work, size_t work_bytes, void* stream);
+
+/*
+ * The same refinement for an uneven batch in ONE call: ngroups size groups
+ * (group g: batch[g] problems of n[g] = N_g - 2 unknowns per axis, padded
+ * nq[g] % 4 == 0, its own FD factors E/W/lam32).  rhs, x (FP64) and alpha2,
+ * alpha2_32 (per problem) are group-major and flat: problem k of group g
+ * follows the earlier problems, n[g]^2 values each.  Each refinement step is
+ * four grouped persistent tensor-core launches over all groups
+ * (jfg_contract_tc_grouped with cfg, NULL = default), ragged FP32 pad/axpy
+ * kernels and the structured FP64 residual over all lines; every per-problem
+ * scalar stays on the device, the step is captured once into a CUDA graph and
+ * replayed until no problem has ||r_b|| > tol ||b_b||.  Stands in for calling
+ * TPMatrices.solve (src/jaxfun/la/tpmatrix.py:429-509) once per problem.
+ */
+size_t jfg_helmholtz_grouped_workspace_size(int ngroups, const int* n, const int* nq,
+                                            const int* batch);
+int jfg_helmholtz_solve_grouped(int family, int ngroups, const int* n, const int* nq,
+                                const int* batch, const float* const* E_hi,
+                                const float* const* E_lo, const float* const* W_hi,
+                                const float* const* W_lo, const float* const* lam32,
+                                const double* alpha2, const float* alpha2_32, const double* rhs,
+                                double* x, double tol, int max_refine, int* refinements,
+                                const jfg_tc_config* cfg, void* work, size_t work_bytes,
+                                void* stream);
 
 /*
  * jfg_fd_solve_f64 without a workspace argument: for callers that cannot

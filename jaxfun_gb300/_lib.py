@@ -43,6 +43,11 @@ class NotConvergedError(JfgError):
     pass
 
 
+class TcConfig(C.Structure):
+    _fields_ = [("operand_a_in_tmem", C.c_int), ("order", C.c_int), ("ctas", C.c_int),
+                ("stages", C.c_int)]
+
+
 class ContractDesc(C.Structure):
     _fields_ = [
         ("batch", C.c_int), ("nseg", C.c_int), ("M", C.c_int), ("P", C.c_int), ("K", C.c_int),
@@ -76,6 +81,8 @@ SIGNATURES = {
     "jfg_contract_f32": (_i, [C.POINTER(ContractDesc), _vp, _vp, _vp, _vp]),
     "jfg_contract_df64": (_i, [C.POINTER(ContractDesc), _vp, _vp, _vp, _vp]),
     "jfg_contract_tc": (_i, [C.POINTER(ContractDesc), _vp, _vp, _vp, _vp, _vp]),
+    "jfg_contract_tc_grouped": (_i, [_i, C.POINTER(ContractDesc), _vp, _vp, _vp, _vp, _vp, _vp]),
+    "jfg_tc_autotune": (_i, [_i, C.POINTER(ContractDesc), _vp, _vp, _vp, _vp, _i, _vp, _vp, _vp]),
     "jfg_split_tf32_host": (None, [_sz, _vp, _vp, _vp]),
     "jfg_tc_set_variant": (_i, [_i]),
     "jfg_device_status": (_i, []),
@@ -94,6 +101,9 @@ SIGNATURES = {
     "jfg_helmholtz_workspace_size": (_sz, [_i, _i]),
     "jfg_helmholtz_apply_f64": (_i, [_i, _i, _i, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
     "jfg_helmholtz_solve_workspace_size": (_sz, [_i, _i, _i]),
+    "jfg_helmholtz_grouped_workspace_size": (_sz, [_i, _vp, _vp, _vp]),
+    "jfg_helmholtz_solve_grouped": (_i, [_i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
+                                         _vp, _vp, _vp, _d, _i, _vp, _vp, _vp, _sz, _vp]),
     "jfg_helmholtz_solve_mixed": (_i, [_i, _i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp,
                                        _vp, _d, _i, C.POINTER(_i), _vp, _sz, _vp]),
     "jfg_fd_solve_noalloc_max_bytes": (_sz, []),

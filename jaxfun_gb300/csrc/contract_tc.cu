@@ -27,6 +27,12 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <algorithm>
+#include <map>
+#include <mutex>
+#include <string>
+#include <vector>
+
 #include "jfg_internal.cuh"
 
 namespace jfg {
@@ -46,15 +52,29 @@ constexpr int NTHREADS = 448;  // 14 warps
 constexpr uint32_t XBYTES = TILE_P * KB * 4;  // 16 KB
 constexpr unsigned long long WAIT_NS = 2000000000ull;  // 2 s budget per wait
 
-struct TcParams {
+constexpr int GMAX = 40;  // groups per launch of the grouped kernel
+
+// One group of problems of a (grouped) launch.
+struct TcGroup {
   jfg_contract_desc d;
-  int Mtile;       // padded operator rows per CTA (multiple of 16, <= 256)
-  int stages;
-  int tmem_cols;
+  float* out;
+  int Mtile;       // padded operator rows per tile (multiple of 16, <= MT_MAX)
   int seg_in_map;  // 1 if the input map has a segment dimension
   int bat_in_map;  // 1 if the input map has a batch dimension
   int seg_op_map;  // 1 if the operator maps have a segment dimension
-  int tmem_a;      // 1: split input tile (MMA operand A) kept in TMEM, not shared memory
+};
+
+// Kernel parameter block (__grid_constant__): groups and their tensor maps
+// (input X, operator hi, operator lo).
+template <int G>
+struct TcLaunch {
+  CUtensorMap maps[G][3];
+  TcGroup g[G];
+  int ngroups;
+  int stages;
+  int tmem_cols;
+  int tmem_a;   // 1: split input tile (MMA operand A) kept in TMEM, not shared memory
+  int mt_max;   // largest Mtile: sets the stage layout
 };
 
 // TMEM column map when operand A lives in TMEM: accumulator buffers at
@@ -209,25 +229,44 @@ __device__ __forceinline__ float tf32_hi(float x) {
   return __uint_as_float(__float_as_uint(x) & 0xFFFFE000u);
 }
 
-// Persistent kernel: each CTA walks the tiles blockIdx.x, blockIdx.x + gridDim.x, ...
-// Tile t = ((bs * mchunks) + mc) * nptiles + pt covers p rows [pt*128, +128) and
-// operator rows [mc*Mt, +Mt) of segment/batch bs.  Two TMEM accumulator buffers
-// let the epilogue of tile i overlap the main loop of tile i+1.
-template <int EPI, bool BETA>
+// Persistent kernel over one or more groups of problems.  Group gi has its own
+// descriptor, operator tile height Mtile and tensor maps; its tiles are
+// t = tb[gi] + ((slot * nseg + s) * mchunks + mc) * nptiles + pt, covering p rows
+// [pt*128, +128) and operator rows [mc*Mtile, +Mtile) of problem slot / segment
+// s.  Each CTA walks t = blockIdx.x, blockIdx.x + gridDim.x, ...; two TMEM
+// accumulator buffers let the epilogue of tile i overlap the main loop of
+// tile i+1.  The tile prefix tb[] is formed on the device from the active
+// counts, so listed (active-subset) groups need no host round trip.
+template <int EPI, bool BETA, int G>
 __global__ void __launch_bounds__(NTHREADS, 1)
-    k_contract_tc(const __grid_constant__ CUtensorMap tmX, const __grid_constant__ CUtensorMap tmOh,
-                  const __grid_constant__ CUtensorMap tmOl, const __grid_constant__ TcParams prm,
-                  float* __restrict__ out) {
+    k_contract_tc(const __grid_constant__ TcLaunch<G> L) {
   extern __shared__ uint8_t smem_raw[];
+  __shared__ long long tb[G + 1];
+  __shared__ int nbs[G];
   uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
-  const jfg_contract_desc& d = prm.d;
-  const int Mt = prm.Mtile;
-  const int S = prm.stages;
-  const uint32_t obytes = (uint32_t)Mt * KB * 4;
-  const bool ta = prm.tmem_a != 0;
+  const int S = L.stages;
+  const bool ta = L.tmem_a != 0;
+  const uint32_t omax = (uint32_t)L.mt_max * KB * 4;
   const uint32_t xbuf = ta ? XBYTES : 2 * XBYTES;  // X tile (+ its lo part when in SMEM)
-  const uint32_t stage_bytes = xbuf + 2 * obytes;
+  const uint32_t stage_bytes = xbuf + 2 * omax;
   const uint32_t acc_stride = ta ? ACC_STRIDE_TA : 256;
+
+  if (threadIdx.x == 0) {
+    long long acc = 0;
+    for (int gi = 0; gi < L.ngroups; ++gi) {
+      const TcGroup& q = L.g[gi];
+      const int nb = active_count(q.d.batch_list, q.d.batch_count, q.d.batch);
+      nbs[gi] = nb;
+      tb[gi] = acc;
+      acc += (long long)((q.d.P + TILE_P - 1) / TILE_P) * ((q.d.M + q.Mtile - 1) / q.Mtile) *
+             nb * q.d.nseg;
+    }
+    tb[L.ngroups] = acc;
+  }
+  __syncthreads();
+  const long long ntiles = tb[L.ngroups];
+  if ((long long)blockIdx.x >= ntiles) return;  // no tile for this CTA (uniform)
+
   uint64_t* bars = (uint64_t*)(smem + (size_t)S * stage_bytes);
   uint64_t* full = bars;
   uint64_t* conv = bars + S;
@@ -237,13 +276,6 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   uint32_t* tmem_slot = (uint32_t*)(bars + 3 * S + 4);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int nkb = (d.K + KB - 1) / KB;
-  const int nptiles = (d.P + TILE_P - 1) / TILE_P;
-  const int mchunks = (d.M + Mt - 1) / Mt;
-  // problems of this launch: the whole batch, or the active list's count
-  const int nb = active_count(d.batch_list, d.batch_count, d.batch);
-  const long long ntiles = (long long)nptiles * mchunks * nb * d.nseg;
-  if ((long long)blockIdx.x >= ntiles) return;  // no tile for this CTA (uniform)
 
   if (threadIdx.x == 0) {
     for (int i = 0; i < S; ++i) {
@@ -260,7 +292,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(
                      smem_u32(tmem_slot)),
-                 "r"(prm.tmem_cols)
+                 "r"(L.tmem_cols)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -272,17 +304,24 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   auto Xh = [&](int st) { return smem + (size_t)st * stage_bytes; };
   auto Xl = [&](int st) { return smem + (size_t)st * stage_bytes + XBYTES; };
   auto Oh = [&](int st) { return smem + (size_t)st * stage_bytes + xbuf; };
-  auto Ol = [&](int st) { return smem + (size_t)st * stage_bytes + xbuf + obytes; };
+  auto Ol = [&](int st) { return smem + (size_t)st * stage_bytes + xbuf + omax; };
   // b = problem index (-1: an out-of-range list entry, computed but not stored)
-  auto decode = [&](long long t, int& pt, int& mc, int& b, int& s) {
-    pt = (int)(t % nptiles);
-    long long r = t / nptiles;
+  auto decode = [&](long long t, int& gi, int& pt, int& mc, int& b, int& s) {
+    gi = 0;
+    while (gi + 1 < L.ngroups && t >= tb[gi + 1]) ++gi;
+    const TcGroup& q = L.g[gi];
+    const int nptiles = (q.d.P + TILE_P - 1) / TILE_P;
+    const int mchunks = (q.d.M + q.Mtile - 1) / q.Mtile;
+    long long r = t - tb[gi];
+    pt = (int)(r % nptiles);
+    r /= nptiles;
     mc = (int)(r % mchunks);
     const int bs = (int)(r / mchunks);
-    const int slot = bs / d.nseg;
-    s = bs - slot * d.nseg;
-    b = active_problem(d.batch_list, nb, d.batch, slot);
+    const int slot = bs / q.d.nseg;
+    s = bs - slot * q.d.nseg;
+    b = active_problem(q.d.batch_list, nbs[gi], q.d.batch, slot);
   };
+  auto nkb_of = [&](int gi) { return (L.g[gi].d.K + KB - 1) / KB; };
 
   if (warp == 0) {
     // ---------------- TMA producer ----------------
@@ -290,11 +329,14 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       long long g = 0, issued = 0;
       bool ok = true;
       for (long long t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
-        int pt, mc, b, s;
-        decode(t, pt, mc, b, s);
-        const int cs = prm.seg_in_map ? s : 0;
-        const int cb = (prm.bat_in_map && b > 0) ? b : 0;
-        const int os = prm.seg_op_map ? s : 0;
+        int gi, pt, mc, b, s;
+        decode(t, gi, pt, mc, b, s);
+        const TcGroup& q = L.g[gi];
+        const int cs = q.seg_in_map ? s : 0;
+        const int cb = (q.bat_in_map && b > 0) ? b : 0;
+        const int os = q.seg_op_map ? s : 0;
+        const uint32_t obytes = (uint32_t)q.Mtile * KB * 4;
+        const int nkb = nkb_of(gi);
         for (int kb = 0; kb < nkb; ++kb, ++g) {
           const int st = (int)(g % S);
           const uint32_t u = (uint32_t)(g / S);
@@ -303,9 +345,9 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             break;
           }
           mbar_expect_tx(&full[st], XBYTES + 2 * obytes);
-          tma_load_4d(Xh(st), &tmX, &full[st], kb * KB, pt * TILE_P, cs, cb);
-          tma_load_3d(Oh(st), &tmOh, &full[st], kb * KB, mc * Mt, os);
-          tma_load_3d(Ol(st), &tmOl, &full[st], kb * KB, mc * Mt, os);
+          tma_load_4d(Xh(st), &L.maps[gi][0], &full[st], kb * KB, pt * TILE_P, cs, cb);
+          tma_load_3d(Oh(st), &L.maps[gi][1], &full[st], kb * KB, mc * q.Mtile, os);
+          tma_load_3d(Ol(st), &L.maps[gi][2], &full[st], kb * KB, mc * q.Mtile, os);
           issued = g + 1;
         }
       }
@@ -316,11 +358,14 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   } else if (warp == 1) {
     // ---------------- MMA issuer ----------------
     if (lane == 0) {
-      const uint32_t idesc = idesc_tf32(TILE_P, Mt);
       long long g = 0;
       int li = 0;
       bool ok = true;
       for (long long t = blockIdx.x; t < ntiles && ok; t += gridDim.x, ++li) {
+        int gi, pt, mc, b, s;
+        decode(t, gi, pt, mc, b, s);
+        const uint32_t idesc = idesc_tf32(TILE_P, L.g[gi].Mtile);
+        const int nkb = nkb_of(gi);
         const int buf = li & 1;
         const uint32_t use = (uint32_t)(li >> 1);
         if (li >= 2 && !mbar_wait(&tempty[buf], (use & 1u) ^ 1u)) {
@@ -364,71 +409,82 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   } else if (warp < 6) {
     // ---------------- split staged input tiles into TF32 hi (in place) / lo ----------------
     const int ct = threadIdx.x - 64;  // 0..127
-    const long long total_kb =
-        ((ntiles - blockIdx.x + gridDim.x - 1) / gridDim.x) * (long long)nkb;
     // TMEM mode: thread = row r of the tile (its warp's lane quarter), reads
     // its 32 values from the 128-byte-swizzled tile and stores hi / lo into
     // its TMEM lane with tcgen05.st.
     const int row = 32 * (warp & 3) + lane;
-    for (long long g = 0; g < total_kb; ++g) {
-      const int st = (int)(g % S);
-      if (!mbar_wait(&full[st], (uint32_t)(g / S) & 1u)) break;
-      if (ta) {
-        const float4* xr = (const float4*)(Xh(st) + row * 128);
-        uint32_t h[32], l[32];
+    long long g = 0;
+    bool ok = true;
+    for (long long t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
+      int gi, pt, mc, b, s;
+      decode(t, gi, pt, mc, b, s);
+      const int nkb = nkb_of(gi);
+      for (int kb = 0; kb < nkb; ++kb, ++g) {
+        const int st = (int)(g % S);
+        if (!mbar_wait(&full[st], (uint32_t)(g / S) & 1u)) {
+          ok = false;
+          break;
+        }
+        if (ta) {
+          const float4* xr = (const float4*)(Xh(st) + row * 128);
+          uint32_t h[32], l[32];
 #pragma unroll
-        for (int c = 0; c < 8; ++c) {
-          const float4 v = xr[c ^ (row & 7)];
-          const float hv[4] = {tf32_hi(v.x), tf32_hi(v.y), tf32_hi(v.z), tf32_hi(v.w)};
-          const float vv[4] = {v.x, v.y, v.z, v.w};
+          for (int c = 0; c < 8; ++c) {
+            const float4 v = xr[c ^ (row & 7)];
+            const float hv[4] = {tf32_hi(v.x), tf32_hi(v.y), tf32_hi(v.z), tf32_hi(v.w)};
+            const float vv[4] = {v.x, v.y, v.z, v.w};
 #pragma unroll
-          for (int e = 0; e < 4; ++e) {
-            h[4 * c + e] = __float_as_uint(hv[e]);
-            l[4 * c + e] = __float_as_uint(vv[e] - hv[e]);
+            for (int e = 0; e < 4; ++e) {
+              h[4 * c + e] = __float_as_uint(hv[e]);
+              l[4 * c + e] = __float_as_uint(vv[e] - hv[e]);
+            }
           }
-        }
-        const uint32_t tbase = tmem + ((uint32_t)(32 * (warp & 3)) << 16) +
-                               (uint32_t)(A_COL0 + 64 * st);
-        tmem_st32(tbase, h);
-        tmem_st32(tbase + 32, l);
-        asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
-        asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
-      } else {
-        float4* xh = (float4*)Xh(st);
-        float4* xl = (float4*)Xl(st);
+          const uint32_t tbase = tmem + ((uint32_t)(32 * (warp & 3)) << 16) +
+                                 (uint32_t)(A_COL0 + 64 * st);
+          tmem_st32(tbase, h);
+          tmem_st32(tbase + 32, l);
+          asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+          asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        } else {
+          float4* xh = (float4*)Xh(st);
+          float4* xl = (float4*)Xl(st);
 #pragma unroll
-        for (int i = 0; i < (int)(XBYTES / 16 / 128); ++i) {
-          const int idx = ct + i * 128;
-          float4 v = xh[idx];
-          float4 h = make_float4(tf32_hi(v.x), tf32_hi(v.y), tf32_hi(v.z), tf32_hi(v.w));
-          xh[idx] = h;
-          xl[idx] = make_float4(v.x - h.x, v.y - h.y, v.z - h.z, v.w - h.w);
+          for (int i = 0; i < (int)(XBYTES / 16 / 128); ++i) {
+            const int idx = ct + i * 128;
+            float4 v = xh[idx];
+            float4 h = make_float4(tf32_hi(v.x), tf32_hi(v.y), tf32_hi(v.z), tf32_hi(v.w));
+            xh[idx] = h;
+            xl[idx] = make_float4(v.x - h.x, v.y - h.y, v.z - h.z, v.w - h.w);
+          }
+          asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
         }
-        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        __syncwarp();
+        if (lane == 0) mbar_arrive(&conv[st]);
       }
-      __syncwarp();
-      if (lane == 0) mbar_arrive(&conv[st]);
     }
   } else {
     // ---------------- epilogue: TMEM -> registers -> global ----------------
     // Eight warps: two per TMEM lane quarter, each taking every other group
     // of 32 accumulator columns; field / eigenvalue loads of a group are all
     // issued before its TMEM load so they are in flight together.
-    const int q = warp & 3;  // TMEM lane quarter this warp may access
+    const int q4 = warp & 3;  // TMEM lane quarter this warp may access
     const int half = (warp - 6) >> 2;
-    const int row = 32 * q + lane;
-    const float alpha = (float)d.alpha, beta = (float)d.beta;
+    const int row = 32 * q4 + lane;
     int li = 0;
     for (long long t = blockIdx.x; t < ntiles; t += gridDim.x, ++li) {
-      int pt, mc, b, s;
-      decode(t, pt, mc, b, s);
+      int gi, pt, mc, b, s;
+      decode(t, gi, pt, mc, b, s);
+      const TcGroup& q = L.g[gi];
+      const jfg_contract_desc& d = q.d;
+      const int Mt = q.Mtile;
+      const float alpha = (float)d.alpha, beta = (float)d.beta;
       const int buf = li & 1;
       if (!mbar_wait(&tfull[buf], (uint32_t)(li >> 1) & 1u)) break;
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       const int p = pt * TILE_P + row;
       const bool pin = p < d.P && b >= 0;
       const int bb = b < 0 ? 0 : b;
-      float* outS = out + (long long)bb * d.out_batch + (long long)s * d.out_seg;
+      float* outS = q.out + (long long)bb * d.out_batch + (long long)s * d.out_seg;
       float c0 = 0.f, c1 = 1.f, lp = 0.f;
       const float* __restrict__ lam_m = (const float*)d.lam_m;
       if (EPI == JFG_EPI_DIV_EIG) {
@@ -439,7 +495,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       const float* __restrict__ fld = nullptr;
       if (EPI == JFG_EPI_MUL_FIELD)
         fld = (const float*)d.field + (long long)bb * d.field_batch + (long long)s * d.field_seg;
-      const uint32_t tacc = tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)buf * acc_stride;
+      const uint32_t tacc = tmem + ((uint32_t)(32 * q4) << 16) + (uint32_t)buf * acc_stride;
       for (int c = half * 2; c < Mt / 16; c += 4) {
         // columns [c*16, c*16+32): two 16-column TMEM loads
         const int mb = mc * Mt + c * 16;
@@ -485,7 +541,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   if (warp == 1) {
     asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
     asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem),
-                 "r"(prm.tmem_cols)
+                 "r"(L.tmem_cols)
                  : "memory");
   }
 }
@@ -524,7 +580,7 @@ int make_map(CUtensorMap* map, const float* base, int rank, const cuuint64_t* di
   return r == CUDA_SUCCESS ? JFG_OK : JFG_ERR_ARG;
 }
 
-// Opt every epilogue variant into the largest dynamic shared-memory size once
+// Opt every kernel variant into the largest dynamic shared-memory size once
 // per device (before any stream capture can be active in the caller).
 int setup_kernel_attr() {
   static bool done[64] = {};
@@ -532,92 +588,115 @@ int setup_kernel_attr() {
   JFG_CUDA_TRY(cudaGetDevice(&dev));
   if (dev < 0 || dev >= 64) return JFG_ERR_UNSUPPORTED;
   if (!done[dev]) {
-    const int mx = 227 * 1024;
-#define JFG_SET_ATTR(E, B)                                                                 \
-  JFG_CUDA_TRY(cudaFuncSetAttribute(k_contract_tc<E, B>,                                   \
+    const int mx = 220 * 1024;
+#define JFG_SET_ATTR(E, B, G)                                                              \
+  JFG_CUDA_TRY(cudaFuncSetAttribute(k_contract_tc<E, B, G>,                                \
                                     cudaFuncAttributeMaxDynamicSharedMemorySize, mx))
-    JFG_SET_ATTR(JFG_EPI_NONE, false);
-    JFG_SET_ATTR(JFG_EPI_NONE, true);
-    JFG_SET_ATTR(JFG_EPI_MUL_FIELD, false);
-    JFG_SET_ATTR(JFG_EPI_MUL_FIELD, true);
-    JFG_SET_ATTR(JFG_EPI_DIV_EIG, false);
-    JFG_SET_ATTR(JFG_EPI_DIV_EIG, true);
+#define JFG_SET_ATTR_G(G)                   \
+  JFG_SET_ATTR(JFG_EPI_NONE, false, G);     \
+  JFG_SET_ATTR(JFG_EPI_NONE, true, G);      \
+  JFG_SET_ATTR(JFG_EPI_MUL_FIELD, false, G); \
+  JFG_SET_ATTR(JFG_EPI_MUL_FIELD, true, G); \
+  JFG_SET_ATTR(JFG_EPI_DIV_EIG, false, G);  \
+  JFG_SET_ATTR(JFG_EPI_DIV_EIG, true, G)
+    JFG_SET_ATTR_G(1);
+    JFG_SET_ATTR_G(GMAX);
+#undef JFG_SET_ATTR_G
 #undef JFG_SET_ATTR
     done[dev] = true;
   }
   return JFG_OK;
 }
 
-}  // namespace
-
-int contract_tc(const jfg_contract_desc& d, const float* op_hi, const float* op_lo,
-                const float* in, float* out, cudaStream_t st) {
+// Validate one group and fill its descriptor, tile height and tensor maps.
+int fill_group(const jfg_contract_desc& d, const float* op_hi, const float* op_lo,
+               const float* in, float* out, TcGroup& q, CUtensorMap* maps) {
   JFG_TRY(validate_desc(d));
   if (!op_hi || !op_lo || !in || !out) return JFG_ERR_ARG;
-  if (d.batch == 0 || d.M == 0 || d.P == 0) return JFG_OK;
   // TMA: 16-byte aligned bases and strides
   auto al16 = [](const void* p) { return ((uintptr_t)p & 15u) == 0; };
   if (!al16(op_hi) || !al16(op_lo) || !al16(in)) return JFG_ERR_ARG;
   if ((d.op_ld & 3) || (d.in_ld & 3) || (d.op_seg & 3) || (d.in_seg & 3) || (d.in_batch & 3))
     return JFG_ERR_ARG;
-  const long long gy = (long long)d.batch * d.nseg;
-  if (gy > 65535) return JFG_ERR_ARG;
-
-  const int Mt = ((d.M > MT_MAX ? MT_MAX : d.M) + 15) / 16 * 16;
-  const int mchunks = (d.M + Mt - 1) / Mt;
-  const int cols = 512;  // two accumulator buffers (+ operand A stages in TMEM mode)
-  const int ta = g_operand_a_in_tmem;
-  const size_t stage = (ta ? 1 : 2) * (size_t)XBYTES + 2 * (size_t)Mt * KB * 4;
-  int stages = (int)((200 * 1024) / stage);
-  if (stages > (ta ? 4 : 6)) stages = ta ? 4 : 6;
-  if (stages < 2) return JFG_ERR_UNSUPPORTED;
-  const size_t smem = 1024 + stages * stage + (3 * stages + 4) * 8 + 16;
-  const long long ntiles = (long long)((d.P + TILE_P - 1) / TILE_P) * mchunks * gy;
-  int dev = 0, nsm = 0;
-  JFG_CUDA_TRY(cudaGetDevice(&dev));
-  JFG_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-
-  TcParams prm;
-  prm.d = d;
-  prm.Mtile = Mt;
-  prm.stages = stages;
-  prm.tmem_cols = cols;
-  prm.seg_in_map = (d.nseg > 1 && d.in_seg != 0) ? 1 : 0;
-  prm.bat_in_map = (d.batch > 1 && d.in_batch != 0) ? 1 : 0;
-  prm.seg_op_map = (d.nseg > 1 && d.op_seg != 0) ? 1 : 0;
-  prm.tmem_a = ta;
-
-  CUtensorMap mx, moh, mol;
+  if ((long long)d.batch * d.nseg > 65535) return JFG_ERR_ARG;
+  q.d = d;
+  q.out = out;
+  q.Mtile = ((d.M > MT_MAX ? MT_MAX : d.M) + 15) / 16 * 16;
+  q.seg_in_map = (d.nseg > 1 && d.in_seg != 0) ? 1 : 0;
+  q.bat_in_map = (d.batch > 1 && d.in_batch != 0) ? 1 : 0;
+  q.seg_op_map = (d.nseg > 1 && d.op_seg != 0) ? 1 : 0;
   {
     cuuint64_t dims[4] = {(cuuint64_t)d.K, (cuuint64_t)d.P,
-                          (cuuint64_t)(prm.seg_in_map ? d.nseg : 1),
-                          (cuuint64_t)(prm.bat_in_map ? d.batch : 1)};
+                          (cuuint64_t)(q.seg_in_map ? d.nseg : 1),
+                          (cuuint64_t)(q.bat_in_map ? d.batch : 1)};
     cuuint64_t str[3] = {(cuuint64_t)d.in_ld * 4,
-                         (cuuint64_t)(prm.seg_in_map ? d.in_seg : d.in_ld * d.P) * 4,
-                         (cuuint64_t)(prm.bat_in_map ? d.in_batch : d.in_ld * d.P) * 4};
+                         (cuuint64_t)(q.seg_in_map ? d.in_seg : d.in_ld * d.P) * 4,
+                         (cuuint64_t)(q.bat_in_map ? d.in_batch : d.in_ld * d.P) * 4};
     cuuint32_t box[4] = {KB, TILE_P, 1, 1};
-    JFG_TRY(make_map(&mx, in, 4, dims, str, box));
+    JFG_TRY(make_map(&maps[0], in, 4, dims, str, box));
   }
   {
     cuuint64_t dims[3] = {(cuuint64_t)d.K, (cuuint64_t)d.M,
-                          (cuuint64_t)(prm.seg_op_map ? d.nseg : 1)};
+                          (cuuint64_t)(q.seg_op_map ? d.nseg : 1)};
     cuuint64_t str[2] = {(cuuint64_t)d.op_ld * 4,
-                         (cuuint64_t)(prm.seg_op_map ? d.op_seg : d.op_ld * d.M) * 4};
-    cuuint32_t box[3] = {KB, (cuuint32_t)Mt, 1};
-    JFG_TRY(make_map(&moh, op_hi, 3, dims, str, box));
-    JFG_TRY(make_map(&mol, op_lo, 3, dims, str, box));
+                         (cuuint64_t)(q.seg_op_map ? d.op_seg : d.op_ld * d.M) * 4};
+    cuuint32_t box[3] = {KB, (cuuint32_t)q.Mtile, 1};
+    JFG_TRY(make_map(&maps[1], op_hi, 3, dims, str, box));
+    JFG_TRY(make_map(&maps[2], op_lo, 3, dims, str, box));
   }
-  dim3 grid((unsigned)(ntiles < nsm ? ntiles : nsm));
+  return JFG_OK;
+}
+
+long long group_tiles(const TcGroup& q) {
+  return (long long)((q.d.P + TILE_P - 1) / TILE_P) * ((q.d.M + q.Mtile - 1) / q.Mtile) *
+         q.d.batch * q.d.nseg;
+}
+
+// One launch over ng <= G groups (same epilogue kind and beta != 0 for all).
+template <int G>
+int launch_groups(int ng, const jfg_contract_desc* const* ds, const float* const* op_hi,
+                  const float* const* op_lo, const float* const* in, float* const* out,
+                  const jfg_tc_config& cfg, cudaStream_t st) {
+  static_assert(sizeof(TcLaunch<G>) <= 32000, "kernel parameter block too large");
+  TcLaunch<G> L;
+  memset(&L, 0, sizeof(L));
+  L.ngroups = ng;
+  const int epi = ds[0]->epilogue;
+  const bool hb = ds[0]->beta != 0.0;
+  long long tiles = 0;
+  int mt_max = 16;
+  for (int i = 0; i < ng; ++i) {
+    if (ds[i]->epilogue != epi || (ds[i]->beta != 0.0) != hb) return JFG_ERR_ARG;
+    JFG_TRY(fill_group(*ds[i], op_hi[i], op_lo[i], in[i], out[i], L.g[i], L.maps[i]));
+    tiles += group_tiles(L.g[i]);
+    if (L.g[i].Mtile > mt_max) mt_max = L.g[i].Mtile;
+  }
+  if (tiles == 0) return JFG_OK;
+  const int ta = cfg.operand_a_in_tmem ? 1 : 0;
+  const size_t stage = (ta ? 1 : 2) * (size_t)XBYTES + 2 * (size_t)mt_max * KB * 4;
+  int stages = (int)((200 * 1024) / stage);
+  if (stages > (ta ? 4 : 6)) stages = ta ? 4 : 6;
+  if (cfg.stages >= 2 && cfg.stages < stages) stages = cfg.stages;
+  if (stages < 2) return JFG_ERR_UNSUPPORTED;
+  L.stages = stages;
+  L.tmem_cols = 512;  // two accumulator buffers (+ operand A stages in TMEM mode)
+  L.tmem_a = ta;
+  L.mt_max = mt_max;
+  const size_t smem = 1024 + stages * stage + (3 * stages + 4) * 8 + 16;
+  int dev = 0, nsm = 0;
+  JFG_CUDA_TRY(cudaGetDevice(&dev));
+  JFG_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  int ctas = cfg.ctas > 0 && cfg.ctas < nsm ? cfg.ctas : nsm;
+  dim3 grid((unsigned)(tiles < ctas ? tiles : ctas));
   JFG_TRY(setup_kernel_attr());
-  const bool hb = d.beta != 0.0;
-#define JFG_LAUNCH(E)                                                                      \
-  do {                                                                                     \
-    if (hb)                                                                                \
-      k_contract_tc<E, true><<<grid, NTHREADS, smem, st>>>(mx, moh, mol, prm, out);        \
-    else                                                                                   \
-      k_contract_tc<E, false><<<grid, NTHREADS, smem, st>>>(mx, moh, mol, prm, out);       \
+#define JFG_LAUNCH(E)                                                       \
+  do {                                                                      \
+    if (hb)                                                                 \
+      k_contract_tc<E, true, G><<<grid, NTHREADS, smem, st>>>(L);           \
+    else                                                                    \
+      k_contract_tc<E, false, G><<<grid, NTHREADS, smem, st>>>(L);          \
   } while (0)
-  switch (d.epilogue) {
+  switch (epi) {
     case JFG_EPI_NONE:
       JFG_LAUNCH(JFG_EPI_NONE);
       break;
@@ -632,6 +711,73 @@ int contract_tc(const jfg_contract_desc& d, const float* op_hi, const float* op_
   }
 #undef JFG_LAUNCH
   JFG_LAUNCHED();
+  return JFG_OK;
+}
+
+}  // namespace
+
+int tc_setup() {
+  if (!encode_fn()) return JFG_ERR_UNSUPPORTED;
+  return setup_kernel_attr();
+}
+
+jfg_tc_config tc_default_config() {
+  jfg_tc_config c;
+  c.operand_a_in_tmem = g_operand_a_in_tmem;
+  c.order = 0;
+  c.ctas = 0;
+  c.stages = 0;
+  return c;
+}
+
+int contract_tc(const jfg_contract_desc& d, const float* op_hi, const float* op_lo,
+                const float* in, float* out, cudaStream_t st) {
+  if (d.batch == 0 || d.M == 0 || d.P == 0) return validate_desc(d);
+  const jfg_contract_desc* dp = &d;
+  return launch_groups<1>(1, &dp, &op_hi, &op_lo, &in, &out, tc_default_config(), st);
+}
+
+int contract_tc_grouped(int ng, const jfg_contract_desc* ds, const float* const* op_hi,
+                        const float* const* op_lo, const float* const* in, float* const* out,
+                        const jfg_tc_config& cfg, cudaStream_t st) {
+  if (ng < 0 || (ng > 0 && (!ds || !op_hi || !op_lo || !in || !out))) return JFG_ERR_ARG;
+  if (cfg.order < 0 || cfg.order > 2 || cfg.stages < 0 || cfg.ctas < 0) return JFG_ERR_ARG;
+  // launch order of the groups: as given, by operator-tile work (K * Mtile,
+  // largest first), or by total work (largest first)
+  std::vector<int> ord;
+  ord.reserve(ng);
+  for (int i = 0; i < ng; ++i)
+    if (ds[i].batch > 0 && ds[i].M > 0 && ds[i].P > 0) ord.push_back(i);
+    else JFG_TRY(validate_desc(ds[i]));
+  auto work = [&](int i) {
+    const double mt = ds[i].M < MT_MAX ? ds[i].M : MT_MAX;
+    const double tile = (double)ds[i].K * mt;
+    if (cfg.order == 1) return tile;
+    return tile * (double)((ds[i].P + TILE_P - 1) / TILE_P) *
+           (double)((ds[i].M + MT_MAX - 1) / MT_MAX) * ds[i].batch * ds[i].nseg;
+  };
+  if (cfg.order != 0)
+    std::stable_sort(ord.begin(), ord.end(), [&](int a, int b) { return work(a) > work(b); });
+  for (size_t c0 = 0; c0 < ord.size(); c0 += GMAX) {
+    const int n = (int)(ord.size() - c0 < (size_t)GMAX ? ord.size() - c0 : GMAX);
+    const jfg_contract_desc* dp[GMAX];
+    const float* oh[GMAX];
+    const float* ol[GMAX];
+    const float* ip[GMAX];
+    float* op[GMAX];
+    for (int k = 0; k < n; ++k) {
+      const int i = ord[c0 + k];
+      dp[k] = &ds[i];
+      oh[k] = op_hi[i];
+      ol[k] = op_lo[i];
+      ip[k] = in[i];
+      op[k] = out[i];
+    }
+    if (n == 1)
+      JFG_TRY(launch_groups<1>(1, dp, oh, ol, ip, op, cfg, st));
+    else
+      JFG_TRY(launch_groups<GMAX>(n, dp, oh, ol, ip, op, cfg, st));
+  }
   return JFG_OK;
 }
 
@@ -653,6 +799,105 @@ extern "C" int jfg_contract_tc(const jfg_contract_desc* d, const float* op_hi,
 extern "C" int jfg_tc_set_variant(int operand_a_in_tmem) {
   if (operand_a_in_tmem != 0 && operand_a_in_tmem != 1) return JFG_ERR_ARG;
   jfg::g_operand_a_in_tmem = operand_a_in_tmem;
+  return JFG_OK;
+}
+
+namespace {
+
+// Tuned configurations by launch signature (shapes, batch, epilogue of every group).
+std::mutex g_tune_mu;
+std::map<std::string, jfg_tc_config> g_tuned;
+
+std::string signature(int ng, const jfg_contract_desc* ds) {
+  std::string key;
+  char buf[160];
+  int dev = 0;
+  cudaGetDevice(&dev);
+  snprintf(buf, sizeof buf, "d%d:", dev);
+  key += buf;
+  for (int i = 0; i < ng; ++i) {
+    const jfg_contract_desc& d = ds[i];
+    snprintf(buf, sizeof buf, "%d,%d,%d,%d,%d,%d,%d;", d.batch, d.nseg, d.M, d.P, d.K,
+             d.epilogue, d.beta != 0.0 ? 1 : 0);
+    key += buf;
+  }
+  return key;
+}
+
+}  // namespace
+
+extern "C" int jfg_contract_tc_grouped(int ngroups, const jfg_contract_desc* descs,
+                                       const float* const* op_hi, const float* const* op_lo,
+                                       const float* const* in, float* const* out,
+                                       const jfg_tc_config* cfg, void* stream) {
+  if (ngroups < 0 || (ngroups > 0 && !descs)) return JFG_ERR_ARG;
+  jfg_tc_config c = jfg::tc_default_config();
+  if (cfg) {
+    c = *cfg;
+  } else {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    auto it = g_tuned.find(signature(ngroups, descs));
+    if (it != g_tuned.end()) c = it->second;
+  }
+  return jfg::contract_tc_grouped(ngroups, descs, op_hi, op_lo, in, out, c,
+                                  (cudaStream_t)stream);
+}
+
+extern "C" int jfg_tc_autotune(int ngroups, const jfg_contract_desc* descs,
+                               const float* const* op_hi, const float* const* op_lo,
+                               const float* const* in, float* const* out, int reps,
+                               jfg_tc_config* best, float* best_ms, void* stream) {
+  if (ngroups < 1 || !descs || reps < 1) return JFG_ERR_ARG;
+  cudaStream_t st = (cudaStream_t)stream;
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  JFG_CUDA_TRY(cudaStreamIsCapturing(st, &cap));
+  if (cap != cudaStreamCaptureStatusNone) return JFG_ERR_ARG;  // timing needs real launches
+  std::vector<jfg_tc_config> cands;
+  const int orders = ngroups > 1 ? 3 : 1;
+  for (int ta = 1; ta >= 0; --ta)
+    for (int o = 0; o < orders; ++o)
+      for (int sg : {0, 3, 2}) {
+        jfg_tc_config c;
+        c.operand_a_in_tmem = ta;
+        c.order = o;
+        c.ctas = 0;
+        c.stages = sg;
+        cands.push_back(c);
+      }
+  cudaEvent_t e0, e1;
+  JFG_CUDA_TRY(cudaEventCreate(&e0));
+  JFG_CUDA_TRY(cudaEventCreate(&e1));
+  float bt = -1.f;
+  jfg_tc_config bc = cands[0];
+  int status = JFG_OK;
+  for (const jfg_tc_config& c : cands) {
+    status = jfg::contract_tc_grouped(ngroups, descs, op_hi, op_lo, in, out, c, st);  // warm
+    if (status != JFG_OK) break;
+    if (cudaEventRecord(e0, st) != cudaSuccess) { status = JFG_ERR_CUDA; break; }
+    for (int r = 0; r < reps && status == JFG_OK; ++r)
+      status = jfg::contract_tc_grouped(ngroups, descs, op_hi, op_lo, in, out, c, st);
+    if (status != JFG_OK) break;
+    float ms = 0.f;
+    if (cudaEventRecord(e1, st) != cudaSuccess || cudaEventSynchronize(e1) != cudaSuccess ||
+        cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) {
+      status = JFG_ERR_CUDA;
+      break;
+    }
+    ms /= (float)reps;
+    if (bt < 0.f || ms < bt) {
+      bt = ms;
+      bc = c;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (status != JFG_OK) return status;
+  {
+    std::lock_guard<std::mutex> lk(g_tune_mu);
+    g_tuned[signature(ngroups, descs)] = bc;
+  }
+  if (best) *best = bc;
+  if (best_ms) *best_ms = bt;
   return JFG_OK;
 }
 

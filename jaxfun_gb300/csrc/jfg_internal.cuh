@@ -69,6 +69,14 @@ int contract_df64(const jfg_contract_desc& d, const double* op, const double* in
                   cudaStream_t st);
 int contract_tc(const jfg_contract_desc& d, const float* op_hi, const float* op_lo,
                 const float* in, float* out, cudaStream_t st);
+// ngroups contractions in persistent grouped launches (contract_tc.cu)
+int contract_tc_grouped(int ng, const jfg_contract_desc* ds, const float* const* op_hi,
+                        const float* const* op_lo, const float* const* in, float* const* out,
+                        const jfg_tc_config& cfg, cudaStream_t st);
+jfg_tc_config tc_default_config();
+// One-time per-device setup of the tensor-core kernels (shared-memory opt-in,
+// tensor-map encoder); call before capturing their first launch into a graph.
+int tc_setup();
 
 inline int contract(Engine e, const jfg_contract_desc& d, OpRef<double> op, const double* in,
                     double* out, cudaStream_t st) {

@@ -1,13 +1,15 @@
 """Batched 2-D Dirichlet Helmholtz solves with uneven N (alpha^2 u - lap u = f).
 
-Each problem b has its own N_b and alpha_b; problems are grouped by size and
-each group is one C-ABI call (``jfg_helmholtz_solve_mixed``): fast-
-diagonalisation corrections on the tensor cores (split-TF32, padded layout)
-inside FP64 iterative refinement whose residual r = b - A x is applied in
-O(n^2) from the closed-form mass and stiffness matrices.  The FD factors are
-those of ``tpmats_lu_factor`` for alpha^2 M (x) M + K (x) M + M (x) K
-(src/jaxfun/la/tpmatrix.py:1089-1233), with the general eigendecomposition for
-the non-symmetric Chebyshev stiffness.
+Each problem b has its own N_b and alpha_b.  Problems are grouped by size and
+the whole batch is ONE C-ABI call (``jfg_helmholtz_solve_grouped``): fast-
+diagonalisation corrections on the tensor cores (split-TF32, padded layout;
+every pass one persistent grouped launch over all size groups, configuration
+chosen by the autotuner ``jfg_tc_autotune``) inside FP64 iterative
+refinement whose residual r = b - A x is applied in O(n^2) from the
+closed-form mass and stiffness matrices, the refinement step captured into a
+CUDA graph.  The FD factors are those of ``tpmats_lu_factor`` for
+alpha^2 M (x) M + K (x) M + M (x) K (src/jaxfun/la/tpmatrix.py:1089-1233), with
+the general eigendecomposition for the non-symmetric Chebyshev stiffness.
 """
 
 from __future__ import annotations
@@ -63,10 +65,92 @@ class UnevenHelmholtzSolver:
             _Group(family, int(N), np.nonzero(self.Ns == N)[0], self.alphas)
             for N in sorted(set(self.Ns.tolist()))
         ]
+        # group-major flat layout of the whole batch
+        self.order = np.concatenate([g.idx for g in self.groups])
+        ng = len(self.groups)
+        self._n = _lib.int_array([g.n for g in self.groups])
+        self._nq = _lib.int_array([g.nq for g in self.groups])
+        self._batch = _lib.int_array([len(g.idx) for g in self.groups])
+        self._ptrs = [_lib.ptr_array([getattr(g, a)[k].data_ptr() for g in self.groups])
+                      for a, k in (("E", 0), ("E", 1), ("W", 0), ("W", 1))]
+        self._lam = _lib.ptr_array([g.lam32.data_ptr() for g in self.groups])
+        a2 = self.alphas[self.order] ** 2
+        self.alpha2 = as_device(a2)
+        self.alpha2_32 = as_device(a2, torch.float32)
+        self.offsets = np.zeros(len(self.order) + 1, dtype=np.int64)
+        self.offsets[1:] = np.cumsum((self.Ns[self.order] - 2) ** 2)
+        L = _lib.lib()
+        self._ws = torch.empty(L.jfg_helmholtz_grouped_workspace_size(ng, self._n, self._nq,
+                                                                       self._batch),
+                               dtype=torch.uint8, device="cuda")
+        self.cfg = None  # tensor-core launch configuration (autotune())
+
+    def autotune(self, reps: int = 3):
+        """Choose the grouped tensor-core launch configuration for this batch's
+        fast-diagonalisation passes (jfg_tc_autotune on scratch operands)."""
+        L = _lib.lib()
+        ng = len(self.groups)
+        tot = sum(len(g.idx) * g.nq * g.nq for g in self.groups)
+        x = torch.randn(tot, device="cuda")
+        y = torch.empty_like(x)
+        descs = (_lib.ContractDesc * ng)()
+        ins, outs = [], []
+        off = 0
+        for i, g in enumerate(self.groups):
+            B, q = len(g.idx), g.nq
+            descs[i] = _lib.ContractDesc(batch=B, nseg=1, M=q, P=q, K=q, op_ld=q, in_ld=q,
+                                         in_batch=q * q, out_ld=q, out_batch=q * q,
+                                         alpha=1.0, beta=0.0)
+            ins.append(x.data_ptr() + 4 * off)
+            outs.append(y.data_ptr() + 4 * off)
+            off += B * q * q
+        best = _lib.TcConfig()
+        ms = C.c_float()
+        _lib.check(L.jfg_tc_autotune(ng, descs, self._ptrs[0], self._ptrs[1],
+                                     _lib.ptr_array(ins), _lib.ptr_array(outs), int(reps),
+                                     C.byref(best), C.byref(ms), _lib.stream_handle()),
+                   "jfg_tc_autotune")
+        self.cfg = best
+        return {"operand_a_in_tmem": best.operand_a_in_tmem, "order": best.order,
+                "ctas": best.ctas, "stages": best.stages, "pass_ms": ms.value}
+
+    def pack(self, rhs: list) -> torch.Tensor:
+        """Per-problem right-hand sides -> the flat group-major FP64 buffer."""
+        return torch.cat([as_device(rhs[i]).reshape(-1) for i in self.order])
+
+    def solve_packed(self, b: torch.Tensor, tol: float = 1e-11, max_refine: int = 8,
+                     out: torch.Tensor | None = None):
+        """One C-ABI call for the whole batch on packed (group-major) data.
+        Returns (x packed, refinements per problem in group-major order)."""
+        L = _lib.lib()
+        x = torch.empty_like(b) if out is None else out
+        nref = (C.c_int * len(self.order))()
+        st = L.jfg_helmholtz_solve_grouped(
+            FAMILY[self.family], len(self.groups), self._n, self._nq, self._batch,
+            *self._ptrs, self._lam, self.alpha2.data_ptr(), self.alpha2_32.data_ptr(),
+            b.data_ptr(), x.data_ptr(), float(tol), int(max_refine), nref,
+            None if self.cfg is None else C.byref(self.cfg), self._ws.data_ptr(),
+            self._ws.numel(), _lib.stream_handle())
+        _lib.check(st, "jfg_helmholtz_solve_grouped")
+        return x, np.array(nref[:])
+
+    def unpack(self, x: torch.Tensor) -> list:
+        out = [None] * len(self.Ns)
+        for k, i in enumerate(self.order):
+            n = int(self.Ns[i]) - 2
+            out[i] = x[self.offsets[k]:self.offsets[k + 1]].view(n, n)
+        return out
 
     def solve(self, rhs: list, tol: float = 1e-11, max_refine: int = 8):
         """rhs: list (one per problem) of (N_b-2, N_b-2) arrays/tensors.
         Returns (solutions list of FP64 device tensors, refinements per problem)."""
+        x, nref = self.solve_packed(self.pack(rhs), tol, max_refine)
+        refs = np.zeros(len(self.Ns), dtype=int)
+        refs[self.order] = nref
+        return self.unpack(x), refs
+
+    def solve_per_group(self, rhs: list, tol: float = 1e-11, max_refine: int = 8):
+        """The same solves, one C-ABI call per size group (jfg_helmholtz_solve_mixed)."""
         L = _lib.lib()
         out = [None] * len(self.Ns)
         refs = np.zeros(len(self.Ns), dtype=int)

@@ -5,6 +5,7 @@ dense Kronecker / general-eigenvector FD solve)."""
 
 import numpy as np
 import pytest
+import torch
 
 from jaxfun_gb300.la.helmholtz import UnevenHelmholtzSolver, helmholtz_apply
 from oracle import spectral as O
@@ -26,8 +27,9 @@ def test_structured_apply_matches_dense(family, N):
         assert np.abs(v[b] - ref).max() < 1e-12 * np.abs(ref).max()
 
 
+@pytest.mark.parametrize("mode", ["grouped", "grouped_tuned", "per_group"])
 @pytest.mark.parametrize("family", ["legendre", "chebyshev"])
-def test_uneven_batch_solve(family):
+def test_uneven_batch_solve(family, mode):
     rng = np.random.default_rng(11)
     Ns = rng.choice([16, 32, 48, 64], size=10)
     alphas = rng.uniform(0, 50, size=10)
@@ -36,7 +38,18 @@ def test_uneven_batch_solve(family):
         fh = O.forcing_coeffs(rng, N, 2)[: N - 2, : N - 2]
         rhs.append(fh)
     S = UnevenHelmholtzSolver(family, Ns, alphas)
-    xs, refs = S.solve(rhs, tol=1e-12)
+    # grouped on a side stream (graph-captured refinement step); tuned on the
+    # default stream (steps launched directly)
+    stream = torch.cuda.Stream() if mode == "grouped" else torch.cuda.current_stream()
+    with torch.cuda.stream(stream):
+        if mode == "grouped_tuned":
+            cfg = S.autotune(reps=1)
+            assert cfg["pass_ms"] > 0
+        if mode == "per_group":
+            xs, refs = S.solve_per_group(rhs, tol=1e-12)
+        else:
+            xs, refs = S.solve(rhs, tol=1e-12)
+    torch.cuda.synchronize()
     for b, N in enumerate(Ns):
         Vo = O.Space1D(family, N, True)
         K, M = Vo.stiffness_matrix(), Vo.mass_matrix()
