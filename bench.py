@@ -323,7 +323,7 @@ def run_transforms(args):
     u = T.backward(c)                       # FP64 grid fields (the inputs)
     u32 = u.float()
     res = {}
-    for prec, x in (("f64", u), ("tc", u32)):
+    for prec, x in (("f64", u), ("tc", u32), ("bf16x3", u32)):
         for _ in range(args.warmup):
             T.backward(T.forward(x, precision=prec), precision=prec)
         torch.cuda.synchronize()
@@ -344,9 +344,10 @@ def run_transforms(args):
     t_roof_tc = max(6 * 2.0 * N * F * N**3 / (pk["bf16_tflops"] / 2 * 1e12),
                     6 * 2 * F * N**3 * 4 / (pk["hbm_gbs"] * 1e9))
     line = {"workload": f"chebyshev-3d-N{N}-{F}fields-roundtrip", "unit": "ms per round trip",
-            "f64": res["f64"], "tc": res["tc"],
+            "f64": res["f64"], "tc": res["tc"], "bf16x3": res["bf16x3"],
             "tc_roofline_ms": 1e3 * t_roof_tc,
             "tc_roofline_frac": 1e3 * t_roof_tc / res["tc"]["ms"],
+            "bf16x3_roofline_frac": 1e3 * t_roof_tc / res["bf16x3"]["ms"],
             "roofline_note": f"max(useful FLOP / (bf16 {kind} / 2), FP32 bytes / HBM {kind})"}
     print(json.dumps(line), flush=True)
     return 0
@@ -437,6 +438,96 @@ def run_helmholtz(args):
             "autotuned_config": tuned,
             "per_group_calls_solves_per_s": nprob / t_pg}
     print(json.dumps(line), flush=True)
+    return 0
+
+
+def run_tour(args):
+    """Every product kernel on moderate sizes (a few launches each), for the
+    all-kernels ncu summary.  Not a measurement: prints the kernels' names."""
+    import numpy as np
+    import torch
+
+    from jaxfun_gb300 import _lib
+    from jaxfun_gb300.galerkin import (DIRICHLET, Chebyshev, FunctionSpace, Legendre,
+                                       TensorProduct)
+    from jaxfun_gb300.galerkin.tensorproductspace import tp_apply_tc
+    from jaxfun_gb300.la import MixedVarCoefSolver, VarCoefMatrix, pcg, poisson_tpmatrices
+    from jaxfun_gb300.la.helmholtz import UnevenHelmholtzSolver, helmholtz_apply
+    from jaxfun_gb300.sno import train as sno_train
+    from jaxfun_gb300.sno.model import SNO, SNOConfig
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    L = _lib.lib()
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
+    rng = np.random.default_rng(0)
+    # 1. transforms: 3-D Chebyshev 128^3, 4 fields (FP64, FP32, split-TF32)
+    C3 = Chebyshev(128)
+    T3 = TensorProduct(C3, C3, C3)
+    c = torch.as_tensor(rng.standard_normal((4, 128, 128, 128)), device="cuda")
+    u = T3.backward(c)
+    T3.forward(u.float(), precision="tc")
+    T3.forward(u.float(), precision="bf16x3")
+    T3.forward(u)
+    # 2. FD solve (FP64 and the no-allocation entry point), 2-D Legendre N=256, 32 rhs
+    D = FunctionSpace(256, Legendre, bcs=DIRICHLET)
+    T = TensorProduct(D, D)
+    fac = poisson_tpmatrices(T, 1.0).lu_factor()
+    b = torch.as_tensor(rng.standard_normal((32, 254, 254)), device="cuda")
+    fac.solve(b)
+    # 3-D FD (eigenvalue-sum kernel), 64^3, 4 rhs
+    D3 = FunctionSpace(64, Legendre, bcs=DIRICHLET)
+    fac3 = poisson_tpmatrices(TensorProduct(D3, D3, D3), 1.0).lu_factor()
+    fac3.solve(torch.as_tensor(rng.standard_normal((4, 62, 62, 62)), device="cuda"))
+    # 3. variable-coefficient 2-D N=256, 32 problems: weighted field, FP64 apply,
+    #    mixed solve (tensor-core PCG, double-FP32 and FP32 residuals), FP64 PCG
+    kap_h, f_h = make_problems(32, 256)
+    kap = torch.as_tensor(kap_h, device="cuda")
+    A = VarCoefMatrix(T, kap)
+    rhs = T.scalar_product(torch.as_tensor(f_h, device="cuda"))
+    A @ rhs
+    S = MixedVarCoefSolver(A)
+
+    def bounded(fn, *a, **k):  # a few iterations of each solver are enough here
+        try:
+            fn(*a, **k)
+        except _lib.NotConvergedError:
+            pass
+
+    w = torch.as_tensor(D.quad_points_and_weights()[1], device="cuda")
+    kw32 = torch.empty(32, 256, 256, dtype=torch.float32, device="cuda")
+    _lib.check(L.jfg_weighted_field_f64(2, 256, 32, kap.data_ptr(), w.data_ptr(),
+                                        A.kw.data_ptr(), kw32.data_ptr(),
+                                        _lib.stream_handle()), "weighted_field")
+    # two outer steps: the second updates the residual in FP32 (CUDA-core pass)
+    bounded(S.solve, rhs, tol=1e-11, max_outer=2, maxiter_inner=200)
+    bounded(pcg, VarCoefMatrix(T, kap[:4]), rhs[:4], tol=1e-10, maxiter=12)
+    # 4. learned guess: features, inference, map back; one training step
+    if os.path.exists(args.weights):
+        model = sno_train.load(args.weights, batch=32)
+        maps = sno_train.GridMaps()
+        X, s = sno_train.features(torch.log(kap), torch.as_tensor(f_h, device="cuda"), maps)
+        g = sno_train.initial_guess(model, maps, X, s)
+        bounded(S.solve, rhs, tol=1e-11, guess=g, max_outer=1, maxiter_inner=12)
+    m = SNO(SNOConfig(batch=8), seed=0)
+    Xs = torch.randn(8 * m.P, 16, device="cuda").to(torch.bfloat16)
+    Bn = m.set_input(Xs)
+    m.forward(Bn)
+    m.backward(Bn, torch.randn(8 * m.P, device="cuda"))
+    m.adam(1e-3)
+    # 5. Helmholtz: structured apply, one group, and the grouped uneven batch
+    Ns = rng.choice(np.arange(32, 257, 16), size=64)
+    al = rng.uniform(0, 50, size=64)
+    H = UnevenHelmholtzSolver("chebyshev", Ns, al)
+    bounded(H.solve, [rng.standard_normal((N - 2, N - 2)) for N in Ns], tol=1e-11,
+            max_refine=2)
+    helmholtz_apply("chebyshev", 130, 4.0, torch.as_tensor(rng.standard_normal((8, 128, 128)),
+                                                            device="cuda"))
+    bounded(H.solve_per_group, [rng.standard_normal((N - 2, N - 2)) for N in Ns],
+            tol=1e-11, max_refine=1)
+    torch.cuda.synchronize()
+    print(json.dumps({"tour": "done", "device_status": int(L.jfg_device_status()),
+                      "launches": int(L.jfg_launch_count())}), flush=True)
     return 0
 
 
@@ -765,9 +856,11 @@ def main():
                          "contraction at the variable-coefficient pass shape; df64 = the same "
                          "pass in double-FP32 arithmetic")
     ap.add_argument("--config", default="varcoef2d",
-                    choices=["varcoef2d", "transforms", "helmholtz", "varcoef3d"],
+                    choices=["varcoef2d", "transforms", "helmholtz", "varcoef3d", "tour"],
                     help="varcoef2d: the headline; transforms: batched 3-D Chebyshev "
-                         "round trip; helmholtz: uneven Helmholtz batch (secondary reports)")
+                         "round trip; helmholtz: uneven Helmholtz batch; varcoef3d: 3-D "
+                         "variable coefficient (secondary reports); tour: every kernel once "
+                         "(for profiling)")
     ap.add_argument("--nprob", type=int, default=1024)
     ap.add_argument("--n3d", type=int, default=128)
     # 3-D stopping rules (calibrated to <= 1e-10 error on the seeded 128^3 problems)
@@ -785,6 +878,8 @@ def main():
         return run_helmholtz(args)
     if args.config == "varcoef3d":
         return run_varcoef3d(args)
+    if args.config == "tour":
+        return run_tour(args)
     if args.kernel_only:
         import torch
 

@@ -122,6 +122,16 @@ int jfg_contract_df64(const jfg_contract_desc* d, const double* op, const double
  */
 int jfg_contract_tc(const jfg_contract_desc* d, const float* op_hi, const float* op_lo,
                     const float* in, float* out, void* stream);
+/* The same contraction with the operator split into BF16 (hi, lo) pairs
+ * (jfg_split_bf16_host) and the FP32 input split into BF16 pairs in the
+ * kernel: three BF16 MMAs (hi*hi + hi*lo + lo*hi, FP32 accumulate) per
+ * product at twice the TF32 rate; ~2^-16 relative per product.  For the
+ * HBM-bound batched transforms.  op_ld, op_seg % 8 == 0. */
+int jfg_contract_tc_bf16x3(const jfg_contract_desc* d, const uint16_t* op_hi,
+                           const uint16_t* op_lo, const float* in, float* out, void* stream);
+/* Split n FP64 values into BF16 hi (round to nearest even) and lo = x - hi
+ * rounded to BF16 (host arrays of BF16 bit patterns). */
+void jfg_split_bf16_host(size_t n, const double* src, uint16_t* hi, uint16_t* lo);
 /* Kernel variant of jfg_contract_tc: 1 (default) keeps the split input tile
  * (MMA operand A) in TMEM, written by the split warps with tcgen05.st, so the
  * MMAs read only operand B from shared memory; 0 keeps A in shared memory. */
@@ -186,6 +196,12 @@ int jfg_tp_apply_f32(int ndim, const int* rows, const int* cols, int batch,
 int jfg_tp_apply_tc(int ndim, const int* rows, const int* cols, int batch,
                     const float* const* mats_hi, const float* const* mats_lo, const float* in,
                     float* out, void* work, size_t work_bytes, void* stream);
+/* ... and with split-BF16 operators (jfg_contract_tc_bf16x3 per pass; cols % 8
+ * == 0 for the BF16 operator rows). */
+int jfg_tp_apply_tc_bf16x3(int ndim, const int* rows, const int* cols, int batch,
+                           const uint16_t* const* mats_hi, const uint16_t* const* mats_lo,
+                           const float* in, float* out, void* work, size_t work_bytes,
+                           void* stream);
 
 /* ---- fast-diagonalisation solve ----------------------------------------
  * TPMatricesLUFactors.solve (src/jaxfun/la/tpmatrix.py:545-587), batched:

@@ -62,6 +62,7 @@ struct TcGroup {
   int seg_in_map;  // 1 if the input map has a segment dimension
   int bat_in_map;  // 1 if the input map has a batch dimension
   int seg_op_map;  // 1 if the operator maps have a segment dimension
+  int mc_inner;    // tile order: operator chunks innermost (inputs beyond L2)
 };
 
 // Kernel parameter block (__grid_constant__): groups and their tensor maps
@@ -189,6 +190,29 @@ __device__ __forceinline__ void mma_tf32_ta(uint32_t tmem, uint32_t a_tmem, uint
       "r"(a_tmem), "l"(b), "r"(idesc), "r"(accum));
 }
 
+// Instruction descriptor: kind::f16 with BF16 A/B, D = F32, both K-major.
+__host__ __device__ constexpr uint32_t idesc_b16(int M, int N) {
+  return (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(N >> 3) << 17) |
+         ((uint32_t)(M >> 4) << 24);
+}
+
+// BF16 MMA (K = 16) with operand A read from TMEM (128 lanes x 8 columns of
+// packed BF16 pairs).
+__device__ __forceinline__ void mma_b16_ta(uint32_t tmem, uint32_t a_tmem, uint64_t b,
+                                           uint32_t idesc, uint32_t accum) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], [%1], %2, %3, p;\n\t}" ::"r"(tmem),
+      "r"(a_tmem), "l"(b), "r"(idesc), "r"(accum));
+}
+
+// Round-to-nearest-even FP32 -> BF16 bits (finite inputs).
+__device__ __forceinline__ uint32_t bf16_bits(float x) {
+  const uint32_t u = __float_as_uint(x);
+  return (u + 0x7FFFu + ((u >> 16) & 1u)) >> 16;
+}
+
 // Store 32 consecutive 32-bit columns of this thread's TMEM lane.
 __device__ __forceinline__ void tmem_st32(uint32_t taddr, const uint32_t* v) {
   asm volatile(
@@ -231,23 +255,28 @@ __device__ __forceinline__ float tf32_hi(float x) {
 
 // Persistent kernel over one or more groups of problems.  Group gi has its own
 // descriptor, operator tile height Mtile and tensor maps; its tiles are
-// t = tb[gi] + ((slot * nseg + s) * mchunks + mc) * nptiles + pt, covering p rows
+// t = tb[gi] + ((slot * nseg + s) * mchunks + mc) * nptiles + pt (or, for inputs
+// larger than L2, ((slot * nseg + s) * nptiles + pt) * mchunks + mc), covering p rows
 // [pt*128, +128) and operator rows [mc*Mtile, +Mtile) of problem slot / segment
 // s.  Each CTA walks t = blockIdx.x, blockIdx.x + gridDim.x, ...; two TMEM
 // accumulator buffers let the epilogue of tile i overlap the main loop of
 // tile i+1.  The tile prefix tb[] is formed on the device from the active
 // counts, so listed (active-subset) groups need no host round trip.
-template <int EPI, bool BETA, int G>
+template <int EPI, bool BETA, int G, bool B16>
 __global__ void __launch_bounds__(NTHREADS, 1)
     k_contract_tc(const __grid_constant__ TcLaunch<G> L) {
+  // K elements per block: 32 TF32 (one 128-byte row) or 64 BF16 (one 128-byte
+  // operator row; the FP32 input block then takes two TMA boxes)
+  constexpr int KE = B16 ? 64 : KB;
+  constexpr uint32_t XB = B16 ? 2 * XBYTES : XBYTES;
   extern __shared__ uint8_t smem_raw[];
   __shared__ long long tb[G + 1];
   __shared__ int nbs[G];
   uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   const int S = L.stages;
-  const bool ta = L.tmem_a != 0;
-  const uint32_t omax = (uint32_t)L.mt_max * KB * 4;
-  const uint32_t xbuf = ta ? XBYTES : 2 * XBYTES;  // X tile (+ its lo part when in SMEM)
+  const bool ta = B16 || L.tmem_a != 0;
+  const uint32_t omax = (uint32_t)L.mt_max * 128;  // Mtile rows of 128 B (hi or lo)
+  const uint32_t xbuf = ta ? XB : 2 * XBYTES;  // X block (+ its lo part when in SMEM)
   const uint32_t stage_bytes = xbuf + 2 * omax;
   const uint32_t acc_stride = ta ? ACC_STRIDE_TA : 256;
 
@@ -313,15 +342,23 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     const int nptiles = (q.d.P + TILE_P - 1) / TILE_P;
     const int mchunks = (q.d.M + q.Mtile - 1) / q.Mtile;
     long long r = t - tb[gi];
-    pt = (int)(r % nptiles);
-    r /= nptiles;
-    mc = (int)(r % mchunks);
-    const int bs = (int)(r / mchunks);
+    int bs;
+    if (q.mc_inner) {  // the CTAs that share an input tile run it at the same time
+      mc = (int)(r % mchunks);
+      r /= mchunks;
+      pt = (int)(r % nptiles);
+      bs = (int)(r / nptiles);
+    } else {           // the CTAs that share an operator chunk run it at the same time
+      pt = (int)(r % nptiles);
+      r /= nptiles;
+      mc = (int)(r % mchunks);
+      bs = (int)(r / mchunks);
+    }
     const int slot = bs / q.d.nseg;
     s = bs - slot * q.d.nseg;
     b = active_problem(q.d.batch_list, nbs[gi], q.d.batch, slot);
   };
-  auto nkb_of = [&](int gi) { return (L.g[gi].d.K + KB - 1) / KB; };
+  auto nkb_of = [&](int gi) { return (L.g[gi].d.K + KE - 1) / KE; };
 
   if (warp == 0) {
     // ---------------- TMA producer ----------------
@@ -335,7 +372,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         const int cs = q.seg_in_map ? s : 0;
         const int cb = (q.bat_in_map && b > 0) ? b : 0;
         const int os = q.seg_op_map ? s : 0;
-        const uint32_t obytes = (uint32_t)q.Mtile * KB * 4;
+        const uint32_t obytes = (uint32_t)q.Mtile * 128;
         const int nkb = nkb_of(gi);
         for (int kb = 0; kb < nkb; ++kb, ++g) {
           const int st = (int)(g % S);
@@ -344,10 +381,13 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             ok = false;
             break;
           }
-          mbar_expect_tx(&full[st], XBYTES + 2 * obytes);
-          tma_load_4d(Xh(st), &L.maps[gi][0], &full[st], kb * KB, pt * TILE_P, cs, cb);
-          tma_load_3d(Oh(st), &L.maps[gi][1], &full[st], kb * KB, mc * q.Mtile, os);
-          tma_load_3d(Ol(st), &L.maps[gi][2], &full[st], kb * KB, mc * q.Mtile, os);
+          mbar_expect_tx(&full[st], XB + 2 * obytes);
+          tma_load_4d(Xh(st), &L.maps[gi][0], &full[st], kb * KE, pt * TILE_P, cs, cb);
+          if (B16)
+            tma_load_4d(Xh(st) + XBYTES, &L.maps[gi][0], &full[st], kb * KE + KB,
+                        pt * TILE_P, cs, cb);
+          tma_load_3d(Oh(st), &L.maps[gi][1], &full[st], kb * KE, mc * q.Mtile, os);
+          tma_load_3d(Ol(st), &L.maps[gi][2], &full[st], kb * KE, mc * q.Mtile, os);
           issued = g + 1;
         }
       }
@@ -364,7 +404,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       for (long long t = blockIdx.x; t < ntiles && ok; t += gridDim.x, ++li) {
         int gi, pt, mc, b, s;
         decode(t, gi, pt, mc, b, s);
-        const uint32_t idesc = idesc_tf32(TILE_P, L.g[gi].Mtile);
+        const uint32_t idesc =
+            B16 ? idesc_b16(TILE_P, L.g[gi].Mtile) : idesc_tf32(TILE_P, L.g[gi].Mtile);
         const int nkb = nkb_of(gi);
         const int buf = li & 1;
         const uint32_t use = (uint32_t)(li >> 1);
@@ -382,7 +423,16 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           }
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
           const uint32_t oh = smem_u32(Oh(st)), ol = smem_u32(Ol(st));
-          if (ta) {
+          if (B16) {
+            const uint32_t ah = tmem + (uint32_t)(A_COL0 + 64 * st), al = ah + 32;
+#pragma unroll
+            for (int kk = 0; kk < 4; ++kk) {
+              const uint32_t off = kk * 32;  // 16 BF16 = 32 B of B per MMA, 8 A columns
+              mma_b16_ta(acc, ah + 8 * kk, sdesc(oh + off), idesc, (kb | kk) ? 1u : 0u);
+              mma_b16_ta(acc, ah + 8 * kk, sdesc(ol + off), idesc, 1u);
+              mma_b16_ta(acc, al + 8 * kk, sdesc(oh + off), idesc, 1u);
+            }
+          } else if (ta) {
             const uint32_t ah = tmem + (uint32_t)(A_COL0 + 64 * st), al = ah + 32;
 #pragma unroll
             for (int kk = 0; kk < KB / 8; ++kk) {
@@ -425,7 +475,37 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           ok = false;
           break;
         }
-        if (ta) {
+        if (B16) {
+          // 64 FP32 of this row (two swizzled 128-byte rows) -> BF16 hi / lo,
+          // packed in pairs (lower k in the lower half) into 32 TMEM columns each
+          uint32_t h[32], l[32];
+#pragma unroll
+          for (int half = 0; half < 2; ++half) {
+            const float4* xr = (const float4*)(Xh(st) + half * XBYTES + row * 128);
+#pragma unroll
+            for (int c = 0; c < 8; ++c) {
+              const float4 v = xr[c ^ (row & 7)];
+              const float vv[4] = {v.x, v.y, v.z, v.w};
+              uint32_t hb[4], lb[4];
+#pragma unroll
+              for (int e = 0; e < 4; ++e) {
+                hb[e] = bf16_bits(vv[e]);
+                lb[e] = bf16_bits(vv[e] - __uint_as_float(hb[e] << 16));
+              }
+              const int w = 16 * half + 2 * c;
+              h[w] = hb[0] | (hb[1] << 16);
+              h[w + 1] = hb[2] | (hb[3] << 16);
+              l[w] = lb[0] | (lb[1] << 16);
+              l[w + 1] = lb[2] | (lb[3] << 16);
+            }
+          }
+          const uint32_t tbase = tmem + ((uint32_t)(32 * (warp & 3)) << 16) +
+                                 (uint32_t)(A_COL0 + 64 * st);
+          tmem_st32(tbase, h);
+          tmem_st32(tbase + 32, l);
+          asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+          asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        } else if (ta) {
           const float4* xr = (const float4*)(Xh(st) + row * 128);
           uint32_t h[32], l[32];
 #pragma unroll
@@ -568,12 +648,13 @@ EncodeTiledFn encode_fn() {
   return fn;
 }
 
-int make_map(CUtensorMap* map, const float* base, int rank, const cuuint64_t* dims,
-             const cuuint64_t* strides_bytes, const cuuint32_t* box) {
+int make_map(CUtensorMap* map, const void* base, int rank, const cuuint64_t* dims,
+             const cuuint64_t* strides_bytes, const cuuint32_t* box,
+             CUtensorMapDataType dt = CU_TENSOR_MAP_DATA_TYPE_FLOAT32) {
   EncodeTiledFn fn = encode_fn();
   if (!fn) return JFG_ERR_UNSUPPORTED;
   cuuint32_t estr[5] = {1, 1, 1, 1, 1};
-  CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, (cuuint32_t)rank, (void*)base, dims,
+  CUresult r = fn(map, dt, (cuuint32_t)rank, (void*)base, dims,
                   strides_bytes, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
                   CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
                   CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
@@ -590,7 +671,9 @@ int setup_kernel_attr() {
   if (!done[dev]) {
     const int mx = 220 * 1024;
 #define JFG_SET_ATTR(E, B, G)                                                              \
-  JFG_CUDA_TRY(cudaFuncSetAttribute(k_contract_tc<E, B, G>,                                \
+  JFG_CUDA_TRY(cudaFuncSetAttribute(k_contract_tc<E, B, G, false>,                         \
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, mx));     \
+  JFG_CUDA_TRY(cudaFuncSetAttribute(k_contract_tc<E, B, G, true>,                          \
                                     cudaFuncAttributeMaxDynamicSharedMemorySize, mx))
 #define JFG_SET_ATTR_G(G)                   \
   JFG_SET_ATTR(JFG_EPI_NONE, false, G);     \
@@ -609,14 +692,16 @@ int setup_kernel_attr() {
 }
 
 // Validate one group and fill its descriptor, tile height and tensor maps.
-int fill_group(const jfg_contract_desc& d, const float* op_hi, const float* op_lo,
-               const float* in, float* out, TcGroup& q, CUtensorMap* maps) {
+// b16: the operator is BF16 (hi, lo) with 64-element K blocks, else TF32 in FP32 words.
+int fill_group(const jfg_contract_desc& d, const void* op_hi, const void* op_lo,
+               const float* in, float* out, TcGroup& q, CUtensorMap* maps, bool b16) {
   JFG_TRY(validate_desc(d));
   if (!op_hi || !op_lo || !in || !out) return JFG_ERR_ARG;
   // TMA: 16-byte aligned bases and strides
   auto al16 = [](const void* p) { return ((uintptr_t)p & 15u) == 0; };
   if (!al16(op_hi) || !al16(op_lo) || !al16(in)) return JFG_ERR_ARG;
-  if ((d.op_ld & 3) || (d.in_ld & 3) || (d.op_seg & 3) || (d.in_seg & 3) || (d.in_batch & 3))
+  const int om = b16 ? 7 : 3;  // operator strides in elements: multiples of 16 bytes
+  if ((d.op_ld & om) || (d.in_ld & 3) || (d.op_seg & om) || (d.in_seg & 3) || (d.in_batch & 3))
     return JFG_ERR_ARG;
   if ((long long)d.batch * d.nseg > 65535) return JFG_ERR_ARG;
   q.d = d;
@@ -625,6 +710,8 @@ int fill_group(const jfg_contract_desc& d, const float* op_hi, const float* op_l
   q.seg_in_map = (d.nseg > 1 && d.in_seg != 0) ? 1 : 0;
   q.bat_in_map = (d.batch > 1 && d.in_batch != 0) ? 1 : 0;
   q.seg_op_map = (d.nseg > 1 && d.op_seg != 0) ? 1 : 0;
+  // inputs that do not stay in L2 are read once if their operator chunks run together
+  q.mc_inner = (double)d.P * d.K * 4.0 * d.batch * d.nseg > 64.0 * 1024 * 1024 ? 1 : 0;
   {
     cuuint64_t dims[4] = {(cuuint64_t)d.K, (cuuint64_t)d.P,
                           (cuuint64_t)(q.seg_in_map ? d.nseg : 1),
@@ -636,13 +723,16 @@ int fill_group(const jfg_contract_desc& d, const float* op_hi, const float* op_l
     JFG_TRY(make_map(&maps[0], in, 4, dims, str, box));
   }
   {
+    const int eb = b16 ? 2 : 4;
     cuuint64_t dims[3] = {(cuuint64_t)d.K, (cuuint64_t)d.M,
                           (cuuint64_t)(q.seg_op_map ? d.nseg : 1)};
-    cuuint64_t str[2] = {(cuuint64_t)d.op_ld * 4,
-                         (cuuint64_t)(q.seg_op_map ? d.op_seg : d.op_ld * d.M) * 4};
-    cuuint32_t box[3] = {KB, (cuuint32_t)q.Mtile, 1};
-    JFG_TRY(make_map(&maps[1], op_hi, 3, dims, str, box));
-    JFG_TRY(make_map(&maps[2], op_lo, 3, dims, str, box));
+    cuuint64_t str[2] = {(cuuint64_t)d.op_ld * eb,
+                         (cuuint64_t)(q.seg_op_map ? d.op_seg : d.op_ld * d.M) * eb};
+    cuuint32_t box[3] = {(cuuint32_t)(128 / eb), (cuuint32_t)q.Mtile, 1};
+    const CUtensorMapDataType dt =
+        b16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+    JFG_TRY(make_map(&maps[1], op_hi, 3, dims, str, box, dt));
+    JFG_TRY(make_map(&maps[2], op_lo, 3, dims, str, box, dt));
   }
   return JFG_OK;
 }
@@ -654,9 +744,9 @@ long long group_tiles(const TcGroup& q) {
 
 // One launch over ng <= G groups (same epilogue kind and beta != 0 for all).
 template <int G>
-int launch_groups(int ng, const jfg_contract_desc* const* ds, const float* const* op_hi,
-                  const float* const* op_lo, const float* const* in, float* const* out,
-                  const jfg_tc_config& cfg, cudaStream_t st) {
+int launch_groups(int ng, const jfg_contract_desc* const* ds, const void* const* op_hi,
+                  const void* const* op_lo, const float* const* in, float* const* out,
+                  const jfg_tc_config& cfg, bool b16, cudaStream_t st) {
   static_assert(sizeof(TcLaunch<G>) <= 32000, "kernel parameter block too large");
   TcLaunch<G> L;
   memset(&L, 0, sizeof(L));
@@ -667,13 +757,13 @@ int launch_groups(int ng, const jfg_contract_desc* const* ds, const float* const
   int mt_max = 16;
   for (int i = 0; i < ng; ++i) {
     if (ds[i]->epilogue != epi || (ds[i]->beta != 0.0) != hb) return JFG_ERR_ARG;
-    JFG_TRY(fill_group(*ds[i], op_hi[i], op_lo[i], in[i], out[i], L.g[i], L.maps[i]));
+    JFG_TRY(fill_group(*ds[i], op_hi[i], op_lo[i], in[i], out[i], L.g[i], L.maps[i], b16));
     tiles += group_tiles(L.g[i]);
     if (L.g[i].Mtile > mt_max) mt_max = L.g[i].Mtile;
   }
   if (tiles == 0) return JFG_OK;
-  const int ta = cfg.operand_a_in_tmem ? 1 : 0;
-  const size_t stage = (ta ? 1 : 2) * (size_t)XBYTES + 2 * (size_t)mt_max * KB * 4;
+  const int ta = (b16 || cfg.operand_a_in_tmem) ? 1 : 0;
+  const size_t stage = (b16 ? 2 : ta ? 1 : 2) * (size_t)XBYTES + 2 * (size_t)mt_max * 128;
   int stages = (int)((200 * 1024) / stage);
   if (stages > (ta ? 4 : 6)) stages = ta ? 4 : 6;
   if (cfg.stages >= 2 && cfg.stages < stages) stages = cfg.stages;
@@ -691,10 +781,17 @@ int launch_groups(int ng, const jfg_contract_desc* const* ds, const float* const
   JFG_TRY(setup_kernel_attr());
 #define JFG_LAUNCH(E)                                                       \
   do {                                                                      \
-    if (hb)                                                                 \
-      k_contract_tc<E, true, G><<<grid, NTHREADS, smem, st>>>(L);           \
-    else                                                                    \
-      k_contract_tc<E, false, G><<<grid, NTHREADS, smem, st>>>(L);          \
+    if (b16) {                                                              \
+      if (hb)                                                               \
+        k_contract_tc<E, true, G, true><<<grid, NTHREADS, smem, st>>>(L);   \
+      else                                                                  \
+        k_contract_tc<E, false, G, true><<<grid, NTHREADS, smem, st>>>(L);  \
+    } else {                                                                \
+      if (hb)                                                               \
+        k_contract_tc<E, true, G, false><<<grid, NTHREADS, smem, st>>>(L);  \
+      else                                                                  \
+        k_contract_tc<E, false, G, false><<<grid, NTHREADS, smem, st>>>(L); \
+    }                                                                       \
   } while (0)
   switch (epi) {
     case JFG_EPI_NONE:
@@ -734,7 +831,18 @@ int contract_tc(const jfg_contract_desc& d, const float* op_hi, const float* op_
                 const float* in, float* out, cudaStream_t st) {
   if (d.batch == 0 || d.M == 0 || d.P == 0) return validate_desc(d);
   const jfg_contract_desc* dp = &d;
-  return launch_groups<1>(1, &dp, &op_hi, &op_lo, &in, &out, tc_default_config(), st);
+  const void* oh = op_hi;
+  const void* ol = op_lo;
+  return launch_groups<1>(1, &dp, &oh, &ol, &in, &out, tc_default_config(), false, st);
+}
+
+int contract_tc_b16(const jfg_contract_desc& d, const uint16_t* op_hi, const uint16_t* op_lo,
+                    const float* in, float* out, cudaStream_t st) {
+  if (d.batch == 0 || d.M == 0 || d.P == 0) return validate_desc(d);
+  const jfg_contract_desc* dp = &d;
+  const void* oh = op_hi;
+  const void* ol = op_lo;
+  return launch_groups<1>(1, &dp, &oh, &ol, &in, &out, tc_default_config(), true, st);
 }
 
 int contract_tc_grouped(int ng, const jfg_contract_desc* ds, const float* const* op_hi,
@@ -761,8 +869,8 @@ int contract_tc_grouped(int ng, const jfg_contract_desc* ds, const float* const*
   for (size_t c0 = 0; c0 < ord.size(); c0 += GMAX) {
     const int n = (int)(ord.size() - c0 < (size_t)GMAX ? ord.size() - c0 : GMAX);
     const jfg_contract_desc* dp[GMAX];
-    const float* oh[GMAX];
-    const float* ol[GMAX];
+    const void* oh[GMAX];
+    const void* ol[GMAX];
     const float* ip[GMAX];
     float* op[GMAX];
     for (int k = 0; k < n; ++k) {
@@ -774,9 +882,9 @@ int contract_tc_grouped(int ng, const jfg_contract_desc* ds, const float* const*
       op[k] = out[i];
     }
     if (n == 1)
-      JFG_TRY(launch_groups<1>(1, dp, oh, ol, ip, op, cfg, st));
+      JFG_TRY(launch_groups<1>(1, dp, oh, ol, ip, op, cfg, false, st));
     else
-      JFG_TRY(launch_groups<GMAX>(n, dp, oh, ol, ip, op, cfg, st));
+      JFG_TRY(launch_groups<GMAX>(n, dp, oh, ol, ip, op, cfg, false, st));
   }
   return JFG_OK;
 }
@@ -794,6 +902,34 @@ extern "C" int jfg_contract_tc(const jfg_contract_desc* d, const float* op_hi,
                                const float* op_lo, const float* in, float* out, void* stream) {
   if (!d) return JFG_ERR_ARG;
   return jfg::contract_tc(*d, op_hi, op_lo, in, out, (cudaStream_t)stream);
+}
+
+extern "C" int jfg_contract_tc_bf16x3(const jfg_contract_desc* d, const uint16_t* op_hi,
+                                      const uint16_t* op_lo, const float* in, float* out,
+                                      void* stream) {
+  if (!d) return JFG_ERR_ARG;
+  return jfg::contract_tc_b16(*d, op_hi, op_lo, in, out, (cudaStream_t)stream);
+}
+
+extern "C" void jfg_split_bf16_host(size_t n, const double* src, uint16_t* hi, uint16_t* lo) {
+  auto bits = [](float f) -> uint32_t {
+    uint32_t u;
+    memcpy(&u, &f, 4);
+    if ((u & 0x7F800000u) == 0x7F800000u) return u >> 16;  // inf / nan: truncate
+    return (u + 0x7FFFu + ((u >> 16) & 1u)) >> 16;         // round to nearest even
+  };
+  auto value = [](uint32_t b) -> float {
+    const uint32_t u = b << 16;
+    float f;
+    memcpy(&f, &u, 4);
+    return f;
+  };
+  for (size_t i = 0; i < n; ++i) {
+    const uint32_t h = bits((float)src[i]);
+    const uint32_t l = bits((float)(src[i] - (double)value(h)));
+    hi[i] = (uint16_t)h;
+    lo[i] = (uint16_t)l;
+  }
 }
 
 extern "C" int jfg_tc_set_variant(int operand_a_in_tmem) {

@@ -58,8 +58,10 @@ struct OpRef {
 };
 
 // Dispatch of one contraction pass to an engine.
-// DF: FP64 data, double-FP32 arithmetic (contract_df.cu).
-enum class Engine { F64, F32, TC, DF };
+// DF: FP64 data, double-FP32 arithmetic (contract_df.cu).  TB: FP32 data on
+// the tensor cores with a split-BF16 operator (OpRef<float> then points at
+// BF16 arrays).
+enum class Engine { F64, F32, TC, DF, TB };
 
 int contract_f64(const jfg_contract_desc& d, const double* op, const double* in, double* out,
                  cudaStream_t st);
@@ -69,6 +71,9 @@ int contract_df64(const jfg_contract_desc& d, const double* op, const double* in
                   cudaStream_t st);
 int contract_tc(const jfg_contract_desc& d, const float* op_hi, const float* op_lo,
                 const float* in, float* out, cudaStream_t st);
+// the same contraction with the operator as BF16 (hi, lo): three BF16 MMAs per product
+int contract_tc_b16(const jfg_contract_desc& d, const uint16_t* op_hi, const uint16_t* op_lo,
+                    const float* in, float* out, cudaStream_t st);
 // ngroups contractions in persistent grouped launches (contract_tc.cu)
 int contract_tc_grouped(int ng, const jfg_contract_desc* ds, const float* const* op_hi,
                         const float* const* op_lo, const float* const* in, float* const* out,
@@ -86,6 +91,8 @@ inline int contract(Engine e, const jfg_contract_desc& d, OpRef<double> op, cons
 inline int contract(Engine e, const jfg_contract_desc& d, OpRef<float> op, const float* in,
                     float* out, cudaStream_t st) {
   if (e == Engine::TC) return contract_tc(d, op.hi, op.lo, in, out, st);
+  if (e == Engine::TB)
+    return contract_tc_b16(d, (const uint16_t*)op.hi, (const uint16_t*)op.lo, in, out, st);
   return contract_f32(d, op.hi, in, out, st);
 }
 

@@ -343,6 +343,20 @@ extern "C" int jfg_tp_apply_tc(int ndim, const int* rows, const int* cols, int b
                               work_bytes, (cudaStream_t)stream);
 }
 
+extern "C" int jfg_tp_apply_tc_bf16x3(int ndim, const int* rows, const int* cols, int batch,
+                                      const uint16_t* const* mats_hi,
+                                      const uint16_t* const* mats_lo, const float* in,
+                                      float* out, void* work, size_t work_bytes, void* stream) {
+  if (!mats_hi || !mats_lo || ndim < 1 || ndim > 3) return JFG_ERR_ARG;
+  OpRef<float> m[3];
+  for (int i = 0; i < ndim; ++i) {
+    if (!mats_hi[i] || !mats_lo[i]) return JFG_ERR_ARG;
+    m[i] = OpRef<float>{(const float*)mats_hi[i], (const float*)mats_lo[i]};
+  }
+  return jfg::tp_apply<float>(Engine::TB, ndim, rows, cols, batch, m, in, out, work,
+                              work_bytes, (cudaStream_t)stream);
+}
+
 extern "C" size_t jfg_fd_solve_workspace_size(int ndim, int n, int batch, int elem_bytes) {
   return jfg::fd_ws(ndim, n, batch, elem_bytes);
 }

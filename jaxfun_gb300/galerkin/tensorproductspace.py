@@ -98,6 +98,51 @@ def tp_apply_tc(mats: list[np.ndarray], x) -> torch.Tensor:
     return out
 
 
+_SPLIT16_CACHE: dict[tuple, tuple] = {}
+
+
+def device_op_split_bf16(mat: np.ndarray):
+    """Upload (once) the BF16 (hi, lo) split of a host FP64 operator."""
+    key = (id(mat), mat.shape, torch.cuda.current_device())
+    t = _SPLIT16_CACHE.get(key)
+    if t is None:
+        a = np.ascontiguousarray(mat, dtype=np.float64)
+        hi = np.empty(a.shape, dtype=np.uint16)
+        lo = np.empty(a.shape, dtype=np.uint16)
+        _lib.lib().jfg_split_bf16_host(a.size, a.ctypes.data, hi.ctypes.data, lo.ctypes.data)
+        t = (torch.as_tensor(hi.view(np.int16), device="cuda"),
+             torch.as_tensor(lo.view(np.int16), device="cuda"), mat)
+        _SPLIT16_CACHE[key] = t
+    return t[0], t[1]
+
+
+def tp_apply_bf16x3(mats: list[np.ndarray], x) -> torch.Tensor:
+    """Tensor-core version of ``tp_apply`` with split-BF16 operators (three BF16
+    MMAs per product, FP32 accumulation): FP32 data, for HBM-bound transforms."""
+    nd = len(mats)
+    x = as_device(x, torch.float32)
+    cols = [m.shape[1] for m in mats]
+    rows = [m.shape[0] for m in mats]
+    if list(x.shape[x.ndim - nd :]) != cols:
+        raise ValueError(f"trailing shape {tuple(x.shape[x.ndim - nd:])} != {tuple(cols)}")
+    lead = x.shape[: x.ndim - nd]
+    batch = int(np.prod(lead)) if lead else 1
+    out = torch.empty(lead + tuple(rows), dtype=torch.float32, device=x.device)
+    if batch == 0:
+        return out
+    L = _lib.lib()
+    r_a, c_a = _lib.int_array(rows), _lib.int_array(cols)
+    ws = workspace(L.jfg_tp_apply_workspace_size(nd, r_a, c_a, batch, 4))
+    ops = [device_op_split_bf16(m) for m in mats]
+    st = L.jfg_tp_apply_tc_bf16x3(nd, r_a, c_a, batch,
+                                  _lib.ptr_array([o[0].data_ptr() for o in ops]),
+                                  _lib.ptr_array([o[1].data_ptr() for o in ops]), x.data_ptr(),
+                                  out.data_ptr(), ws.data_ptr(), ws.numel(),
+                                  _lib.stream_handle())
+    _lib.check(st, "jfg_tp_apply_tc_bf16x3")
+    return out
+
+
 def _apply_1d(mat: np.ndarray, x) -> torch.Tensor:
     return tp_apply([mat], x)
 
@@ -152,11 +197,14 @@ class TensorProductSpace:
         return W
 
     # ---- transforms (tensorproductspace.py:330-417) -------------------------
-    # precision: "f64" (FP64 CUDA cores, parity path) or "tc" (FP32 data,
+    # precision: "f64" (FP64 CUDA cores, parity path), "bf16x3" (FP32 data,
+    # split-BF16 operators, three BF16 MMAs per product) or "tc" (FP32 data,
     # split-TF32 tcgen05 contractions)
     def _apply(self, mats, x, precision):
         if precision == "f64":
             return tp_apply(mats, x)
+        if precision == "bf16x3":
+            return tp_apply_bf16x3(mats, x)
         if precision == "tc":
             return tp_apply_tc(mats, x)
         raise ValueError(f"unknown precision {precision!r}")

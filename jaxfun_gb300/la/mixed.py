@@ -50,13 +50,18 @@ class MixedVarCoefSolver:
     """Solve A(kappa_b) x_b = rhs_b for a batch with the mixed-precision path."""
 
     def __init__(self, A: VarCoefMatrix, M: TPMatricesLUFactors | None = None,
-                 residual: str = "df64"):
+                 residual: str = "df64", fp32_updates: bool | None = None):
         """``residual``: arithmetic of the refinement residual r = b - A x,
-        "df64" (double-FP32 on the FP32 units) or "f64" (FP64 FMAs)."""
+        "df64" (double-FP32 on the FP32 units) or "f64" (FP64 FMAs).
+        ``fp32_updates``: once ||r|| <= 1e-4 ||b||, update r -= ||r|| A d in FP32
+        instead of recomputing it (default: in 2-D only; in 3-D the operator's
+        conditioning turns the FP32 update error into > 1e-10 solution error)."""
         if residual not in ("df64", "f64"):
             raise ValueError(f"residual must be 'df64' or 'f64', not {residual!r}")
         self.A = A
         nd, n, nq = A.ndim, A.n, A.nq
+        if fp32_updates is None:
+            fp32_updates = nd == 2
         s0 = A.T.basespaces[0]
         B = s0.backward_matrix(None, 0)
         D = s0.backward_matrix(None, 1)
@@ -74,7 +79,8 @@ class MixedVarCoefSolver:
                               self.ops_hi.data_ptr(), self.ops_lo.data_ptr(),
                               self.kw32.data_ptr(), self.E_hi.data_ptr(), self.E_lo.data_ptr(),
                               self.W_hi.data_ptr(), self.W_lo.data_ptr(), self.lam.data_ptr(),
-                              None, self.ops32.data_ptr(), 1 if residual == "df64" else 0)
+                              None, self.ops32.data_ptr() if fp32_updates else None,
+                              1 if residual == "df64" else 0)
 
     def workspace_bytes(self) -> int:
         A = self.A
