@@ -274,6 +274,28 @@ def other_kernel_microbench(which: str, B: int, reps: int = 3):
                                        s.cuda_stream)
         flops = 2.0 * M * N * K * B
         name = "k_gemm_bf16"
+    elif which in ("transform", "transform_tf32"):
+        from jaxfun_gb300.galerkin import Chebyshev
+        from jaxfun_gb300.galerkin.tensorproductspace import device_op_split, device_op_split_bf16
+
+        N_ = N_GRID
+        F = Chebyshev(N_).forward_matrix()
+        M, P, K = N_, N_ * N_, N_
+        x = torch.randn(B, P, K, device="cuda")
+        y = torch.empty(B, M, P, device="cuda")
+        d = _lib.ContractDesc(batch=B, nseg=1, M=M, P=P, K=K, op_ld=K, in_ld=K, in_batch=P * K,
+                              out_ld=P, out_batch=M * P, alpha=1.0, beta=0.0)
+        if which == "transform":
+            hi, lo = device_op_split_bf16(F)
+            fn = L.jfg_contract_tc_bf16x3
+        else:
+            hi, lo = device_op_split(F)
+            fn = L.jfg_contract_tc
+        call = lambda: fn(d, hi.data_ptr(), lo.data_ptr(), x.data_ptr(), y.data_ptr(),  # noqa: E731
+                          s.cuda_stream)
+        flops = 2.0 * M * P * K * B
+        name = "k_contract_tc (" + ("split-BF16" if which == "transform" else "split-TF32") + ")"
+        nbytes = 4.0 * B * P * (K + M)
     else:
         N_ = N_GRID
         n = N_ - 2
@@ -298,7 +320,10 @@ def other_kernel_microbench(which: str, B: int, reps: int = 3):
     e1.record(s)
     e1.synchronize()
     t = e0.elapsed_time(e1) / 1e3 / reps
-    return {"kernel": name, "t": t, "tflops": flops / t / 1e12}
+    out = {"kernel": name, "t": t, "tflops": flops / t / 1e12}
+    if which.startswith("transform"):
+        out["gbs"] = nbytes / t / 1e9
+    return out
 
 
 def run_transforms(args):
@@ -848,13 +873,14 @@ def main():
     ap.add_argument("--weights", default=os.path.join(
         ROOT, "jaxfun_gb300", "sno", "weights", "sno_varcoef2d_N256.npz"))
     ap.add_argument("--kernel-only", nargs="?", const="contract", default=None,
-                    choices=["contract", "gemm", "fp64", "df64"],
+                    choices=["contract", "gemm", "fp64", "df64", "transform", "transform_tf32"],
                     help="time one kernel and print its numbers (used for ncu captures): "
                          "contract = tcgen05 split-TF32 contraction, B problems of 256^3; "
                          "gemm = BF16 GEMM of the neural operator's spectral transform "
                          "(1024 x 64 x 4096 per sample, B samples); fp64 = FP64 CUDA-core "
                          "contraction at the variable-coefficient pass shape; df64 = the same "
-                         "pass in double-FP32 arithmetic")
+                         "pass in double-FP32 arithmetic; transform(_tf32) = one split-BF16 "
+                         "(split-TF32) pass of the 3-D 256^3 Chebyshev transform, B fields")
     ap.add_argument("--config", default="varcoef2d",
                     choices=["varcoef2d", "transforms", "helmholtz", "varcoef3d", "tour"],
                     help="varcoef2d: the headline; transforms: batched 3-D Chebyshev "

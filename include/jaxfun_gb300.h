@@ -136,6 +136,11 @@ void jfg_split_bf16_host(size_t n, const double* src, uint16_t* hi, uint16_t* lo
  * (MMA operand A) in TMEM, written by the split warps with tcgen05.st, so the
  * MMAs read only operand B from shared memory; 0 keeps A in shared memory. */
 int jfg_tc_set_variant(int operand_a_in_tmem);
+/* Epilogue output path of the tensor-core contractions: 1 (default) stages
+ * 32 x 32 output boxes in shared memory and writes them with TMA bulk tensor
+ * stores where the output rows are 16-byte aligned (and beta == 0); 0 uses
+ * plain coalesced stores everywhere. */
+int jfg_tc_set_store_path(int tma_store);
 /* Launch configuration of the tensor-core contraction. */
 typedef struct {
   int operand_a_in_tmem; /* 1: split input tile in TMEM; 0: in shared memory          */

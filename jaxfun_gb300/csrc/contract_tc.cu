@@ -42,6 +42,9 @@ __device__ int g_tc_status = 0;
 // Kernel variant: 1 keeps the split input tile in TMEM (default), 0 in shared
 // memory (jfg_tc_set_variant).
 static int g_operand_a_in_tmem = 1;
+// Epilogue output path: 1 TMA stores through shared memory where the layout
+// allows (default), 0 plain coalesced stores (jfg_tc_set_store_path).
+static int g_tma_store = 1;
 
 namespace {
 
@@ -63,19 +66,23 @@ struct TcGroup {
   int bat_in_map;  // 1 if the input map has a batch dimension
   int seg_op_map;  // 1 if the operator maps have a segment dimension
   int mc_inner;    // tile order: operator chunks innermost (inputs beyond L2)
+  int tma_store;   // epilogue stores 32 x 32 boxes through shared memory with TMA
 };
 
 // Kernel parameter block (__grid_constant__): groups and their tensor maps
-// (input X, operator hi, operator lo).
+// (input X, operator hi, operator lo, output for TMA stores).
+constexpr uint32_t STAGE_OUT = 32 * 32 * 4;  // one epilogue warp's output box (4 KB)
+constexpr int SMEM_MAX = 227 * 1024 - 1024;   // dynamic shared memory (static use < 1 KB)
 template <int G>
 struct TcLaunch {
-  CUtensorMap maps[G][3];
+  CUtensorMap maps[G][4];
   TcGroup g[G];
   int ngroups;
   int stages;
   int tmem_cols;
   int tmem_a;   // 1: split input tile (MMA operand A) kept in TMEM, not shared memory
   int mt_max;   // largest Mtile: sets the stage layout
+  int out_stage; // 1 if any group stores through shared memory (8 x 4 KB after the stages)
 };
 
 // TMEM column map when operand A lives in TMEM: accumulator buffers at
@@ -153,6 +160,17 @@ __device__ __forceinline__ void tma_load_4d(void* dst, const CUtensorMap* map, u
       : "memory");
 }
 
+// Bulk tensor store of a shared-memory box (no swizzle) to global, tracked in
+// this thread's bulk async-group.
+__device__ __forceinline__ void tma_store_4d(const CUtensorMap* map, const void* src, int c0,
+                                             int c1, int c2, int c3) {
+  asm volatile(
+      "cp.async.bulk.tensor.4d.global.shared::cta.bulk_group [%0, {%2, %3, %4, %5}], [%1];" ::"l"(
+          reinterpret_cast<uint64_t>(map)),
+      "r"(smem_u32(src)), "r"(c0), "r"(c1), "r"(c2), "r"(c3)
+      : "memory");
+}
+
 // Shared-memory matrix descriptor: K-major operand, 128-byte swizzle, 8-row
 // core-matrix groups 1024 B apart.
 __device__ __forceinline__ uint64_t sdesc(uint32_t saddr) {
@@ -207,10 +225,11 @@ __device__ __forceinline__ void mma_b16_ta(uint32_t tmem, uint32_t a_tmem, uint6
       "r"(a_tmem), "l"(b), "r"(idesc), "r"(accum));
 }
 
-// Round-to-nearest-even FP32 -> BF16 bits (finite inputs).
-__device__ __forceinline__ uint32_t bf16_bits(float x) {
-  const uint32_t u = __float_as_uint(x);
-  return (u + 0x7FFFu + ((u >> 16) & 1u)) >> 16;
+// Two FP32 -> packed BF16 pair (round to nearest even): lo16 <- a, hi16 <- b.
+__device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
+  uint32_t d;
+  asm("cvt.rn.bf16x2.f32 %0, %1, %2;" : "=r"(d) : "f"(b), "f"(a));
+  return d;
 }
 
 // Store 32 consecutive 32-bit columns of this thread's TMEM lane.
@@ -296,7 +315,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   const long long ntiles = tb[L.ngroups];
   if ((long long)blockIdx.x >= ntiles) return;  // no tile for this CTA (uniform)
 
-  uint64_t* bars = (uint64_t*)(smem + (size_t)S * stage_bytes);
+  uint8_t* ostage = smem + (size_t)S * stage_bytes;  // epilogue output boxes (if used)
+  uint64_t* bars = (uint64_t*)(ostage + (L.out_stage ? 8 * STAGE_OUT : 0));
   uint64_t* full = bars;
   uint64_t* conv = bars + S;
   uint64_t* empty = bars + 2 * S;
@@ -485,18 +505,14 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 #pragma unroll
             for (int c = 0; c < 8; ++c) {
               const float4 v = xr[c ^ (row & 7)];
-              const float vv[4] = {v.x, v.y, v.z, v.w};
-              uint32_t hb[4], lb[4];
-#pragma unroll
-              for (int e = 0; e < 4; ++e) {
-                hb[e] = bf16_bits(vv[e]);
-                lb[e] = bf16_bits(vv[e] - __uint_as_float(hb[e] << 16));
-              }
               const int w = 16 * half + 2 * c;
-              h[w] = hb[0] | (hb[1] << 16);
-              h[w + 1] = hb[2] | (hb[3] << 16);
-              l[w] = lb[0] | (lb[1] << 16);
-              l[w + 1] = lb[2] | (lb[3] << 16);
+              const uint32_t h0 = pack_bf16x2(v.x, v.y), h1 = pack_bf16x2(v.z, v.w);
+              h[w] = h0;
+              h[w + 1] = h1;
+              l[w] = pack_bf16x2(v.x - __uint_as_float(h0 << 16),
+                                 v.y - __uint_as_float(h0 & 0xFFFF0000u));
+              l[w + 1] = pack_bf16x2(v.z - __uint_as_float(h1 << 16),
+                                     v.w - __uint_as_float(h1 & 0xFFFF0000u));
             }
           }
           const uint32_t tbase = tmem + ((uint32_t)(32 * (warp & 3)) << 16) +
@@ -596,7 +612,26 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         float v[32];
         tmem_ld16(tacc + (uint32_t)(c * 16), v);
         if (nj == 32) tmem_ld16(tacc + (uint32_t)(c * 16 + 16), v + 16);
-        if (pin) {
+        if (!BETA && q.tma_store) {
+          // stage this warp's 32 (p) x 32 (m) box in shared memory, [m][p] with p
+          // contiguous, and store it with one bulk tensor copy (out-of-range rows
+          // and columns are clipped by the copy)
+          float* box = (float*)(ostage + (size_t)(warp - 6) * STAGE_OUT);
+          if (lane == 0) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+          __syncwarp();
+#pragma unroll
+          for (int j = 0; j < 32; ++j) {
+            float r = v[j];  // rows outside the problem are clipped by the store
+            if (EPI == JFG_EPI_MUL_FIELD) r *= pin ? aux[j] : 0.f;
+            if (EPI == JFG_EPI_DIV_EIG) r = __fdividef(r, c0 + c1 * ((pin ? aux[j] : 1.f) + lp));
+            box[j * 32 + lane] = r * alpha;
+          }
+          asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+          __syncwarp();
+          if (lane == 0 && b >= 0)
+            tma_store_4d(&L.maps[gi][3], box, pt * TILE_P + 32 * q4, mb, s, b);
+          if (lane == 0) asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+        } else if (pin) {
 #pragma unroll
           for (int j = 0; j < 32; ++j) {
             const int m = mb + j;
@@ -615,6 +650,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       __syncwarp();
       if (lane == 0) mbar_arrive(&tempty[buf]);
     }
+    // bulk tensor stores of this warp complete before the kernel ends
+    if (lane == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
   }
   asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
   __syncthreads();
@@ -669,7 +706,7 @@ int setup_kernel_attr() {
   JFG_CUDA_TRY(cudaGetDevice(&dev));
   if (dev < 0 || dev >= 64) return JFG_ERR_UNSUPPORTED;
   if (!done[dev]) {
-    const int mx = 220 * 1024;
+    const int mx = SMEM_MAX;
 #define JFG_SET_ATTR(E, B, G)                                                              \
   JFG_CUDA_TRY(cudaFuncSetAttribute(k_contract_tc<E, B, G, false>,                         \
                                     cudaFuncAttributeMaxDynamicSharedMemorySize, mx));     \
@@ -734,6 +771,25 @@ int fill_group(const jfg_contract_desc& d, const void* op_hi, const void* op_lo,
     JFG_TRY(make_map(&maps[1], op_hi, 3, dims, str, box, dt));
     JFG_TRY(make_map(&maps[2], op_lo, 3, dims, str, box, dt));
   }
+  // output through TMA stores when its rows are 16-byte aligned and every
+  // 32-column group of a tile is full (else plain coalesced stores)
+  q.tma_store = 0;
+  if (al16(out) && (d.out_ld & 3) == 0 && (d.out_seg & 3) == 0 && (d.out_batch & 3) == 0 &&
+      q.Mtile % 32 == 0 && d.beta == 0.0) {
+    cuuint64_t dims[4] = {(cuuint64_t)d.P, (cuuint64_t)d.M, (cuuint64_t)d.nseg,
+                          (cuuint64_t)d.batch};
+    cuuint64_t str[3] = {(cuuint64_t)d.out_ld * 4,
+                         (cuuint64_t)(d.nseg > 1 ? d.out_seg : d.out_ld * d.M) * 4,
+                         (cuuint64_t)(d.batch > 1 ? d.out_batch : d.out_ld * d.M) * 4};
+    cuuint32_t box[4] = {32, 32, 1, 1};
+    EncodeTiledFn fn = encode_fn();
+    cuuint32_t estr[4] = {1, 1, 1, 1};
+    if (fn && fn(&maps[3], CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, (void*)out, dims, str, box, estr,
+                 CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_NONE,
+                 CU_TENSOR_MAP_L2_PROMOTION_NONE,
+                 CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS)
+      q.tma_store = 1;
+  }
   return JFG_OK;
 }
 
@@ -754,17 +810,20 @@ int launch_groups(int ng, const jfg_contract_desc* const* ds, const void* const*
   const int epi = ds[0]->epilogue;
   const bool hb = ds[0]->beta != 0.0;
   long long tiles = 0;
-  int mt_max = 16;
+  int mt_max = 16, ostage = 0;
   for (int i = 0; i < ng; ++i) {
     if (ds[i]->epilogue != epi || (ds[i]->beta != 0.0) != hb) return JFG_ERR_ARG;
     JFG_TRY(fill_group(*ds[i], op_hi[i], op_lo[i], in[i], out[i], L.g[i], L.maps[i], b16));
+    if (!g_tma_store) L.g[i].tma_store = 0;
     tiles += group_tiles(L.g[i]);
     if (L.g[i].Mtile > mt_max) mt_max = L.g[i].Mtile;
+    ostage |= L.g[i].tma_store;
   }
   if (tiles == 0) return JFG_OK;
   const int ta = (b16 || cfg.operand_a_in_tmem) ? 1 : 0;
   const size_t stage = (b16 ? 2 : ta ? 1 : 2) * (size_t)XBYTES + 2 * (size_t)mt_max * 128;
-  int stages = (int)((200 * 1024) / stage);
+  const size_t ob = ostage ? 8 * (size_t)STAGE_OUT : 0;
+  int stages = (int)((SMEM_MAX - 1024 - ob - 64 * 8) / stage);
   if (stages > (ta ? 4 : 6)) stages = ta ? 4 : 6;
   if (cfg.stages >= 2 && cfg.stages < stages) stages = cfg.stages;
   if (stages < 2) return JFG_ERR_UNSUPPORTED;
@@ -772,7 +831,9 @@ int launch_groups(int ng, const jfg_contract_desc* const* ds, const void* const*
   L.tmem_cols = 512;  // two accumulator buffers (+ operand A stages in TMEM mode)
   L.tmem_a = ta;
   L.mt_max = mt_max;
-  const size_t smem = 1024 + stages * stage + (3 * stages + 4) * 8 + 16;
+  L.out_stage = ostage;
+  const size_t smem = 1024 + stages * stage + ob + (3 * stages + 4) * 8 + 16;
+  if (smem > (size_t)SMEM_MAX) return JFG_ERR_UNSUPPORTED;
   int dev = 0, nsm = 0;
   JFG_CUDA_TRY(cudaGetDevice(&dev));
   JFG_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
@@ -930,6 +991,12 @@ extern "C" void jfg_split_bf16_host(size_t n, const double* src, uint16_t* hi, u
     hi[i] = (uint16_t)h;
     lo[i] = (uint16_t)l;
   }
+}
+
+extern "C" int jfg_tc_set_store_path(int tma_store) {
+  if (tma_store != 0 && tma_store != 1) return JFG_ERR_ARG;
+  jfg::g_tma_store = tma_store;
+  return JFG_OK;
 }
 
 extern "C" int jfg_tc_set_variant(int operand_a_in_tmem) {

@@ -112,3 +112,32 @@ def test_tc_rejects_misaligned_strides():
     st = L.jfg_contract_tc(d, x.data_ptr(), x.data_ptr(), x.data_ptr(), x.data_ptr(),
                            _lib.stream_handle())
     assert st == _lib.JFG_ERR_ARG
+
+
+@pytest.mark.parametrize("B,S,M,P,K,epi", [
+    (2, 1, 256, 256, 256, 0),
+    (3, 2, 200, 300, 96, 1),
+    (2, 1, 128, 130, 64, 2),
+    (1, 1, 512, 1024, 128, 0),
+])
+def test_tc_store_paths_agree(B, S, M, P, K, epi):
+    """TMA bulk-tensor stores through shared memory and plain stores write the
+    same values (out-of-range rows and columns clipped)."""
+    L = _lib.lib()
+    rng = np.random.default_rng(B + M + P)
+    op = rng.standard_normal((S, M, K))
+    x = rng.standard_normal((B, S, P, K)).astype(np.float32)
+    kw = {}
+    if epi == 1:
+        kw["field"] = rng.uniform(0.5, 2, (B, S, M, P))
+    if epi == 2:
+        kw.update(lam_m=rng.uniform(1, 2, M), lam_p=rng.uniform(1, 2, P),
+                  c0=rng.uniform(0, 1, B), c1=rng.uniform(1, 2, B))
+    outs = []
+    for path in (1, 0):
+        assert L.jfg_tc_set_store_path(path) == 0
+        try:
+            outs.append(run_tc(op, x, out0=np.full((B, S, M, P), 7.0), epi=epi, **kw))
+        finally:
+            L.jfg_tc_set_store_path(1)
+    assert np.array_equal(outs[0], outs[1])
