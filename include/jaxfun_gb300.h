@@ -208,6 +208,23 @@ int jfg_tp_apply_tc_bf16x3(int ndim, const int* rows, const int* cols, int batch
                            const float* in, float* out, void* work, size_t work_bytes,
                            void* stream);
 
+/* ---- batched banded LU (wavenumber solver) ------------------------------
+ * TPMatricesWavenumberSolver (src/jaxfun/la/tpmatrix.py:590-1013): one 1-D
+ * banded system per Fourier wavenumber, factored without pivoting
+ * (_lu_banded_no_pivot_kernel, src/jaxfun/la/diamatrix.py:1937-1973) and
+ * solved by forward / backward substitution, one GPU thread per system.
+ * data (nsys, ndiag, n) uses jaxfun's column-aligned DIA convention:
+ * data[s][d][j] = A_s[j - offsets[d]][j]; offsets (host) distinct, one of them
+ * 0.  p = max(0, -min offset), q = max(0, max offset); lu holds
+ * jfg_banded_lu_size(nsys, n, p, q) bytes.  The solve reads element i of
+ * system s at rhs[s*sys_stride + i*elem_stride] and writes x the same way
+ * (x may equal rhs). */
+size_t jfg_banded_lu_size(int nsys, int n, int p, int q);
+int jfg_banded_lu_factor_f64(int nsys, int n, int ndiag, const int* offsets, const double* data,
+                             double* lu, void* stream);
+int jfg_banded_lu_solve_f64(int nsys, int n, int p, int q, const double* lu, const double* rhs,
+                            double* x, long long sys_stride, long long elem_stride, void* stream);
+
 /* ---- fast-diagonalisation solve ----------------------------------------
  * TPMatricesLUFactors.solve (src/jaxfun/la/tpmatrix.py:545-587), batched:
  *   U_b = (x_ax W) [ (x_ax E) F_b / (c0[b] + c1[b] * sum_ax lam[i_ax]) ]

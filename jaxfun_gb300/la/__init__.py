@@ -16,3 +16,4 @@ from .varcoef import (  # noqa: F401
     pcg,
     poisson_tpmatrices,
 )
+from .wavenumber import TPMatricesWavenumberSolver  # noqa: F401

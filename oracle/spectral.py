@@ -481,3 +481,33 @@ def random_field_coeffs(rng, N, d):
         shp[ax] = -1
         k2 = k2 + (np.arange(N, dtype=np.float64) ** 2).reshape(shp)
     return z * (1.0 + k2) ** -1.5
+
+
+# ---------------------------------------------------------------------------
+# Per-wavenumber banded systems (Fourier x polynomial)
+# ---------------------------------------------------------------------------
+
+
+def dia_to_dense(data_s, offsets, n):
+    """Dense matrix of one system from column-aligned DIA data:
+    A[j - off][j] = data[d][j] (``DiaMatrix`` storage, src/jaxfun/la/
+    diamatrix.py:108-120, band convention of :1944)."""
+    A = np.zeros((n, n))
+    for d, off in enumerate(offsets):
+        for j in range(n):
+            i = j - off
+            if 0 <= i < n:
+                A[i, j] = data_s[d][j]
+    return A
+
+
+def wavenumber_solve(data, offsets, rhs_2d):
+    """Solve B_k x_k = b_k for every wavenumber k (rows of rhs_2d, the
+    polynomial axis last), as TPMatricesWavenumberSolver.solve
+    (src/jaxfun/la/tpmatrix.py:590-1013) does with banded LU; here with a
+    dense LAPACK solve per system (same solution to rounding)."""
+    n = rhs_2d.shape[1]
+    out = np.empty_like(rhs_2d)
+    for k in range(rhs_2d.shape[0]):
+        out[k] = np.linalg.solve(dia_to_dense(data[k], offsets, n), rhs_2d[k])
+    return out

@@ -150,3 +150,34 @@ def test_sno_training_reduces_loss():
         losses.append(m.backward(Bt, tgt))
         m.adam(3e-3)
     assert losses[-1] < 0.3 * losses[0], losses[::10]
+
+
+def test_learned_guess_saves_iterations():
+    """What the trained network gains: on held-out seeded problems of the
+    variable-coefficient benchmark (N = 256), starting the first inner solve
+    from the learned guess needs fewer inner PCG iterations than the zero
+    start, and both answers are within 1e-10 of a tight FP64 solve."""
+    import os
+
+    from jaxfun_gb300.la import MixedVarCoefSolver, VarCoefMatrix, pcg
+    from jaxfun_gb300.sno import train as T
+
+    path = os.path.join(os.path.dirname(T.__file__), "weights", "sno_varcoef2d_N256.npz")
+    model = T.load(path, batch=16)
+    maps = T.GridMaps()
+    data = T.generate(16, seed=7, maps=maps, keep_fine=True, log=lambda *_: None)
+    kap, f, b, _ = data["fine"][0]
+    A = VarCoefMatrix(maps.T, kap)
+    S = MixedVarCoefSolver(A)
+    xt, _ = pcg(A, b, tol=1e-14, maxiter=3000)
+    g = T.initial_guess(model, maps, data["X"], data["s"])
+    res = {}
+    for name, guess in (("zero", None), ("learned", g)):
+        x, it_in, _ = S.solve(b, tol=1e-11, inner_tol=1e-5, guess=guess)
+        err = float(((x - xt).abs().amax(dim=(1, 2)) / xt.abs().amax(dim=(1, 2))).max())
+        assert err <= 1e-10, (name, err)
+        res[name] = float(np.mean(it_in))
+    assert res["learned"] < 0.97 * res["zero"], res
+    # the guess itself is a usable approximation (coefficient-space L2, 32 modes)
+    rel = ((g - xt).norm(dim=(1, 2)) / xt.norm(dim=(1, 2))).mean()
+    assert float(rel) < 0.3

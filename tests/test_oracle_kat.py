@@ -120,3 +120,21 @@ def test_chebyshev_eigh_fd_is_wrong_general_eig_is_right():
     lam2, W2 = scipy.linalg.eigh(K, M)  # reads one triangle only
     bad = O.fd_solve(b, [W2, W2], [W2.T, W2.T], [lam2, lam2], c0=10.0)
     assert np.abs(bad - ref).max() > 1e-3 * np.abs(ref).max()
+
+
+def test_oracle_dia_convention():
+    """Column-aligned DIA: data[d][j] = A[j - off_d][j] (diamatrix.py:108-120)."""
+    from oracle import spectral as O
+
+    A = np.arange(1.0, 26.0).reshape(5, 5)
+    offsets = (-1, 0, 2)
+    data = np.zeros((3, 5))
+    for d, off in enumerate(offsets):
+        for j in range(5):
+            if 0 <= j - off < 5:
+                data[d, j] = A[j - off, j]
+    D = O.dia_to_dense(data, offsets, 5)
+    mask = np.zeros((5, 5), bool)
+    for off in offsets:
+        mask |= np.eye(5, k=off, dtype=bool)
+    assert np.array_equal(D, np.where(mask, A, 0.0))
