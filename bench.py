@@ -593,6 +593,32 @@ def run_varcoef3d(args):
         x, it_in, it_out = S.solve(b, tol=args.tol3d)
     torch.cuda.synchronize()
     t = (time.perf_counter() - t0) / args.steps
+    # learned initial guess (3-D spectral neural operator: 32^3 grid, 16^3 modes,
+    # width 32), its inference inside the timed region
+    learned = None
+    w3 = os.path.join(ROOT, "jaxfun_gb300", "sno", "weights", "sno_varcoef3d_N128.npz")
+    if os.path.exists(w3) and N == 128:
+        from jaxfun_gb300.sno import train as sno_train
+
+        model = sno_train.load(w3, batch=min(B, 16))
+        maps = sno_train.GridMaps(N=N, n=model.cfg.n, guess_modes=model.cfg.modes, ndim=3)
+        f_grid = To.backward(fh)
+
+        def solve_learned():
+            X, sc = sno_train.features(torch.log(kap), f_grid, maps)
+            guess = sno_train.initial_guess(model, maps, X, sc)
+            return S.solve(b, tol=args.tol3d, guess=guess)
+
+        for _ in range(args.warmup):
+            xl, il, ol = solve_learned()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            xl, il, ol = solve_learned()
+        torch.cuda.synchronize()
+        tl = (time.perf_counter() - t0) / args.steps
+        learned = {"solves_per_s": B / tl, "inner_iterations_mean": float(il.mean()),
+                   "outer_iterations_mean": float(ol.mean()), "x": xl}
     nf = min(B, 4)
     A4 = VarCoefMatrix(T, kap[:nf])
     torch.cuda.synchronize()
@@ -608,6 +634,14 @@ def run_varcoef3d(args):
             "mixed_outer_iterations_mean": float(it_out.mean()), "mixed_max_rel_err": err,
             "fp64_pcg_solves_per_s": nf / t64, "fp64_pcg_iterations_mean": float(it64.mean()),
             "fp64_pcg_max_rel_err": err64, "speedup": (B / t) / (nf / t64)}
+    if learned is not None:
+        xl = learned.pop("x")
+        learned["max_rel_err"] = float(((xl[:nf] - xt).abs().amax(dim=(1, 2, 3))
+                                        / xt.abs().amax(dim=(1, 2, 3))).max())
+        learned["inner_iterations_saved_mean"] = (line["mixed_inner_iterations_mean"]
+                                                  - learned["inner_iterations_mean"])
+        learned["speedup_vs_fp64_pcg"] = learned["solves_per_s"] / (nf / t64)
+        line["learned_mixed"] = learned
     print(json.dumps(line), flush=True)
     return 0
 

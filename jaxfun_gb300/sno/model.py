@@ -1,13 +1,13 @@
 """Spectral neural operator (SNO) for the variable-coefficient initial guess.
 
-Architecture (on an n x n Legendre-Gauss grid, channel width C, L spectral
-layers, nm x nm retained Legendre modes):
+Architecture (on an n^d Legendre-Gauss grid, d = 2 or 3, channel width C, L
+spectral layers, nm^d retained Legendre modes):
 
-    lift     U0 = X W_lift^T + b_lift                       X: (logk, f/s, x, y, 0...) 16 ch
+    lift     U0 = X W_lift^T + b_lift                       X: (logk, f/s, x, y[, z], 0...) 16 ch
     layer l  U_{l+1} = act( Psi (R_l . (Phi U_l)) + U_l W_l^T + b_l )   act = GELU except last
     project  Q = GELU(U_L W_p1^T + b_p1);  u = Q W_p2^T + b_p2   (channel 0)
 
-Phi (nm^2 x n^2) is the truncated Legendre forward transform, Psi (n^2 x nm^2)
+Phi (nm^d x n^d) is the truncated Legendre forward transform, Psi (n^d x nm^d)
 the backward transform, R_l[q] a C x C channel mixing per mode q.  Every
 contraction runs on the tensor cores through ``jfg_gemm_bf16`` (BF16 operands,
 FP32 accumulation, fused bias/GELU/residual/GELU-derivative epilogues that write
@@ -41,15 +41,20 @@ class SNOConfig:
     modes: int = 32    # retained modes per axis
     layers: int = 4
     batch: int = 32    # training batch
+    ndim: int = 2      # 2 (n x n grid) or 3 (n x n x n grid)
 
 
-def transform_matrices(n: int, modes: int) -> tuple[np.ndarray, np.ndarray]:
-    """Phi (modes^2 x n^2): truncated orthogonal Legendre forward transform on
-    the n-point Gauss grid; Psi (n^2 x modes^2): the backward transform."""
+def transform_matrices(n: int, modes: int, ndim: int = 2) -> tuple[np.ndarray, np.ndarray]:
+    """Phi (modes^d x n^d): truncated orthogonal Legendre forward transform on
+    the n-point Gauss grid in d = ndim dimensions; Psi (n^d x modes^d): the
+    backward transform."""
     L = Legendre(n)
     F = L.forward_matrix()[:modes, :]      # (modes, n)
     B = L.backward_matrix()[:, :modes]     # (n, modes)
-    return np.kron(F, F), np.kron(B, B)
+    Phi, Psi = F, B
+    for _ in range(ndim - 1):
+        Phi, Psi = np.kron(Phi, F), np.kron(Psi, B)
+    return Phi, Psi
 
 
 def _dev(a, dtype):
@@ -62,10 +67,10 @@ class SNO:
     def __init__(self, cfg: SNOConfig, seed: int = 0):
         self.cfg = cfg
         n, C_, m, L = cfg.n, cfg.width, cfg.modes, cfg.layers
-        self.P = n * n
-        self.NM = m * m
+        self.P = n ** cfg.ndim
+        self.NM = m ** cfg.ndim
         rng = np.random.default_rng(seed)
-        Phi, Psi = transform_matrices(n, m)
+        Phi, Psi = transform_matrices(n, m, cfg.ndim)
         self.Phi = _dev(Phi, BF)
         self.Psi = _dev(Psi, BF)
         self.PhiT = _dev(Phi.T, BF)
@@ -73,7 +78,7 @@ class SNO:
         # ---- parameters (FP32 masters) ----
         p = {}
         p["W_lift"] = rng.standard_normal((C_, CIN)) * np.sqrt(1.0 / 4)
-        p["W_lift"][:, 4:] = 0.0
+        p["W_lift"][:, 2 + cfg.ndim:] = 0.0  # inputs: log kappa, f, coordinates
         p["b_lift"] = np.zeros(C_)
         for l in range(L):
             p[f"W{l}"] = rng.standard_normal((C_, C_)) * np.sqrt(1.0 / C_)
@@ -106,7 +111,8 @@ class SNO:
 
     def state_dict(self) -> dict[str, np.ndarray]:
         out = {k: v.detach().cpu().numpy() for k, v in self.params.items()}
-        out["_config"] = np.array([self.cfg.n, self.cfg.width, self.cfg.modes, self.cfg.layers])
+        out["_config"] = np.array([self.cfg.n, self.cfg.width, self.cfg.modes, self.cfg.layers,
+                                   self.cfg.ndim])
         return out
 
     def load_state_dict(self, sd: dict[str, np.ndarray]):

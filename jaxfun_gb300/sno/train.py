@@ -1,15 +1,16 @@
 """Training data from the solver itself, training loop, and the learned
 initial guess for the variable-coefficient PCG.
 
-Data: seeded problems of the 2-D variable-coefficient Poisson benchmark
-(N = 256 Legendre Dirichlet; kappa = exp(g), g a Gaussian random field with
-Legendre coefficients N(0,1)(1+|k|^2)^-1.5 rescaled to std 1; forcing
-coefficients N(0,1)(1+j)^-2(1+k)^-2), solved by ``MixedVarCoefSolver``.
-Fields are moved to the network's 64 x 64 Legendre-Gauss grid by spectral
-truncation; the forcing and the solution are scaled by the forcing's RMS
-(the problem is linear in f).
+Data: seeded problems of the variable-coefficient Poisson benchmarks (2-D:
+N = 256 Legendre Dirichlet, network grid 64^2, 32^2 modes; 3-D: N = 128, grid
+32^3, 16^3 modes; kappa = exp(g), g a Gaussian random field with Legendre
+coefficients N(0,1)(1+|k|^2)^-1.5 rescaled to std 1; forcing coefficients
+N(0,1) prod_i (1+k_i)^-2), solved by ``MixedVarCoefSolver``.  Fields are moved
+to the network's Legendre-Gauss grid by spectral truncation; the forcing and
+the solution are scaled by the forcing's RMS (the problem is linear in f).
 
     python -m jaxfun_gb300.sno.train --train 20000 --test 1000 --epochs 8 --out ckpt.npz
+    python -m jaxfun_gb300.sno.train --ndim 3 --N 128 --n 32 --modes 16 --width 32 ...
 """
 
 from __future__ import annotations
@@ -33,8 +34,8 @@ N_FINE = 256
 class GridMaps:
     """Per-axis FP64 operators between the solver's space and the network grid."""
 
-    def __init__(self, N: int = N_FINE, n: int = 64, guess_modes: int = 32):
-        self.N, self.n = N, n
+    def __init__(self, N: int = N_FINE, n: int = 64, guess_modes: int = 32, ndim: int = 2):
+        self.N, self.n, self.ndim = N, n, ndim
         Lo, lo = Legendre(N), Legendre(n)
         # fine-grid field -> first n Legendre modes -> values on the n-point grid
         self.to_net = lo.backward_matrix() @ Lo.forward_matrix()[:n, :]
@@ -51,21 +52,35 @@ class GridMaps:
         G[:m] = d.forward_matrix()[:m]
         self.net_to_coef = G
         x = lo.mesh()
-        self.X, self.Y = np.meshgrid(x, x, indexing="ij")
+        self.coords = np.meshgrid(*([x] * ndim), indexing="ij")
         self.D = D
-        self.T = TensorProduct(D, D)
-        self.To = TensorProduct(Lo, Lo)
+        self.T = TensorProduct(*([D] * ndim))
+        self.To = TensorProduct(*([Lo] * ndim))
+
+
+def _axes(maps: GridMaps) -> tuple[int, ...]:
+    return tuple(range(1, 1 + maps.ndim))
+
+
+def _bcast(v: torch.Tensor, ndim: int) -> torch.Tensor:
+    return v.reshape((-1,) + (1,) * ndim)
 
 
 def synth_batch(gen: torch.Generator, B: int, N: int, maps: GridMaps):
     """Seeded coefficients -> (kappa, f) on the fine Gauss grid (FP64, GPU)."""
+    nd = maps.ndim
     k = torch.arange(N, dtype=torch.float64, device="cuda")
-    grf = (1.0 + k[:, None] ** 2 + k[None, :] ** 2) ** -1.5
-    fs = ((1.0 + k[:, None]) ** -2.0) * ((1.0 + k[None, :]) ** -2.0)
-    gh = torch.randn((B, N, N), generator=gen, dtype=torch.float64, device="cuda") * grf
-    fh = torch.randn((B, N, N), generator=gen, dtype=torch.float64, device="cuda") * fs
+    ks = [k.reshape((-1,) + (1,) * (nd - 1 - i)) for i in range(nd)]
+    grf = (1.0 + sum(kk ** 2 for kk in ks)) ** -1.5
+    fs = 1.0
+    for kk in ks:
+        fs = fs * (1.0 + kk) ** -2.0
+    shape = (B,) + (N,) * nd
+    gh = torch.randn(shape, generator=gen, dtype=torch.float64, device="cuda") * grf
+    fh = torch.randn(shape, generator=gen, dtype=torch.float64, device="cuda") * fs
     g = maps.To.backward(gh)
-    g = (g - g.mean(dim=(1, 2), keepdim=True)) / g.std(dim=(1, 2), keepdim=True)
+    ax = _axes(maps)
+    g = (g - g.mean(dim=ax, keepdim=True)) / g.std(dim=ax, keepdim=True)
     f = maps.To.backward(fh)
     return g, f
 
@@ -73,17 +88,17 @@ def synth_batch(gen: torch.Generator, B: int, N: int, maps: GridMaps):
 def features(g, f, maps: GridMaps):
     """Network inputs (B*n^2, 16) FP32 and the per-sample forcing scale."""
     B = g.shape[0]
-    n = maps.n
+    n, nd = maps.n, maps.ndim
     # spectral truncation onto the network grid on the tensor cores (FP32 data)
-    g64 = tp_apply_tc([maps.to_net, maps.to_net], g)
-    f64 = tp_apply_tc([maps.to_net, maps.to_net], f)
-    s = f64.pow(2).mean(dim=(1, 2)).sqrt().clamp_min(1e-30)
-    X = torch.zeros((B, n, n, CIN), dtype=torch.float32, device="cuda")
+    g64 = tp_apply_tc([maps.to_net] * nd, g)
+    f64 = tp_apply_tc([maps.to_net] * nd, f)
+    s = f64.pow(2).mean(dim=_axes(maps)).sqrt().clamp_min(1e-30)
+    X = torch.zeros((B,) + (n,) * nd + (CIN,), dtype=torch.float32, device="cuda")
     X[..., 0] = g64.float()
-    X[..., 1] = (f64 / s[:, None, None]).float()
-    X[..., 2] = torch.as_tensor(maps.X, device="cuda").float()
-    X[..., 3] = torch.as_tensor(maps.Y, device="cuda").float()
-    return X.reshape(B * n * n, CIN), s
+    X[..., 1] = (f64 / _bcast(s, nd)).float()
+    for i, c in enumerate(maps.coords):
+        X[..., 2 + i] = torch.as_tensor(c, device="cuda").float()
+    return X.reshape(B * n ** nd, CIN), s
 
 
 def generate(nsamples: int, seed: int, maps: GridMaps, chunk: int = 128, tol: float = 1e-8,
@@ -104,9 +119,9 @@ def generate(nsamples: int, seed: int, maps: GridMaps, chunk: int = 128, tol: fl
         A = VarCoefMatrix(maps.T, kap)
         x, _, _ = MixedVarCoefSolver(A).solve(b, tol=tol)
         X, s = features(g, f, maps)
-        u64 = tp_apply([maps.coef_to_net, maps.coef_to_net], x)
+        u64 = tp_apply([maps.coef_to_net] * maps.ndim, x)
         Xs.append(X.to(torch.bfloat16))
-        Ts.append((u64 / s[:, None, None]).float().reshape(-1))
+        Ts.append((u64 / _bcast(s, maps.ndim)).float().reshape(-1))
         Ss.append(s)
         if keep_fine:
             fine.append((kap, f, b, x))
@@ -161,13 +176,13 @@ def predict(model: SNO, X: torch.Tensor, Bt: int | None = None) -> torch.Tensor:
         pred = model.forward(B)
         out[i:i + B] = pred[:, 0].reshape(B, P)
     n = model.cfg.n
-    return out.reshape(nsamp, n, n)
+    return out.reshape((nsamp,) + (n,) * model.cfg.ndim)
 
 
 def initial_guess(model: SNO, maps: GridMaps, X: torch.Tensor, s: torch.Tensor) -> torch.Tensor:
-    """Learned initial guess in the solver's coefficient space (B, N-2, N-2) FP64."""
-    u = predict(model, X) * s[:, None, None].float()
-    return tp_apply_tc([maps.net_to_coef, maps.net_to_coef], u).double()
+    """Learned initial guess in the solver's coefficient space (B, (N-2,)*d) FP64."""
+    u = predict(model, X) * _bcast(s, maps.ndim).float()
+    return tp_apply_tc([maps.net_to_coef] * maps.ndim, u).double()
 
 
 def relative_l2(model: SNO, data: dict) -> float:
@@ -179,17 +194,22 @@ def relative_l2(model: SNO, data: dict) -> float:
 
 
 def evaluate_gain(model: SNO, maps: GridMaps, nprob: int = 128, seed: int = 3,
-                  tol: float = 3e-11, inner_tol: float = 1e-5) -> dict:
+                  tol: float | None = None, inner_tol: float = 1e-5) -> dict:
     """Mixed-precision solves of held-out problems from a zero start and from the
-    learned guess: iterations, time, and error against a tight FP64 solve."""
+    learned guess: iterations, time, and error against a tight FP64 solve.
+    Default tolerance: the benchmarks' calibrated stopping rule (2-D 1e-11 on
+    the relative residual, 3-D 1e-12)."""
     from ..la import pcg
 
+    if tol is None:
+        tol = 1e-11 if maps.ndim == 2 else 1e-12
     data = generate(nprob, seed, maps, keep_fine=True, log=lambda *_: None)
     kap, f, b, _ = data["fine"][0] if len(data["fine"]) == 1 else [
         torch.cat([c[i] for c in data["fine"]]) for i in range(4)]
     A = VarCoefMatrix(maps.T, kap)
     S = MixedVarCoefSolver(A)
-    xt, _ = pcg(A, b, tol=1e-14, maxiter=3000)
+    xt, _ = pcg(A, b, tol=1e-14, maxiter=4000)
+    ax = _axes(maps)
     out = {}
     for name in ("zero", "learned"):
         for rep in range(2):  # second repetition is timed
@@ -199,12 +219,13 @@ def evaluate_gain(model: SNO, maps: GridMaps, nprob: int = 128, seed: int = 3,
             x, it_in, it_out = S.solve(b, guess=x0, tol=tol, inner_tol=inner_tol)
             torch.cuda.synchronize()
             dt = time.perf_counter() - t0
-        err = float(((x - xt).abs().amax(dim=(1, 2)) / xt.abs().amax(dim=(1, 2))).max())
+        err = float(((x - xt).abs().amax(dim=ax) / xt.abs().amax(dim=ax)).max())
         out[name] = {"inner_iterations_mean": float(it_in.mean()),
                      "outer_iterations_mean": float(it_out.mean()), "ms": 1e3 * dt,
                      "solves_per_s": nprob / dt, "max_rel_err": err}
     x0 = initial_guess(model, maps, data["X"], data["s"])
-    out["guess_rel_err_mean"] = float(((x0 - xt).norm(dim=(1, 2)) / xt.norm(dim=(1, 2))).mean())
+    vn = torch.linalg.vector_norm
+    out["guess_rel_err_mean"] = float((vn(x0 - xt, dim=ax) / vn(xt, dim=ax)).mean())
     return out
 
 
@@ -219,8 +240,11 @@ def save(model: SNO, path: str, meta: dict | None = None):
 
 def load(path: str, batch: int = 32) -> SNO:
     z = np.load(path)
-    n, width, modes, layers = (int(v) for v in z["_config"])
-    model = SNO(SNOConfig(n=n, width=width, modes=modes, layers=layers, batch=batch))
+    cfg = [int(v) for v in z["_config"]]
+    n, width, modes, layers = cfg[:4]
+    ndim = cfg[4] if len(cfg) > 4 else 2
+    model = SNO(SNOConfig(n=n, width=width, modes=modes, layers=layers, batch=batch,
+                          ndim=ndim))
     model.load_state_dict({k: z[k] for k in z.files if not k.startswith("_")})
     return model
 
@@ -233,19 +257,29 @@ def main():
     ap.add_argument("--batch", type=int, default=32)
     ap.add_argument("--lr", type=float, default=1e-3)
     ap.add_argument("--out", default="sno_varcoef2d_N256.npz")
+    ap.add_argument("--ndim", type=int, default=2)
+    ap.add_argument("--N", type=int, default=N_FINE, help="solver modes per axis")
+    ap.add_argument("--n", type=int, default=64, help="network grid points per axis")
+    ap.add_argument("--modes", type=int, default=32, help="network modes per axis")
+    ap.add_argument("--width", type=int, default=64)
+    ap.add_argument("--chunk", type=int, default=128, help="problems per generating solve")
+    ap.add_argument("--gain-problems", type=int, default=128)
     args = ap.parse_args()
     torch.cuda.set_device(0)
-    maps = GridMaps()
+    maps = GridMaps(N=args.N, n=args.n, guess_modes=args.modes, ndim=args.ndim)
     s = torch.cuda.Stream()
     with torch.cuda.stream(s):
-        tr = generate(args.train, seed=1, maps=maps)
-        te = generate(args.test, seed=2, maps=maps)
-        model = SNO(SNOConfig(batch=args.batch), seed=0)
+        tr = generate(args.train, seed=1, maps=maps, chunk=args.chunk)
+        te = generate(args.test, seed=2, maps=maps, chunk=args.chunk)
+        model = SNO(SNOConfig(n=args.n, width=args.width, modes=args.modes, batch=args.batch,
+                              ndim=args.ndim), seed=0)
         t0 = time.perf_counter()
         hist = train(model, tr, args.epochs, lr=args.lr)
         t_train = time.perf_counter() - t0
         err = relative_l2(model, te)
-        gain = evaluate_gain(model, maps)
+        save(model, args.out, {"train": args.train, "test": args.test, "epochs": args.epochs,
+                               "test_rel_l2": err})
+        gain = evaluate_gain(model, maps, nprob=args.gain_problems)
     meta = {"train": args.train, "test": args.test, "epochs": args.epochs, "lr": args.lr,
             "test_rel_l2": err, "train_loss": hist, "train_seconds": t_train, "gain": gain}
     print(json.dumps(meta))

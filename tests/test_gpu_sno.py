@@ -135,6 +135,40 @@ def test_sno_gradients_match_oracle():
         assert err < 3e-2, (k, err)
 
 
+def test_sno3d_gradients_match_oracle():
+    """The same network on a 3-D grid (8^3 points, 4^3 modes): forward and
+    backward against the oracle's explicit chain rule."""
+    cfg = SNOConfig(n=8, width=16, modes=4, layers=2, batch=2, ndim=3)
+    m = SNO(cfg, seed=4)
+    rng = np.random.default_rng(9)
+    for k, p in m.params.items():
+        if k.startswith("b") or k == "W_p2":
+            p.copy_(torch.as_tensor(0.1 * rng.standard_normal(p.shape), dtype=torch.float32))
+    m._sync_bf16()
+    Bt, P = cfg.batch, cfg.n ** 3
+    X = np.zeros((Bt * P, CIN), dtype=np.float32)
+    X[:, :5] = rng.standard_normal((Bt * P, 5))
+    Xb = torch.as_tensor(X, device="cuda").to(torch.bfloat16)
+    tgt = torch.as_tensor(rng.standard_normal(Bt * P), dtype=torch.float32, device="cuda")
+    m.set_input(Xb)
+    pred = m.forward(Bt)[:, 0].clone()
+    loss = m.backward(Bt, tgt)
+    bf = lambda t: t.to(torch.bfloat16).double().cpu().numpy()  # noqa: E731
+    params = {k: (bf(v) if k in m.matrix_names() else v.double().cpu().numpy())
+              for k, v in m.params.items()}
+    Phi, Psi = transform_matrices(cfg.n, cfg.modes, 3)
+    Phi = bf(torch.as_tensor(Phi))
+    Psi = bf(torch.as_tensor(Psi))
+    loss_o, pred_o, g_o = OS.forward_backward(params, Phi, Psi, bf(Xb), tgt.double().cpu().numpy(),
+                                              Bt, cfg.layers)
+    assert abs(loss - loss_o) < 2e-2 * loss_o
+    assert np.abs(pred.cpu().numpy() - pred_o[:, 0]).max() < 2e-2 * np.abs(pred_o[:, 0]).max()
+    for k, go in g_o.items():
+        gg = m.grads[k].double().cpu().numpy()
+        err = np.linalg.norm(gg - go) / max(np.linalg.norm(go), 1e-30)
+        assert err < 3e-2, (k, err)
+
+
 def test_sno_training_reduces_loss():
     m, cfg = _small_model(seed=3)
     Bt, P = cfg.batch, cfg.n * cfg.n
@@ -181,3 +215,30 @@ def test_learned_guess_saves_iterations():
     # the guess itself is a usable approximation (coefficient-space L2, 32 modes)
     rel = ((g - xt).norm(dim=(1, 2)) / xt.norm(dim=(1, 2))).mean()
     assert float(rel) < 0.3
+
+
+def test_learned_guess_saves_iterations_3d():
+    """The 3-D network (32^3 grid, 16^3 modes, width 32) on held-out 128^3
+    problems: fewer inner iterations than the zero start, both answers within
+    1e-10 of a tight FP64 solve (3-D stopping rule 1e-12)."""
+    import os
+
+    from jaxfun_gb300.la import MixedVarCoefSolver, VarCoefMatrix, pcg
+    from jaxfun_gb300.sno import train as T
+
+    path = os.path.join(os.path.dirname(T.__file__), "weights", "sno_varcoef3d_N128.npz")
+    model = T.load(path, batch=8)
+    maps = T.GridMaps(N=128, n=model.cfg.n, guess_modes=model.cfg.modes, ndim=3)
+    data = T.generate(8, seed=11, maps=maps, chunk=8, keep_fine=True, log=lambda *_: None)
+    kap, f, b, _ = data["fine"][0]
+    A = VarCoefMatrix(maps.T, kap)
+    S = MixedVarCoefSolver(A)
+    xt, _ = pcg(A, b, tol=1e-14, maxiter=4000)
+    g = T.initial_guess(model, maps, data["X"], data["s"])
+    res = {}
+    for name, guess in (("zero", None), ("learned", g)):
+        x, it_in, _ = S.solve(b, tol=1e-12, inner_tol=1e-5, guess=guess)
+        err = float(((x - xt).abs().amax(dim=(1, 2, 3)) / xt.abs().amax(dim=(1, 2, 3))).max())
+        assert err <= 1e-10, (name, err)
+        res[name] = float(np.mean(it_in))
+    assert res["learned"] < res["zero"], res
