@@ -34,7 +34,7 @@ METRIC = "var-coef solves/s at 1e-10 err: learned+mixed vs plain FP64 PCG, 1 GB3
 N_GRID = 256
 # DRAM bytes (read + write) of one k_contract_tc launch at M = 512, P = K = 256,
 # 128 problems, from ncu (dram__bytes_read.sum + dram__bytes_write.sum).
-TC_TRAFFIC_PER_LAUNCH_B128 = 34.662912e6 + 9.000960e6
+TC_TRAFFIC_PER_LAUNCH_B128 = 34.681088e6 + 9.693184e6
 
 
 def peaks():
