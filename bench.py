@@ -550,6 +550,19 @@ def run_tour(args):
                                                             device="cuda"))
     bounded(H.solve_per_group, [rng.standard_normal((N - 2, N - 2)) for N in Ns],
             tol=1e-11, max_refine=1)
+    # 6. per-wavenumber banded solves: 4096 systems k^2 M + K (Legendre, n = 254)
+    from jaxfun_gb300.la import TPMatricesWavenumberSolver
+
+    Kd, Md = D.stiffness_matrix(), D.mass_matrix()
+    n = Kd.shape[0]
+    offs = (-2, 0, 2)
+    k2 = np.arange(4096, dtype=float) ** 2 / 64.0
+    band = np.zeros((4096, 3, n))
+    for di, off in enumerate(offs):
+        j = np.arange(max(off, 0), n + min(off, 0))
+        band[:, di, j] = k2[:, None] * Md[j - off, j][None, :] + Kd[j - off, j][None, :]
+    WS = TPMatricesWavenumberSolver(1, (4096, n), band, offs)
+    WS.solve(torch.as_tensor(rng.standard_normal((4096, n)), device="cuda"))
     torch.cuda.synchronize()
     print(json.dumps({"tour": "done", "device_status": int(L.jfg_device_status()),
                       "launches": int(L.jfg_launch_count())}), flush=True)

@@ -148,6 +148,7 @@ typedef struct {
                             work, 2 by total work (largest first)                    */
   int ctas;              /* persistent CTAs (0: one per SM)                          */
   int stages;            /* pipeline stages (0: as many as fit, else >= 2)           */
+  int mtile;             /* operator rows per tile = MMA N (0: up to 128, else 64)   */
 } jfg_tc_config;
 /*
  * Grouped tensor-core contraction: ngroups independent contractions (each a
@@ -163,7 +164,7 @@ int jfg_contract_tc_grouped(int ngroups, const jfg_contract_desc* descs,
                             const jfg_tc_config* cfg, void* stream);
 /*
  * Autotuner: times every candidate configuration (operand A in TMEM or shared
- * memory x group order x pipeline depth) of the grouped contraction on the
+ * memory x group order x pipeline depth x tile height) of the grouped contraction on the
  * given operands with CUDA events (reps launches each; the contraction runs,
  * so out is written), keeps the fastest for this launch signature (shapes,
  * batches, epilogue) and returns it with its time.  Not during stream capture.

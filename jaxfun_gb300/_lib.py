@@ -45,7 +45,7 @@ class NotConvergedError(JfgError):
 
 class TcConfig(C.Structure):
     _fields_ = [("operand_a_in_tmem", C.c_int), ("order", C.c_int), ("ctas", C.c_int),
-                ("stages", C.c_int)]
+                ("stages", C.c_int), ("mtile", C.c_int)]
 
 
 class ContractDesc(C.Structure):

@@ -731,7 +731,8 @@ int setup_kernel_attr() {
 // Validate one group and fill its descriptor, tile height and tensor maps.
 // b16: the operator is BF16 (hi, lo) with 64-element K blocks, else TF32 in FP32 words.
 int fill_group(const jfg_contract_desc& d, const void* op_hi, const void* op_lo,
-               const float* in, float* out, TcGroup& q, CUtensorMap* maps, bool b16) {
+               const float* in, float* out, TcGroup& q, CUtensorMap* maps, bool b16,
+               int mt_cap) {
   JFG_TRY(validate_desc(d));
   if (!op_hi || !op_lo || !in || !out) return JFG_ERR_ARG;
   // TMA: 16-byte aligned bases and strides
@@ -743,7 +744,8 @@ int fill_group(const jfg_contract_desc& d, const void* op_hi, const void* op_lo,
   if ((long long)d.batch * d.nseg > 65535) return JFG_ERR_ARG;
   q.d = d;
   q.out = out;
-  q.Mtile = ((d.M > MT_MAX ? MT_MAX : d.M) + 15) / 16 * 16;
+  const int cap = (mt_cap > 0 && mt_cap < MT_MAX) ? mt_cap : MT_MAX;
+  q.Mtile = ((d.M > cap ? cap : d.M) + 15) / 16 * 16;
   q.seg_in_map = (d.nseg > 1 && d.in_seg != 0) ? 1 : 0;
   q.bat_in_map = (d.batch > 1 && d.in_batch != 0) ? 1 : 0;
   q.seg_op_map = (d.nseg > 1 && d.op_seg != 0) ? 1 : 0;
@@ -813,7 +815,8 @@ int launch_groups(int ng, const jfg_contract_desc* const* ds, const void* const*
   int mt_max = 16, ostage = 0;
   for (int i = 0; i < ng; ++i) {
     if (ds[i]->epilogue != epi || (ds[i]->beta != 0.0) != hb) return JFG_ERR_ARG;
-    JFG_TRY(fill_group(*ds[i], op_hi[i], op_lo[i], in[i], out[i], L.g[i], L.maps[i], b16));
+    JFG_TRY(fill_group(*ds[i], op_hi[i], op_lo[i], in[i], out[i], L.g[i], L.maps[i], b16,
+                       cfg.mtile));
     if (!g_tma_store) L.g[i].tma_store = 0;
     tiles += group_tiles(L.g[i]);
     if (L.g[i].Mtile > mt_max) mt_max = L.g[i].Mtile;
@@ -885,6 +888,7 @@ jfg_tc_config tc_default_config() {
   c.order = 0;
   c.ctas = 0;
   c.stages = 0;
+  c.mtile = 0;
   return c;
 }
 
@@ -910,7 +914,9 @@ int contract_tc_grouped(int ng, const jfg_contract_desc* ds, const float* const*
                         const float* const* op_lo, const float* const* in, float* const* out,
                         const jfg_tc_config& cfg, cudaStream_t st) {
   if (ng < 0 || (ng > 0 && (!ds || !op_hi || !op_lo || !in || !out))) return JFG_ERR_ARG;
-  if (cfg.order < 0 || cfg.order > 2 || cfg.stages < 0 || cfg.ctas < 0) return JFG_ERR_ARG;
+  if (cfg.order < 0 || cfg.order > 2 || cfg.stages < 0 || cfg.ctas < 0 ||
+      (cfg.mtile != 0 && cfg.mtile != 64))
+    return JFG_ERR_ARG;
   // launch order of the groups: as given, by operator-tile work (K * Mtile,
   // largest first), or by total work (largest first)
   std::vector<int> ord;
@@ -1059,14 +1065,16 @@ extern "C" int jfg_tc_autotune(int ngroups, const jfg_contract_desc* descs,
   const int orders = ngroups > 1 ? 3 : 1;
   for (int ta = 1; ta >= 0; --ta)
     for (int o = 0; o < orders; ++o)
-      for (int sg : {0, 3, 2}) {
-        jfg_tc_config c;
-        c.operand_a_in_tmem = ta;
-        c.order = o;
-        c.ctas = 0;
-        c.stages = sg;
-        cands.push_back(c);
-      }
+      for (int sg : {0, 3, 2})
+        for (int mt : {0, 64}) {
+          jfg_tc_config c;
+          c.operand_a_in_tmem = ta;
+          c.order = o;
+          c.ctas = 0;
+          c.stages = sg;
+          c.mtile = mt;
+          cands.push_back(c);
+        }
   cudaEvent_t e0, e1;
   JFG_CUDA_TRY(cudaEventCreate(&e0));
   JFG_CUDA_TRY(cudaEventCreate(&e1));

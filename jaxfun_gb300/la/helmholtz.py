@@ -112,7 +112,8 @@ class UnevenHelmholtzSolver:
                    "jfg_tc_autotune")
         self.cfg = best
         return {"operand_a_in_tmem": best.operand_a_in_tmem, "order": best.order,
-                "ctas": best.ctas, "stages": best.stages, "pass_ms": ms.value}
+                "ctas": best.ctas, "stages": best.stages, "mtile": best.mtile or 128,
+                "pass_ms": ms.value}
 
     def pack(self, rhs: list) -> torch.Tensor:
         """Per-problem right-hand sides -> the flat group-major FP64 buffer."""

@@ -66,16 +66,19 @@ def test_grouped_equals_single(epi):
     torch.cuda.synchronize()
     for ta in (1, 0):
         for order in (0, 1, 2):
-            for stages in (0, 2):
+            for stages, mt in ((0, 0), (2, 0), (0, 64)):
                 outs = [torch.full_like(r, float("nan")) for r in ref]
                 descs, oh, ol, ins, ops = _arrays(gs, outs)
-                cfg = _lib.TcConfig(ta, order, 0, stages)
+                cfg = _lib.TcConfig(ta, order, 0, stages, mt)
                 st = L.jfg_contract_tc_grouped(len(gs), descs, oh, ol, ins, ops, C.byref(cfg), sh)
                 assert st == 0, _lib.status_string(st)
                 torch.cuda.synchronize()
                 assert L.jfg_device_status() == 0
                 for o, r in zip(outs, ref):
-                    assert torch.equal(o, r), (ta, order, stages)
+                    if mt == 0:
+                        assert torch.equal(o, r), (ta, order, stages)
+                    else:  # another tile height: same products, other summation order
+                        assert torch.allclose(o, r, rtol=1e-5, atol=1e-5 * float(r.abs().max()))
 
 
 def test_autotune_picks_a_candidate():
@@ -89,6 +92,7 @@ def test_autotune_picks_a_candidate():
                            _lib.stream_handle())
     assert st == 0, _lib.status_string(st)
     assert best.operand_a_in_tmem in (0, 1) and best.order in (0, 1, 2)
+    assert best.mtile in (0, 64)
     assert ms.value > 0
     # the cached choice is used when no configuration is passed
     outs2 = [torch.empty_like(o) for o in outs]
