@@ -98,10 +98,11 @@ extern "C" int jfg_banded_lu_factor_f64(int nsys, int n, int ndiag, const int* o
   if (!has_main) return JFG_ERR_ARG;
   if (nsys == 0) return JFG_OK;
   cudaStream_t st = (cudaStream_t)stream;
-  const int blocks = (nsys + 127) / 128;
-  jfg::k_band_pack<<<blocks, 128, 0, st>>>(nsys, n, ndiag, off, p, q, data, lu);
+  // one warp per block: few thousand systems still spread over every SM
+  const int blocks = (nsys + 31) / 32;
+  jfg::k_band_pack<<<blocks, 32, 0, st>>>(nsys, n, ndiag, off, p, q, data, lu);
   JFG_LAUNCHED();
-  jfg::k_band_lu<<<blocks, 128, 0, st>>>(nsys, n, p, q, lu);
+  jfg::k_band_lu<<<blocks, 32, 0, st>>>(nsys, n, p, q, lu);
   JFG_LAUNCHED();
   return JFG_OK;
 }
@@ -112,7 +113,7 @@ extern "C" int jfg_banded_lu_solve_f64(int nsys, int n, int p, int q, const doub
   if (nsys < 0 || n < 1 || p < 0 || q < 0 || p >= n || q >= n || !lu || !rhs || !x)
     return JFG_ERR_ARG;
   if (nsys == 0) return JFG_OK;
-  jfg::k_band_solve<<<(nsys + 127) / 128, 128, 0, (cudaStream_t)stream>>>(
+  jfg::k_band_solve<<<(nsys + 31) / 32, 32, 0, (cudaStream_t)stream>>>(
       nsys, n, p, q, lu, rhs, x, sys_stride, elem_stride);
   JFG_LAUNCHED();
   return JFG_OK;
