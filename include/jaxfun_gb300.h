@@ -440,6 +440,15 @@ typedef struct {
                             r -= ||r|| A d once ||r|| <= 1e-4 ||rhs|| (else FP64 r = b - A x) */
   int residual;          /* arithmetic of r = b - A x: 0 FP64 (DFMA), 1 double-FP32
                             (jfg_contract_df64 passes)                                */
+  int precond_bf16;      /* 1: the inner preconditioner's FD passes use split-BF16
+                            operators (E/W_hi16, _lo16: jfg_split_bf16_host of the
+                            padded factors), 0: split-TF32 (E/W_hi, _lo).  The
+                            operator passes stay split-TF32: with split-BF16 they
+                            stall the inner solve near its 1e-5 tolerance           */
+  const uint16_t* E_hi16;
+  const uint16_t* E_lo16;
+  const uint16_t* W_hi16;
+  const uint16_t* W_lo16;
 } jfg_mixed_plan;
 
 size_t jfg_pcg_mixed_workspace_size(int ndim, int n, int nq, int batch);

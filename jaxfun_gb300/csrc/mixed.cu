@@ -191,7 +191,9 @@ extern "C" int jfg_pcg_varcoef_mixed_guess(const jfg_mixed_plan* plan, const dou
   const jfg_mixed_plan& P = *plan;
   if ((P.ndim != 2 && P.ndim != 3) || P.n < 1 || P.nq < P.n || P.batch < 1 || !P.ops64 ||
       !P.kw64 || !P.ops_hi || !P.ops_lo || !P.kw32 || !P.E_hi || !P.E_lo || !P.W_hi ||
-      !P.W_lo || !P.lam || (P.residual != 0 && P.residual != 1))
+      !P.W_lo || !P.lam || (P.residual != 0 && P.residual != 1) ||
+      (P.precond_bf16 != 0 && P.precond_bf16 != 1) ||
+      (P.precond_bf16 && (!P.E_hi16 || !P.E_lo16 || !P.W_hi16 || !P.W_lo16)))
     return JFG_ERR_ARG;
   const int ndim = P.ndim, n = P.n, nq = P.nq, batch = P.batch;
   const MixedLayout Lo = layout(ndim, n, nq, batch);
@@ -216,14 +218,18 @@ extern "C" int jfg_pcg_varcoef_mixed_guess(const jfg_mixed_plan* plan, const dou
 
   PcgProblem<float> pb;
   pb.engine = Engine::TC;
+  const bool pbf = P.precond_bf16 != 0;
+  pb.m_engine = pbf ? Engine::TB : Engine::TC;
   pb.ndim = ndim;
   pb.n = nq;
   pb.nq = nq;
   pb.batch = batch;
   pb.ops = OpRef<float>{P.ops_hi, P.ops_lo};
   pb.kw = P.kw32;
-  pb.E = OpRef<float>{P.E_hi, P.E_lo};
-  pb.W = OpRef<float>{P.W_hi, P.W_lo};
+  pb.E = pbf ? OpRef<float>{(const float*)P.E_hi16, (const float*)P.E_lo16}
+             : OpRef<float>{P.E_hi, P.E_lo};
+  pb.W = pbf ? OpRef<float>{(const float*)P.W_hi16, (const float*)P.W_lo16}
+             : OpRef<float>{P.W_hi, P.W_lo};
   pb.lam = P.lam;
   pb.fd_scale = P.fd_scale;
   pb.rhs = r32;

@@ -254,7 +254,7 @@ int pcg_run(const PcgProblem<T>& pb, T* x, int use_x0, double tol, int maxiter, 
                             inner_bytes, st, a);
   };
   auto applyM = [&](const T* in, T* out, Active a) -> int {
-    return fd_solve<T>(pb.engine, ndim, n, batch, pb.E, pb.W, pb.lam, nullptr, pb.fd_scale, in,
+    return fd_solve<T>(pb.m_engine, ndim, n, batch, pb.E, pb.W, pb.lam, nullptr, pb.fd_scale, in,
                        out, inner, inner_bytes, st, a);
   };
 
@@ -411,6 +411,7 @@ extern "C" int jfg_pcg_varcoef_f64(int ndim, int n, int nq, int batch, const dou
   if (!ops || !kw || !E || !W || !lam) return JFG_ERR_ARG;
   jfg::PcgProblem<double> pb;
   pb.engine = jfg::Engine::F64;
+  pb.m_engine = jfg::Engine::F64;
   pb.ndim = ndim;
   pb.n = n;
   pb.nq = nq;

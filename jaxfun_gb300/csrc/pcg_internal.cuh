@@ -10,6 +10,8 @@ namespace jfg {
 template <typename T>
 struct PcgProblem {
   Engine engine = Engine::F64;
+  Engine m_engine = Engine::F64;   // engine of the preconditioner (E, W point at BF16
+                                   // pairs when it is Engine::TB)
   int ndim = 2, n = 0, nq = 0, batch = 0;
   OpRef<T> ops{nullptr, nullptr};  // packed variable-coefficient operators
   const T* kw = nullptr;           // (batch, nq^ndim) kappa * quadrature weights
