@@ -27,101 +27,143 @@ namespace {
 constexpr double PI = 3.14159265358979323846;
 constexpr double PI2 = 1.5707963267948966192;
 
-// Diagonal of the orthogonal mass matrix, h_i = (P_i, P_i)_w.
-__device__ __forceinline__ double hnorm(int family, int i) {
-  return family == 0 ? 2.0 / (2.0 * i + 1.0) : (i == 0 ? PI : PI2);
-}
-
-// Stiffness part of one row of the backward sweep.  With t = S^T x and
-// w_i = -(D2 t)_i = -sum_{j >= i+2, j = i mod 2} c(i, j) t_j, the closed forms
-// c(i, j) = j(j+1) - i(i+1) (Legendre) and (pi/2) j (j^2 - i^2) (Chebyshev)
-// give the two-term recurrence, per parity class,
-//   V(i) = V(i+2) + (4i+6) sum_{j>=i+2} t_j        (Legendre; w_i = -V(i))
-//   V(i) = V(i+2) + (4i+4) sum_{j>=i+2} j t_j      (Chebyshev; w_i = -(pi/2) V(i))
+// Per-row coefficients of the sweeps, filled once per block into shared memory
+// (the sweep then spends its FP64 issue slots on the arithmetic only):
+//   h[i] = (P_i, P_i)_w                       diagonal of the orthogonal mass
+//   c[i] = -(4i+6)       (Legendre)           stiffness recurrence coefficient,
+//        = -(pi/2)(4i+4) (Chebyshev)          sign and scale of w folded in
+//   s[i] = 1 (Legendre), i (Chebyshev)        weight of t_i in the suffix sum
+// With t = S^T x and w_i = -(D2 t)_i = -sum_{j >= i+2, j = i mod 2} c(i, j) t_j,
+// the closed forms c(i, j) = j(j+1) - i(i+1) (Legendre) and (pi/2) j (j^2 - i^2)
+// (Chebyshev) give, per parity class, the two-term recurrence
+//   w_i = V(i) = V(i+2) + c[i] * sum_{j >= i+2} s[j] t_j
 // so no large suffix sums cancel and each row costs two FMAs.
-__device__ __forceinline__ double stiff_step(int family, double di, double t, double& S,
-                                             double& V) {
-  if (family == 0) {
-    V = fma(4.0 * di + 6.0, S, V);
-    S += t;
-    return -V;
+constexpr int HTAB = 1026;  // rows per line supported: n + 2 <= HTAB
+
+struct HelmTab {
+  double h[HTAB], c[HTAB], s[HTAB];
+};
+
+__device__ __forceinline__ void fill_tab(int family, int m, HelmTab& T) {
+  for (int i = threadIdx.x; i < m; i += blockDim.x) {
+    const double di = (double)i;
+    T.h[i] = family == 0 ? 2.0 / (2.0 * di + 1.0) : (i == 0 ? PI : PI2);
+    T.c[i] = family == 0 ? -(4.0 * di + 6.0) : -PI2 * (4.0 * di + 4.0);
+    T.s[i] = family == 0 ? 1.0 : di;
   }
-  V = fma(4.0 * di + 4.0, S, V);
-  S = fma(di, t, S);
-  return -PI2 * V;
+  __syncthreads();
 }
 
 // One row (stride sx): U1 = M x and U2 = K x in a single backward sweep
 // i = n+1 .. 0 over t_i = x_i - x_{i-2}, w = diag(h) t or -(D2 t), y_i = w_i - w_{i+2}.
-__device__ __forceinline__ void helm_row(int family, int n, const double* __restrict__ x,
+// The two parity classes are independent recurrences, each with its state in
+// registers; the sweep runs in chunks of SW steps whose loads are all issued
+// before the chunk's arithmetic (memory-level parallelism for the serial walk).
+constexpr int SW = 8;  // steps per chunk (even: a chunk starts on the class of n+1)
+
+struct RowClass {
+  double S = 0.0, V = 0.0, x = 0.0;  // suffix sums and the class's pending x_i
+};
+
+__device__ __forceinline__ void helm_row(const HelmTab& T, int n, const double* __restrict__ x,
                                          long long sx, double* __restrict__ U1,
                                          double* __restrict__ U2) {
-  double S[2] = {0.0, 0.0}, V[2] = {0.0, 0.0}, xs[2] = {0.0, 0.0};
+  RowClass A, B;  // A: the parity of n+1, B: the other
   double wm1 = 0.0, wm2 = 0.0, wk1 = 0.0, wk2 = 0.0;  // w at i+1, i+2
-  for (int i = n + 1; i >= 0; --i) {
-    const int p = i & 1;
-    const double xi = xs[p];  // x_i (loaded as x_{(i+2)-2}); 0 beyond n-1
-    const double xim2 = i >= 2 ? x[(long long)(i - 2) * sx] : 0.0;
-    xs[p] = xim2;
-    const double t = xi - xim2;
-    const double wm = hnorm(family, i) * t;
-    const double wk = stiff_step(family, (double)i, t, S[p], V[p]);
-    if (i < n) {
-      U1[(long long)i * sx] = wm - wm2;
-      U2[(long long)i * sx] = wk - wk2;
+  for (int i0 = n + 1; i0 >= 0; i0 -= SW) {
+    double xl[SW];
+#pragma unroll
+    for (int k = 0; k < SW; ++k) {
+      const int i = i0 - k;
+      xl[k] = i >= 2 ? x[(long long)(i - 2) * sx] : 0.0;
     }
-    wm2 = wm1;
-    wm1 = wm;
-    wk2 = wk1;
-    wk1 = wk;
+#pragma unroll
+    for (int k = 0; k < SW; ++k) {
+      const int i = i0 - k;
+      if (i < 0) break;
+      RowClass& c = (k & 1) ? B : A;
+      const double t = c.x - xl[k];  // c.x = x_i (loaded as x_{(i+2)-2}); 0 beyond n-1
+      c.x = xl[k];
+      const double wm = T.h[i] * t;
+      c.V = fma(T.c[i], c.S, c.V);
+      c.S = fma(T.s[i], t, c.S);
+      const double wk = c.V;
+      if (i < n) {
+        U1[(long long)i * sx] = wm - wm2;
+        U2[(long long)i * sx] = wk - wk2;
+      }
+      wm2 = wm1;
+      wm1 = wm;
+      wk2 = wk1;
+      wk1 = wk;
+    }
   }
 }
 
 // One column (stride sx): v = M (a2 U1 + U2) + K U1 = (a2 M + K) U1 + M U2 in a
 // single sweep; r = b - v when b is given, else r = v.
-__device__ __forceinline__ void helm_col(int family, int n, const double* __restrict__ U1,
+struct ColClass {
+  double S = 0.0, V = 0.0, u1 = 0.0, u2 = 0.0;
+};
+
+__device__ __forceinline__ void helm_col(const HelmTab& T, int n, const double* __restrict__ U1,
                                          const double* __restrict__ U2, long long sx, double a2,
                                          const double* __restrict__ b, double* __restrict__ r) {
-  double S[2] = {0.0, 0.0}, V[2] = {0.0, 0.0}, u1s[2] = {0.0, 0.0}, u2s[2] = {0.0, 0.0};
+  ColClass A, B;
   double w1 = 0.0, w2 = 0.0;
-  for (int i = n + 1; i >= 0; --i) {
-    const int p = i & 1;
-    const double u1 = u1s[p], u2 = u2s[p];
-    const double u1m = i >= 2 ? U1[(long long)(i - 2) * sx] : 0.0;
-    const double u2m = i >= 2 ? U2[(long long)(i - 2) * sx] : 0.0;
-    u1s[p] = u1m;
-    u2s[p] = u2m;
-    const double t1 = u1 - u1m;
-    const double tz = fma(a2, t1, u2 - u2m);
-    const double w = fma(hnorm(family, i), tz, stiff_step(family, (double)i, t1, S[p], V[p]));
-    if (i < n) {
-      const long long o = (long long)i * sx;
-      const double v = w - w2;
-      r[o] = b ? b[o] - v : v;
+  for (int i0 = n + 1; i0 >= 0; i0 -= SW) {
+    double l1[SW], l2[SW], lb[SW];
+#pragma unroll
+    for (int k = 0; k < SW; ++k) {
+      const int i = i0 - k;
+      l1[k] = i >= 2 ? U1[(long long)(i - 2) * sx] : 0.0;
+      l2[k] = i >= 2 ? U2[(long long)(i - 2) * sx] : 0.0;
+      lb[k] = (b && i >= 0 && i < n) ? b[(long long)i * sx] : 0.0;
     }
-    w2 = w1;
-    w1 = w;
+#pragma unroll
+    for (int k = 0; k < SW; ++k) {
+      const int i = i0 - k;
+      if (i < 0) break;
+      ColClass& c = (k & 1) ? B : A;
+      const double t1 = c.u1 - l1[k];
+      const double tz = fma(a2, t1, c.u2 - l2[k]);
+      c.u1 = l1[k];
+      c.u2 = l2[k];
+      c.V = fma(T.c[i], c.S, c.V);
+      c.S = fma(T.s[i], t1, c.S);
+      const double w = fma(T.h[i], tz, c.V);
+      if (i < n) {
+        const double v = w - w2;
+        r[(long long)i * sx] = b ? lb[k] - v : v;
+      }
+      w2 = w1;
+      w1 = w;
+    }
   }
 }
 
 // axis 1 (contiguous): U1 = rows through M, U2 = rows through K
 __global__ void k_helm_rows(int family, int n, long long nlines, const double* __restrict__ u,
                             double* __restrict__ U1, double* __restrict__ U2) {
+  __shared__ HelmTab T;
+  fill_tab(family, n + 2, T);
   const long long line = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (line >= nlines) return;
-  helm_row(family, n, u + line * n, 1, U1 + line * n, U2 + line * n);
+  helm_row(T, n, u + line * n, 1, U1 + line * n, U2 + line * n);
 }
 
 // axis 0 (stride n): v = (alpha2 M + K) U1 + M U2 (columns), optionally r = b - v
 __global__ void k_helm_cols(int family, int n, int batch, const double* __restrict__ U1,
                             const double* __restrict__ U2, const double* __restrict__ alpha2,
                             const double* __restrict__ b, double* __restrict__ v) {
+  __shared__ HelmTab T;
+  fill_tab(family, n + 2, T);
   const long long line = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (line >= (long long)batch * n) return;
   const long long bi = line / n, j = line % n;
   const long long off = bi * (long long)n * n + j;
   const double a2 = alpha2 ? alpha2[bi] : 0.0;
-  helm_col(family, n, U1 + off, U2 + off, n, a2, b ? b + off : nullptr, v + off);
+  helm_col(T, n, U1 + off, U2 + off, n, a2, b ? b + off : nullptr, v + off);
 }
 
 }  // namespace
@@ -135,6 +177,7 @@ extern "C" int jfg_helmholtz_apply_f64(int family, int n, int batch, const doubl
                                        const double* u, const double* b, double* v, void* work,
                                        size_t work_bytes, void* stream) {
   if ((family != 0 && family != 1) || n < 1 || batch < 0 || !u || !v) return JFG_ERR_ARG;
+  if (n + 2 > jfg::HTAB) return JFG_ERR_UNSUPPORTED;
   const size_t need = jfg_helmholtz_workspace_size(n, batch);
   if (!work || work_bytes < need) return JFG_ERR_WORKSPACE;
   if (batch == 0) return JFG_OK;
@@ -380,31 +423,36 @@ __device__ __forceinline__ int find_prob(const HelmProb* tb, int nprob, long lon
 }
 
 // rows (contiguous axis) of every problem: U1 = rows through M, U2 through K
-__global__ void k_rag_rows(int family, int nprob, long long nlines, const HelmProb* __restrict__ tb,
-                           const double* __restrict__ gate, const double* __restrict__ u,
-                           double* __restrict__ U1, double* __restrict__ U2) {
+__global__ void k_rag_rows(int family, int nprob, int mmax, long long nlines,
+                           const HelmProb* __restrict__ tb, const double* __restrict__ gate,
+                           const double* __restrict__ u, double* __restrict__ U1,
+                           double* __restrict__ U2) {
+  __shared__ HelmTab T;
+  fill_tab(family, mmax, T);
   const long long line = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (line >= nlines) return;
   const int p = find_prob(tb, nprob, line);
   if (gate[p] == 0.0) return;  // x unchanged: its residual stands
   const HelmProb q = tb[p];
   const long long off = q.off64 + (line - q.line0) * q.n;
-  helm_row(family, q.n, u + off, 1, U1 + off, U2 + off);
+  helm_row(T, q.n, u + off, 1, U1 + off, U2 + off);
 }
 
 // columns: r = b - [(alpha2 M + K) U1 + M U2]
-__global__ void k_rag_cols(int family, int nprob, long long nlines,
+__global__ void k_rag_cols(int family, int nprob, int mmax, long long nlines,
                            const HelmProb* __restrict__ tb, const double* __restrict__ gate,
                            const double* __restrict__ U1, const double* __restrict__ U2,
                            const double* __restrict__ alpha2, const double* __restrict__ b,
                            double* __restrict__ r) {
+  __shared__ HelmTab T;
+  fill_tab(family, mmax, T);
   const long long line = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (line >= nlines) return;
   const int p = find_prob(tb, nprob, line);
   if (gate[p] == 0.0) return;
   const HelmProb q = tb[p];
   const long long off = q.off64 + (line - q.line0);
-  helm_col(family, q.n, U1 + off, U2 + off, q.n, alpha2[p], b + off, r + off);
+  helm_col(T, q.n, U1 + off, U2 + off, q.n, alpha2[p], b + off, r + off);
 }
 
 struct GroupedLayout {
@@ -456,10 +504,14 @@ extern "C" int jfg_helmholtz_solve_grouped(
       !W_hi || !W_lo || !lam32 || !alpha2 || !alpha2_32 || !rhs || !x || !(tol > 0.0) ||
       max_refine < 1)
     return JFG_ERR_ARG;
-  for (int g = 0; g < ngroups; ++g)
+  int mmax = 0;
+  for (int g = 0; g < ngroups; ++g) {
     if (n[g] < 1 || nq[g] < n[g] || (nq[g] & 3) || batch[g] < 1 || !E_hi[g] || !E_lo[g] ||
         !W_hi[g] || !W_lo[g] || !lam32[g])
       return JFG_ERR_ARG;
+    if (n[g] + 2 > mmax) mmax = n[g] + 2;
+  }
+  if (mmax > HTAB) return JFG_ERR_UNSUPPORTED;
   const GroupedLayout Lo = grouped_layout(ngroups, n, nq, batch);
   if (!work || work_bytes < Lo.total) return JFG_ERR_WORKSPACE;
   cudaStream_t st = (cudaStream_t)stream;
@@ -572,9 +624,9 @@ extern "C" int jfg_helmholtz_solve_grouped(
                                 out3.data(), tc, st));
     k_rag_axpy<<<vgrid, 256, 0, st>>>(tb, d32, hout, x, nref);
     JFG_LAUNCHED();
-    k_rag_rows<<<lblocks, 128, 0, st>>>(family, np, Lo.lines, tb, hout, x, U1, U2);
+    k_rag_rows<<<lblocks, 128, 0, st>>>(family, np, mmax, Lo.lines, tb, hout, x, U1, U2);
     JFG_LAUNCHED();
-    k_rag_cols<<<lblocks, 128, 0, st>>>(family, np, Lo.lines, tb, hout, U1, U2, alpha2, rhs,
+    k_rag_cols<<<lblocks, 128, 0, st>>>(family, np, mmax, Lo.lines, tb, hout, U1, U2, alpha2, rhs,
                                         r64);
     JFG_LAUNCHED();
     k_rag_sq_part<<<sgrid, 256, 0, st>>>(tb, r64, hout, part);
