@@ -209,6 +209,21 @@ int jfg_tp_apply_tc_bf16x3(int ndim, const int* rows, const int* cols, int batch
                            const float* in, float* out, void* work, size_t work_bytes,
                            void* stream);
 
+/* ---- affine transforms (inhomogeneous boundary lifting) -----------------
+ * out[b] = (x_ax mats[ax]) in[b] + shift, one shift array (rows[0] x ... x
+ * rows[ndim-1]) for every b, added in the epilogue of the last pass (the pass
+ * accumulates, beta = 1, into out pre-filled with shift).  The DirectSum
+ * spaces' maps are affine in the coefficients: to_orthogonal adds the boundary
+ * lift, from_orthogonal / forward subtract it, backward adds the lift's grid
+ * values (DirectSum.to_orthogonal/from_orthogonal/backward/forward,
+ * src/jaxfun/galerkin/composite.py:585-600, 617-621; DirectSumTPS,
+ * src/jaxfun/galerkin/tensorproductspace.py:777-851).  out must not overlap
+ * in; otherwise as jfg_tp_apply_f64 (same workspace size).
+ */
+int jfg_tp_apply_affine_f64(int ndim, const int* rows, const int* cols, int batch,
+                            const double* const* mats, const double* in, const double* shift,
+                            double* out, void* work, size_t work_bytes, void* stream);
+
 /* ---- batched banded LU (wavenumber solver) ------------------------------
  * TPMatricesWavenumberSolver (src/jaxfun/la/tpmatrix.py:590-1013): one 1-D
  * banded system per Fourier wavenumber, factored without pivoting

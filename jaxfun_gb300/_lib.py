@@ -101,6 +101,8 @@ SIGNATURES = {
                               _vp, _sz, _vp]),
     "jfg_tp_apply_tc": (_i, [_i, C.POINTER(_i), C.POINTER(_i), _i, C.POINTER(_vp),
                              C.POINTER(_vp), _vp, _vp, _vp, _sz, _vp]),
+    "jfg_tp_apply_affine_f64": (_i, [_i, C.POINTER(_i), C.POINTER(_i), _i, C.POINTER(_vp),
+                                     _vp, _vp, _vp, _vp, _sz, _vp]),
     "jfg_fd_solve_workspace_size": (_sz, [_i, _i, _i, _i]),
     "jfg_fd_solve_f64": (_i, [_i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
     "jfg_fd_solve_f32": (_i, [_i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),

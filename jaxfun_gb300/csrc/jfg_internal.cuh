@@ -143,7 +143,7 @@ int validate_desc(const jfg_contract_desc& d);
 template <typename T>
 int tp_apply(Engine e, int ndim, const int* rows, const int* cols, int batch,
              const OpRef<T>* mats, const T* in, T* out, void* work, size_t work_bytes,
-             cudaStream_t st);
+             cudaStream_t st, const T* shift = nullptr);
 template <typename T>
 int fd_solve(Engine e, int ndim, int n, int batch, OpRef<T> E, OpRef<T> W, const T* lam,
              const T* c0, const T* c1, const T* rhs, T* out, void* work, size_t work_bytes,

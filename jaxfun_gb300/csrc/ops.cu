@@ -33,10 +33,22 @@ size_t tp_apply_ws(int ndim, const int* rows, const int* cols, int batch, int eb
   return 2 * align_up(mx * eb, 256);
 }
 
+// out[i] = shift[i % per] for i < total: the constant field of an affine
+// transform, written before the last pass accumulates into it (beta = 1)
+template <typename T>
+__global__ void k_bcast_fill(const T* __restrict__ shift, long long per, long long total,
+                             T* __restrict__ out) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < total; i += stride)
+    out[i] = shift[i % per];
+}
+
+// shift (optional): out[b] = (x_ax mats[ax]) in[b] + shift, the same shift
+// (shape rows[0] x ... x rows[ndim-1]) for every b; out must not overlap in
 template <typename T>
 int tp_apply(Engine e, int ndim, const int* rows, const int* cols, int batch,
              const OpRef<T>* mats, const T* in, T* out, void* work, size_t work_bytes,
-             cudaStream_t st) {
+             cudaStream_t st, const T* shift) {
   if (ndim < 1 || ndim > 3 || !rows || !cols || !mats || !in || !out || batch < 0)
     return JFG_ERR_ARG;
   for (int i = 0; i < ndim; ++i)
@@ -56,6 +68,19 @@ int tp_apply(Engine e, int ndim, const int* rows, const int* cols, int batch,
     const int M = rows[ax];
     T* dst = (t == ndim - 1) ? out : buf[t & 1];
     jfg_contract_desc d = make_desc(batch, M, (int)P, K);
+    if (shift && t == ndim - 1) {
+      long long per = 1;
+      for (int i = 0; i < ndim; ++i) per *= rows[i];
+      const long long total = per * batch;
+      long long blocks = (total + 255) / 256;
+      if (blocks > 4 * 152) blocks = 4 * 152;
+      if (total > 0) {
+        k_bcast_fill<T><<<(int)blocks, 256, 0, st>>>(shift, per, total, out);
+        JFG_CHECK_LAUNCH();
+        count_launches(1);
+      }
+      d.beta = 1.0;
+    }
     JFG_TRY(contract(e, d, mats[ax], src, dst, st));
     for (int i = ndim - 1; i > 0; --i) shape[i] = shape[i - 1], order[i] = order[i - 1];
     shape[0] = M;
@@ -265,9 +290,10 @@ __global__ void k_weighted_field(int ndim, int nq, long long total, const T* __r
 }
 
 template int tp_apply<double>(Engine, int, const int*, const int*, int, const OpRef<double>*,
-                              const double*, double*, void*, size_t, cudaStream_t);
+                              const double*, double*, void*, size_t, cudaStream_t,
+                              const double*);
 template int tp_apply<float>(Engine, int, const int*, const int*, int, const OpRef<float>*,
-                             const float*, float*, void*, size_t, cudaStream_t);
+                             const float*, float*, void*, size_t, cudaStream_t, const float*);
 template int fd_solve<double>(Engine, int, int, int, OpRef<double>, OpRef<double>,
                               const double*, const double*, const double*, const double*,
                               double*, void*, size_t, cudaStream_t, Active);
@@ -355,6 +381,18 @@ extern "C" int jfg_tp_apply_tc_bf16x3(int ndim, const int* rows, const int* cols
   }
   return jfg::tp_apply<float>(Engine::TB, ndim, rows, cols, batch, m, in, out, work,
                               work_bytes, (cudaStream_t)stream);
+}
+
+extern "C" int jfg_tp_apply_affine_f64(int ndim, const int* rows, const int* cols, int batch,
+                                       const double* const* mats, const double* in,
+                                       const double* shift, double* out, void* work,
+                                       size_t work_bytes, void* stream) {
+  if (!mats || !shift || ndim < 1 || ndim > 3) return JFG_ERR_ARG;
+  if (in == out) return JFG_ERR_ARG;
+  OpRef<double> m[3];
+  for (int i = 0; i < ndim; ++i) m[i] = OpRef<double>{mats[i], nullptr};
+  return jfg::tp_apply<double>(Engine::F64, ndim, rows, cols, batch, m, in, out, work,
+                               work_bytes, (cudaStream_t)stream, shift);
 }
 
 extern "C" size_t jfg_fd_solve_workspace_size(int ndim, int n, int batch, int elem_bytes) {

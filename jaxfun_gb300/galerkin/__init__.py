@@ -2,6 +2,9 @@
 
 from .spaces import (  # noqa: F401
     DIRICHLET,
+    BCGeneric,
+    BCValue,
+    DirectSum,
     Chebyshev,
     Composite,
     FunctionSpace,
@@ -10,4 +13,10 @@ from .spaces import (  # noqa: F401
     chebyshev_gauss,
     legendre_gauss,
 )
-from .tensorproductspace import TensorProduct, TensorProductSpace, tp_apply  # noqa: F401
+from .tensorproductspace import (  # noqa: F401
+    DirectSumTPS,
+    TensorProduct,
+    TensorProductSpace,
+    tp_apply,
+    tp_apply_affine,
+)

@@ -12,6 +12,7 @@ from .mixed import MixedVarCoefSolver, split_tf32  # noqa: F401
 from .varcoef import (  # noqa: F401
     VarCoefMatrix,
     fd_preconditioner,
+    helmholtz_system,
     pack_varcoef_ops,
     pcg,
     poisson_tpmatrices,

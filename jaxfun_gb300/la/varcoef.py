@@ -101,6 +101,70 @@ def poisson_tpmatrices(T: TensorProductSpace, alpha2: float = 0.0) -> TPMatrices
     return TPMatrices(terms)
 
 
+def helmholtz_system(T: TensorProductSpace, f, alpha2: float = 0.0):
+    """(A, b) of alpha^2 u - div grad u = f on T, Dirichlet data included:
+    what ``inner(alpha**2*u*v - v*Div(Grad(u)) - v*f, kind="system")`` returns
+    (inner.py:520-562, 809-984).  For a DirectSumTPS the trial function is
+    u = u_h + lift; the lift's part of the bilinear form moves to the
+    right-hand side, b = (f, v) - a(lift, v), so ``A.solve(b)`` gives the
+    homogeneous coefficients and ``T.backward`` adds the lift back.
+
+    A is built per axis (unequal sizes allowed; the fast solver needs equal
+    axes).  ``f`` is sampled on the quadrature grid (leading batch axes
+    allowed); b is one affine contraction on the GPU: the scalar product of f
+    with the boundary term (a_bc is fixed, computed once in FP64) added in the
+    last pass's epilogue."""
+    from ..galerkin.tensorproductspace import DirectSumTPS, tp_apply_affine
+
+    H = T.get_homogeneous().basespaces
+    nd = len(H)
+    K = [s.stiffness_matrix() for s in H]
+    M = [s.mass_matrix() for s in H]
+    terms = []
+    if alpha2 != 0.0:
+        terms.append(TPMatrix(M, alpha2))
+    for ax in range(nd):
+        mats = list(M)
+        mats[ax] = K[ax]
+        terms.append(TPMatrix(mats, 1.0))
+    A = TPMatrices(terms)
+    if not isinstance(T, DirectSumTPS):
+        return A, T.scalar_product(f)
+    mats, shift = helmholtz_lifting(T, alpha2)
+    return A, tp_apply_affine(mats, f, shift)
+
+
+def helmholtz_lifting(T, alpha2: float = 0.0):
+    """(scalar-product matrices, -a(lift, v)) of a DirectSumTPS: the boundary
+    lift's part of alpha^2 (u, v) + (grad u, grad v) with the homogeneous test
+    functions, FP64 host setup cached on T (the lift is fixed by the data)."""
+    from ..galerkin.tensorproductspace import kron_apply_host
+
+    key = ("rhs", float(alpha2))
+    cached = T._maps.get(key)
+    if cached is not None:
+        return cached
+    H = T.get_homogeneous().basespaces
+    nd = len(H)
+    KM = [s.test_orthogonal_matrices() for s in H]
+    Kr = [km[0] for km in KM]
+    Mr = [km[1] for km in KM]
+    bc = np.zeros(tuple(s.dim for s in H))
+    if alpha2 != 0.0:
+        bc += alpha2 * kron_apply_host(Mr, T.lift)
+    for ax in range(nd):
+        mats = list(Mr)
+        mats[ax] = Kr[ax]
+        bc += kron_apply_host(mats, T.lift)
+    nf = tuple(s.num_quad_points for s in H)
+    sp_mats = [np.ascontiguousarray(s.scalar_product_matrix(nf[i])) for i, s in enumerate(H)]
+    shift = np.ascontiguousarray(-bc)
+    shift.setflags(write=False)
+    cached = (sp_mats, shift)
+    T._maps[key] = cached
+    return cached
+
+
 def fd_preconditioner(T: TensorProductSpace):
     """Constant-coefficient (kappa = 1) fast-diagonalisation factors."""
     return tpmats_lu_factor(poisson_tpmatrices(T).tpmats)

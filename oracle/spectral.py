@@ -511,3 +511,246 @@ def wavenumber_solve(data, offsets, rhs_2d):
     for k in range(rhs_2d.shape[0]):
         out[k] = np.linalg.solve(dia_to_dense(data[k], offsets, n), rhs_2d[k])
     return out
+
+
+# ---------------------------------------------------------------------------
+# Inhomogeneous Dirichlet data: DirectSum and DirectSumTPS
+# ---------------------------------------------------------------------------
+
+
+def bc_basis(family: str, N: int) -> np.ndarray:
+    """Dirichlet boundary basis as orthogonal-coefficient rows (2 x N).
+
+    Restates ``get_bc_basis`` (src/jaxfun/galerkin/composite.py:835-880) for
+    {"left": D, "right": D}: A[side][j] = psi_j(x_side) for j = 0, 1 (the
+    search start ``first`` = 0 gives an invertible A), S = (A^{-1})^T, so
+    basis function k is 1 at boundary k and 0 at the other.
+    """
+    A = Space1D(family, N).vandermonde_orth(np.array([-1.0, 1.0]))[:, :2]
+    S = np.zeros((2, N))
+    S[:, :2] = np.linalg.solve(A, np.eye(2)).T
+    return S
+
+
+def _bc_eval(v, coords):
+    shape = np.broadcast_shapes(*[np.shape(c) for c in coords])
+    if callable(v):
+        return np.broadcast_to(np.asarray(v(*coords), dtype=np.float64), shape)
+    return np.full(shape, float(v))
+
+
+def _solve_along0(P, b):
+    """P^{-1} b along axis 0 of an array of any rank."""
+    return np.linalg.solve(P, b.reshape(b.shape[0], -1)).reshape(b.shape)
+
+
+class DirectSum1D:
+    """Composite (+) BCGeneric with Dirichlet values (left, right), the
+    reference's ``DirectSum`` (src/jaxfun/galerkin/composite.py:502-631)."""
+
+    def __init__(self, family: str, N: int, left: float, right: float):
+        self.V = Space1D(family, N, dirichlet=True)
+        self.O = Space1D(family, N)
+        self.B = bc_basis(family, N)
+        self.vals = np.array([float(left), float(right)])
+
+    def lift(self):
+        """to_orthogonal of the boundary part: bnd_vals @ S_B (composite.py:585-591)."""
+        return self.vals @ self.B
+
+    def to_orthogonal(self, c):
+        lift = self.lift().reshape((-1,) + (1,) * (np.ndim(c) - 1))
+        return self.V.to_orthogonal(c) + lift
+
+    def from_orthogonal(self, a):
+        """P.solve(S (a - c_b)) with P = S S^T (composite.py:282-285, 593-600)."""
+        lift = self.lift().reshape((-1,) + (1,) * (np.ndim(a) - 1))
+        S = self.V.S
+        return _solve_along0(S @ S.T, np.tensordot(S, a - lift, axes=(1, 0)))
+
+    def forward(self, u):
+        """orthogonal forward, then from_orthogonal (composite.py:612-616)."""
+        return self.from_orthogonal(self.O.forward(u))
+
+    def backward(self, c, Nq=None):
+        return self.O.backward(self.to_orthogonal(c), Nq)
+
+    def evaluate(self, X, c):
+        return self.O.vandermonde_orth(np.asarray(X, dtype=np.float64)) @ self.to_orthogonal(c)
+
+
+class LiftedTPS:
+    """DirectSumTPS (src/jaxfun/galerkin/tensorproductspace.py:560-851) for
+    Legendre/Chebyshev axes.  ``axes``: list of (family, N, bc) with bc
+    "orth" (orthogonal space), None (homogeneous Dirichlet composite) or a
+    (left, right) pair of Dirichlet values, each a number or a callable of
+    all coordinates (the boundary's own coordinate fixed at the boundary).
+
+    tpspaces are keyed by a tuple of "h" (homogeneous factor) / "b" (boundary
+    factor) per axis; bndvals follow the reference's cases (:609-745).
+    """
+
+    def __init__(self, axes):
+        self.axes = list(axes)
+        nd = len(axes)
+        self.nd = nd
+        self.isbc = [isinstance(a[2], tuple) for a in axes]
+        bcind = [i for i in range(nd) if self.isbc[i]]
+        if nd == 3 and bcind[0] == 0:
+            raise ValueError("DirectSum cannot be the first space in a 3D tensor product.")
+        self.hom = [Space1D(f, N, dirichlet=(bc != "orth")) for f, N, bc in axes]
+        self.orth = [Space1D(f, N) for f, N, _ in axes]
+        self.Bs = [bc_basis(f, N) for f, N, _ in axes]
+        self.mesh = [self.orth[i].quad()[0] for i in range(nd)]
+        ends = (-1.0, 1.0)
+        two = len(bcind) == 2
+        # projected_bcs (:624-668): the other DirectSum's data at this one's ends
+        if two:
+            i0, i1 = bcind
+            h0, h1 = axes[i0][2], axes[i1][2]
+            proj = [[], []]
+            for a in range(2):
+                proj[0].append(tuple(self._fix(h0[a], {i0: ends[a], i1: ends[s]})
+                                     for s in range(2)))
+                proj[1].append(tuple(self._fix(h1[a], {i1: ends[a], i0: ends[s]})
+                                     for s in range(2)))
+        self.bndvals = {}
+        keys = [("h", "b") if self.isbc[i] else ("h",) for i in range(nd)]
+        import itertools
+
+        for key in itertools.product(*keys):
+            nb = [i for i in range(nd) if key[i] == "b"]
+            other = [i for i in range(nd) if key[i] == "h"]
+            if not nb:
+                continue
+            if not other:  # all boundary (2-D corners)
+                self.bndvals[key] = np.array(
+                    [[float(_bc_eval(v, [np.zeros(())] * nd)) for v in proj[0][a]]
+                     for a in range(2)])
+            elif len(other) == 1 and len(nb) == 1:  # 2-D, one boundary factor
+                b, o = nb[0], other[0]
+                uh = []
+                for j in range(2):
+                    g = _bc_eval(axes[b][2][j],
+                                 [self.mesh[o] if i == o else np.array(ends[j])
+                                  for i in range(nd)])
+                    if two:
+                        corner = proj[bcind.index(b)][j]
+                        f, N, _ = axes[o]
+                        cv = [float(_bc_eval(v, [np.zeros(())] * nd)) for v in corner]
+                        uh.append(DirectSum1D(f, N, cv[0], cv[1]).forward(g))
+                    else:
+                        uh.append(self.hom[o].forward(g))
+                self.bndvals[key] = np.array(uh) if b == 0 else np.array(uh).T
+            elif len(other) == 2 and len(nb) == 1:  # 3-D, one boundary factor
+                b = nb[0]
+                o = 1 if b == 2 else 2
+                uh = []
+                for j in range(2):
+                    G = _bc_eval(axes[b][2][j],
+                                 [self.mesh[0][:, None] if i == 0 else
+                                  (self.mesh[o][None, :] if i == o else np.array(ends[j]))
+                                  for i in range(nd)])
+                    if two:
+                        # the other DirectSum's data at this boundary, as a
+                        # function of (x, other coordinate)
+                        vals = axes[b][2][j]
+                        sub = tuple(
+                            (lambda x, y, v=vals, s=s, o=o, b=b, e=ends[j]:
+                             _bc_eval(v, [x, *( [ends[s], e] if o == 1 else [e, ends[s]] )]))
+                            for s in range(2))
+                        inner = LiftedTPS([(axes[0][0], axes[0][1], axes[0][2]),
+                                           (axes[o][0], axes[o][1], sub)])
+                        uh.append(inner.forward(G))
+                    else:
+                        uh.append(tp_forward([self.hom[0], self.hom[o]], G))
+                arr = np.array(uh)
+                self.bndvals[key] = arr.transpose(1, 2, 0) if b == 2 else arr.transpose(1, 0, 2)
+            else:  # 3-D, two boundary factors (:739-745)
+                uh = []
+                for a in range(2):
+                    for s in range(2):
+                        g = _bc_eval(axes[1][2][a], [self.mesh[0], np.array(ends[a]),
+                                                     np.array(ends[s])])
+                        uh.append(self.hom[0].forward(g))
+                self.bndvals[key] = np.array(uh).T.reshape((-1, 2, 2))
+
+    @staticmethod
+    def _fix(v, fixed):
+        """Value of v with the coordinates in ``fixed`` substituted."""
+        def f(*coords):
+            c = list(coords)
+            for i, e in fixed.items():
+                c[i] = np.full(np.shape(c[i]), e)
+            return _bc_eval(v, c)
+        return f
+
+    def _factor_to_orth(self, key, c):
+        for ax in range(self.nd):
+            S = self.Bs[ax] if key[ax] == "b" else self.hom[ax].S
+            c = _along(ax, lambda b, S=S: np.tensordot(S.T, b, axes=(1, 0)), c)
+        return c
+
+    def lift(self):
+        a = 0.0
+        for key, v in self.bndvals.items():
+            a = a + self._factor_to_orth(key, v)
+        return a
+
+    def to_orthogonal(self, c):
+        """homogeneous to_orthogonal plus every boundary factor's (:808-823)."""
+        return self._factor_to_orth(("h",) * self.nd, c) + self.lift()
+
+    def from_orthogonal(self, a):
+        """subtract the boundary factors, then the homogeneous from_orthogonal
+        per axis (:825-851)."""
+        d = a - self.lift()
+        for ax in range(self.nd):
+            if self.axes[ax][2] == "orth":
+                continue
+            S = self.hom[ax].S
+            d = _along(ax, lambda b, S=S: _solve_along0(S @ S.T, np.tensordot(S, b, axes=(1, 0))),
+                       d)
+        return d
+
+    def forward(self, u):
+        return self.from_orthogonal(tp_forward(self.orth, u))
+
+    def backward(self, c, Nq=None):
+        return tp_backward(self.orth, self.to_orthogonal(c), Nq)
+
+    def evaluate_grid(self, xs, c):
+        """u on the tensor grid of points xs (one array per axis)."""
+        a = self.to_orthogonal(c)
+        for ax, x in enumerate(xs):
+            V = self.orth[ax].vandermonde_orth(np.asarray(x, dtype=np.float64))
+            a = _along(ax, lambda b, V=V: np.tensordot(V, b, axes=(1, 0)), a)
+        return a
+
+    def helmholtz_rhs(self, f, alpha2=0.0):
+        """b = (f, v) - a(lift, v) for alpha^2 u - div grad u = f: the trial
+        lift on the orthogonal basis with test functions of the homogeneous
+        space, by quadrature (inner.py:809-911 with a DirectSum trial)."""
+        b = tp_scalar_product(self.hom, f)
+        lift = self.lift()
+        mats_M, mats_K = [], []
+        for ax in range(self.nd):
+            x, w = self.orth[ax].quad()
+            P0 = self.orth[ax].vandermonde_orth(x, 0)
+            P2 = self.orth[ax].vandermonde_orth(x, 2)
+            S = self.hom[ax].S
+            mats_M.append(S @ ((P0.T * w[None, :]) @ P0))
+            mats_K.append(-(S @ ((P0.T * w[None, :]) @ P2)))
+        terms = []
+        if alpha2 != 0.0:
+            terms.append((alpha2, mats_M))
+        for ax in range(self.nd):
+            m = list(mats_M)
+            m[ax] = mats_K[ax]
+            terms.append((1.0, m))
+        for s, mats in terms:
+            Z = lift
+            for ax, A in enumerate(mats):
+                Z = np.moveaxis(np.tensordot(A, Z, axes=(1, ax)), 0, ax)
+            b = b - s * Z
+        return b
