@@ -24,7 +24,10 @@ def as_device(a, dtype=torch.float64) -> torch.Tensor:
         if t.dtype != dtype:
             t = t.to(dtype)
         return t.contiguous()
-    return torch.as_tensor(np.ascontiguousarray(a), dtype=dtype, device=device())
+    a = np.ascontiguousarray(a)
+    if not a.flags.writeable:  # cached read-only operators: torch wants a writable view
+        a = a.copy()
+    return torch.as_tensor(a, dtype=dtype, device=device())
 
 
 def workspace(nbytes: int, slot: int = 0) -> torch.Tensor:
