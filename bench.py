@@ -531,7 +531,8 @@ def run_tour(args):
     if os.path.exists(args.weights):
         model = sno_train.load(args.weights, batch=32)
         maps = sno_train.GridMaps()
-        X, s = sno_train.features(torch.log(kap), torch.as_tensor(f_h, device="cuda"), maps)
+        X, s = sno_train.features(torch.log(kap.float()), torch.as_tensor(f_h, device="cuda"),
+                                  maps)
         g = sno_train.initial_guess(model, maps, X, s)
         bounded(S.solve, rhs, tol=1e-11, guess=g, max_outer=1, maxiter_inner=12)
     m = SNO(SNOConfig(batch=8), seed=0)
@@ -618,7 +619,7 @@ def run_varcoef3d(args):
         f_grid = To.backward(fh)
 
         def solve_learned():
-            X, sc = sno_train.features(torch.log(kap), f_grid, maps)
+            X, sc = sno_train.features(torch.log(kap.float()), f_grid, maps)
             guess = sno_train.initial_guess(model, maps, X, sc)
             return S.solve(b, tol=args.tol3d, guess=guess)
 
@@ -707,25 +708,28 @@ def run_ours(args):
         if not args.no_learned and os.path.exists(args.weights):
             from jaxfun_gb300.sno import train as sno_train
 
-            model = sno_train.load(args.weights, batch=min(B, 64))
+            model = sno_train.load(args.weights, batch=min(B, 128))
             maps = sno_train.GridMaps()
         guess = torch.empty(B, n, n, dtype=torch.float64, device="cuda")
 
     def learned_guess():
         # network inputs (log kappa, f / rms(f), x, y) on its 64^2 grid, inference
-        # on the tensor cores, and the map back to the first 32^2 coefficients
-        X, s = sno_train.features(torch.log(kap), fgrid, maps)
+        # on the tensor cores, and the map back to the first 32^2 coefficients;
+        # the network reads FP32, so log kappa is taken in FP32 (the FP64 log
+        # alone cost ~0.5 ms per 128 problems on the FP64 units)
+        X, s = sno_train.features(torch.log(kap.float()), fgrid, maps)
         guess.copy_(sno_train.initial_guess(model, maps, X, s))
         return guess
 
     def prepare(kap_d, f_d):
-        # kw = kappa * w (x) w in FP64 and FP32; rhs = (f, v) scalar product
+        # kw = kappa * w (x) w in FP64 and FP32; rhs = (f, v) scalar product in
+        # double-FP32 arithmetic (FP64-class, ~3x the FP64 pipe's rate)
         _lib.check(L.jfg_weighted_field_f64(2, N, B, kap_d.data_ptr(), w.data_ptr(),
                                             A.kw.data_ptr(), solver.kw32.data_ptr(), sh),
                    "weighted_field")
-        _lib.check(L.jfg_tp_apply_f64(2, rows, cols, B, _lib.ptr_array([SP.data_ptr()] * 2),
-                                      f_d.data_ptr(), rhs.data_ptr(), tp_ws.data_ptr(),
-                                      tp_ws.numel(), sh), "scalar_product")
+        _lib.check(L.jfg_tp_apply_df64(2, rows, cols, B, _lib.ptr_array([SP.data_ptr()] * 2),
+                                       f_d.data_ptr(), rhs.data_ptr(), tp_ws.data_ptr(),
+                                       tp_ws.numel(), sh), "scalar_product")
 
     def solve(use_model=True):
         g = learned_guess() if (use_model and model is not None) else None

@@ -193,6 +193,12 @@ size_t jfg_tp_apply_workspace_size(int ndim, const int* rows, const int* cols, i
 int jfg_tp_apply_f64(int ndim, const int* rows, const int* cols, int batch,
                      const double* const* mats, const double* in, double* out,
                      void* work, size_t work_bytes, void* stream);
+/* FP64 data in double-FP32 arithmetic (jfg_contract_df64 per pass, about
+ * 1e-14 relative per contraction, ~3x the FP64 pipe's rate on GB300): for
+ * FP64-class right-hand sides, e.g. the scalar product of a forcing. */
+int jfg_tp_apply_df64(int ndim, const int* rows, const int* cols, int batch,
+                      const double* const* mats, const double* in, double* out,
+                      void* work, size_t work_bytes, void* stream);
 int jfg_tp_apply_f32(int ndim, const int* rows, const int* cols, int batch,
                      const float* const* mats, const float* in, float* out,
                      void* work, size_t work_bytes, void* stream);

@@ -99,6 +99,8 @@ SIGNATURES = {
                               _vp, _sz, _vp]),
     "jfg_tp_apply_f32": (_i, [_i, C.POINTER(_i), C.POINTER(_i), _i, C.POINTER(_vp), _vp, _vp,
                               _vp, _sz, _vp]),
+    "jfg_tp_apply_df64": (_i, [_i, C.POINTER(_i), C.POINTER(_i), _i, C.POINTER(_vp), _vp, _vp,
+                               _vp, _sz, _vp]),
     "jfg_tp_apply_tc": (_i, [_i, C.POINTER(_i), C.POINTER(_i), _i, C.POINTER(_vp),
                              C.POINTER(_vp), _vp, _vp, _vp, _sz, _vp]),
     "jfg_tp_apply_affine_f64": (_i, [_i, C.POINTER(_i), C.POINTER(_i), _i, C.POINTER(_vp),

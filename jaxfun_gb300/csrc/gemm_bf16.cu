@@ -311,11 +311,18 @@ extern "C" int jfg_gemm_bf16(const jfg_gemm_desc* dp, const void* A, const void*
   while (cols < prm.Nt) cols <<= 1;
   prm.tmem_cols = cols;
   const size_t stage = ABYTES + (size_t)prm.Nt * KBE * 2;
-  int stages = (int)((200 * 1024) / stage);
-  if (stages > 6) stages = 6;
-  prm.stages = stages;
   const int nkb = (d.K + KBE - 1) / KBE;
   prm.kb_per_split = (nkb + d.ksplit - 1) / d.ksplit;
+  // pipeline depth: no deeper than the K blocks a CTA has (the channel-mixing
+  // GEMMs have one, so several CTAs share an SM and their epilogues overlap);
+  // long-K GEMMs keep >= 3 stages but leave room for a second CTA per SM
+  int stages = (int)((200 * 1024) / stage);
+  if (stages > 6) stages = 6;
+  const int two_per_sm = (int)((113 * 1024 - 1100) / stage);
+  if (stages > 3 && two_per_sm >= 3 && two_per_sm < stages) stages = two_per_sm;
+  if (stages > prm.kb_per_split) stages = prm.kb_per_split;
+  if (stages < 1) stages = 1;
+  prm.stages = stages;
   prm.a_bat = (d.batch > 1 && d.a_batch != 0) ? 1 : 0;
   prm.b_bat = (d.batch > 1 && d.b_batch != 0) ? 1 : 0;
   const int ksplit = (nkb + prm.kb_per_split - 1) / prm.kb_per_split;

@@ -345,6 +345,16 @@ extern "C" int jfg_tp_apply_f64(int ndim, const int* rows, const int* cols, int 
                                work_bytes, (cudaStream_t)stream);
 }
 
+extern "C" int jfg_tp_apply_df64(int ndim, const int* rows, const int* cols, int batch,
+                                 const double* const* mats, const double* in, double* out,
+                                 void* work, size_t work_bytes, void* stream) {
+  if (!mats || ndim < 1 || ndim > 3) return JFG_ERR_ARG;
+  OpRef<double> m[3];
+  for (int i = 0; i < ndim; ++i) m[i] = OpRef<double>{mats[i], nullptr};
+  return jfg::tp_apply<double>(Engine::DF, ndim, rows, cols, batch, m, in, out, work,
+                               work_bytes, (cudaStream_t)stream);
+}
+
 extern "C" int jfg_tp_apply_f32(int ndim, const int* rows, const int* cols, int batch,
                                 const float* const* mats, const float* in, float* out,
                                 void* work, size_t work_bytes, void* stream) {

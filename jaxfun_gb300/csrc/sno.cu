@@ -1,6 +1,7 @@
 // CUDA-core kernels of the spectral neural operator that are too small or too
 // irregular for the tensor cores: per-mode channel mixing (forward/backward),
 // bias gradients, the loss and its gradient, and the Adam update.
+#include <algorithm>
 #include <cuda_bf16.h>
 #include <math.h>
 
@@ -12,23 +13,54 @@ namespace {
 constexpr int MAXC = 64;  // channel width limit of the mode-mixing kernels
 
 // out[b][co][q] = sum_ci R[q][co][ci] x[b][q][ci]
-__global__ void k_modemix_fwd(int batch, int nq, int C, const float* __restrict__ R,
-                              const float* __restrict__ x, __nv_bfloat16* __restrict__ out) {
-  __shared__ float Rs[MAXC * (MAXC + 1)];
-  __shared__ float xs[MAXC];
-  const int q = blockIdx.x;
-  const int t = threadIdx.x;  // output channel
-  for (int i = t; i < C * C; i += blockDim.x) Rs[(i / C) * (C + 1) + i % C] = R[(long long)q * C * C + i];
+//
+// A block owns MM_Q consecutive modes and a slice of the samples; thread
+// (co, ql) keeps the row R[q0+ql][co][:] in registers for the whole slice.
+// Per sample the block stages x[b][q0 .. q0+MM_Q)[:] (contiguous, one float
+// per thread) in shared memory, double-buffered so one barrier per sample
+// suffices, and the MM_Q threads of one output channel write MM_Q
+// consecutive modes (16 bytes).  The number of modes must be a multiple of
+// MM_Q (checked by the launcher).
+constexpr int MM_Q = 8;
+
+constexpr int MM_LD = MAXC + 4;  // 16-byte rows; the MM_Q rows of a warp's float4 reads hit distinct banks
+
+__global__ void __launch_bounds__(MM_Q * MAXC) k_modemix_fwd(
+    int batch, int nq, int C, int per_block, const float* __restrict__ R,
+    const float* __restrict__ x, __nv_bfloat16* __restrict__ out) {
+  __shared__ __align__(16) float xs[2][MM_Q][MM_LD];
+  const int t = threadIdx.x;
+  // channels ci >= C stay zero (their R entries are zero too)
+  for (int i = t; i < 2 * MM_Q * MM_LD; i += blockDim.x) (&xs[0][0][0])[i] = 0.f;
   __syncthreads();
-  for (int b = 0; b < batch; ++b) {
-    if (t < C) xs[t] = x[((long long)b * nq + q) * C + t];
+  const int ql = t % MM_Q;
+  const int co = t / MM_Q;
+  const int q0 = blockIdx.x * MM_Q;
+  const int b0 = blockIdx.y * per_block;
+  const int b1 = min(batch, b0 + per_block);
+  const bool active = co < C;
+  float r[MAXC];
+  const float* Rrow = R + ((long long)(q0 + ql) * C + (active ? co : 0)) * C;
+#pragma unroll
+  for (int ci = 0; ci < MAXC; ++ci) r[ci] = (active && ci < C) ? __ldg(Rrow + ci) : 0.f;
+  const int nload = MM_Q * C;
+  for (int b = b0; b < b1; ++b) {
+    float (*xb)[MM_LD] = xs[b & 1];
+    if (t < nload) xb[t / C][t % C] = x[((long long)b * nq + q0) * C + t];
     __syncthreads();
-    if (t < C) {
+    if (active) {
+      const float4* xv = reinterpret_cast<const float4*>(xb[ql]);
       float s = 0.f;
-      for (int ci = 0; ci < C; ++ci) s += Rs[t * (C + 1) + ci] * xs[ci];
-      out[((long long)b * C + t) * nq + q] = __float2bfloat16(s);
+#pragma unroll
+      for (int c4 = 0; c4 < MAXC / 4; ++c4) {
+        const float4 v = xv[c4];
+        s = fmaf(r[4 * c4], v.x, s);
+        s = fmaf(r[4 * c4 + 1], v.y, s);
+        s = fmaf(r[4 * c4 + 2], v.z, s);
+        s = fmaf(r[4 * c4 + 3], v.w, s);
+      }
+      out[((long long)b * C + co) * nq + q0 + ql] = __float2bfloat16(s);
     }
-    __syncthreads();
   }
 }
 
@@ -152,8 +184,15 @@ extern "C" int jfg_sno_modemix_fwd(int batch, int nmodes, int C, const float* R,
                                    void* out, void* stream) {
   if (batch < 0 || nmodes < 0 || C < 1 || C > MAXC || !R || !x || !out) return JFG_ERR_ARG;
   if (batch == 0 || nmodes == 0) return JFG_OK;
-  k_modemix_fwd<<<nmodes, ((C + 31) / 32) * 32, 0, (cudaStream_t)stream>>>(
-      batch, nmodes, C, R, x, (__nv_bfloat16*)out);
+  if (nmodes % MM_Q != 0) return JFG_ERR_ARG;
+  // enough blocks for every SM, at least 8 samples per block
+  const int mblocks = nmodes / MM_Q;
+  int groups = (2 * 152 + mblocks - 1) / mblocks;
+  groups = std::max(1, std::min(groups, (batch + 7) / 8));
+  const int per_block = (batch + groups - 1) / groups;
+  groups = (batch + per_block - 1) / per_block;
+  k_modemix_fwd<<<dim3(mblocks, groups), MM_Q * MAXC, 0, (cudaStream_t)stream>>>(
+      batch, nmodes, C, per_block, R, x, (__nv_bfloat16*)out);
   JFG_LAUNCHED();
   return JFG_OK;
 }

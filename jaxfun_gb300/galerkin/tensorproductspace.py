@@ -31,9 +31,12 @@ def device_op(mat: np.ndarray, dtype=torch.float64) -> torch.Tensor:
     return t
 
 
-def tp_apply(mats: list[np.ndarray], x, dtype=torch.float64) -> torch.Tensor:
-    """out = (x_ax mats[ax]) x over the trailing len(mats) axes of ``x``."""
+def tp_apply(mats: list[np.ndarray], x, dtype=torch.float64, df: bool = False) -> torch.Tensor:
+    """out = (x_ax mats[ax]) x over the trailing len(mats) axes of ``x``.
+    ``df``: FP64 data with double-FP32 arithmetic (``jfg_tp_apply_df64``)."""
     nd = len(mats)
+    if df and dtype != torch.float64:
+        raise ValueError("the double-FP32 engine takes FP64 data")
     x = as_device(x, dtype)
     if x.ndim < nd:
         raise ValueError(f"array of rank {x.ndim} for a {nd}-axis transform")
@@ -52,7 +55,8 @@ def tp_apply(mats: list[np.ndarray], x, dtype=torch.float64) -> torch.Tensor:
     ws_bytes = L.jfg_tp_apply_workspace_size(nd, r_a, c_a, batch, eb)
     ws = workspace(ws_bytes)
     ops = [device_op(m, dtype) for m in mats]
-    fn = L.jfg_tp_apply_f64 if dtype == torch.float64 else L.jfg_tp_apply_f32
+    fn = (L.jfg_tp_apply_df64 if df else L.jfg_tp_apply_f64) if dtype == torch.float64 \
+        else L.jfg_tp_apply_f32
     st = fn(nd, r_a, c_a, batch, _lib.ptr_array([o.data_ptr() for o in ops]), x.data_ptr(),
             out.data_ptr(), ws.data_ptr(), ws.numel(), _lib.stream_handle())
     _lib.check(st, "jfg_tp_apply")
@@ -241,12 +245,15 @@ class TensorProductSpace:
         return W
 
     # ---- transforms (tensorproductspace.py:330-417) -------------------------
-    # precision: "f64" (FP64 CUDA cores, parity path), "bf16x3" (FP32 data,
+    # precision: "f64" (FP64 CUDA cores, parity path), "df64" (FP64 data,
+    # double-FP32 arithmetic on the FP32 pipe, ~1e-14), "bf16x3" (FP32 data,
     # split-BF16 operators, three BF16 MMAs per product) or "tc" (FP32 data,
     # split-TF32 tcgen05 contractions)
     def _apply(self, mats, x, precision):
         if precision == "f64":
             return tp_apply(mats, x)
+        if precision == "df64":
+            return tp_apply(mats, x, df=True)
         if precision == "bf16x3":
             return tp_apply_bf16x3(mats, x)
         if precision == "tc":

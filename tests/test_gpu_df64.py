@@ -74,3 +74,22 @@ def test_mixed_residual_df64_vs_f64():
         xm, it_in, it_out = MixedVarCoefSolver(A, residual=res).solve(b, tol=1e-11)
         err = float(((xm - xt).abs().amax(dim=(1, 2)) / xt.abs().amax(dim=(1, 2))).max())
         assert err <= 1e-10, (res, err)
+
+
+@pytest.mark.parametrize("family", ["legendre", "chebyshev"])
+def test_scalar_product_df64(family):
+    """TensorProductSpace.scalar_product(precision="df64") (the right-hand side
+    assembly of the end-to-end solve) against the FP64 path and the oracle."""
+    from jaxfun_gb300.galerkin import DIRICHLET, Chebyshev, FunctionSpace, Legendre, TensorProduct
+    from oracle import spectral as O
+
+    N = 64
+    D = FunctionSpace(N, Legendre if family == "legendre" else Chebyshev, bcs=DIRICHLET)
+    T = TensorProduct(D, D)
+    f = np.random.default_rng(2).standard_normal((3, N, N))
+    b64 = T.scalar_product(f).cpu().numpy()
+    bdf = T.scalar_product(f, precision="df64").cpu().numpy()
+    assert np.abs(bdf - b64).max() <= DF_TOL * np.abs(b64).max()
+    V = O.Space1D(family, N, True)
+    bo = np.stack([O.tp_scalar_product([V, V], fi) for fi in f])
+    assert np.abs(bdf - bo).max() <= 1e-12 * np.abs(bo).max()
