@@ -41,6 +41,7 @@ constexpr uint32_t ABYTES = TM * KBE * 2;  // 16 KB
 struct GemmParams {
   jfg_gemm_desc d;
   int Nt, stages, tmem_cols, kb_per_split, a_bat, b_bat;
+  int nb;              // samples per CTA: B tiles of nb consecutive samples side by side (N = nb * Nt)
   int a_perm, b_perm;  // 1: tensor map dims ordered (K, batch, rows)
   int vec_ok;          // 1: every row-major operand allows 16-byte vector access
 };
@@ -59,8 +60,9 @@ __global__ void __launch_bounds__(NTH, 1)
   extern __shared__ uint8_t smem_raw[];
   uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   const jfg_gemm_desc& d = prm.d;
-  const int Nt = prm.Nt, S = prm.stages;
-  const uint32_t bbytes = (uint32_t)Nt * KBE * 2;
+  const int Nt = prm.Nt, S = prm.stages, NB = prm.nb;
+  const uint32_t bbytes = (uint32_t)(NB * Nt) * KBE * 2;
+  const uint32_t bbytes1 = (uint32_t)Nt * KBE * 2;  // one sample's B tile
   const uint32_t stage_bytes = ABYTES + bbytes;
   uint64_t* full = (uint64_t*)(smem + (size_t)S * stage_bytes);
   uint64_t* empty = full + S;
@@ -69,7 +71,7 @@ __global__ void __launch_bounds__(NTH, 1)
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int m0 = blockIdx.x * TM;
-  const int b = blockIdx.y;
+  const int b0 = blockIdx.y * NB;  // first sample of this CTA
   const int nkb_all = (d.K + KBE - 1) / KBE;
   const int kb0 = blockIdx.z * prm.kb_per_split;
   const int kb1 = min(nkb_all, kb0 + prm.kb_per_split);
@@ -104,15 +106,18 @@ __global__ void __launch_bounds__(NTH, 1)
         if (i >= S && !tc::mbar_wait(&empty[st], (u & 1u) ^ 1u, &g_gemm_status)) break;
         uint8_t* sa = smem + (size_t)st * stage_bytes;
         tc::mbar_expect_tx(&full[st], stage_bytes);
-        const int ab = prm.a_bat ? b : 0, bb = prm.b_bat ? b : 0;
+        const int ab = prm.a_bat ? b0 : 0, bb = prm.b_bat ? b0 : 0;
         if (prm.a_perm)
           tc::tma_load_3d(sa, &tmA, &full[st], (kb0 + i) * KBE, ab, m0);
         else
           tc::tma_load_3d(sa, &tmA, &full[st], (kb0 + i) * KBE, m0, ab);
-        if (prm.b_perm)
-          tc::tma_load_3d(sa + ABYTES, &tmB, &full[st], (kb0 + i) * KBE, bb, 0);
-        else
-          tc::tma_load_3d(sa + ABYTES, &tmB, &full[st], (kb0 + i) * KBE, 0, bb);
+        for (int j = 0; j < NB; ++j) {  // sample j's rows follow sample j-1's
+          uint8_t* sbj = sa + ABYTES + (size_t)j * bbytes1;
+          if (prm.b_perm)
+            tc::tma_load_3d(sbj, &tmB, &full[st], (kb0 + i) * KBE, bb + j, 0);
+          else
+            tc::tma_load_3d(sbj, &tmB, &full[st], (kb0 + i) * KBE, 0, bb + j);
+        }
         issued = i + 1;
       }
       for (int i = (issued > S ? issued - S : 0); i < issued; ++i)
@@ -120,7 +125,7 @@ __global__ void __launch_bounds__(NTH, 1)
     }
   } else if (warp == 1) {
     if (lane == 0 && nkb > 0) {
-      const uint32_t idesc = tc::idesc_bf16(TM, Nt);
+      const uint32_t idesc = tc::idesc_bf16(TM, NB * Nt);
       bool ok = true;
       for (int i = 0; i < nkb; ++i) {
         const int st = i % S;
@@ -149,10 +154,13 @@ __global__ void __launch_bounds__(NTH, 1)
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       const bool mok = m < d.M;
       const bool split = prm.kb_per_split < nkb_all || d.d32_accumulate;
-      for (int c = 0; c < Nt / 16; ++c) {
+      for (int cc = 0; cc < NB * Nt / 16; ++cc) {
         float v[16];
-        tc::tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(c * 16), v);
+        tc::tmem_ld16(tmem + ((uint32_t)(32 * q) << 16) + (uint32_t)(cc * 16), v);
         if (!mok) continue;
+        // TMEM columns [j Nt, (j+1) Nt) belong to sample b0 + j (Nt % 16 == 0)
+        const int b = b0 + (cc * 16) / Nt;
+        const int c = ((cc * 16) % Nt) / 16;
         if (!split && c * 16 + 16 <= d.N && prm.vec_ok) {
           // whole 16-column group of this thread's row: 16-byte vector accesses
           const int n0 = c * 16;
@@ -307,12 +315,25 @@ extern "C" int jfg_gemm_bf16(const jfg_gemm_desc* dp, const void* A, const void*
   GemmParams prm;
   prm.d = d;
   prm.Nt = (d.N + 15) / 16 * 16;
-  int cols = 32;
-  while (cols < prm.Nt) cols <<= 1;
-  prm.tmem_cols = cols;
-  const size_t stage = ABYTES + (size_t)prm.Nt * KBE * 2;
   const int nkb = (d.K + KBE - 1) / KBE;
   prm.kb_per_split = (nkb + d.ksplit - 1) / d.ksplit;
+  prm.a_bat = (d.batch > 1 && d.a_batch != 0) ? 1 : 0;
+  prm.b_bat = (d.batch > 1 && d.b_batch != 0) ? 1 : 0;
+  // A shared by every sample and narrow per-sample B (the spectral transforms:
+  // N = 64 channels): up to 256 / N samples per CTA in one N <= 256 MMA, so
+  // the shared A tile is staged once for all of them
+  prm.nb = 1;
+  if (prm.b_bat && !prm.a_bat && d.ksplit == 1 && d.N % 16 == 0)
+    for (int nb = 256 / d.N; nb > 1; --nb)
+      if (d.batch % nb == 0) {
+        prm.nb = nb;
+        break;
+      }
+  const int ntot = prm.nb * prm.Nt;
+  int cols = 32;
+  while (cols < ntot) cols <<= 1;
+  prm.tmem_cols = cols;
+  const size_t stage = ABYTES + (size_t)ntot * KBE * 2;
   // pipeline depth: no deeper than the K blocks a CTA has (the channel-mixing
   // GEMMs have one, so several CTAs share an SM and their epilogues overlap);
   // long-K GEMMs keep >= 3 stages but leave room for a second CTA per SM
@@ -323,8 +344,6 @@ extern "C" int jfg_gemm_bf16(const jfg_gemm_desc* dp, const void* A, const void*
   if (stages > prm.kb_per_split) stages = prm.kb_per_split;
   if (stages < 1) stages = 1;
   prm.stages = stages;
-  prm.a_bat = (d.batch > 1 && d.a_batch != 0) ? 1 : 0;
-  prm.b_bat = (d.batch > 1 && d.b_batch != 0) ? 1 : 0;
   const int ksplit = (nkb + prm.kb_per_split - 1) / prm.kb_per_split;
   {
     auto f4 = [](const void* p, long long ld, long long bs) {
@@ -356,7 +375,7 @@ extern "C" int jfg_gemm_bf16(const jfg_gemm_desc* dp, const void* A, const void*
                                       227 * 1024));
     attr_done[dev] = true;
   }
-  dim3 grid((d.M + TM - 1) / TM, d.batch, ksplit);
+  dim3 grid((d.M + TM - 1) / TM, d.batch / prm.nb, ksplit);
   k_gemm_bf16<<<grid, NTH, smem, (cudaStream_t)stream>>>(ma, mb, prm);
   JFG_LAUNCHED();
   return JFG_OK;
