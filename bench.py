@@ -378,6 +378,130 @@ def run_transforms(args):
     return 0
 
 
+def run_poisson2d(args):
+    """Secondary measurement (config 0): 2-D Poisson, Legendre Dirichlet, N = 64.
+    One step = scalar product of f, fast-diagonalisation solve, backward to
+    the grid and forward back (the reference's solve + round trip), 8 FP64
+    contraction passes.  Launch/latency bound: reported as the latency of one
+    problem (direct C-ABI calls, and the same step replayed as a CUDA graph)
+    and as solves/s with 1024 problems per step (graph replay).  f: seeded
+    coefficients z (1+j)^-2 (1+k)^-2 on 64 x 64 orthogonal Legendre modes,
+    backward to the Gauss grid."""
+    import numpy as np
+    import torch
+
+    from jaxfun_gb300 import _lib
+    from jaxfun_gb300.galerkin import DIRICHLET, FunctionSpace, Legendre, TensorProduct
+    from jaxfun_gb300.la import poisson_tpmatrices
+
+    torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
+    L = _lib.lib()
+    N = 64
+    n = N - 2
+    D = FunctionSpace(N, Legendre, bcs=DIRICHLET)
+    T = TensorProduct(D, D)
+    To = TensorProduct(Legendre(N), Legendre(N))
+    E, W, lam = poisson_tpmatrices(T).lu_factor().device_factors()
+    SP = torch.as_tensor(np.ascontiguousarray(D.scalar_product_matrix()), device="cuda")
+    BW = torch.as_tensor(np.ascontiguousarray(D.backward_matrix()), device="cuda")
+    FW = torch.as_tensor(np.ascontiguousarray(D.forward_matrix(N)), device="cuda")
+    i = np.arange(N, dtype=np.float64)
+    decay = 1.0 / np.outer((1.0 + i) ** 2, (1.0 + i) ** 2)
+    ia = _lib.int_array
+
+    def make(batch, stream):
+        with torch.cuda.stream(stream):
+            fh = np.stack([np.random.default_rng(k).standard_normal((N, N)) * decay
+                           for k in range(batch)])
+            f = To.backward(fh)
+            buf = {"f": f, "b": torch.empty(batch, n, n, dtype=torch.float64, device="cuda"),
+                   "u": torch.empty(batch, n, n, dtype=torch.float64, device="cuda"),
+                   "uj": torch.empty(batch, N, N, dtype=torch.float64, device="cuda"),
+                   "c": torch.empty(batch, n, n, dtype=torch.float64, device="cuda"),
+                   "c0": torch.zeros(batch, dtype=torch.float64, device="cuda"),
+                   "c1": torch.ones(batch, dtype=torch.float64, device="cuda")}
+            wtp = L.jfg_tp_apply_workspace_size(2, ia([N, N]), ia([N, N]), batch, 8)
+            buf["wtp"] = torch.empty(wtp, dtype=torch.uint8, device="cuda")
+            buf["wfd"] = torch.empty(L.jfg_fd_solve_workspace_size(2, n, batch, 8),
+                                     dtype=torch.uint8, device="cuda")
+        sh = stream.cuda_stream
+        p2 = lambda t: _lib.ptr_array([t.data_ptr()] * 2)  # noqa: E731
+        args_sp = (2, ia([n, n]), ia([N, N]), batch, p2(SP))
+        args_bw = (2, ia([N, N]), ia([n, n]), batch, p2(BW))
+        args_fw = (2, ia([n, n]), ia([N, N]), batch, p2(FW))
+        wp, wn = buf["wtp"].data_ptr(), buf["wtp"].numel()
+
+        def step():
+            _lib.check(L.jfg_tp_apply_f64(*args_sp, buf["f"].data_ptr(), buf["b"].data_ptr(),
+                                          wp, wn, sh), "scalar_product")
+            _lib.check(L.jfg_fd_solve_f64(2, n, batch, E.data_ptr(), W.data_ptr(),
+                                          lam.data_ptr(), buf["c0"].data_ptr(),
+                                          buf["c1"].data_ptr(), buf["b"].data_ptr(),
+                                          buf["u"].data_ptr(), buf["wfd"].data_ptr(),
+                                          buf["wfd"].numel(), sh), "fd_solve")
+            _lib.check(L.jfg_tp_apply_f64(*args_bw, buf["u"].data_ptr(), buf["uj"].data_ptr(),
+                                          wp, wn, sh), "backward")
+            _lib.check(L.jfg_tp_apply_f64(*args_fw, buf["uj"].data_ptr(), buf["c"].data_ptr(),
+                                          wp, wn, sh), "forward")
+        return step, buf
+
+    def timed(fn, stream, reps):
+        for _ in range(max(3, args.warmup)):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        t0 = time.perf_counter()
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        e1.synchronize()
+        return e0.elapsed_time(e1) / 1e3 / reps, (time.perf_counter() - t0) / reps
+
+    out = {"workload": "poisson-2d-legendre-dirichlet-N64", "unit": "us / solves/s"}
+    stream = torch.cuda.Stream()
+    for batch, key in ((1, "single"), (args.nprob, "batched")):
+        step, buf = make(batch, stream)
+        with torch.cuda.stream(stream):
+            dev_direct, host_direct = timed(step, stream, 200 if batch == 1 else 20)
+            torch.cuda.synchronize()
+            L.jfg_reset_launch_count()
+            step()
+            launches = int(L.jfg_launch_count())
+            g = torch.cuda.CUDAGraph()
+            with torch.cuda.graph(g, stream=stream):
+                step()
+            dev_graph, _ = timed(g.replay, stream, 200 if batch == 1 else 20)
+        rec = {"batch": batch, "launches_per_step": launches,
+               "us_per_step_direct_calls": 1e6 * host_direct,
+               "us_per_step_graph": 1e6 * dev_graph,
+               "solves_per_s_graph": batch / dev_graph,
+               "roundtrip_max_rel": float((buf["c"] - buf["u"]).abs().max()
+                                          / buf["u"].abs().max())}
+        out[key] = rec
+        if batch == 1:
+            f1, u1 = buf["f"][0].cpu().numpy(), buf["u"][0].cpu().numpy()
+    # the oracle port of the same step on the host (CPU baseline and checker)
+    from oracle import spectral as O
+
+    Vo = O.Space1D("legendre", N, True)
+    K, M = Vo.stiffness_matrix(), Vo.mass_matrix()
+    lamo, Wo = O.fd_factor_symmetric(K, M)
+    reps = 20
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        bo = O.tp_scalar_product([Vo, Vo], f1)
+        uo = O.fd_solve(bo, [Wo, Wo], [Wo.T, Wo.T], [lamo, lamo])
+        ujo = O.tp_backward([Vo, Vo], uo)
+        O.tp_forward([Vo, Vo], ujo)
+    tcpu = (time.perf_counter() - t0) / reps
+    out["max_rel_err_vs_oracle"] = float(np.abs(u1 - uo).max() / np.abs(uo).max())
+    out["cpu_baseline"] = {"us_per_step": 1e6 * tcpu, "kind": "port",
+                           "cores": os.cpu_count(), "sample": f"{reps} single-problem steps"}
+    print(json.dumps(out), flush=True)
+    return 0
+
+
 def run_helmholtz(args):
     """Secondary measurement (not the headline): 1024 Chebyshev Dirichlet Helmholtz
     problems, N ~ U{32,48,...,512}, alpha ~ U[0,50], forcing coefficients
@@ -933,8 +1057,10 @@ def main():
                          "pass in double-FP32 arithmetic; transform(_tf32) = one split-BF16 "
                          "(split-TF32) pass of the 3-D 256^3 Chebyshev transform, B fields")
     ap.add_argument("--config", default="varcoef2d",
-                    choices=["varcoef2d", "transforms", "helmholtz", "varcoef3d", "tour"],
-                    help="varcoef2d: the headline; transforms: batched 3-D Chebyshev "
+                    choices=["varcoef2d", "poisson2d", "transforms", "helmholtz", "varcoef3d",
+                             "tour"],
+                    help="varcoef2d: the headline; poisson2d: N = 64 Poisson solve + round "
+                         "trip, latency and batched; transforms: batched 3-D Chebyshev "
                          "round trip; helmholtz: uneven Helmholtz batch; varcoef3d: 3-D "
                          "variable coefficient (secondary reports); tour: every kernel once "
                          "(for profiling)")
@@ -949,6 +1075,8 @@ def main():
     args = ap.parse_args()
     if args.impl == "reference":
         return run_reference(args)
+    if args.config == "poisson2d":
+        return run_poisson2d(args)
     if args.config == "transforms":
         return run_transforms(args)
     if args.config == "helmholtz":

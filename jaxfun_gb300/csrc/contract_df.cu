@@ -45,10 +45,23 @@ __device__ __forceinline__ void df_mac(float ah, float al, float bh, float bl, f
   sh = t;
 }
 
+__global__ void k_split_pairs(const double* __restrict__ src, float2* __restrict__ dst,
+                              long long n) {
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  for (long long i = (long long)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += stride) {
+    float h, l;
+    split2(src[i], h, l);
+    dst[i] = make_float2(h, l);
+  }
+}
+
+// op_pairs (optional): the operator pre-split into (hi, lo) pairs, so the
+// operator tile, which every p tile reloads, costs no FP64 work per load
 template <int EPI>
 __global__ void __launch_bounds__(NT)
     k_contract_df(const jfg_contract_desc d, const double* __restrict__ op,
-                  const double* __restrict__ in, double* __restrict__ out) {
+                  const float2* __restrict__ op_pairs, const double* __restrict__ in,
+                  double* __restrict__ out) {
   __shared__ __align__(16) float Ah[TK][TM + 4], Al[TK][TM + 4];
   __shared__ __align__(16) float Bh[TK][TP + 4], Bl[TK][TP + 4];
 
@@ -81,7 +94,15 @@ __global__ void __launch_bounds__(NT)
       const int kk = idx % TK;
       const int m = m0 + r, k = k0 + kk;
       float h, l;
-      split2((m < d.M && k < d.K) ? opS[(long long)m * d.op_ld + k] : 0.0, h, l);
+      if (op_pairs) {
+        const float2 t = (m < d.M && k < d.K)
+                             ? op_pairs[(long long)s * d.op_seg + (long long)m * d.op_ld + k]
+                             : make_float2(0.f, 0.f);
+        h = t.x;
+        l = t.y;
+      } else {
+        split2((m < d.M && k < d.K) ? opS[(long long)m * d.op_ld + k] : 0.0, h, l);
+      }
       Ah[kk][r] = h;
       Al[kk][r] = l;
       const int p = p0 + r;
@@ -149,8 +170,18 @@ __global__ void __launch_bounds__(NT)
 
 }  // namespace
 
-int contract_df64(const jfg_contract_desc& d, const double* op, const double* in, double* out,
-                  cudaStream_t st) {
+int split_pairs_f64(const double* src, float2* dst, long long n, cudaStream_t st) {
+  if (n < 0 || (n > 0 && (!src || !dst))) return JFG_ERR_ARG;
+  if (n == 0) return JFG_OK;
+  long long blocks = (n + 255) / 256;
+  if (blocks > 4 * 152) blocks = 4 * 152;
+  k_split_pairs<<<(int)blocks, 256, 0, st>>>(src, dst, n);
+  JFG_LAUNCHED();
+  return JFG_OK;
+}
+
+int contract_df64(const jfg_contract_desc& d, const double* op, const float2* op_pairs,
+                  const double* in, double* out, cudaStream_t st) {
   JFG_TRY(validate_desc(d));
   if (!op || !in || !out) return JFG_ERR_ARG;
   if (d.batch == 0 || d.M == 0 || d.P == 0) return JFG_OK;
@@ -160,13 +191,13 @@ int contract_df64(const jfg_contract_desc& d, const double* op, const double* in
   if (grid.y > 65535) return JFG_ERR_ARG;
   switch (d.epilogue) {
     case JFG_EPI_NONE:
-      k_contract_df<JFG_EPI_NONE><<<grid, NT, 0, st>>>(d, op, in, out);
+      k_contract_df<JFG_EPI_NONE><<<grid, NT, 0, st>>>(d, op, op_pairs, in, out);
       break;
     case JFG_EPI_MUL_FIELD:
-      k_contract_df<JFG_EPI_MUL_FIELD><<<grid, NT, 0, st>>>(d, op, in, out);
+      k_contract_df<JFG_EPI_MUL_FIELD><<<grid, NT, 0, st>>>(d, op, op_pairs, in, out);
       break;
     case JFG_EPI_DIV_EIG:
-      k_contract_df<JFG_EPI_DIV_EIG><<<grid, NT, 0, st>>>(d, op, in, out);
+      k_contract_df<JFG_EPI_DIV_EIG><<<grid, NT, 0, st>>>(d, op, op_pairs, in, out);
       break;
     default:
       return JFG_ERR_ARG;
@@ -180,5 +211,5 @@ int contract_df64(const jfg_contract_desc& d, const double* op, const double* in
 extern "C" int jfg_contract_df64(const jfg_contract_desc* d, const double* op, const double* in,
                                  double* out, void* stream) {
   if (!d) return JFG_ERR_ARG;
-  return jfg::contract_df64(*d, op, in, out, (cudaStream_t)stream);
+  return jfg::contract_df64(*d, op, nullptr, in, out, (cudaStream_t)stream);
 }

@@ -14,15 +14,18 @@ namespace jfg {
 
 namespace {
 
-constexpr int TM = 64;   // rows of the operator per CTA
-constexpr int TP = 64;   // columns (p) per CTA
 constexpr int TK = 16;   // contraction step
-constexpr int NT = 256;  // threads: 16 x 16, each 4 x 4 outputs
+constexpr int NT = 256;  // threads: 16 x 16, each R x R outputs
 
-template <typename T, int EPI>
+// Tile (16 R) x (16 R): R = 4 (64 x 64) for large launches; small launches
+// take R = 2 or 1 so that they still spread over the SMs (on GB300 one SM
+// issues only about 2 DFMA per clock, so a lone 64 x 64 FP64 tile is slow).
+template <typename T, int EPI, int R>
 __global__ void __launch_bounds__(NT)
     k_contract_simt(const jfg_contract_desc d, const T* __restrict__ op,
                     const T* __restrict__ in, T* __restrict__ out) {
+  constexpr int TM = 16 * R;  // rows of the operator per CTA
+  constexpr int TP = 16 * R;  // columns (p) per CTA
   __shared__ T As[TK][TM + 4];
   __shared__ T Bs[TK][TP + 4];
 
@@ -41,11 +44,11 @@ __global__ void __launch_bounds__(NT)
   const int tx = tid & 15;
   const int ty = tid >> 4;
 
-  T acc[4][4];
+  T acc[R][R];
 #pragma unroll
-  for (int i = 0; i < 4; ++i)
+  for (int i = 0; i < R; ++i)
 #pragma unroll
-    for (int j = 0; j < 4; ++j) acc[i][j] = T(0);
+    for (int j = 0; j < R; ++j) acc[i][j] = T(0);
 
   for (int k0 = 0; k0 < d.K; k0 += TK) {
 #pragma unroll
@@ -61,15 +64,15 @@ __global__ void __launch_bounds__(NT)
     __syncthreads();
 #pragma unroll
     for (int kk = 0; kk < TK; ++kk) {
-      T a[4], bb[4];
+      T a[R], bb[R];
 #pragma unroll
-      for (int i = 0; i < 4; ++i) a[i] = As[kk][ty * 4 + i];
+      for (int i = 0; i < R; ++i) a[i] = As[kk][ty * R + i];
 #pragma unroll
-      for (int j = 0; j < 4; ++j) bb[j] = Bs[kk][tx * 4 + j];
+      for (int j = 0; j < R; ++j) bb[j] = Bs[kk][tx * R + j];
 #pragma unroll
-      for (int i = 0; i < 4; ++i)
+      for (int i = 0; i < R; ++i)
 #pragma unroll
-        for (int j = 0; j < 4; ++j) acc[i][j] = fma(a[i], bb[j], acc[i][j]);
+        for (int j = 0; j < R; ++j) acc[i][j] = fma(a[i], bb[j], acc[i][j]);
     }
     __syncthreads();
   }
@@ -78,8 +81,8 @@ __global__ void __launch_bounds__(NT)
   const T alpha = T(d.alpha);
   const T beta = T(d.beta);
 #pragma unroll
-  for (int i = 0; i < 4; ++i) {
-    const int m = m0 + ty * 4 + i;
+  for (int i = 0; i < R; ++i) {
+    const int m = m0 + ty * R + i;
     if (m >= d.M) continue;
     T denom_m = T(0), c0 = T(0), c1 = T(1);
     if (EPI == JFG_EPI_DIV_EIG) {
@@ -88,8 +91,8 @@ __global__ void __launch_bounds__(NT)
       c1 = d.c1 ? ((const T*)d.c1)[b] : T(1);
     }
 #pragma unroll
-    for (int j = 0; j < 4; ++j) {
-      const int p = p0 + tx * 4 + j;
+    for (int j = 0; j < R; ++j) {
+      const int p = p0 + tx * R + j;
       if (p >= d.P) continue;
       T v = acc[i][j];
       if (EPI == JFG_EPI_MUL_FIELD) {
@@ -115,21 +118,42 @@ int launch_simt(const jfg_contract_desc& d, const T* op, const T* in, T* out,
   if (d.batch == 0 || d.M == 0 || d.P == 0) return JFG_OK;
   const long long gz = (long long)d.batch * d.nseg;
   if (gz > 65535) return JFG_ERR_ARG;
-  dim3 grid((d.P + TP - 1) / TP, (d.M + TM - 1) / TM, (unsigned)gz);
+  if (d.epilogue != JFG_EPI_NONE && d.epilogue != JFG_EPI_MUL_FIELD &&
+      d.epilogue != JFG_EPI_DIV_EIG)
+    return JFG_ERR_ARG;
+  // largest tile that still gives two CTAs per SM (the list-restricted
+  // launches count their full batch: the active count is not known here)
+  static int nsm[64] = {};
+  int dev = 0;
+  JFG_CUDA_TRY(cudaGetDevice(&dev));
+  if (dev < 0 || dev >= 64) return JFG_ERR_UNSUPPORTED;
+  if (!nsm[dev]) JFG_CUDA_TRY(cudaDeviceGetAttribute(&nsm[dev], cudaDevAttrMultiProcessorCount, dev));
+  auto ctas = [&](int t) {
+    return (long long)((d.P + t - 1) / t) * ((d.M + t - 1) / t) * gz;
+  };
+  const int R = ctas(64) >= 2 * nsm[dev] ? 4 : ctas(32) >= 2 * nsm[dev] ? 2 : 1;
+  const int tile = 16 * R;
+  dim3 grid((d.P + tile - 1) / tile, (d.M + tile - 1) / tile, (unsigned)gz);
   if (grid.y > 65535) return JFG_ERR_ARG;
+#define JFG_SIMT_LAUNCH(E)                                                         \
+  if (R == 4)                                                                     \
+    k_contract_simt<T, E, 4><<<grid, NT, 0, st>>>(d, op, in, out);                \
+  else if (R == 2)                                                                \
+    k_contract_simt<T, E, 2><<<grid, NT, 0, st>>>(d, op, in, out);                \
+  else                                                                            \
+    k_contract_simt<T, E, 1><<<grid, NT, 0, st>>>(d, op, in, out)
   switch (d.epilogue) {
     case JFG_EPI_NONE:
-      k_contract_simt<T, JFG_EPI_NONE><<<grid, NT, 0, st>>>(d, op, in, out);
+      JFG_SIMT_LAUNCH(JFG_EPI_NONE);
       break;
     case JFG_EPI_MUL_FIELD:
-      k_contract_simt<T, JFG_EPI_MUL_FIELD><<<grid, NT, 0, st>>>(d, op, in, out);
-      break;
-    case JFG_EPI_DIV_EIG:
-      k_contract_simt<T, JFG_EPI_DIV_EIG><<<grid, NT, 0, st>>>(d, op, in, out);
+      JFG_SIMT_LAUNCH(JFG_EPI_MUL_FIELD);
       break;
     default:
-      return JFG_ERR_ARG;
+      JFG_SIMT_LAUNCH(JFG_EPI_DIV_EIG);
+      break;
   }
+#undef JFG_SIMT_LAUNCH
   JFG_CHECK_LAUNCH();
   count_launches(1);
   return JFG_OK;

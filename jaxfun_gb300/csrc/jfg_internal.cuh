@@ -67,8 +67,11 @@ int contract_f64(const jfg_contract_desc& d, const double* op, const double* in,
                  cudaStream_t st);
 int contract_f32(const jfg_contract_desc& d, const float* op, const float* in, float* out,
                  cudaStream_t st);
-int contract_df64(const jfg_contract_desc& d, const double* op, const double* in, double* out,
+int contract_df64(const jfg_contract_desc& d, const double* op, const float2* op_pairs,
+                  const double* in, double* out,
                   cudaStream_t st);
+// dst[i] = (hi, lo) FP32 split of src[i] (the DF engine's pre-split operator)
+int split_pairs_f64(const double* src, float2* dst, long long n, cudaStream_t st);
 int contract_tc(const jfg_contract_desc& d, const float* op_hi, const float* op_lo,
                 const float* in, float* out, cudaStream_t st);
 // the same contraction with the operator as BF16 (hi, lo): three BF16 MMAs per product
@@ -85,7 +88,9 @@ int tc_setup();
 
 inline int contract(Engine e, const jfg_contract_desc& d, OpRef<double> op, const double* in,
                     double* out, cudaStream_t st) {
-  if (e == Engine::DF) return contract_df64(d, op.hi, in, out, st);
+  // DF: op.lo, when set, holds the operator pre-split into interleaved FP32
+  // (hi, lo) pairs with the FP64 operator's element indexing (split_pairs_f64)
+  if (e == Engine::DF) return contract_df64(d, op.hi, (const float2*)op.lo, in, out, st);
   return contract_f64(d, op.hi, in, out, st);
 }
 inline int contract(Engine e, const jfg_contract_desc& d, OpRef<float> op, const float* in,

@@ -96,7 +96,7 @@ inline int blocks_for(long long n, int cap) {
 
 struct MixedLayout {
   long long Nun, Npad;
-  size_t vec64, part, sc, vec32, ws64, wsin, total;
+  size_t vec64, part, sc, vec32, ws64, wsin, opdf, total;
 };
 
 MixedLayout layout(int ndim, int n, int nq, int batch) {
@@ -110,7 +110,10 @@ MixedLayout layout(int ndim, int n, int nq, int batch) {
   L.vec32 = align_up((size_t)L.Npad * batch * 4, 256);
   L.ws64 = align_up(varcoef_ws(ndim, n, nq, batch, 8), 256);
   L.wsin = pcg_ws<float>(ndim, nq, nq, batch);
-  L.total = L.vec64 + L.part + 2 * L.sc + 2 * L.vec32 + L.ws64 + L.wsin;
+  // the FP64 operator split once per solve into (hi, lo) pairs for the
+  // double-FP32 residual passes
+  L.opdf = align_up((size_t)8 * n * nq * sizeof(float2), 256);
+  L.total = L.vec64 + L.part + 2 * L.sc + 2 * L.vec32 + L.ws64 + L.wsin + L.opdf;
   return L;
 }
 
@@ -215,6 +218,9 @@ extern "C" int jfg_pcg_varcoef_mixed_guess(const jfg_mixed_plan* plan, const dou
   void* ws64 = w;
   w += Lo.ws64;
   void* wsin = w;
+  w += Lo.wsin;
+  float2* opdf = (float2*)w;
+  if (P.residual == 1) JFG_TRY(split_pairs_f64(P.ops64, opdf, 8LL * n * nq, st));
 
   PcgProblem<float> pb;
   pb.engine = Engine::TC;
@@ -255,10 +261,10 @@ extern "C" int jfg_pcg_varcoef_mixed_guess(const jfg_mixed_plan* plan, const dou
     return JFG_OK;
   };
   auto residual = [&]() -> int {
-    JFG_TRY(varcoef_apply<double>(P.residual == 1 ? Engine::DF : Engine::F64, ndim, n, nq,
-                                  batch,
-                                  OpRef<double>{P.ops64, nullptr}, P.kw64, x, r64, ws64,
-                                  Lo.ws64, st));
+    JFG_TRY(varcoef_apply<double>(
+        P.residual == 1 ? Engine::DF : Engine::F64, ndim, n, nq, batch,
+        OpRef<double>{P.ops64, P.residual == 1 ? (const double*)opdf : nullptr}, P.kw64, x, r64,
+        ws64, Lo.ws64, st));
     k_sub_from64<<<blocks_for(tot64, 4096), 256, 0, st>>>(rhs, r64, tot64);
     JFG_LAUNCHED();
     return JFG_OK;
