@@ -57,11 +57,14 @@ __global__ void k_split_pairs(const double* __restrict__ src, float2* __restrict
 
 // op_pairs (optional): the operator pre-split into (hi, lo) pairs, so the
 // operator tile, which every p tile reloads, costs no FP64 work per load
+// in_pairs / out_pairs: the input / output arrays hold (hi, lo) FP32 pairs
+// (8 bytes, the same element indexing as FP64): a chain of passes keeps its
+// intermediates split, so no tile load needs FP64 work
 template <int EPI>
 __global__ void __launch_bounds__(NT)
     k_contract_df(const jfg_contract_desc d, const double* __restrict__ op,
                   const float2* __restrict__ op_pairs, const double* __restrict__ in,
-                  double* __restrict__ out) {
+                  double* __restrict__ out, bool in_pairs, bool out_pairs) {
   __shared__ __align__(16) float Ah[TK][TM + 4], Al[TK][TM + 4];
   __shared__ __align__(16) float Bh[TK][TP + 4], Bl[TK][TP + 4];
 
@@ -106,7 +109,15 @@ __global__ void __launch_bounds__(NT)
       Ah[kk][r] = h;
       Al[kk][r] = l;
       const int p = p0 + r;
-      split2((p < d.P && k < d.K) ? inS[(long long)p * d.in_ld + k] : 0.0, h, l);
+      if (in_pairs) {
+        const float2 t = (p < d.P && k < d.K)
+                             ? ((const float2*)inS)[(long long)p * d.in_ld + k]
+                             : make_float2(0.f, 0.f);
+        h = t.x;
+        l = t.y;
+      } else {
+        split2((p < d.P && k < d.K) ? inS[(long long)p * d.in_ld + k] : 0.0, h, l);
+      }
       Bh[kk][r] = h;
       Bl[kk][r] = l;
     }
@@ -162,8 +173,19 @@ __global__ void __launch_bounds__(NT)
       }
       double* o = outS + (long long)m * d.out_ld + p;
       v = alpha * v;
-      if (beta != 0.0) v += beta * *o;
-      *o = v;
+      if (out_pairs) {
+        float2* o2 = (float2*)o;
+        if (beta != 0.0) {
+          const float2 t = *o2;
+          v += beta * ((double)t.x + (double)t.y);
+        }
+        float h, l;
+        split2(v, h, l);
+        *o2 = make_float2(h, l);
+      } else {
+        if (beta != 0.0) v += beta * *o;
+        *o = v;
+      }
     }
   }
 }
@@ -181,7 +203,8 @@ int split_pairs_f64(const double* src, float2* dst, long long n, cudaStream_t st
 }
 
 int contract_df64(const jfg_contract_desc& d, const double* op, const float2* op_pairs,
-                  const double* in, double* out, cudaStream_t st) {
+                  const double* in, double* out, cudaStream_t st, bool in_pairs,
+                  bool out_pairs) {
   JFG_TRY(validate_desc(d));
   if (!op || !in || !out) return JFG_ERR_ARG;
   if (d.batch == 0 || d.M == 0 || d.P == 0) return JFG_OK;
@@ -191,13 +214,16 @@ int contract_df64(const jfg_contract_desc& d, const double* op, const float2* op
   if (grid.y > 65535) return JFG_ERR_ARG;
   switch (d.epilogue) {
     case JFG_EPI_NONE:
-      k_contract_df<JFG_EPI_NONE><<<grid, NT, 0, st>>>(d, op, op_pairs, in, out);
+      k_contract_df<JFG_EPI_NONE><<<grid, NT, 0, st>>>(d, op, op_pairs, in, out, in_pairs,
+                                                        out_pairs);
       break;
     case JFG_EPI_MUL_FIELD:
-      k_contract_df<JFG_EPI_MUL_FIELD><<<grid, NT, 0, st>>>(d, op, op_pairs, in, out);
+      k_contract_df<JFG_EPI_MUL_FIELD><<<grid, NT, 0, st>>>(d, op, op_pairs, in, out,
+                                                             in_pairs, out_pairs);
       break;
     case JFG_EPI_DIV_EIG:
-      k_contract_df<JFG_EPI_DIV_EIG><<<grid, NT, 0, st>>>(d, op, op_pairs, in, out);
+      k_contract_df<JFG_EPI_DIV_EIG><<<grid, NT, 0, st>>>(d, op, op_pairs, in, out, in_pairs,
+                                                           out_pairs);
       break;
     default:
       return JFG_ERR_ARG;

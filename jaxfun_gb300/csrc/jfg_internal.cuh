@@ -68,8 +68,8 @@ int contract_f64(const jfg_contract_desc& d, const double* op, const double* in,
 int contract_f32(const jfg_contract_desc& d, const float* op, const float* in, float* out,
                  cudaStream_t st);
 int contract_df64(const jfg_contract_desc& d, const double* op, const float2* op_pairs,
-                  const double* in, double* out,
-                  cudaStream_t st);
+                  const double* in, double* out, cudaStream_t st, bool in_pairs = false,
+                  bool out_pairs = false);
 // dst[i] = (hi, lo) FP32 split of src[i] (the DF engine's pre-split operator)
 int split_pairs_f64(const double* src, float2* dst, long long n, cudaStream_t st);
 int contract_tc(const jfg_contract_desc& d, const float* op_hi, const float* op_lo,

@@ -7,6 +7,8 @@
 // FIRST ("rotate"), so a d-dimensional field returns to its original axis
 // order after d passes and every pass is the same strided GEMM shape with the
 // contracted index contiguous in memory.
+#include <type_traits>
+
 #include "jfg_internal.cuh"
 
 namespace jfg {
@@ -181,9 +183,25 @@ int varcoef_apply(Engine e, int ndim, int n, int nq, int batch, OpRef<T> ops, co
   T* bufB = (T*)((char*)work + align_up(a_elems * batch * sizeof(T), 256));
 
   if (ndim == 2) {
+    // Double-FP32 with a pre-split operator: u is split once into (hi, lo)
+    // pairs (in bufB, free until pass 2) and the intermediates stay split
+    // between the passes, so no tile load does FP64 work.
+    const bool dfp = std::is_same<T, double>::value && e == Engine::DF && ops.lo != nullptr;
+    auto pass = [&](const jfg_contract_desc& d, OpRef<T> op, const T* in, T* out, bool pin,
+                    bool pout) -> int {
+      if (dfp)
+        return contract_df64(d, (const double*)op.hi, (const float2*)op.lo, (const double*)in,
+                             (double*)out, st, pin, pout);
+      return contract(e, d, op, in, out, st);
+    };
+    const T* u1 = u;
+    if (dfp) {
+      JFG_TRY(split_pairs_f64((const double*)u, (float2*)bufB, (long long)batch * n * n, st));
+      u1 = bufB;
+    }
     // 1: T[b][r][j] = sum_l [B;D][r][l] U[b][j][l]            (M=2nq, P=n, K=n)
     jfg_contract_desc d1 = make_desc(batch, 2 * nq, n, n, act);
-    JFG_TRY(contract(e, d1, ops, u, bufA, st));
+    JFG_TRY(pass(d1, ops, u1, bufA, dfp, dfp));
     // 2: G[b][s][p][q] = kw[b][p][q] * sum_j {D,B}[p][j] T[b][s][q][j]
     jfg_contract_desc d2 = make_desc(batch, nq, nq, n, act);
     d2.nseg = 2;
@@ -197,7 +215,7 @@ int varcoef_apply(Engine e, int ndim, int n, int nq, int batch, OpRef<T> ops, co
     d2.field_ld = nq;
     d2.field_seg = 0;
     d2.field_batch = (long long)nq * nq;
-    JFG_TRY(contract(e, d2, ops.offset(2 * nn), bufA, bufB, st));
+    JFG_TRY(pass(d2, ops.offset(2 * nn), bufA, bufB, dfp, dfp));
     // 3: H[b][k][s][p] = sum_q {B^T,D^T}[k][q] G[b][s][p][q]   (M=n, P=nq, K=nq)
     jfg_contract_desc d3 = make_desc(batch, n, nq, nq, act);
     d3.nseg = 2;
@@ -207,10 +225,10 @@ int varcoef_apply(Engine e, int ndim, int n, int nq, int batch, OpRef<T> ops, co
     d3.out_ld = 2LL * nq;
     d3.out_seg = nq;
     d3.out_batch = 2 * nn;
-    JFG_TRY(contract(e, d3, ops.offset(4 * nn), bufB, bufA, st));
+    JFG_TRY(pass(d3, ops.offset(4 * nn), bufB, bufA, dfp, dfp));
     // 4: V[b][i][k] = sum_{s,p} [D^T|B^T][i][(s,p)] H[b][k][(s,p)]   (M=n, P=n, K=2nq)
     jfg_contract_desc d4 = make_desc(batch, n, n, 2 * nq, act);
-    JFG_TRY(contract(e, d4, ops.offset(6 * nn), bufA, v, st));
+    JFG_TRY(pass(d4, ops.offset(6 * nn), bufA, v, dfp, false));
     return JFG_OK;
   }
 
