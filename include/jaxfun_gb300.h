@@ -100,6 +100,21 @@ void jfg_reset_launch_count(void);
 int jfg_weighted_field_f64(int ndim, int nq, int batch, const double* kappa, const double* w,
                            double* kw, float* kw32, void* stream);
 
+/* The coefficient of a variable-coefficient form evaluated from its
+ * logarithm on the quadrature grid: kappa = exp(scale[b] (g - shift[b])) and
+ * kw = kappa * prod_ax w[i_ax] (kw32: FP32 copy, may be NULL; kappa: may be
+ * NULL), one pass -- evaluate_jaxfunction_expr_quad for exp(g) of a
+ * JAXFunction g (src/jaxfun/galerkin/arguments.py:928-990, the backward
+ * transform of g being jfg_tp_apply_f64) fused with the weighting of
+ * jfg_weighted_field_f64.  scale / shift: per problem, NULL for 1 / 0. */
+int jfg_exp_weighted_field_f64(int ndim, int nq, int batch, const double* g,
+                               const double* scale, const double* shift, const double* w,
+                               double* kappa, double* kw, float* kw32, void* stream);
+/* Per problem: mean of g and 1 / population standard deviation (FP64, two
+ * passes), for standardising g before exp (shift = mean, scale = 1 / std). */
+int jfg_field_moments_f64(int ndim, int nq, int batch, const double* g, double* mean,
+                          double* inv_std, void* stream);
+
 /* ---- generic contraction (FP64 / FP32 CUDA cores) ---------------------- */
 int jfg_contract_f64(const jfg_contract_desc* d, const double* op, const double* in,
                      double* out, void* stream);

@@ -77,6 +77,8 @@ SIGNATURES = {
     "jfg_launch_count": (C.c_longlong, []),
     "jfg_reset_launch_count": (None, []),
     "jfg_weighted_field_f64": (_i, [_i, _i, _i, _vp, _vp, _vp, _vp, _vp]),
+    "jfg_exp_weighted_field_f64": (_i, [_i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
+    "jfg_field_moments_f64": (_i, [_i, _i, _i, _vp, _vp, _vp, _vp]),
     "jfg_contract_f64": (_i, [C.POINTER(ContractDesc), _vp, _vp, _vp, _vp]),
     "jfg_contract_f32": (_i, [C.POINTER(ContractDesc), _vp, _vp, _vp, _vp]),
     "jfg_contract_df64": (_i, [C.POINTER(ContractDesc), _vp, _vp, _vp, _vp]),

@@ -182,23 +182,25 @@ int varcoef_apply(Engine e, int ndim, int n, int nq, int batch, OpRef<T> ops, co
   T* bufA = (T*)work;
   T* bufB = (T*)((char*)work + align_up(a_elems * batch * sizeof(T), 256));
 
+  // Double-FP32 with a pre-split operator: u is split once into (hi, lo)
+  // pairs (in bufB, free until the second pass) and the intermediates stay
+  // split between the passes, so no tile load does FP64 work.
+  const bool dfp = std::is_same<T, double>::value && e == Engine::DF && ops.lo != nullptr;
+  auto pass = [&](const jfg_contract_desc& d, OpRef<T> op, const T* in, T* out, bool pin,
+                  bool pout) -> int {
+    if (dfp)
+      return contract_df64(d, (const double*)op.hi, (const float2*)op.lo, (const double*)in,
+                           (double*)out, st, pin, pout);
+    return contract(e, d, op, in, out, st);
+  };
+  const T* u1 = u;
+  if (dfp) {
+    long long nu = batch;
+    for (int i = 0; i < ndim; ++i) nu *= n;
+    JFG_TRY(split_pairs_f64((const double*)u, (float2*)bufB, nu, st));
+    u1 = bufB;
+  }
   if (ndim == 2) {
-    // Double-FP32 with a pre-split operator: u is split once into (hi, lo)
-    // pairs (in bufB, free until pass 2) and the intermediates stay split
-    // between the passes, so no tile load does FP64 work.
-    const bool dfp = std::is_same<T, double>::value && e == Engine::DF && ops.lo != nullptr;
-    auto pass = [&](const jfg_contract_desc& d, OpRef<T> op, const T* in, T* out, bool pin,
-                    bool pout) -> int {
-      if (dfp)
-        return contract_df64(d, (const double*)op.hi, (const float2*)op.lo, (const double*)in,
-                             (double*)out, st, pin, pout);
-      return contract(e, d, op, in, out, st);
-    };
-    const T* u1 = u;
-    if (dfp) {
-      JFG_TRY(split_pairs_f64((const double*)u, (float2*)bufB, (long long)batch * n * n, st));
-      u1 = bufB;
-    }
     // 1: T[b][r][j] = sum_l [B;D][r][l] U[b][j][l]            (M=2nq, P=n, K=n)
     jfg_contract_desc d1 = make_desc(batch, 2 * nq, n, n, act);
     JFG_TRY(pass(d1, ops, u1, bufA, dfp, dfp));
@@ -239,16 +241,16 @@ int varcoef_apply(Engine e, int ndim, int n, int nq, int batch, OpRef<T> ops, co
   const OpRef<T> Q4 = ops.offset(5 * nn);    // B^T, B^T, D^T
   // 1: T1[b][(s2,q2)][(i0,i1)] = sum_i2 [B;D] U                 (M=2nq, P=n^2, K=n)
   jfg_contract_desc d1 = make_desc(batch, 2 * nq, (int)n2, n, act);
-  JFG_TRY(contract(e, d1, BD, u, bufA, st));
+  JFG_TRY(pass(d1, BD, u1, bufA, dfp, dfp));
   // 2a: s2=0 rows with [B;D]: T2[b][(c,q1)][(q2,i0)], c in {0,1}  (M=2nq, P=nq*n, K=n)
   jfg_contract_desc d2 = make_desc(batch, 2 * nq, (int)nn, n, act);
   d2.in_batch = 2 * nq * n2;
   d2.out_batch = 3 * q2 * n;
-  JFG_TRY(contract(e, d2, BD, bufA, bufB, st));
+  JFG_TRY(pass(d2, BD, bufA, bufB, dfp, dfp));
   // 2b: s2=1 rows with B -> c = 2
   jfg_contract_desc d2b = d2;
   d2b.M = nq;
-  JFG_TRY(contract(e, d2b, BD, bufA + nq * n2, bufB + 2 * q2 * n, st));
+  JFG_TRY(pass(d2b, BD, bufA + nq * n2, bufB + 2 * q2 * n, dfp, dfp));
   // 3: G[b][c][p0][(q1,q2)] = kw * sum_i0 {D,B,B}[p0][i0] T2[b][c][(q1,q2)][i0]
   jfg_contract_desc d3 = make_desc(batch, nq, (int)q2, n, act);
   d3.nseg = 3;
@@ -262,7 +264,7 @@ int varcoef_apply(Engine e, int ndim, int n, int nq, int batch, OpRef<T> ops, co
   d3.field_ld = q2;
   d3.field_seg = 0;
   d3.field_batch = q2 * nq;
-  JFG_TRY(contract(e, d3, Q3, bufB, bufA, st));
+  JFG_TRY(pass(d3, Q3, bufB, bufA, dfp, dfp));
   // 4: H1[b][c][k2][(p0,q1)] = sum_q2 {B^T,B^T,D^T}[k2][q2] G     (M=n, P=nq^2, K=nq)
   jfg_contract_desc d4 = make_desc(batch, n, (int)q2, nq, act);
   d4.nseg = 3;
@@ -271,21 +273,21 @@ int varcoef_apply(Engine e, int ndim, int n, int nq, int batch, OpRef<T> ops, co
   d4.in_batch = 3 * q2 * nq;
   d4.out_seg = q2 * n;
   d4.out_batch = 3 * q2 * n;
-  JFG_TRY(contract(e, d4, Q4, bufA, bufB, st));
+  JFG_TRY(pass(d4, Q4, bufA, bufB, dfp, dfp));
   // 5: H2a = B^T (c=0), H2b = D^T (c=1) + B^T (c=2)      (M=n, P=n*nq, K=nq)
   T* H2a = bufA;
   T* H2b = bufA + (size_t)batch * n2 * nq;
   jfg_contract_desc d5 = make_desc(batch, n, (int)nn, nq, act);
   d5.in_batch = 3 * q2 * n;
-  JFG_TRY(contract(e, d5, Q4, bufB, H2a, st));
-  JFG_TRY(contract(e, d5, Q4.offset(2 * nn), bufB + q2 * n, H2b, st));
+  JFG_TRY(pass(d5, Q4, bufB, H2a, dfp, dfp));
+  JFG_TRY(pass(d5, Q4.offset(2 * nn), bufB + q2 * n, H2b, dfp, dfp));
   d5.beta = 1.0;
-  JFG_TRY(contract(e, d5, Q4, bufB + 2 * q2 * n, H2b, st));
+  JFG_TRY(pass(d5, Q4, bufB + 2 * q2 * n, H2b, dfp, dfp));
   // 6: V = D^T (x) on H2a + B^T (x) on H2b                 (M=n, P=n^2, K=nq)
   jfg_contract_desc d6 = make_desc(batch, n, (int)n2, nq, act);
-  JFG_TRY(contract(e, d6, Q4.offset(2 * nn), H2a, v, st));
+  JFG_TRY(pass(d6, Q4.offset(2 * nn), H2a, v, dfp, false));
   d6.beta = 1.0;
-  JFG_TRY(contract(e, d6, Q4, H2b, v, st));
+  JFG_TRY(pass(d6, Q4, H2b, v, dfp, false));
   return JFG_OK;
 }
 
@@ -302,6 +304,66 @@ __global__ void k_weighted_field(int ndim, int nq, long long total, const T* __r
       r /= nq;
     }
     const T v = kappa[i] * s;
+    kw[i] = v;
+    if (kw32) kw32[i] = (float)v;
+  }
+}
+
+// Per problem b (one block each): mean of g[b] and 1 / (population standard
+// deviation), two passes over the grid values in FP64 (block tree reductions).
+__global__ void k_field_moments(long long per, const double* __restrict__ g,
+                                double* __restrict__ mean, double* __restrict__ inv_std) {
+  __shared__ double red[256];
+  const int b = blockIdx.x;
+  const double* gb = g + (long long)b * per;
+  auto block_sum = [&](double v) -> double {
+    red[threadIdx.x] = v;
+    __syncthreads();
+    for (int o = blockDim.x / 2; o > 0; o >>= 1) {
+      if ((int)threadIdx.x < o) red[threadIdx.x] += red[threadIdx.x + o];
+      __syncthreads();
+    }
+    const double r = red[0];
+    __syncthreads();
+    return r;
+  };
+  double s = 0.0;
+  for (long long i = threadIdx.x; i < per; i += blockDim.x) s += gb[i];
+  const double m = block_sum(s) / (double)per;
+  double q = 0.0;
+  for (long long i = threadIdx.x; i < per; i += blockDim.x) {
+    const double d = gb[i] - m;
+    q = fma(d, d, q);
+  }
+  const double var = block_sum(q) / (double)per;
+  if (threadIdx.x == 0) {
+    mean[b] = m;
+    inv_std[b] = var > 0.0 ? 1.0 / sqrt(var) : 1.0;
+  }
+}
+
+// kappa = exp(scale[b] (g - shift[b])) and kw = kappa * prod_ax w[i_ax] (FP64,
+// plus an FP32 copy) in one pass over the grid
+__global__ void k_exp_weighted_field(int ndim, int nq, long long per, long long total,
+                                     const double* __restrict__ g,
+                                     const double* __restrict__ scale,
+                                     const double* __restrict__ shift,
+                                     const double* __restrict__ w, double* __restrict__ kappa,
+                                     double* __restrict__ kw, float* __restrict__ kw32) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+       i += (long long)gridDim.x * blockDim.x) {
+    const long long b = i / per;
+    long long r = i;
+    double wt = 1.0;
+    for (int a = 0; a < ndim; ++a) {
+      wt *= w[r % nq];
+      r /= nq;
+    }
+    const double sc = scale ? scale[b] : 1.0;
+    const double sh = shift ? shift[b] : 0.0;
+    const double k = exp(sc * (g[i] - sh));
+    if (kappa) kappa[i] = k;
+    const double v = k * wt;
     kw[i] = v;
     if (kw32) kw32[i] = (float)v;
   }
@@ -342,6 +404,37 @@ extern "C" int jfg_weighted_field_f64(int ndim, int nq, int batch, const double*
   if (blocks > 4096) blocks = 4096;
   jfg::k_weighted_field<double><<<(int)blocks, 256, 0, (cudaStream_t)stream>>>(
       ndim, nq, total, kappa, w, kw, kw32);
+  JFG_CHECK_LAUNCH();
+  jfg::count_launches(1);
+  return JFG_OK;
+}
+
+extern "C" int jfg_field_moments_f64(int ndim, int nq, int batch, const double* g,
+                                     double* mean, double* inv_std, void* stream) {
+  if (ndim < 1 || ndim > 3 || nq < 1 || batch < 0 || !g || !mean || !inv_std)
+    return JFG_ERR_ARG;
+  if (batch == 0) return JFG_OK;
+  long long per = 1;
+  for (int i = 0; i < ndim; ++i) per *= nq;
+  jfg::k_field_moments<<<batch, 256, 0, (cudaStream_t)stream>>>(per, g, mean, inv_std);
+  JFG_CHECK_LAUNCH();
+  jfg::count_launches(1);
+  return JFG_OK;
+}
+
+extern "C" int jfg_exp_weighted_field_f64(int ndim, int nq, int batch, const double* g,
+                                          const double* scale, const double* shift,
+                                          const double* w, double* kappa, double* kw,
+                                          float* kw32, void* stream) {
+  if (ndim < 1 || ndim > 3 || nq < 1 || batch < 0 || !g || !w || !kw) return JFG_ERR_ARG;
+  long long per = 1;
+  for (int i = 0; i < ndim; ++i) per *= nq;
+  const long long total = per * batch;
+  if (total == 0) return JFG_OK;
+  long long blocks = (total + 255) / 256;
+  if (blocks > 8 * 152) blocks = 8 * 152;
+  jfg::k_exp_weighted_field<<<(int)blocks, 256, 0, (cudaStream_t)stream>>>(
+      ndim, nq, per, total, g, scale, shift, w, kappa, kw, kw32);
   JFG_CHECK_LAUNCH();
   jfg::count_launches(1);
   return JFG_OK;

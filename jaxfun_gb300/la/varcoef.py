@@ -52,12 +52,66 @@ class VarCoefMatrix:
             raise ValueError("kappa must be sampled on the quadrature grid")
         self.batch_shape = tuple(kappa.shape[: kappa.ndim - self.ndim])
         W = as_device(T.weights())
-        self.kw = (kappa * W).contiguous()
+        self._finish(kappa, (kappa * W).contiguous())
+
+    def _finish(self, kappa, kw):
+        s0 = self.T.basespaces[0]
+        self.kappa = kappa
+        self.kw = kw
         B = s0.backward_matrix(None, 0)
         D = s0.backward_matrix(None, 1)
         self.ops_host = pack_varcoef_ops(self.ndim, B, D)
         self.ops = as_device(self.ops_host)
         self.kappa_mean = kappa.reshape(kappa.shape[: kappa.ndim - self.ndim] + (-1,)).mean(-1)
+
+    @classmethod
+    def from_log(cls, T: TensorProductSpace, g, standardize: bool = False) -> "VarCoefMatrix":
+        """A(kappa) for kappa = exp(g), g sampled on the quadrature grid
+        (``(*batch, nq, ..., nq)``); with ``standardize`` every problem's g is
+        first shifted and scaled to mean 0 and standard deviation 1.  The
+        exponential and the quadrature weighting kappa w (x) w run as one
+        kernel (``jfg_exp_weighted_field_f64``), the moments as another
+        (``jfg_field_moments_f64``): ``evaluate_jaxfunction_expr_quad`` for
+        exp(g) (src/jaxfun/galerkin/arguments.py:928-990) without a pass over
+        kappa of its own."""
+        obj = cls.__new__(cls)
+        s0 = T.basespaces[0]
+        if any(s != s0 for s in T.basespaces):
+            raise ValueError("VarCoefMatrix needs the same 1-D space on every axis")
+        obj.T = T
+        obj.ndim = nd = len(T)
+        obj.n = s0.dim
+        obj.nq = nq = s0.num_quad_points
+        g = as_device(g).contiguous()
+        if tuple(g.shape[g.ndim - nd :]) != (nq,) * nd:
+            raise ValueError("g must be sampled on the quadrature grid")
+        obj.batch_shape = tuple(g.shape[: g.ndim - nd])
+        batch = obj.batch
+        L = _lib.lib()
+        st = _lib.stream_handle()
+        w = as_device(s0.quad_points_and_weights()[1])
+        kappa = torch.empty_like(g)
+        kw = torch.empty_like(g)
+        scale = shift = None
+        if standardize:
+            shift = torch.empty(batch, dtype=torch.float64, device=g.device)
+            scale = torch.empty(batch, dtype=torch.float64, device=g.device)
+            _lib.check(L.jfg_field_moments_f64(nd, nq, batch, g.data_ptr(), shift.data_ptr(),
+                                               scale.data_ptr(), st), "field_moments")
+        _lib.check(L.jfg_exp_weighted_field_f64(
+            nd, nq, batch, g.data_ptr(), None if scale is None else scale.data_ptr(),
+            None if shift is None else shift.data_ptr(), w.data_ptr(), kappa.data_ptr(),
+            kw.data_ptr(), None, st), "exp_weighted_field")
+        obj._finish(kappa, kw)
+        return obj
+
+    @classmethod
+    def from_expansion(cls, T: TensorProductSpace, g_coef, standardize: bool = False
+                       ) -> "VarCoefMatrix":
+        """A(exp(g)) for g given by its orthogonal-basis coefficients (a
+        JAXFunction's coefficients, ``(*batch, N, ..., N)``): the backward
+        transform to the quadrature grid, then ``from_log``."""
+        return cls.from_log(T, T.get_orthogonal().backward(g_coef), standardize=standardize)
 
     @property
     def batch(self) -> int:
