@@ -8,6 +8,8 @@
 // kernel is DFMA-bound long before it is memory-bound.
 #include <stdio.h>
 
+#include <type_traits>
+
 #include "jfg_internal.cuh"
 
 namespace jfg {
@@ -110,6 +112,14 @@ __global__ void __launch_bounds__(NT)
   }
 }
 
+// 128 x 128 tiles for FP32 only (64 FP64 accumulators would not fit)
+template <typename T, int E>
+void launch_r8(dim3 grid, const jfg_contract_desc& d, const T* op, const T* in, T* out,
+               cudaStream_t st) {
+  if constexpr (std::is_same<T, float>::value)
+    k_contract_simt<T, E, 8><<<grid, NT, 0, st>>>(d, op, in, out);
+}
+
 template <typename T>
 int launch_simt(const jfg_contract_desc& d, const T* op, const T* in, T* out,
                 cudaStream_t st) {
@@ -131,12 +141,17 @@ int launch_simt(const jfg_contract_desc& d, const T* op, const T* in, T* out,
   auto ctas = [&](int t) {
     return (long long)((d.P + t - 1) / t) * ((d.M + t - 1) / t) * gz;
   };
-  const int R = ctas(64) >= 2 * nsm[dev] ? 4 : ctas(32) >= 2 * nsm[dev] ? 2 : 1;
+  // FP32 launches big enough for 128 x 128 tiles take them (8 x 8 outputs per
+  // thread: half the shared-memory loads per FMA of the 64 x 64 tile)
+  const bool r8 = std::is_same<T, float>::value && ctas(128) >= 2 * nsm[dev];
+  const int R = r8 ? 8 : ctas(64) >= 2 * nsm[dev] ? 4 : ctas(32) >= 2 * nsm[dev] ? 2 : 1;
   const int tile = 16 * R;
   dim3 grid((d.P + tile - 1) / tile, (d.M + tile - 1) / tile, (unsigned)gz);
   if (grid.y > 65535) return JFG_ERR_ARG;
 #define JFG_SIMT_LAUNCH(E)                                                         \
-  if (R == 4)                                                                     \
+  if (R == 8)                                                                     \
+    launch_r8<T, E>(grid, d, op, in, out, st);                                    \
+  else if (R == 4)                                                                \
     k_contract_simt<T, E, 4><<<grid, NT, 0, st>>>(d, op, in, out);                \
   else if (R == 2)                                                                \
     k_contract_simt<T, E, 2><<<grid, NT, 0, st>>>(d, op, in, out);                \
