@@ -24,7 +24,6 @@ import statistics
 import subprocess
 import sys
 import tempfile
-import threading
 import time
 
 ROOT = os.path.dirname(os.path.abspath(__file__))
@@ -599,7 +598,6 @@ def run_tour(args):
     from jaxfun_gb300 import _lib
     from jaxfun_gb300.galerkin import (DIRICHLET, Chebyshev, FunctionSpace, Legendre,
                                        TensorProduct)
-    from jaxfun_gb300.galerkin.tensorproductspace import tp_apply_tc
     from jaxfun_gb300.la import MixedVarCoefSolver, VarCoefMatrix, pcg, poisson_tpmatrices
     from jaxfun_gb300.la.helmholtz import UnevenHelmholtzSolver, helmholtz_apply
     from jaxfun_gb300.sno import train as sno_train
@@ -699,7 +697,6 @@ def run_varcoef3d(args):
     on 128^3 Legendre Dirichlet, kappa = exp(g) from the 3-D random-field recipe,
     mixed-precision solve vs plain FP64 PCG (on a subset), error vs a tight FP64
     solve."""
-    import numpy as np
     import torch
 
     from jaxfun_gb300.galerkin import DIRICHLET, FunctionSpace, Legendre, TensorProduct
