@@ -138,3 +138,61 @@ def test_oracle_dia_convention():
     for off in offsets:
         mask |= np.eye(5, k=off, dtype=bool)
     assert np.array_equal(D, np.where(mask, A, 0.0))
+
+
+# ---------------------------------------------------------------------------
+# Docstring known answers of the Petrov-Galerkin test spaces (LegPhi_1/2,
+# ChebPhi_1/2): src/jaxfun/galerkin/Legendre.py:520-546, 598-626 and
+# Chebyshev.py:551-577, 629-656.  The test functions are restated from the
+# reference's stencils (Legendre.py LegPhi_1 {0: 1/2, 2: -1/2}, LegPhi_2
+# {0: 1/(2(2k+3)), 2: -(2k+5)/((2k+7)(2k+3)), 4: 1/(2(2k+7))}; Chebyshev.py
+# ChebPhi_1 {0: 1/(pi(k+1)), 2: -1/(pi(k+1))}, ChebPhi_2 {0: 1/(2 pi (k+1)(k+2)),
+# 2: -1/(pi (k^2+4k+3)), 4: 1/(2 pi (k+2)(k+3))}) on N+1 resp. N+2 orthogonal
+# modes; the trial spaces are the orthogonal one, the left-Dirichlet stencil
+# {0: 1, 1: 1} and the homogeneous Dirichlet composite {0: 1, 2: -1}.
+# ---------------------------------------------------------------------------
+
+
+def _pg_matrix(family, N, order, trial_stencil):
+    M = N + order  # orthogonal modes of the test space
+    Nq = N + order + 2
+    big = O.Space1D(family, M)
+    x, w = big.quad(Nq)
+    P = big.vandermonde_orth(x, 0)  # (Nq, M)
+    k = np.arange(M - 2 * order, dtype=np.float64)
+    pi = np.pi
+    if family == "legendre" and order == 1:
+        st = {0: 0.5 + 0 * k, 2: -0.5 + 0 * k}
+    elif family == "legendre":
+        st = {0: 1 / (2 * (2 * k + 3)), 2: -(2 * k + 5) / (2 * k + 7) / (2 * k + 3),
+              4: 1 / (2 * (2 * k + 7))}
+    elif order == 1:
+        st = {0: 1 / pi / (k + 1), 2: -1 / pi / (k + 1)}
+    else:
+        st = {0: 1 / (2 * pi * (k + 1) * (k + 2)), 2: -1 / (pi * (k**2 + 4 * k + 3)),
+              4: 1 / (2 * pi * (k + 2) * (k + 3))}
+    S = np.zeros((len(k), M))
+    for off, c in st.items():
+        S[np.arange(len(k)), np.arange(len(k)) + off] = c
+    phi = P @ S.T  # test functions at the nodes
+    V = O.Space1D(family, N).vandermonde_orth(x, order)  # trial derivatives
+    n_trial = N - max(trial_stencil)
+    T = np.zeros((n_trial, N))
+    for off, c in trial_stencil.items():
+        T[np.arange(n_trial), np.arange(n_trial) + off] = c
+    return (phi.T * w[None, :]) @ (V @ T.T)
+
+
+@pytest.mark.parametrize("family", ["legendre", "chebyshev"])
+def test_petrov_galerkin_docstring_matrices(family):
+    ident1 = np.eye(5, 6, k=1)
+    A = _pg_matrix(family, 6, 1, {0: 1.0})
+    np.testing.assert_allclose(A, ident1, atol=1e-13)
+    A = _pg_matrix(family, 6, 1, {0: 1.0, 1: 1.0})  # {"left": {"D": 0}}
+    np.testing.assert_allclose(A, np.eye(5) + np.eye(5, k=1), atol=1e-13)
+    ident2 = np.eye(5, 7, k=2)
+    A = _pg_matrix(family, 7, 2, {0: 1.0})
+    np.testing.assert_allclose(A, ident2, atol=1e-12)
+    # the homogeneous Dirichlet composite of the GPU path (phi_k = P_k - P_{k+2})
+    A = _pg_matrix(family, 7, 2, {0: 1.0, 2: -1.0})
+    np.testing.assert_allclose(A, -np.eye(5) + np.eye(5, k=2), atol=1e-12)
