@@ -686,6 +686,17 @@ def run_tour(args):
         band[:, di, j] = k2[:, None] * Md[j - off, j][None, :] + Kd[j - off, j][None, :]
     WS = TPMatricesWavenumberSolver(1, (4096, n), band, offs)
     WS.solve(torch.as_tensor(rng.standard_normal((4096, n)), device="cuda"))
+    # 7. inhomogeneous Dirichlet lifting (affine transforms) and the coefficient
+    #    evaluated from its logarithm (exp + weighting, moments), 32 problems
+    def gb(x, y):
+        return np.exp(-(x**2 + y**2))
+
+    Dl = FunctionSpace(256, Legendre, bcs={"left": {"D": gb}, "right": {"D": gb}})
+    TL = TensorProduct(Dl, Dl)
+    cl = TL.backward(torch.as_tensor(rng.standard_normal((32, 254, 254)), device="cuda"))
+    TL.forward(cl)
+    VarCoefMatrix.from_log(T, torch.as_tensor(rng.standard_normal((32, 256, 256)),
+                                              device="cuda"), standardize=True)
     torch.cuda.synchronize()
     print(json.dumps({"tour": "done", "device_status": int(L.jfg_device_status()),
                       "launches": int(L.jfg_launch_count())}), flush=True)
