@@ -17,8 +17,8 @@ namespace jfg {
 // separable transforms: out = (x_ax mats[ax]) in
 // ---------------------------------------------------------------------------
 
-size_t tp_apply_ws(int ndim, const int* rows, const int* cols, int batch, int eb) {
-  if (ndim < 1 || ndim > 3) return 0;
+// bytes of one intermediate buffer (the largest field between two passes)
+static size_t tp_inter_bytes(int ndim, const int* rows, const int* cols, int batch, int eb) {
   int shape[3];
   int order[3];
   for (int i = 0; i < ndim; ++i) shape[i] = cols[i], order[i] = i;
@@ -32,7 +32,16 @@ size_t tp_apply_ws(int ndim, const int* rows, const int* cols, int batch, int eb
     for (int i = 0; i < ndim; ++i) sz *= (size_t)shape[i];
     if (sz > mx) mx = sz;
   }
-  return 2 * align_up(mx * eb, 256);
+  return align_up(mx * eb, 256);
+}
+
+// two intermediate buffers, then room for the operators split into FP32
+// (hi, lo) pairs (used by the double-FP32 engine)
+size_t tp_apply_ws(int ndim, const int* rows, const int* cols, int batch, int eb) {
+  if (ndim < 1 || ndim > 3) return 0;
+  size_t ops = 0;
+  for (int i = 0; i < ndim; ++i) ops += (size_t)rows[i] * cols[i];
+  return 2 * tp_inter_bytes(ndim, rows, cols, batch, eb) + align_up(ops * sizeof(float2), 256);
 }
 
 // out[i] = shift[i % per] for i < total: the constant field of an affine
@@ -57,7 +66,23 @@ int tp_apply(Engine e, int ndim, const int* rows, const int* cols, int batch,
     if (rows[i] < 1 || cols[i] < 1 || !mats[i].hi) return JFG_ERR_ARG;
   const size_t need = tp_apply_ws(ndim, rows, cols, batch, (int)sizeof(T));
   if (ndim > 1 && (!work || work_bytes < need)) return JFG_ERR_WORKSPACE;
-  T* buf[2] = {(T*)work, (T*)((char*)work + need / 2)};
+  const size_t inter = tp_inter_bytes(ndim, rows, cols, batch, (int)sizeof(T));
+  T* buf[2] = {(T*)work, (T*)((char*)work + inter)};
+  // Double-FP32: split every operator once into (hi, lo) pairs and keep the
+  // intermediates split between the passes (no FP64 work in the tile loads)
+  const bool dfp = std::is_same<T, double>::value && e == Engine::DF && work &&
+                   work_bytes >= need && batch > 0;
+  OpRef<T> opr[3];
+  for (int i = 0; i < ndim; ++i) opr[i] = mats[i];
+  if (dfp) {
+    float2* pairs = (float2*)((char*)work + 2 * inter);
+    for (int i = 0; i < ndim; ++i) {
+      const long long cnt = (long long)rows[i] * cols[i];
+      JFG_TRY(split_pairs_f64((const double*)mats[i].hi, pairs, cnt, st));
+      opr[i] = OpRef<T>{mats[i].hi, (const T*)pairs};
+      pairs += cnt;
+    }
+  }
 
   int shape[3], order[3];
   for (int i = 0; i < ndim; ++i) shape[i] = cols[i], order[i] = i;
@@ -83,7 +108,11 @@ int tp_apply(Engine e, int ndim, const int* rows, const int* cols, int batch,
       }
       d.beta = 1.0;
     }
-    JFG_TRY(contract(e, d, mats[ax], src, dst, st));
+    if (dfp)
+      JFG_TRY(contract_df64(d, (const double*)opr[ax].hi, (const float2*)opr[ax].lo,
+                            (const double*)src, (double*)dst, st, t > 0, t < ndim - 1));
+    else
+      JFG_TRY(contract(e, d, mats[ax], src, dst, st));
     for (int i = ndim - 1; i > 0; --i) shape[i] = shape[i - 1], order[i] = order[i - 1];
     shape[0] = M;
     order[0] = ax;
