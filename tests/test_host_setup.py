@@ -86,3 +86,43 @@ def test_varcoef_pack_layout(lib):
     assert np.array_equal(p[nn:2 * nn].reshape(6, 4), D)
     assert np.array_equal(p[4 * nn:5 * nn].reshape(4, 6), B.T)
     assert np.array_equal(p[6 * nn:].reshape(4, 12), np.hstack([D.T, B.T]))
+
+
+def test_new_entry_points_reject_bad_arguments(lib):
+    """Entry points added with the lifting, the coefficient evaluation and the
+    double-FP32 apply validate on the host before any CUDA call."""
+    from jaxfun_gb300 import _lib
+
+    ERR = _lib.JFG_ERR_ARG
+    rows, cols = _lib.int_array([6, 6]), _lib.int_array([8, 8])
+    fake = 4096  # never dereferenced: the checks fail first
+    # affine apply: no shift, or output aliasing the input
+    assert lib.jfg_tp_apply_affine_f64(2, rows, cols, 1, _lib.ptr_array([fake, fake]), fake,
+                                       None, fake, fake, 1 << 20, None) == ERR
+    assert lib.jfg_tp_apply_affine_f64(2, rows, cols, 1, _lib.ptr_array([fake, fake]), fake,
+                                       fake, fake, fake, 1 << 20, None) == ERR
+    assert lib.jfg_tp_apply_df64(0, rows, cols, 1, None, None, None, None, 0, None) == ERR
+    # coefficient from its logarithm / moments
+    assert lib.jfg_exp_weighted_field_f64(2, 8, 1, None, None, None, fake, None, fake, None,
+                                          None) == ERR
+    assert lib.jfg_field_moments_f64(4, 8, 1, fake, fake, fake, None) == ERR
+    # mode mixing: the block owns 8 consecutive modes
+    assert lib.jfg_sno_modemix_fwd(2, 10, 64, fake, fake, fake, None) == ERR
+    assert lib.jfg_sno_modemix_fwd(2, 16, 65, fake, fake, fake, None) == ERR
+
+
+def test_tp_apply_workspace_includes_operator_pairs(lib):
+    """Two intermediate buffers (256-byte aligned) plus the operators split
+    into 8-byte (hi, lo) pairs for the double-FP32 engine."""
+    from jaxfun_gb300 import _lib
+
+    def al(x):
+        return (x + 255) // 256 * 256
+
+    rows, cols = [30, 20], [32, 24]
+    batch = 3
+    # pass 1 contracts axis 1: (30... rotate) -> the field between passes is (20, 32)
+    inter = al(batch * 20 * 32 * 8)
+    ops = al((30 * 32 + 20 * 24) * 8)
+    got = lib.jfg_tp_apply_workspace_size(2, _lib.int_array(rows), _lib.int_array(cols), batch, 8)
+    assert got == 2 * inter + ops
