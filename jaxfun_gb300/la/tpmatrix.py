@@ -81,14 +81,23 @@ class TPMatrices:
             self._lu_cache = tpmats_lu_factor(self.tpmats)
         return self._lu_cache
 
-    def solve(self, rhs, *, method: str = "auto") -> torch.Tensor:
+    def solve(self, rhs, *, method: str = "auto", kron_method: str = "auto",
+              auto_threshold: int = 100) -> torch.Tensor:
         """Solve A x = rhs (leading batch axes allowed).
 
         method "lu": fast diagonalisation on the GPU (raises SolverNotApplicable if
         the structure does not allow it); "kron": dense Kronecker LU (small
         problems only, cuSOLVER through torch.linalg); "auto": lu, else kron —
-        the dispatch of TPMatrices.solve (tpmatrix.py:429-509).
+        the dispatch of TPMatrices.solve (tpmatrix.py:429-509).  ``kron_method``
+        ("auto", "banded", "rcm", "dense") and ``auto_threshold`` keep the
+        reference's signature; they choose among the reference's sparse
+        Kronecker solvers, whereas the Kronecker path here is always the dense
+        LU, so they are validated and otherwise have no effect.
         """
+        if kron_method not in ("auto", "banded", "rcm", "dense"):
+            raise ValueError(f"unknown kron_method {kron_method!r}")
+        if int(auto_threshold) < 0:
+            raise ValueError("auto_threshold must be non-negative")
         if method in ("auto", "lu"):
             try:
                 return self.lu_factor().solve(rhs)

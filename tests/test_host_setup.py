@@ -126,3 +126,20 @@ def test_tp_apply_workspace_includes_operator_pairs(lib):
     ops = al((30 * 32 + 20 * 24) * 8)
     got = lib.jfg_tp_apply_workspace_size(2, _lib.int_array(rows), _lib.int_array(cols), batch, 8)
     assert got == 2 * inter + ops
+
+
+def test_tpmatrices_solve_signature():
+    """TPMatrices.solve keeps the reference's keywords (tpmatrix.py:429-436)
+    and rejects unknown choices before any device work."""
+    import inspect
+
+    from jaxfun_gb300.la import TPMatrices
+
+    sig = inspect.signature(TPMatrices.solve)
+    for k in ("method", "kron_method", "auto_threshold"):
+        assert sig.parameters[k].kind is inspect.Parameter.KEYWORD_ONLY
+    A = TPMatrices([])
+    with pytest.raises(ValueError):
+        A.solve(np.zeros((2, 2)), kron_method="cholesky")
+    with pytest.raises(ValueError):
+        A.solve(np.zeros((2, 2)), method="qr")
