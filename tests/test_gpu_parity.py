@@ -205,3 +205,28 @@ def test_bad_workspace_is_reported():
     st = L.jfg_tp_apply_f64(2, rows, rows, 1, _lib.ptr_array([m.data_ptr()] * 2), x.data_ptr(),
                             x.data_ptr(), None, 0, _lib.stream_handle())
     assert st == _lib.JFG_ERR_WORKSPACE
+
+
+@pytest.mark.parametrize("ndim", [2, 3])
+def test_tpmatrices_apply_vs_numpy_kron(ndim):
+    """Separable apply (TPMatrix / TPMatrices @ u, tpmatrix.py:152-156,
+    287-289) against the explicit numpy.kron product, as the reference's
+    test_kron.py:206-369 checks its Kronecker assembly: random dense factors
+    of unequal sizes, three terms with coefficients, a batch of 2."""
+    from functools import reduce
+
+    from jaxfun_gb300.la import TPMatrices, TPMatrix
+
+    rng = np.random.default_rng(21)
+    shape = (5, 7, 4)[:ndim]
+    terms = []
+    for s in (1.0, -0.5, 2.0):
+        terms.append(TPMatrix([rng.standard_normal((n, n)) for n in shape], s))
+    A = TPMatrices(terms)
+    u = rng.standard_normal((2,) + shape)
+    v = (A @ u).cpu().numpy()
+    K = A.todense()
+    ref = np.stack([(K @ ui.ravel()).reshape(shape) for ui in u])
+    np.testing.assert_allclose(v, ref, atol=1e-13 * np.abs(ref).max())
+    K2 = sum(t.coefficient * reduce(np.kron, t.mats) for t in terms)
+    np.testing.assert_allclose(K, K2, atol=1e-15 * np.abs(K2).max())
