@@ -3,11 +3,10 @@
 // the library carries, instead of a workspace the caller provides.
 //
 // Who needs this: callers that cannot call cudaMalloc (or any allocating
-// routine) at the point where they solve -- for example code that runs while
-// a CUDA graph is being captured, a custom-call handler inside another
-// runtime that owns all device memory and hands out no workspace, or a
-// real-time loop that must not block on the allocator.  They pass only the
-// inputs and the output.
+// routine) at the point where they solve -- for example a custom-call handler
+// inside another runtime that owns all device memory and hands out no
+// workspace, or a real-time loop that must not block on the allocator.  They
+// pass only the inputs and the output.
 //
 // Limits and sharing: the scratch array is JFG_NOALLOC_SCRATCH_BYTES (32 MiB)
 // and every GPU that loads this library holds one copy until the process
@@ -20,8 +19,10 @@
 // reads, so nothing needs clearing.
 //
 // Set-up: the first call on each device looks up the device address of the
-// array (cudaGetSymbolAddress) with that device current, and caches it.  Make
-// that first call outside any stream capture.
+// array (cudaGetSymbolAddress) with that device current, and caches it for
+// the life of the process.  Make that first call before any stream capture.
+// The cache is not refreshed after cudaDeviceReset: a process that resets a
+// device must not call this entry point on it again.
 #include <mutex>
 
 #include "jfg_internal.cuh"
@@ -63,6 +64,15 @@ extern "C" int jfg_fd_solve_f64_noalloc(int ndim, int n, int batch, const double
                                         const double* c1, const double* rhs, double* out,
                                         void* stream) {
   if ((ndim != 2 && ndim != 3) || n < 1 || batch < 0) return JFG_ERR_ARG;
+  // Size check by division, so that no product below can wrap around: one
+  // field of the batch (batch * n^ndim doubles) must fit in the array.
+  const size_t cap_elems = JFG_NOALLOC_SCRATCH_BYTES / sizeof(double);
+  size_t per = 1;
+  for (int i = 0; i < ndim; ++i) {
+    if (per > cap_elems / (size_t)n) return JFG_ERR_WORKSPACE;
+    per *= (size_t)n;
+  }
+  if ((size_t)batch > cap_elems / per) return JFG_ERR_WORKSPACE;
   const size_t need = jfg::fd_ws(ndim, n, batch, (int)sizeof(double));
   if (need > JFG_NOALLOC_SCRATCH_BYTES) return JFG_ERR_WORKSPACE;
   void* scratch = nullptr;

@@ -1,7 +1,7 @@
 """The allocation-free fast-diagonalisation entry point (jfg_fd_solve_f64_noalloc).
 
 It exists for callers that cannot allocate device memory at the point where
-they solve (inside CUDA-graph capture, inside a host runtime that hands out no
+they solve (inside a host runtime that owns all device memory and hands out no
 workspace, in loops that must not block on an allocator): they pass only
 inputs and outputs, and the library uses a fixed scratch array of its own.
 This file is collected last so that a run stopping at the first failure has
@@ -25,8 +25,13 @@ def _factors(space, N, ndim, alpha2):
     return tpmats_lu_factor(poisson_tpmatrices(T, alpha2).tpmats)
 
 
-def _solve_both(fac, rhs, c0, c1):
-    """Run the workspace entry point and the allocation-free one on the same data."""
+def _solve_both(fac, rhs, c0, c1, check_memory=False):
+    """Run the workspace entry point and the allocation-free one on the same data.
+
+    With check_memory, also check that the allocation-free call leaves the
+    device's free memory and torch's allocated bytes unchanged (only after a
+    first call: with lazy module loading the first call loads the library's
+    kernels and its scratch array)."""
     L = _lib.lib()
     nd, n = fac.ndim, fac.n
     batch = rhs.shape[0]
@@ -42,11 +47,17 @@ def _solve_both(fac, rhs, c0, c1):
                             t_c0.data_ptr(), t_c1.data_ptr(), t_rhs.data_ptr(), ref.data_ptr(),
                             ws.data_ptr(), ws.numel(), sh)
     assert st == 0, _lib.status_string(st)
+    torch.cuda.synchronize()
+    free0 = torch.cuda.mem_get_info()[0]
+    used0 = torch.cuda.memory_allocated()
     st = L.jfg_fd_solve_f64_noalloc(nd, n, batch, E.data_ptr(), W.data_ptr(), lam.data_ptr(),
                                     t_c0.data_ptr(), t_c1.data_ptr(), t_rhs.data_ptr(),
                                     out.data_ptr(), sh)
     assert st == 0, _lib.status_string(st)
     torch.cuda.synchronize()
+    if check_memory:
+        assert torch.cuda.memory_allocated() == used0
+        assert torch.cuda.mem_get_info()[0] == free0
     return ref.cpu().numpy(), out.cpu().numpy()
 
 
@@ -63,7 +74,7 @@ def test_noalloc_matches_workspace_entry_point_twice(space, N, ndim, alpha2):
         rhs = rng.standard_normal((batch,) + (fac.n,) * ndim)
         c0 = np.full(batch, alpha2) + call
         c1 = np.ones(batch)
-        ref, out = _solve_both(fac, rhs, c0, c1)
+        ref, out = _solve_both(fac, rhs, c0, c1, check_memory=call == 1)
         assert np.all(np.isfinite(out))
         assert np.abs(out - ref).max() <= 1e-12 * np.abs(ref).max()
 
@@ -80,3 +91,9 @@ def test_noalloc_rejects_oversized_request():
     st = L.jfg_fd_solve_f64_noalloc(nd, n, batch, p, p, p, None, None, p, p,
                                     _lib.stream_handle())
     assert st == _lib.JFG_ERR_WORKSPACE
+    # sizes whose byte count would wrap around in size_t are rejected as well
+    for n_, nd_, b_ in ((2048, 3, 2**28), (2**20, 3, 1), (65536, 2, 2**31 - 1)):
+        st = L.jfg_fd_solve_f64_noalloc(nd_, n_, b_, p, p, p, None, None, p, p,
+                                        _lib.stream_handle())
+        assert st == _lib.JFG_ERR_WORKSPACE, (n_, nd_, b_)
+    torch.cuda.synchronize()
