@@ -96,6 +96,8 @@ SIGNATURES = {
     "jfg_split_tf32_host": (None, [_sz, _vp, _vp, _vp]),
     "jfg_tc_set_variant": (_i, [_i]),
     "jfg_device_status": (_i, []),
+    "jfg_tc_set_wait_budget_ns": (_i, [C.c_ulonglong]),
+    "jfg_tc_test_hold": (_i, [_i]),
     "jfg_tp_apply_workspace_size": (_sz, [_i, C.POINTER(_i), C.POINTER(_i), _i, _i]),
     "jfg_tp_apply_f64": (_i, [_i, C.POINTER(_i), C.POINTER(_i), _i, C.POINTER(_vp), _vp, _vp,
                               _vp, _sz, _vp]),

@@ -38,6 +38,13 @@
 namespace jfg {
 
 __device__ int g_tc_status = 0;
+// Budget of the pipeline waits (ns) and the test hook that makes the epilogue
+// first wait on a barrier nothing arrives on (jfg_tc_set_wait_budget_ns,
+// jfg_tc_test_hold): the timeout path can then be exercised without any
+// broken kernel.  Drain waits always use the full WAIT_NS budget.
+constexpr unsigned long long WAIT_NS_DEFAULT = 2000000000ull;
+__device__ unsigned long long g_tc_wait_ns = WAIT_NS_DEFAULT;
+__device__ int g_tc_test_hold = 0;
 
 // Kernel variant: 1 keeps the split input tile in TMEM (default), 0 in shared
 // memory (jfg_tc_set_variant).
@@ -128,13 +135,14 @@ __device__ __forceinline__ bool mbar_try(uint64_t* bar, uint32_t parity) {
 }
 
 // Bounded wait: false (and the status word set) if the budget runs out.
-__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity) {
+__device__ __forceinline__ bool mbar_wait(uint64_t* bar, uint32_t parity,
+                                          unsigned long long budget) {
   if (mbar_try(bar, parity)) return true;
   const unsigned long long t0 = gtimer();
   while (true) {
     for (int i = 0; i < 256; ++i)
       if (mbar_try(bar, parity)) return true;
-    if (gtimer() - t0 > WAIT_NS) {
+    if (gtimer() - t0 > budget) {
       atomicExch(&g_tc_status, JFG_ERR_DEVICE_TIMEOUT);
       return false;
     }
@@ -291,6 +299,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   extern __shared__ uint8_t smem_raw[];
   __shared__ long long tb[G + 1];
   __shared__ int nbs[G];
+  __shared__ unsigned long long s_budget;
+  __shared__ int s_hold;
   uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   const int S = L.stages;
   const bool ta = B16 || L.tmem_a != 0;
@@ -310,8 +320,11 @@ __global__ void __launch_bounds__(NTHREADS, 1)
              nb * q.d.nseg;
     }
     tb[L.ngroups] = acc;
+    s_budget = g_tc_wait_ns;
+    s_hold = g_tc_test_hold;
   }
   __syncthreads();
+  const unsigned long long budget = s_budget;
   const long long ntiles = tb[L.ngroups];
   if ((long long)blockIdx.x >= ntiles) return;  // no tile for this CTA (uniform)
 
@@ -322,7 +335,9 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   uint64_t* empty = bars + 2 * S;
   uint64_t* tfull = bars + 3 * S;       // [2] accumulator ready
   uint64_t* tempty = bars + 3 * S + 2;  // [2] accumulator drained
-  uint32_t* tmem_slot = (uint32_t*)(bars + 3 * S + 4);
+  uint64_t* hold = bars + 3 * S + 4;    // test hook: nothing arrives on it
+  uint64_t* mma_done = bars + 3 * S + 5;  // MMA drain after a timeout
+  uint32_t* tmem_slot = (uint32_t*)(bars + 3 * S + 6);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
@@ -336,6 +351,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       mbar_init(&tfull[i], 1);
       mbar_init(&tempty[i], 8);
     }
+    mbar_init(hold, 1);
+    mbar_init(mma_done, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 1) {
@@ -397,7 +414,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         for (int kb = 0; kb < nkb; ++kb, ++g) {
           const int st = (int)(g % S);
           const uint32_t u = (uint32_t)(g / S);
-          if (g >= S && !mbar_wait(&empty[st], (u & 1u) ^ 1u)) {
+          if (g >= S && !mbar_wait(&empty[st], (u & 1u) ^ 1u, budget)) {
             ok = false;
             break;
           }
@@ -413,14 +430,14 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       }
       // drain: the latest use of every stage must have landed before exit
       for (long long q = (issued > S ? issued - S : 0); q < issued; ++q)
-        mbar_wait(&full[q % S], (uint32_t)(q / S) & 1u);
+        mbar_wait(&full[q % S], (uint32_t)(q / S) & 1u, WAIT_NS);
     }
   } else if (warp == 1) {
     // ---------------- MMA issuer ----------------
     if (lane == 0) {
       long long g = 0;
       int li = 0;
-      bool ok = true;
+      bool ok = true, issued_any = false;
       for (long long t = blockIdx.x; t < ntiles && ok; t += gridDim.x, ++li) {
         int gi, pt, mc, b, s;
         decode(t, gi, pt, mc, b, s);
@@ -429,7 +446,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         const int nkb = nkb_of(gi);
         const int buf = li & 1;
         const uint32_t use = (uint32_t)(li >> 1);
-        if (li >= 2 && !mbar_wait(&tempty[buf], (use & 1u) ^ 1u)) {
+        if (li >= 2 && !mbar_wait(&tempty[buf], (use & 1u) ^ 1u, budget)) {
           ok = false;
           break;
         }
@@ -437,10 +454,11 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         const uint32_t acc = tmem + (uint32_t)buf * acc_stride;
         for (int kb = 0; kb < nkb; ++kb, ++g) {
           const int st = (int)(g % S);
-          if (!mbar_wait(&conv[st], (uint32_t)(g / S) & 1u)) {
+          if (!mbar_wait(&conv[st], (uint32_t)(g / S) & 1u, budget)) {
             ok = false;
             break;
           }
+          issued_any = true;
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
           const uint32_t oh = smem_u32(Oh(st)), ol = smem_u32(Ol(st));
           if (B16) {
@@ -475,6 +493,12 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         }
         if (ok) mma_commit(&tfull[buf]);
       }
+      // after a timeout the MMAs already issued must finish before the TMEM
+      // they write is freed: one more commit tracks all of them
+      if (!ok && issued_any) {
+        mma_commit(mma_done);
+        mbar_wait(mma_done, 0, WAIT_NS);
+      }
     }
   } else if (warp < 6) {
     // ---------------- split staged input tiles into TF32 hi (in place) / lo ----------------
@@ -491,7 +515,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       const int nkb = nkb_of(gi);
       for (int kb = 0; kb < nkb; ++kb, ++g) {
         const int st = (int)(g % S);
-        if (!mbar_wait(&full[st], (uint32_t)(g / S) & 1u)) {
+        if (!mbar_wait(&full[st], (uint32_t)(g / S) & 1u, budget)) {
           ok = false;
           break;
         }
@@ -567,7 +591,10 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     const int half = (warp - 6) >> 2;
     const int row = 32 * q4 + lane;
     int li = 0;
-    for (long long t = blockIdx.x; t < ntiles; t += gridDim.x, ++li) {
+    // test hook: a barrier nothing arrives on; its wait runs out (status set)
+    // and this warp skips its tiles, so every other role's waits run out too
+    const bool held = s_hold != 0 && !mbar_wait(hold, 0, budget);
+    for (long long t = blockIdx.x; t < ntiles && !held; t += gridDim.x, ++li) {
       int gi, pt, mc, b, s;
       decode(t, gi, pt, mc, b, s);
       const TcGroup& q = L.g[gi];
@@ -575,7 +602,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       const int Mt = q.Mtile;
       const float alpha = (float)d.alpha, beta = (float)d.beta;
       const int buf = li & 1;
-      if (!mbar_wait(&tfull[buf], (uint32_t)(li >> 1) & 1u)) break;
+      if (!mbar_wait(&tfull[buf], (uint32_t)(li >> 1) & 1u, budget)) break;
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       const int p = pt * TILE_P + row;
       const bool pin = p < d.P && b >= 0;
@@ -835,7 +862,7 @@ int launch_groups(int ng, const jfg_contract_desc* const* ds, const void* const*
   L.tmem_a = ta;
   L.mt_max = mt_max;
   L.out_stage = ostage;
-  const size_t smem = 1024 + stages * stage + ob + (3 * stages + 4) * 8 + 16;
+  const size_t smem = 1024 + stages * stage + ob + (3 * stages + 6) * 8 + 16;
   if (smem > (size_t)SMEM_MAX) return JFG_ERR_UNSUPPORTED;
   int dev = 0, nsm = 0;
   JFG_CUDA_TRY(cudaGetDevice(&dev));
@@ -1002,6 +1029,18 @@ extern "C" void jfg_split_bf16_host(size_t n, const double* src, uint16_t* hi, u
 extern "C" int jfg_tc_set_store_path(int tma_store) {
   if (tma_store != 0 && tma_store != 1) return JFG_ERR_ARG;
   jfg::g_tma_store = tma_store;
+  return JFG_OK;
+}
+
+extern "C" int jfg_tc_set_wait_budget_ns(unsigned long long ns) {
+  const unsigned long long v = ns == 0 ? jfg::WAIT_NS_DEFAULT : ns;
+  JFG_CUDA_TRY(cudaMemcpyToSymbol(jfg::g_tc_wait_ns, &v, sizeof(v)));
+  return JFG_OK;
+}
+
+extern "C" int jfg_tc_test_hold(int on) {
+  if (on != 0 && on != 1) return JFG_ERR_ARG;
+  JFG_CUDA_TRY(cudaMemcpyToSymbol(jfg::g_tc_test_hold, &on, sizeof(on)));
   return JFG_OK;
 }
 

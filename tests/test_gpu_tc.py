@@ -141,3 +141,38 @@ def test_tc_store_paths_agree(B, S, M, P, K, epi):
         finally:
             L.jfg_tc_set_store_path(1)
     assert np.array_equal(outs[0], outs[1])
+
+
+def test_bounded_wait_times_out_and_context_stays_usable(variant):
+    """The timeout path of the bounded mbarrier waits, in the allowed form: with
+    a 200 us wait budget the epilogue waits on a barrier that nothing arrives
+    on; the wait runs out, JFG_ERR_DEVICE_TIMEOUT is recorded, every other
+    role's waits run out, and the kernel drains and returns.  The next launch
+    with the default budget is correct against FP64 and leaves status OK."""
+    L = _lib.lib()
+    rng = np.random.default_rng(21)
+    op = rng.standard_normal((1, 256, 256))
+    x = rng.standard_normal((8, 1, 256, 256)).astype(np.float32)
+    assert L.jfg_device_status() == 0
+    assert L.jfg_tc_set_wait_budget_ns(200_000) == 0
+    assert L.jfg_tc_test_hold(1) == 0
+    try:
+        hi, lo = split(op)
+        dev = lambda a: torch.as_tensor(np.ascontiguousarray(a), device="cuda")  # noqa: E731
+        t_hi, t_lo, t_x = dev(hi), dev(lo), dev(x)
+        out = torch.zeros(8, 1, 256, 256, dtype=torch.float32, device="cuda")
+        d = _lib.ContractDesc(batch=8, nseg=1, M=256, P=256, K=256, op_ld=256, op_seg=0,
+                              in_ld=256, in_seg=0, in_batch=256 * 256, out_ld=256, out_seg=0,
+                              out_batch=256 * 256, alpha=1.0, beta=0.0)
+        st = L.jfg_contract_tc(d, t_hi.data_ptr(), t_lo.data_ptr(), t_x.data_ptr(),
+                               out.data_ptr(), _lib.stream_handle())
+        assert st == 0, _lib.status_string(st)
+        torch.cuda.synchronize()
+    finally:
+        assert L.jfg_tc_test_hold(0) == 0
+        assert L.jfg_tc_set_wait_budget_ns(0) == 0
+    assert L.jfg_device_status() == _lib.JFG_ERR_DEVICE_TIMEOUT
+    assert L.jfg_device_status() == 0  # read and cleared
+    got = run_tc(op, x)
+    ref = np.einsum("smk,bspk->bsmp", op, x.astype(np.float64))
+    assert np.abs(got - ref).max() <= TC_TOL * np.abs(ref).max()
