@@ -1,0 +1,119 @@
+"""Parity at the benchmark sizes against the FP64 oracle (NumPy/SciPy).
+
+Config 3 (variable-coefficient 2-D Poisson, Legendre Dirichlet, N = 256):
+problems built by the benchmark's seeded recipe, solved on the GPU by the
+learned-guess mixed path (the headline), the mixed path from a zero start and
+the plain FP64 PCG, each compared with the oracle's FP64 PCG run to 1e-13:
+mixed and learned <= 1e-10, plain FP64 <= 1e-12 relative (max norm).
+
+Config 2 (uneven Chebyshev Dirichlet Helmholtz): N = 256 and 512 problems in
+one grouped call against the oracle's general-eigenvector fast-
+diagonalisation solve, refined with the oracle's dense-operator FP64 residual:
+<= 1e-10.
+"""
+
+import os
+
+import numpy as np
+import pytest
+import torch
+
+from oracle import spectral as O
+
+pytestmark = pytest.mark.gpu
+
+N = 256
+
+
+def _recipe(seed: int):
+    """The benchmark's config-3 inputs for one seed: g from Legendre
+    coefficients z (1+j^2+k^2)^-1.5 standardised, kappa = exp(g), forcing
+    coefficients z (1+j)^-2 (1+k)^-2, both taken to the Gauss grid."""
+    rng = np.random.default_rng(seed)
+    k2 = np.add.outer(np.arange(N) ** 2.0, np.arange(N) ** 2.0)
+    gh = rng.standard_normal((N, N)) * (1.0 + k2) ** -1.5
+    s = np.outer((1.0 + np.arange(N)) ** -2.0, (1.0 + np.arange(N)) ** -2.0)
+    fh = rng.standard_normal((N, N)) * s
+    Vo = O.Space1D("legendre", N, False)
+    g = O.tp_backward([Vo, Vo], gh)
+    g = (g - g.mean()) / g.std()
+    return g, O.tp_backward([Vo, Vo], fh)
+
+
+def _oracle_solve(kap, b, tol=1e-13):
+    V = O.Space1D("legendre", N, True)
+    lam, W = O.fd_factor_symmetric(V.stiffness_matrix(), V.mass_matrix())
+    x, it = O.pcg(lambda u: O.varcoef_apply(V, kap, u), b,
+                  lambda r: O.fd_solve(r, [W, W], [W.T, W.T], [lam, lam]), tol=tol)
+    return x
+
+
+def test_headline_config3_against_oracle():
+    from jaxfun_gb300.galerkin import DIRICHLET, FunctionSpace, Legendre, TensorProduct
+    from jaxfun_gb300.la import MixedVarCoefSolver, VarCoefMatrix, pcg
+    from jaxfun_gb300.sno import train as TR
+
+    seeds = (0, 1)
+    gs, fs = zip(*(_recipe(s) for s in seeds))
+    g = np.stack(gs)
+    f = np.stack(fs)
+    kap = np.exp(g)
+    Vd = O.Space1D("legendre", N, True)
+    b = np.stack([O.tp_scalar_product([Vd, Vd], fi) for fi in f])
+    ref = np.stack([_oracle_solve(kap[i], b[i]) for i in range(len(seeds))])
+
+    D = FunctionSpace(N, Legendre, bcs=DIRICHLET)
+    T = TensorProduct(D, D)
+    A = VarCoefMatrix(T, kap)
+    S = MixedVarCoefSolver(A)
+    path = os.path.join(os.path.dirname(TR.__file__), "weights", "sno_varcoef2d_N256.npz")
+    model = TR.load(path, batch=len(seeds))
+    maps = TR.GridMaps()
+    X, sc = TR.features(torch.as_tensor(g, device="cuda").float(),
+                        torch.as_tensor(f, device="cuda"), maps)
+    guess = TR.initial_guess(model, maps, X, sc)
+
+    def err(x):
+        x = x.cpu().numpy() if torch.is_tensor(x) else x
+        return max(float(np.abs(x[i] - ref[i]).max() / np.abs(ref[i]).max())
+                   for i in range(len(seeds)))
+
+    # the headline path and its stopping rules (outer relres 1e-11, inner 1e-5)
+    x_l, _, _ = S.solve(b, tol=1e-11, inner_tol=1e-5, guess=guess)
+    x_z, _, _ = S.solve(b, tol=1e-11, inner_tol=1e-5)
+    assert err(x_l) <= 1e-10, err(x_l)
+    assert err(x_z) <= 1e-10, err(x_z)
+    # the plain FP64 GPU path, run tight, agrees with the oracle to 1e-12
+    x64, _ = pcg(A, b, tol=1e-14, maxiter=3000)
+    assert err(x64) <= 1e-12, err(x64)
+
+
+def test_uneven_helmholtz_large_n_against_oracle():
+    from jaxfun_gb300.la.helmholtz import UnevenHelmholtzSolver
+
+    rng = np.random.default_rng(5)
+    Ns = np.array([256, 512, 256])
+    alphas = np.array([0.0, 37.5, 12.0])
+    rhs = [O.forcing_coeffs(rng, n_, 2)[: n_ - 2, : n_ - 2] for n_ in Ns]
+    S = UnevenHelmholtzSolver("chebyshev", Ns, alphas)
+    stream = torch.cuda.Stream()
+    with torch.cuda.stream(stream):
+        xs, refs = S.solve(rhs, tol=1e-12)
+    torch.cuda.synchronize()
+    facs = {}
+    for b_, n_ in enumerate(Ns):
+        if n_ not in facs:
+            Vo = O.Space1D("chebyshev", int(n_), True)
+            K, M = Vo.stiffness_matrix(), Vo.mass_matrix()
+            facs[n_] = (K, M, *O.fd_factor_general(K, M))
+        K, M, lam, W, E = facs[n_]
+        a2 = alphas[b_] ** 2
+        terms = [(a2, [M, M]), (1.0, [K, M]), (1.0, [M, K])]
+        ref = O.fd_solve(rhs[b_], [W, W], [E, E], [lam, lam], c0=a2)
+        for _ in range(3):  # FP64 refinement with the oracle's dense residual
+            r = rhs[b_] - O.tp_apply(terms, ref)
+            ref = ref + O.fd_solve(r, [W, W], [E, E], [lam, lam], c0=a2)
+        res = np.linalg.norm(rhs[b_] - O.tp_apply(terms, ref)) / np.linalg.norm(rhs[b_])
+        assert res < 1e-13, (n_, res)
+        x = xs[b_].cpu().numpy()
+        assert np.abs(x - ref).max() <= 1e-10 * np.abs(ref).max(), (n_, refs[b_])
