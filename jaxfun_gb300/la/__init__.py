@@ -17,4 +17,4 @@ from .varcoef import (  # noqa: F401
     pcg,
     poisson_tpmatrices,
 )
-from .wavenumber import TPMatricesWavenumberSolver  # noqa: F401
+from .wavenumber import DiaMatrix, TPMatricesWavenumberSolver  # noqa: F401

@@ -12,6 +12,8 @@ the reference's transposes.
 
 from __future__ import annotations
 
+from dataclasses import dataclass
+
 import numpy as np
 import torch
 
@@ -19,14 +21,84 @@ from .. import _lib
 from ..device import as_device
 
 
+@dataclass(frozen=True)
+class DiaMatrix:
+    """Square banded matrix in jaxfun's column-aligned DIA storage
+    (src/jaxfun/la/diamatrix.py:100-160): ``data[d][j] = A[j - offsets[d]][j]``
+    (upper diagonals start at column ``off``, lower ones at column 0), shape
+    ``(n_diags, n)``.  A host-side container for the per-wavenumber systems."""
+
+    data: np.ndarray
+    offsets: tuple[int, ...]
+
+    @staticmethod
+    def from_dense(a, offsets: tuple[int, ...]) -> "DiaMatrix":
+        a = np.asarray(a, dtype=np.float64)
+        n = a.shape[0]
+        if a.shape != (n, n):
+            raise ValueError("DiaMatrix.from_dense needs a square matrix")
+        data = np.zeros((len(offsets), n))
+        for d, off in enumerate(offsets):
+            j = np.arange(max(0, off), min(n, n + off))
+            data[d, j] = a[j - off, j]
+        return DiaMatrix(data, tuple(int(o) for o in offsets))
+
+    @property
+    def shape(self) -> tuple[int, int]:
+        n = self.data.shape[1]
+        return (n, n)
+
+    def todense(self) -> np.ndarray:
+        n = self.data.shape[1]
+        a = np.zeros((n, n))
+        for d, off in enumerate(self.offsets):
+            j = np.arange(max(0, off), min(n, n + off))
+            a[j - off, j] = self.data[d, j]
+        return a
+
+
+def _stack_dia(B_matrices) -> tuple[np.ndarray, tuple[int, ...]]:
+    """Per-wavenumber DIA matrices (objects with ``data`` and ``offsets``, or
+    ``(data, offsets)`` pairs) aligned on the union of their offsets:
+    (n_F, n_diags, n_P) band data, the legacy ``B_matrices`` input of the
+    reference (src/jaxfun/la/tpmatrix.py:823-845)."""
+    mats = []
+    for B in B_matrices:
+        data, offs = (B.data, B.offsets) if hasattr(B, "offsets") else B
+        data = np.asarray(data.cpu() if torch.is_tensor(data) else data, dtype=np.float64)
+        offs = tuple(int(o) for o in offs)
+        if data.ndim != 2 or data.shape[0] != len(offs):
+            raise ValueError("each B matrix needs data of shape (len(offsets), n)")
+        mats.append((data, offs))
+    if not mats:
+        raise ValueError("B_matrices is empty")
+    n_P = mats[0][0].shape[1]
+    if any(d.shape[1] != n_P for d, _ in mats):
+        raise ValueError("all B matrices must have the same size")
+    union = tuple(sorted({o for _, offs in mats for o in offs}))
+    out = np.zeros((len(mats), len(union), n_P))
+    for k, (data, offs) in enumerate(mats):
+        for d, o in enumerate(offs):
+            out[k, union.index(o)] += data[d]
+    return out, union
+
+
 class TPMatricesWavenumberSolver:
     """``B_data_batch`` (n_F, n_diags, n_P): the per-wavenumber band data in
     jaxfun's column-aligned DIA convention (data[k][d][j] = B_k[j - off_d][j]),
     wavenumbers in C order over the Fourier axes of ``shape``; ``poly_offsets``
-    the diagonal offsets; ``poly_axis`` the polynomial axis of ``shape``."""
+    the diagonal offsets; ``poly_axis`` the polynomial axis of ``shape``.
+    Alternatively ``B_matrices``: one DIA matrix per wavenumber (``DiaMatrix``
+    or any object with ``data`` and ``offsets``), stacked on the union of
+    their offsets and factored by the same batched kernel.  The argument
+    order is the reference's (src/jaxfun/la/tpmatrix.py:718-725)."""
 
-    def __init__(self, poly_axis: int, shape: tuple[int, ...], B_data_batch,
-                 poly_offsets: tuple[int, ...]):
+    def __init__(self, poly_axis: int, shape: tuple[int, ...], B_matrices=None,
+                 B_data_batch=None, poly_offsets: tuple[int, ...] | None = None):
+        if B_data_batch is None or poly_offsets is None:
+            if B_matrices is None:
+                raise ValueError("either B_data_batch + poly_offsets or B_matrices is required")
+            B_data_batch, poly_offsets = _stack_dia(B_matrices)
         self.poly_axis = int(poly_axis)
         self.shape = tuple(int(s) for s in shape)
         nd = len(self.shape)

@@ -29,7 +29,7 @@ def _check(shape, poly_axis, offsets, seed):
     n_P = shape[poly_axis]
     data = _random_band(rng, n_F, n_P, offsets)
     rhs = rng.standard_normal(shape)
-    S = TPMatricesWavenumberSolver(poly_axis, shape, data, offsets)
+    S = TPMatricesWavenumberSolver(poly_axis, shape, B_data_batch=data, poly_offsets=offsets)
     x = S.solve(rhs).cpu().numpy()
     order = fourier + [poly_axis]
     rhs_2d = np.transpose(rhs, order).reshape(n_F, n_P)
@@ -64,8 +64,38 @@ def test_fourier_legendre_helmholtz():
                 if 0 <= i < n:
                     data[kk, d, j] = B[i, j]
     rhs = np.random.default_rng(3).standard_normal((nk, n))
-    S = TPMatricesWavenumberSolver(1, (nk, n), data, offsets)
+    S = TPMatricesWavenumberSolver(1, (nk, n), B_data_batch=data, poly_offsets=offsets)
     x = S.solve(torch.as_tensor(rhs)).cpu().numpy()
     for kk in range(nk):
         ref = np.linalg.solve(k2[kk] * M + K, rhs[kk])
         assert np.abs(x[kk] - ref).max() <= 1e-12 * np.abs(ref).max()
+
+
+def test_b_matrices_constructor_matches_batched_data():
+    """The reference's legacy constructor (one DIA matrix per wavenumber, with
+    differing offset sets) gives the same solution as the batched band data and
+    as the dense solve of each system."""
+    from jaxfun_gb300.la import DiaMatrix
+
+    rng = np.random.default_rng(17)
+    nk, n = 9, 31
+    dense, mats = [], []
+    for kk in range(nk):
+        offs = (-2, 0, 2) if kk % 2 == 0 else (-1, 0, 1, 3)
+        A = np.zeros((n, n))
+        for o in offs:
+            A += np.diag(rng.standard_normal(n - abs(o)), o)
+        A += np.diag(2.0 * len(offs) + np.abs(rng.standard_normal(n)))
+        dense.append(A)
+        mats.append(DiaMatrix.from_dense(A, offs))
+        assert np.array_equal(mats[-1].todense(), A)
+    rhs = rng.standard_normal((nk, n))
+    x = TPMatricesWavenumberSolver(1, (nk, n), B_matrices=mats).solve(rhs).cpu().numpy()
+    union = (-2, -1, 0, 1, 2, 3)
+    data = np.stack([DiaMatrix.from_dense(A, union).data for A in dense])
+    xb = TPMatricesWavenumberSolver(1, (nk, n), B_data_batch=data,
+                                    poly_offsets=union).solve(rhs).cpu().numpy()
+    for kk in range(nk):
+        ref = np.linalg.solve(dense[kk], rhs[kk])
+        assert np.abs(x[kk] - ref).max() <= 1e-12 * np.abs(ref).max()
+    assert np.abs(x - xb).max() <= 1e-14 * np.abs(xb).max()
