@@ -193,6 +193,18 @@ void jfg_split_tf32_host(size_t n, const double* src, float* hi, float* lo);
 /* Reads and clears the device status word the tensor-core kernels set when a
  * bounded wait expires (JFG_OK or JFG_ERR_DEVICE_TIMEOUT); synchronous. */
 int jfg_device_status(void);
+/* Testing the bounded waits (no counterpart in the reference).  Budget of
+ * every pipeline wait of the tcgen05 contraction kernels in ns (0 restores
+ * the default 2 s); waits that drain the kernel's own copies and MMAs after
+ * a timeout keep the default.  Affects launches made after the call. */
+int jfg_tc_set_wait_budget_ns(unsigned long long ns);
+/* Test hook (1 on, 0 off): the epilogue warps of the tcgen05 contraction
+ * first wait on a barrier that nothing arrives on, so that wait runs out
+ * after the wait budget, JFG_ERR_DEVICE_TIMEOUT is recorded for
+ * jfg_device_status(), every other role's waits run out in turn and the
+ * kernel drains its copies and MMAs, frees its TMEM and returns.  The output
+ * of such a launch is not written completely. */
+int jfg_tc_test_hold(int on);
 
 /* ---- TensorProductSpace transforms -------------------------------------
  * out[b] = (x_ax mats[ax]) in[b]: mats[ax] is rows[ax] x cols[ax] row-major,
@@ -336,16 +348,18 @@ int jfg_helmholtz_solve_grouped(int family, int ngroups, const int* n, const int
 
 /*
  * jfg_fd_solve_f64 without a workspace argument: for callers that cannot
- * allocate device memory where they solve (inside CUDA-graph capture, inside
- * a host runtime that owns all device memory and offers no workspace, in a
- * loop that must not block on an allocator).  No counterpart in the
+ * allocate device memory where they solve (inside a host runtime that owns
+ * all device memory and offers no workspace, in a loop that must not block on
+ * an allocator).  No counterpart in the
  * reference.  Scratch comes from a fixed 32 MiB device array inside the
  * library (jfg_fd_solve_noalloc_max_bytes()); every GPU that loads the library
  * holds it until exit.  A call whose scratch need (jfg_fd_solve_workspace_size)
  * exceeds it returns JFG_ERR_WORKSPACE and launches nothing.  All calls share
  * the array: calls whose kernels overlap on the GPU race; calls ordered on one
  * stream are safe.  The first call on a device resolves the array's device
- * address (with that device current); make it outside stream capture.
+ * address (with that device current) and caches it for the life of the
+ * process; make it before any stream capture, and do not call again on a
+ * device after cudaDeviceReset (the cached address is then stale).
  * Allocates nothing (no cudaMalloc/cudaFree, no allocating library call).
  */
 size_t jfg_fd_solve_noalloc_max_bytes(void);

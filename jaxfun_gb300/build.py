@@ -80,7 +80,47 @@ def build(force: bool = False, verbose: bool = False) -> Path:
     if r.returncode != 0:
         raise RuntimeError(f"link failed:\n{r.stdout}\n{r.stderr}")
     os.replace(tmp, lib)
+    build_xla_ffi(nvcc, lib, verbose)
     return lib
+
+
+def xla_include_dir() -> Path | None:
+    """Directory holding xla/ffi/api/ffi.h: JFG_XLA_INCLUDE, else jaxlib's own
+    include directory (jax.ffi.include_dir()) when JAX is installed."""
+    cands = []
+    if os.environ.get("JFG_XLA_INCLUDE"):
+        cands.append(Path(os.environ["JFG_XLA_INCLUDE"]))
+    import importlib.util
+
+    if importlib.util.find_spec("jax") is not None:
+        r = subprocess.run([sys.executable, "-c", "import jax.ffi; print(jax.ffi.include_dir())"],
+                           capture_output=True, text=True)
+        if r.returncode == 0 and r.stdout.strip():
+            cands.append(Path(r.stdout.strip()))
+    for c in cands:
+        if (c / "xla" / "ffi" / "api" / "ffi.h").exists():
+            return c
+    return None
+
+
+def build_xla_ffi(nvcc: str, lib: Path, verbose: bool = False) -> Path | None:
+    """Compile the XLA FFI handlers (ffi/jfg_xla.cc) into _lib/libjfg_xla.so,
+    linked against the C-ABI library, when XLA's FFI header is available;
+    returns None (and builds nothing) otherwise."""
+    inc = xla_include_dir()
+    if inc is None:
+        return None
+    src = PKG / "ffi" / "jfg_xla.cc"
+    out = OUTDIR / "libjfg_xla.so"
+    cmd = [nvcc, "-x", "c++", "-std=c++17", "-O2", "-Xcompiler", "-fPIC", "-shared",
+           "-I", str(INCLUDE), "-I", str(inc), str(src), "-o", str(out),
+           "-L", str(OUTDIR), "-ljaxfun_gb300", "-lcudart", "-Xlinker", "-rpath=$ORIGIN"]
+    if verbose:
+        print(" ".join(cmd), flush=True)
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError(f"nvcc failed for {src.name}:\n{r.stdout}\n{r.stderr}")
+    return out
 
 
 if __name__ == "__main__":

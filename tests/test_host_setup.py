@@ -143,3 +143,26 @@ def test_tpmatrices_solve_signature():
         A.solve(np.zeros((2, 2)), kron_method="cholesky")
     with pytest.raises(ValueError):
         A.solve(np.zeros((2, 2)), method="qr")
+
+
+def test_xla_ffi_handlers_declared_and_build_is_optional():
+    """The jax.ffi handler source defines one handler symbol per registered
+    target, the Python binding imports without JAX, and the build step skips
+    the handlers cleanly when XLA's FFI header is absent."""
+    import re
+    from pathlib import Path
+
+    from jaxfun_gb300 import build, ffi
+
+    src = (Path(ffi.__file__).parent / "jfg_xla.cc").read_text()
+    defined = set(re.findall(r"XLA_FFI_DEFINE_HANDLER_SYMBOL\((\w+),", src))
+    assert defined == set(ffi.TARGETS.values())
+    for entry in ("jfg_tp_apply_f64", "jfg_fd_solve_f64", "jfg_varcoef_apply_f64",
+                  "jfg_pcg_varcoef_f64"):
+        assert entry + "(" in src
+    import importlib.util
+    import os
+
+    if importlib.util.find_spec("jax") is None and not os.environ.get("JFG_XLA_INCLUDE"):
+        assert build.xla_include_dir() is None
+        assert build.build_xla_ffi("nvcc", build.OUTDIR / build.LIBNAME) is None
