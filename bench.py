@@ -31,9 +31,10 @@ sys.path.insert(0, ROOT)
 
 METRIC = "var-coef solves/s at 1e-10 err: learned+mixed vs plain FP64 PCG, 1 GB300"
 N_GRID = 256
-# DRAM bytes (read + write) of one k_contract_tc launch at M = 512, P = K = 256,
-# 128 problems, from ncu (dram__bytes_read.sum + dram__bytes_write.sum).
-TC_TRAFFIC_PER_LAUNCH_B128 = 34.681088e6 + 9.693184e6
+# DRAM bytes (read + write) of one scaled split-FP16 k_contract_tc launch at
+# M = 512, P = K = 256, 128 problems, from ncu (dram__bytes_read.sum +
+# dram__bytes_write.sum); None until captured.
+TC_TRAFFIC_PER_LAUNCH_B128 = None
 
 
 def peaks():
@@ -210,12 +211,15 @@ def run_reference(args):
 # ---------------------------------------------------------------------------
 
 
-def roofline_microbench(B: int, N: int, reps: int = 20, M: int | None = None):
-    """Time the dominant kernel -- the tcgen05 split-TF32 contraction at the
-    first variable-coefficient pass shape of the inner solve (stacked [B; D]
+def roofline_microbench(B: int, N: int, reps: int = 20, M: int | None = None,
+                        prec: str = "f16x3"):
+    """Time the dominant kernel -- the tcgen05 contraction at the first
+    variable-coefficient pass shape of the inner solve (stacked [B; D]
     operator: M = 2N quadrature rows, P = K = N padded coefficients, B problems;
     M = N gives the preconditioner pass) -- with CUDA events on its launch
-    stream.  Returns achieved numbers; FLOPs count each contraction once."""
+    stream.  prec "f16x3": scaled split FP16 (kind::f16, the inner solve's
+    operator passes); "tf32": split TF32 (kind::tf32).  Returns achieved
+    numbers; FLOPs count each contraction once."""
     import numpy as np
     import torch
 
@@ -226,14 +230,30 @@ def roofline_microbench(B: int, N: int, reps: int = 20, M: int | None = None):
     P = K = N
     M = 2 * N if M is None else M
     rng = np.random.default_rng(0)
-    hi, lo = split_tf32(rng.standard_normal((M, K)))
+    op = rng.standard_normal((M, K))
     x = torch.randn(B, P, K, dtype=torch.float32, device="cuda")
     y = torch.empty(B, M, P, dtype=torch.float32, device="cuda")
     d = _lib.ContractDesc(batch=B, nseg=1, M=M, P=P, K=K, op_ld=K, in_ld=K, in_batch=P * K,
                           out_ld=P, out_batch=M * P, alpha=1.0, beta=0.0)
     s = torch.cuda.current_stream()
-    call = lambda: L.jfg_contract_tc(d, hi.data_ptr(), lo.data_ptr(), x.data_ptr(),  # noqa: E731
-                                     y.data_ptr(), s.cuda_stream)
+    if prec == "f16x3":
+        hi = np.empty((M, K), np.uint16)
+        lo = np.empty((M, K), np.uint16)
+        inv = np.empty(M, np.float32)
+        L.jfg_split_f16_rowscaled_host(M, K, op.ctypes.data, hi.ctypes.data, lo.ctypes.data,
+                                       inv.ctypes.data)
+        t_hi = torch.as_tensor(hi.view(np.int16), device="cuda")
+        t_lo = torch.as_tensor(lo.view(np.int16), device="cuda")
+        t_inv = torch.as_tensor(inv, device="cuda")
+        in_max = x.abs().amax(dim=(1, 2)).contiguous().view(torch.int32)
+        out_max = torch.zeros(B, dtype=torch.int32, device="cuda")
+        call = lambda: L.jfg_contract_tc_f16x3(  # noqa: E731
+            d, t_hi.data_ptr(), t_lo.data_ptr(), t_inv.data_ptr(), M, in_max.data_ptr(),
+            out_max.data_ptr(), x.data_ptr(), y.data_ptr(), s.cuda_stream)
+    else:
+        hi, lo = split_tf32(op)
+        call = lambda: L.jfg_contract_tc(d, hi.data_ptr(), lo.data_ptr(),  # noqa: E731
+                                         x.data_ptr(), y.data_ptr(), s.cuda_stream)
     for _ in range(3):
         _lib.check(call(), "contract_tc")
     e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -246,7 +266,7 @@ def roofline_microbench(B: int, N: int, reps: int = 20, M: int | None = None):
     t = e0.elapsed_time(e1) / 1e3 / reps
     flops = 2.0 * M * P * K * B
     nbytes = 4.0 * B * P * (K + M)
-    return {"M": M, "P": P, "K": K, "t": t, "flops": flops, "bytes": nbytes,
+    return {"M": M, "P": P, "K": K, "t": t, "flops": flops, "bytes": nbytes, "prec": prec,
             "tflops_alg": flops / t / 1e12,
             "tflops_issued": 3 * flops / t / 1e12, "gbs": nbytes / t / 1e9}
 
@@ -942,6 +962,14 @@ def run_ours(args):
     value = replicas.throughput(B * args.steps, world, t)
     its_in, its_out = np.array(it_in[:]), np.array(it_out[:])
     dev_status = int(L.jfg_device_status())
+    if args.profile:
+        # profiling run (launch lists): the setup, warm-up and timed solves only
+        if rank == 0:
+            print(json.dumps({"profile": "varcoef2d", "batch": B, "steps": args.steps,
+                              "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
+                              "launches_timed": launches, "device_status": dev_status}),
+                  flush=True)
+        return 0
     x_learned = x.clone()
 
     # ---- the same mixed solve from a zero start (what the learned guess gains)
@@ -1034,8 +1062,10 @@ def run_ours(args):
     pk, pk_kind = peaks()
     with torch.cuda.stream(stream):
         rf = roofline_microbench(B, N)
+        rf32 = roofline_microbench(B, N, prec="tf32")
+    f16_peak = pk["bf16_tflops"]           # dense FP16 rate = dense BF16 rate
     tf32_peak = pk["bf16_tflops"] / 2.0
-    t_tensor = rf["flops"] / (tf32_peak * 1e12)
+    t_tensor = rf["flops"] / (f16_peak * 1e12)
     t_hbm = rf["bytes"] / (pk["hbm_gbs"] * 1e9)
     hbm_bound = t_hbm >= t_tensor
     tr = None
@@ -1066,31 +1096,34 @@ def run_ours(args):
     if rank == 0:
         rl = {"bound": "hbm" if hbm_bound else "tensor",
               "achieved": rf["gbs"] if hbm_bound else rf["tflops_alg"],
-              "peak": pk["hbm_gbs"] if hbm_bound else tf32_peak,
+              "peak": pk["hbm_gbs"] if hbm_bound else f16_peak,
               "unit": "GB/s" if hbm_bound else "TFLOP/s",
               "frac": max(t_tensor, t_hbm) / rf["t"],
               "traffic": (None if TC_TRAFFIC_PER_LAUNCH_B128 is None
                           else TC_TRAFFIC_PER_LAUNCH_B128 * B / 128),
               "traffic_source": "ncu dram__bytes_read.sum + dram__bytes_write.sum of one launch "
                                 "at this shape with 128 problems, scaled by problems per launch",
-              "kernel": "k_contract_tc (tcgen05 kind::tf32, 3 MMAs per K block)",
+              "kernel": "k_contract_tc<..., PREC=2> (tcgen05 kind::f16, scaled split FP16: "
+                        "3 MMAs per K step)",
               "launch_M": rf["M"], "launch_P": rf["P"], "launch_K": rf["K"], "launch_batch": B,
               "launch_us": 1e6 * rf["t"], "flops_per_launch": rf["flops"],
               "bytes_per_launch": rf["bytes"],
               "roofline_us": 1e6 * max(t_tensor, t_hbm),
               "tensor_term_us": 1e6 * t_tensor, "hbm_term_us": 1e6 * t_hbm,
               "tflops_algorithmic": rf["tflops_alg"], "hbm_gbs_algorithmic": rf["gbs"],
-              "tensor_frac_tf32": t_tensor / rf["t"],
-              "tensor_frac_bf16_rate": rf["flops"] / (pk["bf16_tflops"] * 1e12) / rf["t"],
+              "tensor_frac": t_tensor / rf["t"],
               "issued_tflops": rf["tflops_issued"],
-              "issued_frac_tf32": rf["tflops_issued"] / tf32_peak,
+              "issued_frac": rf["tflops_issued"] / f16_peak,
               "hbm_frac": t_hbm / rf["t"],
-              "peak_kind": f"{pk_kind}: HBM copy GB/s; tensor = bf16 burst / 2 (dense TF32 rate, "
-                           "no measured TF32 figure)"}
+              "tf32_variant_us": 1e6 * rf32["t"],
+              "tf32_variant_frac": max(rf32["flops"] / (tf32_peak * 1e12), t_hbm) / rf32["t"],
+              "peak_kind": f"{pk_kind}: HBM copy GB/s; tensor = bf16 burst (dense FP16 rate; "
+                           "the split-TF32 variant against bf16 burst / 2)"}
         cfg = {"workload": "varcoef-poisson-2d-legendre-N256", "N": N, "batch": B,
                "path": ("learned guess (BF16 tcgen05 spectral neural operator) + "
                         if model is not None else "") +
-                       "mixed: tcgen05 split-TF32 PCG + FP64 refinement",
+                       "mixed: tcgen05 PCG (scaled split-FP16 operator, split-BF16 "
+                       "preconditioner) + FP64 refinement",
                "tol_relres": args.tol, "inner_tol": args.inner_tol,
                "inner_iterations_mean": float(its_in.mean()),
                "outer_iterations_mean": float(its_out.mean()),
@@ -1118,7 +1151,7 @@ def run_ours(args):
             "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
             "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
-            "dtype": "f32/tf32x3+f64",
+            "dtype": "f32/f16x3+bf16x3+f64",
             "data": "synthetic (seeded; kappa=exp(GRF), config-3 recipe)",
             "config": cfg,
             "e2e": {"value": world * B * e2e_steps / t_e2e, "unit": "solves/s",
@@ -1145,7 +1178,7 @@ def main():
     # <= 1e-10 max relative error against a tight FP64 solve (checked below)
     ap.add_argument("--tol", type=float, default=1e-11, help="outer relative residual")
     ap.add_argument("--inner-tol", type=float, default=1e-5)
-    ap.add_argument("--fp64-tol", type=float, default=2e-11)
+    ap.add_argument("--fp64-tol", type=float, default=5e-12)
     ap.add_argument("--fp64-batch", type=int, default=128)
     ap.add_argument("--fp64-steps", type=int, default=1)
     ap.add_argument("--skip-transforms", action="store_true",
@@ -1153,13 +1186,18 @@ def main():
     ap.add_argument("--maxiter", type=int, default=1000)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--profile", action="store_true",
+                    help="stop after the timed solves (for ncu launch lists of the headline)")
     ap.add_argument("--no-learned", action="store_true", help="mixed solve from a zero start")
     ap.add_argument("--weights", default=os.path.join(
         ROOT, "jaxfun_gb300", "sno", "weights", "sno_varcoef2d_N256.npz"))
     ap.add_argument("--kernel-only", nargs="?", const="contract", default=None,
-                    choices=["contract", "gemm", "fp64", "df64", "transform", "transform_tf32"],
+                    choices=["contract", "contract_tf32", "gemm", "fp64", "df64", "transform",
+                             "transform_tf32"],
                     help="time one kernel and print its numbers (used for ncu captures): "
-                         "contract = tcgen05 split-TF32 contraction, B problems of 256^3; "
+                         "contract = tcgen05 scaled split-FP16 contraction at the variable-"
+                         "coefficient pass shape (M = 512, P = K = 256), B problems; "
+                         "contract_tf32 = its split-TF32 variant; "
                          "gemm = BF16 GEMM of the neural operator's spectral transform "
                          "(1024 x 64 x 4096 per sample, B samples); fp64 = FP64 CUDA-core "
                          "contraction at the variable-coefficient pass shape; df64 = the same "
@@ -1198,8 +1236,10 @@ def main():
         import torch
 
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-        if args.kernel_only == "contract":
-            out = {"kernel": "k_contract_tc", **roofline_microbench(args.batch, N_GRID, reps=3)}
+        if args.kernel_only in ("contract", "contract_tf32"):
+            prec = "tf32" if args.kernel_only == "contract_tf32" else "f16x3"
+            out = {"kernel": "k_contract_tc",
+                   **roofline_microbench(args.batch, N_GRID, reps=3, prec=prec)}
         else:
             out = other_kernel_microbench(args.kernel_only, args.batch)
         print(json.dumps({"batch": args.batch, **out}), flush=True)

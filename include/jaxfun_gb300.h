@@ -147,6 +147,25 @@ int jfg_contract_tc_bf16x3(const jfg_contract_desc* d, const uint16_t* op_hi,
 /* Split n FP64 values into BF16 hi (round to nearest even) and lo = x - hi
  * rounded to BF16 (host arrays of BF16 bit patterns). */
 void jfg_split_bf16_host(size_t n, const double* src, uint16_t* hi, uint16_t* lo);
+/* The same contraction in scaled split FP16 (kind::f16 with FP16 operands,
+ * three MMAs per product at the BF16 rate, ~2^-22 relative to each row's
+ * maximum like split TF32).  The operator is FP16 (hi, lo), each row m of
+ * segment s scaled by a power of two (jfg_split_f16_rowscaled_host), with the
+ * inverse scales at op_inv[s * op_inv_seg + m].  The input of problem b is
+ * scaled in the kernel by the power of two that puts in_max[b] -- the float
+ * bits of an upper bound on max |in[b]| -- in [2^14, 2^15) (a bound 0 means
+ * no scaling; inputs beyond 65504 / 2 then overflow).  out_max (may be NULL)
+ * receives, by atomicMax on the float bits, max |out[b]| of every written
+ * problem; clear it before the call.  op_ld, op_seg % 8 == 0. */
+int jfg_contract_tc_f16x3(const jfg_contract_desc* d, const uint16_t* op_hi,
+                          const uint16_t* op_lo, const float* op_inv, long long op_inv_seg,
+                          const unsigned* in_max, unsigned* out_max, const float* in,
+                          float* out, void* stream);
+/* rows x cols FP64 matrix -> FP16 hi / lo bit patterns with each row scaled
+ * by the power of two that puts its max |entry| in [2^14, 2^15); inv[r] is
+ * the inverse scale of row r.  Host arrays. */
+void jfg_split_f16_rowscaled_host(size_t rows, size_t cols, const double* src, uint16_t* hi,
+                                  uint16_t* lo, float* inv);
 /* Kernel variant of jfg_contract_tc: 1 (default) keeps the split input tile
  * (MMA operand A) in TMEM, written by the split warps with tcgen05.st, so the
  * MMAs read only operand B from shared memory; 0 keeps A in shared memory. */
@@ -499,7 +518,27 @@ typedef struct {
   const uint16_t* E_lo16;
   const uint16_t* W_hi16;
   const uint16_t* W_lo16;
+  int apply_f16;         /* 1 (2-D only): the inner operator passes run as scaled
+                            split FP16 (jfg_split_f16_rows_host of the packed padded
+                            operators, rows scaled by powers of two; the inputs of
+                            each pass scaled per problem from a recorded max |x|):
+                            the accuracy of split TF32 at the BF16 rate.  0: split
+                            TF32 (ops_hi, ops_lo)                                   */
+  const uint16_t* ops_hi16;  /* FP16 hi of the row-scaled packed padded operators   */
+  const uint16_t* ops_lo16;  /* FP16 lo                                             */
+  const float* ops_inv16;    /* inverse row scales, jfg_varcoef_f16_rows(n, nq) of them:
+                                [B;D] 2nq | D, B 2nq | B^T, D^T 2n | [D^T|B^T] n     */
 } jfg_mixed_plan;
+
+/* Rows of the 2-D packed operator set (jfg_varcoef_pack_ops_host(2, n, nq))
+ * in the order their inverse scales are stored: 4 nq + 3 n. */
+size_t jfg_varcoef_f16_rows(int n, int nq);
+/* Split the 2-D packed operators (FP64, jfg_varcoef_pack_ops_host layout)
+ * into FP16 hi / lo bit patterns, each operator row scaled by the power of
+ * two that puts its max |entry| in [2^14, 2^15); inv receives the inverse
+ * scales (jfg_varcoef_f16_rows(n, nq) floats).  Host arrays. */
+void jfg_split_f16_rows_host(int n, int nq, const double* ops, uint16_t* hi, uint16_t* lo,
+                             float* inv);
 
 size_t jfg_pcg_mixed_workspace_size(int ndim, int n, int nq, int batch);
 int jfg_pcg_varcoef_mixed(const jfg_mixed_plan* plan, const double* rhs, double* x, int use_x0,

@@ -125,6 +125,11 @@ SIGNATURES = {
     "jfg_fd_solve_noalloc_max_bytes": (_sz, []),
     "jfg_fd_solve_f64_noalloc": (_i, [_i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "jfg_varcoef_ops_count": (_sz, [_i, _i, _i]),
+    "jfg_varcoef_f16_rows": (_sz, [_i, _i]),
+    "jfg_split_f16_rows_host": (None, [_i, _i, _vp, _vp, _vp, _vp]),
+    "jfg_split_f16_rowscaled_host": (None, [_sz, _sz, _vp, _vp, _vp, _vp]),
+    "jfg_contract_tc_f16x3": (_i, [C.POINTER(ContractDesc), _vp, _vp, _vp, C.c_longlong, _vp, _vp,
+                                   _vp, _vp, _vp]),
     "jfg_varcoef_pack_ops_host": (None, [_i, _i, _i, _vp, _vp, _vp]),
     "jfg_varcoef_workspace_size": (_sz, [_i, _i, _i, _i, _i]),
     "jfg_varcoef_apply_f64": (_i, [_i, _i, _i, _i, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),

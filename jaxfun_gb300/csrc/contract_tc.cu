@@ -24,6 +24,7 @@
 // kernel records JFG_ERR_DEVICE_TIMEOUT in a device status word, drains its own
 // TMA copies (bounded), frees its TMEM and returns.
 #include <cuda.h>
+#include <cuda_fp16.h>
 #include <stdio.h>
 #include <string.h>
 
@@ -74,6 +75,13 @@ struct TcGroup {
   int seg_op_map;  // 1 if the operator maps have a segment dimension
   int mc_inner;    // tile order: operator chunks innermost (inputs beyond L2)
   int tma_store;   // epilogue stores 32 x 32 boxes through shared memory with TMA
+  // scaled split-FP16 variant: per-problem max |input| (float bits) that sets
+  // the power-of-two input scale, per-problem max |output| recorded for the
+  // next pass, and the inverse power-of-two row scales of the operator
+  const unsigned* in_max;
+  unsigned* out_max;
+  const float* op_inv;  // op_inv[s * op_inv_seg + m]
+  long long op_inv_seg;
 };
 
 // Kernel parameter block (__grid_constant__): groups and their tensor maps
@@ -240,6 +248,40 @@ __device__ __forceinline__ uint32_t pack_bf16x2(float a, float b) {
   return d;
 }
 
+// Two FP32 -> packed FP16 pair (round to nearest even): lo16 <- a, hi16 <- b.
+__device__ __forceinline__ uint32_t pack_f16x2(float a, float b) {
+  uint32_t d;
+  asm("cvt.rn.f16x2.f32 %0, %1, %2;" : "=r"(d) : "f"(b), "f"(a));
+  return d;
+}
+
+__device__ __forceinline__ float2 unpack_f16x2(uint32_t h) {
+  return __half22float2(*reinterpret_cast<const __half2*>(&h));
+}
+
+// Instruction descriptor: kind::f16 with FP16 A/B, D = F32, both K-major.
+__host__ __device__ constexpr uint32_t idesc_f16(int M, int N) {
+  return (1u << 4) | ((uint32_t)(N >> 3) << 17) | ((uint32_t)(M >> 4) << 24);
+}
+
+// Power-of-two input scale of the split-FP16 variant from the float bits of
+// an upper bound on max |x|: the scaled values are below 2^15 (FP16 max is
+// 65504) and the largest is at least 2^14, so FP16 hi and lo keep ~22 bits
+// relative to the maximum and nothing overflows.  Zero, non-finite or
+// missing bounds give scale 1; the exponent is clamped to [2^-126, 2^126]
+// so the inverse is exact as well.
+__device__ __forceinline__ void h16_scale(const unsigned* in_max, int b, float& sc, float& inv) {
+  sc = inv = 1.f;
+  if (!in_max || b < 0) return;
+  const unsigned bits = __ldg(in_max + b) & 0x7FFFFFFFu;
+  const int e = (int)(bits >> 23);
+  if (bits == 0 || e == 0xFF) return;
+  int eb = 268 - e;  // biased exponent of 2^(15 - E), max |x| < 2^E, E = e - 126
+  eb = eb < 1 ? 1 : (eb > 253 ? 253 : eb);
+  sc = __uint_as_float((unsigned)eb << 23);
+  inv = __uint_as_float((unsigned)(254 - eb) << 23);
+}
+
 // Store 32 consecutive 32-bit columns of this thread's TMEM lane.
 __device__ __forceinline__ void tmem_st32(uint32_t taddr, const uint32_t* v) {
   asm volatile(
@@ -289,9 +331,13 @@ __device__ __forceinline__ float tf32_hi(float x) {
 // accumulator buffers let the epilogue of tile i overlap the main loop of
 // tile i+1.  The tile prefix tb[] is formed on the device from the active
 // counts, so listed (active-subset) groups need no host round trip.
-template <int EPI, bool BETA, int G, bool B16>
+template <int EPI, bool BETA, int G, int PREC>
 __global__ void __launch_bounds__(NTHREADS, 1)
     k_contract_tc(const __grid_constant__ TcLaunch<G> L) {
+  // PREC: 0 split TF32 (kind::tf32), 1 split BF16, 2 scaled split FP16 (both
+  // kind::f16: 16-bit operator pairs, 64-element K blocks)
+  constexpr bool B16 = PREC != 0;
+  constexpr bool H16 = PREC == 2;
   // K elements per block: 32 TF32 (one 128-byte row) or 64 BF16 (one 128-byte
   // operator row; the FP32 input block then takes two TMA boxes)
   constexpr int KE = B16 ? 64 : KB;
@@ -441,8 +487,9 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       for (long long t = blockIdx.x; t < ntiles && ok; t += gridDim.x, ++li) {
         int gi, pt, mc, b, s;
         decode(t, gi, pt, mc, b, s);
-        const uint32_t idesc =
-            B16 ? idesc_b16(TILE_P, L.g[gi].Mtile) : idesc_tf32(TILE_P, L.g[gi].Mtile);
+        const uint32_t idesc = H16   ? idesc_f16(TILE_P, L.g[gi].Mtile)
+                               : B16 ? idesc_b16(TILE_P, L.g[gi].Mtile)
+                                     : idesc_tf32(TILE_P, L.g[gi].Mtile);
         const int nkb = nkb_of(gi);
         const int buf = li & 1;
         const uint32_t use = (uint32_t)(li >> 1);
@@ -513,13 +560,40 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       int gi, pt, mc, b, s;
       decode(t, gi, pt, mc, b, s);
       const int nkb = nkb_of(gi);
+      float xsc = 1.f, xinv = 1.f;
+      if (H16) h16_scale(L.g[gi].in_max, b, xsc, xinv);
       for (int kb = 0; kb < nkb; ++kb, ++g) {
         const int st = (int)(g % S);
         if (!mbar_wait(&full[st], (uint32_t)(g / S) & 1u, budget)) {
           ok = false;
           break;
         }
-        if (B16) {
+        if (H16) {
+          // 64 FP32 of this row, scaled by 2^k, -> FP16 hi / lo pairs
+          uint32_t h[32], l[32];
+#pragma unroll
+          for (int half = 0; half < 2; ++half) {
+            const float4* xr = (const float4*)(Xh(st) + half * XBYTES + row * 128);
+#pragma unroll
+            for (int c = 0; c < 8; ++c) {
+              const float4 v = xr[c ^ (row & 7)];
+              const float a0 = v.x * xsc, a1 = v.y * xsc, a2 = v.z * xsc, a3 = v.w * xsc;
+              const int w = 16 * half + 2 * c;
+              const uint32_t h0 = pack_f16x2(a0, a1), h1 = pack_f16x2(a2, a3);
+              const float2 f0 = unpack_f16x2(h0), f1 = unpack_f16x2(h1);
+              h[w] = h0;
+              h[w + 1] = h1;
+              l[w] = pack_f16x2(a0 - f0.x, a1 - f0.y);
+              l[w + 1] = pack_f16x2(a2 - f1.x, a3 - f1.y);
+            }
+          }
+          const uint32_t tbase = tmem + ((uint32_t)(32 * (warp & 3)) << 16) +
+                                 (uint32_t)(A_COL0 + 64 * st);
+          tmem_st32(tbase, h);
+          tmem_st32(tbase + 32, l);
+          asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
+          asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+        } else if (B16) {
           // 64 FP32 of this row (two swizzled 128-byte rows) -> BF16 hi / lo,
           // packed in pairs (lower k in the lower half) into 32 TMEM columns each
           uint32_t h[32], l[32];
@@ -618,12 +692,18 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       const float* __restrict__ fld = nullptr;
       if (EPI == JFG_EPI_MUL_FIELD)
         fld = (const float*)d.field + (long long)bb * d.field_batch + (long long)s * d.field_seg;
+      float xsc = 1.f, xinv = 1.f, omax = 0.f;
+      const float* __restrict__ oinv = nullptr;
+      if (H16) {
+        h16_scale(q.in_max, b, xsc, xinv);
+        oinv = q.op_inv + (long long)s * q.op_inv_seg;
+      }
       const uint32_t tacc = tmem + ((uint32_t)(32 * q4) << 16) + (uint32_t)buf * acc_stride;
       for (int c = half * 2; c < Mt / 16; c += 4) {
         // columns [c*16, c*16+32): two 16-column TMEM loads
         const int mb = mc * Mt + c * 16;
         const int nj = (c + 1 < Mt / 16) ? 32 : 16;
-        float aux[32], prev[32];
+        float aux[32], prev[32], osc[32];
         if (pin) {
 #pragma unroll
           for (int j = 0; j < 32; ++j) {
@@ -633,6 +713,17 @@ __global__ void __launch_bounds__(NTHREADS, 1)
               aux[j] = ok ? __ldg(fld + (long long)m * d.field_ld + p) : 0.f;
             else if (EPI == JFG_EPI_DIV_EIG)
               aux[j] = ok ? __ldg(lam_m + m) : 1.f;
+            if (H16) {
+              // output scale (operator row and input scale) folded into aux
+              // where the epilogue allows
+              const float sc = ok ? __ldg(oinv + m) * xinv : 0.f;
+              if (EPI == JFG_EPI_DIV_EIG)
+                osc[j] = sc;
+              else if (EPI == JFG_EPI_MUL_FIELD)
+                aux[j] *= sc;
+              else
+                aux[j] = sc;
+            }
             if (BETA) prev[j] = ok ? outS[(long long)m * d.out_ld + p] : 0.f;
           }
         }
@@ -649,9 +740,13 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 #pragma unroll
           for (int j = 0; j < 32; ++j) {
             float r = v[j];  // rows outside the problem are clipped by the store
+            if (H16 && EPI == JFG_EPI_NONE) r *= pin ? aux[j] : 0.f;
+            if (H16 && EPI == JFG_EPI_DIV_EIG) r *= pin ? osc[j] : 0.f;
             if (EPI == JFG_EPI_MUL_FIELD) r *= pin ? aux[j] : 0.f;
             if (EPI == JFG_EPI_DIV_EIG) r = __fdividef(r, c0 + c1 * ((pin ? aux[j] : 1.f) + lp));
-            box[j * 32 + lane] = r * alpha;
+            r *= alpha;
+            if (H16) omax = fmaxf(omax, fabsf(r));
+            box[j * 32 + lane] = r;
           }
           asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
           __syncwarp();
@@ -664,10 +759,13 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             const int m = mb + j;
             if (j < nj && m < d.M) {
               float r = v[j];
+              if (H16 && EPI == JFG_EPI_NONE) r *= aux[j];
+              if (H16 && EPI == JFG_EPI_DIV_EIG) r *= osc[j];
               if (EPI == JFG_EPI_MUL_FIELD) r *= aux[j];
               if (EPI == JFG_EPI_DIV_EIG) r = __fdividef(r, c0 + c1 * (aux[j] + lp));
               r *= alpha;
               if (BETA) r += beta * prev[j];
+              if (H16) omax = fmaxf(omax, fabsf(r));
               outS[(long long)m * d.out_ld + p] = r;
             }
           }
@@ -676,6 +774,13 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
       __syncwarp();
       if (lane == 0) mbar_arrive(&tempty[buf]);
+      if (H16 && q.out_max != nullptr) {
+        // max |output| of this tile for the next pass's input scale (float
+        // bits of non-negative values order like unsigned integers)
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) omax = fmaxf(omax, __shfl_xor_sync(0xffffffffu, omax, o));
+        if (lane == 0 && b >= 0) atomicMax(q.out_max + b, __float_as_uint(omax));
+      }
     }
     // bulk tensor stores of this warp complete before the kernel ends
     if (lane == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
@@ -735,9 +840,12 @@ int setup_kernel_attr() {
   if (!done[dev]) {
     const int mx = SMEM_MAX;
 #define JFG_SET_ATTR(E, B, G)                                                              \
-  JFG_CUDA_TRY(cudaFuncSetAttribute(k_contract_tc<E, B, G, false>,                         \
+  JFG_CUDA_TRY(cudaFuncSetAttribute(k_contract_tc<E, B, G, 0>,                             \
                                     cudaFuncAttributeMaxDynamicSharedMemorySize, mx));     \
-  JFG_CUDA_TRY(cudaFuncSetAttribute(k_contract_tc<E, B, G, true>,                          \
+  JFG_CUDA_TRY(cudaFuncSetAttribute(k_contract_tc<E, B, G, 1>,                             \
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, mx));     \
+  if (G == 1)                                                                              \
+  JFG_CUDA_TRY(cudaFuncSetAttribute(k_contract_tc<E, B, 1, 2>,                             \
                                     cudaFuncAttributeMaxDynamicSharedMemorySize, mx))
 #define JFG_SET_ATTR_G(G)                   \
   JFG_SET_ATTR(JFG_EPI_NONE, false, G);     \
@@ -756,10 +864,12 @@ int setup_kernel_attr() {
 }
 
 // Validate one group and fill its descriptor, tile height and tensor maps.
-// b16: the operator is BF16 (hi, lo) with 64-element K blocks, else TF32 in FP32 words.
+// prec: 0 the operator is TF32 in FP32 words; 1 BF16 (hi, lo) and 2 FP16
+// (hi, lo), both with 64-element K blocks.
 int fill_group(const jfg_contract_desc& d, const void* op_hi, const void* op_lo,
-               const float* in, float* out, TcGroup& q, CUtensorMap* maps, bool b16,
+               const float* in, float* out, TcGroup& q, CUtensorMap* maps, int prec,
                int mt_cap) {
+  const bool b16 = prec != 0;
   JFG_TRY(validate_desc(d));
   if (!op_hi || !op_lo || !in || !out) return JFG_ERR_ARG;
   // TMA: 16-byte aligned bases and strides
@@ -795,8 +905,9 @@ int fill_group(const jfg_contract_desc& d, const void* op_hi, const void* op_lo,
     cuuint64_t str[2] = {(cuuint64_t)d.op_ld * eb,
                          (cuuint64_t)(q.seg_op_map ? d.op_seg : d.op_ld * d.M) * eb};
     cuuint32_t box[3] = {(cuuint32_t)(128 / eb), (cuuint32_t)q.Mtile, 1};
-    const CUtensorMapDataType dt =
-        b16 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+    const CUtensorMapDataType dt = prec == 2   ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16
+                                   : prec == 1 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16
+                                               : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
     JFG_TRY(make_map(&maps[1], op_hi, 3, dims, str, box, dt));
     JFG_TRY(make_map(&maps[2], op_lo, 3, dims, str, box, dt));
   }
@@ -828,10 +939,27 @@ long long group_tiles(const TcGroup& q) {
 }
 
 // One launch over ng <= G groups (same epilogue kind and beta != 0 for all).
+// The scaled split-FP16 kernel exists for single-group launches only.
+template <int E, bool BETA, int G>
+void launch_h16(dim3 grid, size_t smem, cudaStream_t st, const TcLaunch<G>& L) {
+  if constexpr (G == 1) k_contract_tc<E, BETA, 1, 2><<<grid, NTHREADS, smem, st>>>(L);
+}
+
+// h16 (one group only): the scaled split-FP16 auxiliaries of that group.
+struct H16Aux {
+  const unsigned* in_max;
+  unsigned* out_max;
+  const float* op_inv;
+  long long op_inv_seg;
+};
+
 template <int G>
 int launch_groups(int ng, const jfg_contract_desc* const* ds, const void* const* op_hi,
                   const void* const* op_lo, const float* const* in, float* const* out,
-                  const jfg_tc_config& cfg, bool b16, cudaStream_t st) {
+                  const jfg_tc_config& cfg, int prec, cudaStream_t st,
+                  const H16Aux* h16 = nullptr) {
+  const bool b16 = prec != 0;
+  if (prec == 2 && (G != 1 || ng != 1 || !h16 || !h16->op_inv)) return JFG_ERR_ARG;
   static_assert(sizeof(TcLaunch<G>) <= 32000, "kernel parameter block too large");
   TcLaunch<G> L;
   memset(&L, 0, sizeof(L));
@@ -842,8 +970,14 @@ int launch_groups(int ng, const jfg_contract_desc* const* ds, const void* const*
   int mt_max = 16, ostage = 0;
   for (int i = 0; i < ng; ++i) {
     if (ds[i]->epilogue != epi || (ds[i]->beta != 0.0) != hb) return JFG_ERR_ARG;
-    JFG_TRY(fill_group(*ds[i], op_hi[i], op_lo[i], in[i], out[i], L.g[i], L.maps[i], b16,
+    JFG_TRY(fill_group(*ds[i], op_hi[i], op_lo[i], in[i], out[i], L.g[i], L.maps[i], prec,
                        cfg.mtile));
+    if (h16) {
+      L.g[i].in_max = h16->in_max;
+      L.g[i].out_max = h16->out_max;
+      L.g[i].op_inv = h16->op_inv;
+      L.g[i].op_inv_seg = h16->op_inv_seg;
+    }
     if (!g_tma_store) L.g[i].tma_store = 0;
     tiles += group_tiles(L.g[i]);
     if (L.g[i].Mtile > mt_max) mt_max = L.g[i].Mtile;
@@ -870,19 +1004,24 @@ int launch_groups(int ng, const jfg_contract_desc* const* ds, const void* const*
   int ctas = cfg.ctas > 0 && cfg.ctas < nsm ? cfg.ctas : nsm;
   dim3 grid((unsigned)(tiles < ctas ? tiles : ctas));
   JFG_TRY(setup_kernel_attr());
-#define JFG_LAUNCH(E)                                                       \
-  do {                                                                      \
-    if (b16) {                                                              \
-      if (hb)                                                               \
-        k_contract_tc<E, true, G, true><<<grid, NTHREADS, smem, st>>>(L);   \
-      else                                                                  \
-        k_contract_tc<E, false, G, true><<<grid, NTHREADS, smem, st>>>(L);  \
-    } else {                                                                \
-      if (hb)                                                               \
-        k_contract_tc<E, true, G, false><<<grid, NTHREADS, smem, st>>>(L);  \
-      else                                                                  \
-        k_contract_tc<E, false, G, false><<<grid, NTHREADS, smem, st>>>(L); \
-    }                                                                       \
+#define JFG_LAUNCH(E)                                                          \
+  do {                                                                         \
+    if (prec == 2) {                                                           \
+      if (hb)                                                                  \
+        launch_h16<E, true, G>(grid, smem, st, L);                             \
+      else                                                                     \
+        launch_h16<E, false, G>(grid, smem, st, L);                            \
+    } else if (b16) {                                                          \
+      if (hb)                                                                  \
+        k_contract_tc<E, true, G, 1><<<grid, NTHREADS, smem, st>>>(L);         \
+      else                                                                     \
+        k_contract_tc<E, false, G, 1><<<grid, NTHREADS, smem, st>>>(L);        \
+    } else {                                                                   \
+      if (hb)                                                                  \
+        k_contract_tc<E, true, G, 0><<<grid, NTHREADS, smem, st>>>(L);         \
+      else                                                                     \
+        k_contract_tc<E, false, G, 0><<<grid, NTHREADS, smem, st>>>(L);        \
+    }                                                                          \
   } while (0)
   switch (epi) {
     case JFG_EPI_NONE:
@@ -925,7 +1064,7 @@ int contract_tc(const jfg_contract_desc& d, const float* op_hi, const float* op_
   const jfg_contract_desc* dp = &d;
   const void* oh = op_hi;
   const void* ol = op_lo;
-  return launch_groups<1>(1, &dp, &oh, &ol, &in, &out, tc_default_config(), false, st);
+  return launch_groups<1>(1, &dp, &oh, &ol, &in, &out, tc_default_config(), 0, st);
 }
 
 int contract_tc_b16(const jfg_contract_desc& d, const uint16_t* op_hi, const uint16_t* op_lo,
@@ -934,7 +1073,19 @@ int contract_tc_b16(const jfg_contract_desc& d, const uint16_t* op_hi, const uin
   const jfg_contract_desc* dp = &d;
   const void* oh = op_hi;
   const void* ol = op_lo;
-  return launch_groups<1>(1, &dp, &oh, &ol, &in, &out, tc_default_config(), true, st);
+  return launch_groups<1>(1, &dp, &oh, &ol, &in, &out, tc_default_config(), 1, st);
+}
+
+int contract_tc_h16(const jfg_contract_desc& d, const uint16_t* op_hi, const uint16_t* op_lo,
+                    const float* op_inv, long long op_inv_seg, const unsigned* in_max,
+                    unsigned* out_max, const float* in, float* out, cudaStream_t st) {
+  if (d.batch == 0 || d.M == 0 || d.P == 0) return validate_desc(d);
+  if (!op_inv || !in_max) return JFG_ERR_ARG;
+  const jfg_contract_desc* dp = &d;
+  const void* oh = op_hi;
+  const void* ol = op_lo;
+  const H16Aux aux{in_max, out_max, op_inv, op_inv_seg};
+  return launch_groups<1>(1, &dp, &oh, &ol, &in, &out, tc_default_config(), 2, st, &aux);
 }
 
 int contract_tc_grouped(int ng, const jfg_contract_desc* ds, const float* const* op_hi,
@@ -976,9 +1127,9 @@ int contract_tc_grouped(int ng, const jfg_contract_desc* ds, const float* const*
       op[k] = out[i];
     }
     if (n == 1)
-      JFG_TRY(launch_groups<1>(1, dp, oh, ol, ip, op, cfg, false, st));
+      JFG_TRY(launch_groups<1>(1, dp, oh, ol, ip, op, cfg, 0, st));
     else
-      JFG_TRY(launch_groups<GMAX>(n, dp, oh, ol, ip, op, cfg, false, st));
+      JFG_TRY(launch_groups<GMAX>(n, dp, oh, ol, ip, op, cfg, 0, st));
   }
   return JFG_OK;
 }
@@ -1003,6 +1154,16 @@ extern "C" int jfg_contract_tc_bf16x3(const jfg_contract_desc* d, const uint16_t
                                       void* stream) {
   if (!d) return JFG_ERR_ARG;
   return jfg::contract_tc_b16(*d, op_hi, op_lo, in, out, (cudaStream_t)stream);
+}
+
+extern "C" int jfg_contract_tc_f16x3(const jfg_contract_desc* d, const uint16_t* op_hi,
+                                     const uint16_t* op_lo, const float* op_inv,
+                                     long long op_inv_seg, const unsigned* in_max,
+                                     unsigned* out_max, const float* in, float* out,
+                                     void* stream) {
+  if (!d) return JFG_ERR_ARG;
+  return jfg::contract_tc_h16(*d, op_hi, op_lo, op_inv, op_inv_seg, in_max, out_max, in, out,
+                              (cudaStream_t)stream);
 }
 
 extern "C" void jfg_split_bf16_host(size_t n, const double* src, uint16_t* hi, uint16_t* lo) {

@@ -60,8 +60,17 @@ struct OpRef {
 // Dispatch of one contraction pass to an engine.
 // DF: FP64 data, double-FP32 arithmetic (contract_df.cu).  TB: FP32 data on
 // the tensor cores with a split-BF16 operator (OpRef<float> then points at
-// BF16 arrays).
-enum class Engine { F64, F32, TC, DF, TB };
+// BF16 arrays).  TH: FP32 data on the tensor cores as scaled split-FP16 pairs
+// with a split-FP16 operator scaled per row (variable-coefficient apply only).
+enum class Engine { F64, F32, TC, DF, TB, TH };
+
+// Auxiliaries of the TH engine: the inverse row scales of the packed FP16
+// operators and four per-problem max |x| slots (float bits, [4][batch]): the
+// apply's input (slot 0) and the inputs of its passes 2-4 (slots 1-3).
+struct H16Ops {
+  const float* op_inv = nullptr;
+  unsigned* slots = nullptr;
+};
 
 int contract_f64(const jfg_contract_desc& d, const double* op, const double* in, double* out,
                  cudaStream_t st);
@@ -77,6 +86,13 @@ int contract_tc(const jfg_contract_desc& d, const float* op_hi, const float* op_
 // the same contraction with the operator as BF16 (hi, lo): three BF16 MMAs per product
 int contract_tc_b16(const jfg_contract_desc& d, const uint16_t* op_hi, const uint16_t* op_lo,
                     const float* in, float* out, cudaStream_t st);
+// the same contraction in scaled split FP16: operator (hi, lo) FP16 scaled per
+// row with inverse scales op_inv[s * op_inv_seg + m]; the input of problem b
+// is scaled by a power of two from in_max[b] (float bits of an upper bound on
+// max |in[b]|); out_max[b] (optional, atomicMax) receives max |out[b]|
+int contract_tc_h16(const jfg_contract_desc& d, const uint16_t* op_hi, const uint16_t* op_lo,
+                    const float* op_inv, long long op_inv_seg, const unsigned* in_max,
+                    unsigned* out_max, const float* in, float* out, cudaStream_t st);
 // ngroups contractions in persistent grouped launches (contract_tc.cu)
 int contract_tc_grouped(int ng, const jfg_contract_desc* ds, const float* const* op_hi,
                         const float* const* op_lo, const float* const* in, float* const* out,
@@ -156,7 +172,9 @@ int fd_solve(Engine e, int ndim, int n, int batch, OpRef<T> E, OpRef<T> W, const
 template <typename T>
 int varcoef_apply(Engine e, int ndim, int n, int nq, int batch, OpRef<T> ops, const T* kw,
                   const T* u, T* v, void* work, size_t work_bytes, cudaStream_t st,
-                  Active act = Active());
+                  Active act = Active(), const H16Ops* h16 = nullptr);
+// number of inverse row scales of the 2-D packed operators (TH engine)
+inline long long varcoef_h16_rows(int n, int nq) { return 4LL * nq + 3LL * n; }
 
 // Read and clear the device status word of the BF16 GEMM kernel.
 int gemm_status_take(int* status);

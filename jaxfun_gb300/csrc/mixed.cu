@@ -196,7 +196,10 @@ extern "C" int jfg_pcg_varcoef_mixed_guess(const jfg_mixed_plan* plan, const dou
       !P.kw64 || !P.ops_hi || !P.ops_lo || !P.kw32 || !P.E_hi || !P.E_lo || !P.W_hi ||
       !P.W_lo || !P.lam || (P.residual != 0 && P.residual != 1) ||
       (P.precond_bf16 != 0 && P.precond_bf16 != 1) ||
-      (P.precond_bf16 && (!P.E_hi16 || !P.E_lo16 || !P.W_hi16 || !P.W_lo16)))
+      (P.precond_bf16 && (!P.E_hi16 || !P.E_lo16 || !P.W_hi16 || !P.W_lo16)) ||
+      (P.apply_f16 != 0 && P.apply_f16 != 1) ||
+      (P.apply_f16 && (P.ndim != 2 || (P.nq & 7) || !P.ops_hi16 || !P.ops_lo16 ||
+                       !P.ops_inv16)))
     return JFG_ERR_ARG;
   const int ndim = P.ndim, n = P.n, nq = P.nq, batch = P.batch;
   const MixedLayout Lo = layout(ndim, n, nq, batch);
@@ -223,14 +226,16 @@ extern "C" int jfg_pcg_varcoef_mixed_guess(const jfg_mixed_plan* plan, const dou
   if (P.residual == 1) JFG_TRY(split_pairs_f64(P.ops64, opdf, 8LL * n * nq, st));
 
   PcgProblem<float> pb;
-  pb.engine = Engine::TC;
+  pb.engine = P.apply_f16 ? Engine::TH : Engine::TC;
   const bool pbf = P.precond_bf16 != 0;
   pb.m_engine = pbf ? Engine::TB : Engine::TC;
   pb.ndim = ndim;
   pb.n = nq;
   pb.nq = nq;
   pb.batch = batch;
-  pb.ops = OpRef<float>{P.ops_hi, P.ops_lo};
+  pb.ops = P.apply_f16 ? OpRef<float>{(const float*)P.ops_hi16, (const float*)P.ops_lo16}
+                       : OpRef<float>{P.ops_hi, P.ops_lo};
+  pb.ops_inv = P.apply_f16 ? P.ops_inv16 : nullptr;
   pb.kw = P.kw32;
   pb.E = pbf ? OpRef<float>{(const float*)P.E_hi16, (const float*)P.E_lo16}
              : OpRef<float>{P.E_hi, P.E_lo};

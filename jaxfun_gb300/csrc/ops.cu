@@ -7,6 +7,9 @@
 // FIRST ("rotate"), so a d-dimensional field returns to its original axis
 // order after d passes and every pass is the same strided GEMM shape with the
 // contracted index contiguous in memory.
+#include <math.h>
+#include <string.h>
+
 #include <type_traits>
 
 #include "jfg_internal.cuh"
@@ -200,7 +203,7 @@ size_t varcoef_ws(int ndim, int n, int nq, int batch, int eb) {
 template <typename T>
 int varcoef_apply(Engine e, int ndim, int n, int nq, int batch, OpRef<T> ops, const T* kw,
                   const T* u, T* v, void* work, size_t work_bytes, cudaStream_t st,
-                  Active act) {
+                  Active act, const H16Ops* h16) {
   if ((ndim != 2 && ndim != 3) || n < 1 || nq < 1 || batch < 0 || !ops.hi || !kw || !u || !v)
     return JFG_ERR_ARG;
   const size_t need = varcoef_ws(ndim, n, nq, batch, (int)sizeof(T));
@@ -229,9 +232,52 @@ int varcoef_apply(Engine e, int ndim, int n, int nq, int batch, OpRef<T> ops, co
     JFG_TRY(split_pairs_f64((const double*)u, (float2*)bufB, nu, st));
     u1 = bufB;
   }
+  if (e == Engine::TH && (ndim != 2 || !h16 || !h16->op_inv || !h16->slots))
+    return JFG_ERR_ARG;
   if (ndim == 2) {
     // 1: T[b][r][j] = sum_l [B;D][r][l] U[b][j][l]            (M=2nq, P=n, K=n)
     jfg_contract_desc d1 = make_desc(batch, 2 * nq, n, n, act);
+    if constexpr (std::is_same<T, float>::value) {
+      if (e == Engine::TH) {
+        // Scaled split FP16: the operators are FP16 (hi, lo) arrays with the
+        // packed layout (offsets in 16-bit elements); each pass reads its
+        // input's max from slot t and records its output's max in slot t+1.
+        const uint16_t* oh = (const uint16_t*)ops.hi;
+        const uint16_t* ol = (const uint16_t*)ops.lo;
+        unsigned* sl = h16->slots;
+        const float* inv = h16->op_inv;
+        const long long B = batch;
+        JFG_TRY(contract_tc_h16(d1, oh, ol, inv, 0, sl, sl + B, u, bufA, st));
+        jfg_contract_desc d2 = make_desc(batch, nq, nq, n, act);
+        d2.nseg = 2;
+        d2.op_seg = nn;
+        d2.in_seg = nn;
+        d2.in_batch = 2 * nn;
+        d2.out_seg = (long long)nq * nq;
+        d2.out_batch = 2LL * nq * nq;
+        d2.epilogue = JFG_EPI_MUL_FIELD;
+        d2.field = kw;
+        d2.field_ld = nq;
+        d2.field_seg = 0;
+        d2.field_batch = (long long)nq * nq;
+        JFG_TRY(contract_tc_h16(d2, oh + 2 * nn, ol + 2 * nn, inv + 2LL * nq, nq, sl + B,
+                                sl + 2 * B, bufA, bufB, st));
+        jfg_contract_desc d3 = make_desc(batch, n, nq, nq, act);
+        d3.nseg = 2;
+        d3.op_seg = nn;
+        d3.in_seg = (long long)nq * nq;
+        d3.in_batch = 2LL * nq * nq;
+        d3.out_ld = 2LL * nq;
+        d3.out_seg = nq;
+        d3.out_batch = 2 * nn;
+        JFG_TRY(contract_tc_h16(d3, oh + 4 * nn, ol + 4 * nn, inv + 4LL * nq, n, sl + 2 * B,
+                                sl + 3 * B, bufB, bufA, st));
+        jfg_contract_desc d4 = make_desc(batch, n, n, 2 * nq, act);
+        JFG_TRY(contract_tc_h16(d4, oh + 6 * nn, ol + 6 * nn, inv + 4LL * nq + 2LL * n, 0,
+                                sl + 3 * B, nullptr, bufA, v, st));
+        return JFG_OK;
+      }
+    }
     JFG_TRY(pass(d1, ops, u1, bufA, dfp, dfp));
     // 2: G[b][s][p][q] = kw[b][p][q] * sum_j {D,B}[p][j] T[b][s][q][j]
     jfg_contract_desc d2 = make_desc(batch, nq, nq, n, act);
@@ -410,9 +456,11 @@ template int fd_solve<float>(Engine, int, int, int, OpRef<float>, OpRef<float>, 
                              const float*, const float*, const float*, float*, void*, size_t,
                              cudaStream_t, Active);
 template int varcoef_apply<double>(Engine, int, int, int, int, OpRef<double>, const double*,
-                                   const double*, double*, void*, size_t, cudaStream_t, Active);
+                                   const double*, double*, void*, size_t, cudaStream_t, Active,
+                                   const H16Ops*);
 template int varcoef_apply<float>(Engine, int, int, int, int, OpRef<float>, const float*,
-                                  const float*, float*, void*, size_t, cudaStream_t, Active);
+                                  const float*, float*, void*, size_t, cudaStream_t, Active,
+                                  const H16Ops*);
 
 }  // namespace jfg
 
@@ -611,6 +659,84 @@ extern "C" void jfg_varcoef_pack_ops_host(int ndim, int n, int nq, const double*
         o[6 * nn + (size_t)k * nq + q] = B[(size_t)q * n + k];
         o[7 * nn + (size_t)k * nq + q] = D[(size_t)q * n + k];
       }
+  }
+}
+
+namespace {
+
+// FP32 -> FP16 bit pattern, round to nearest even (normal, subnormal,
+// overflow to infinity), in portable host code.
+uint16_t f32_to_f16_rne(float f) {
+  uint32_t x;
+  memcpy(&x, &f, 4);
+  const uint32_t sign = (x >> 16) & 0x8000u;
+  const uint32_t ax = x & 0x7FFFFFFFu;
+  if (ax >= 0x7F800000u) return (uint16_t)(sign | (ax > 0x7F800000u ? 0x7E00u : 0x7C00u));
+  if (ax >= 0x477FF000u) return (uint16_t)(sign | 0x7C00u);  // >= 65520: infinity
+  if (ax <= 0x33000000u) return (uint16_t)sign;              // <= 2^-25: zero (ties to even)
+  const int e = (int)(ax >> 23) - 127;
+  const uint32_t mant = (ax & 0x7FFFFFu) | 0x800000u;
+  uint32_t h, rem, half;
+  if (e >= -14) {  // normal: 10 of the 23 fraction bits kept
+    h = ((uint32_t)(e + 15) << 10) | ((mant >> 13) & 0x3FFu);
+    rem = mant & 0x1FFFu;
+    half = 0x1000u;
+  } else {         // subnormal: units of 2^-24
+    const int sh = -e - 1;
+    h = mant >> sh;
+    rem = mant & ((1u << sh) - 1u);
+    half = 1u << (sh - 1);
+  }
+  if (rem > half || (rem == half && (h & 1u))) h += 1u;  // a carry moves to the next binade
+  return (uint16_t)(sign | h);
+}
+
+double f16_to_double(uint16_t h) {
+  const int e = (h >> 10) & 0x1F;
+  const int m = h & 0x3FF;
+  double v = e == 0 ? ldexp((double)m, -24) : ldexp(1024.0 + m, e - 25);
+  if (e == 31) v = m ? NAN : INFINITY;
+  return (h & 0x8000u) ? -v : v;
+}
+
+}  // namespace
+
+extern "C" size_t jfg_varcoef_f16_rows(int n, int nq) {
+  return n < 1 || nq < 1 ? 0 : (size_t)jfg::varcoef_h16_rows(n, nq);
+}
+
+extern "C" void jfg_split_f16_rowscaled_host(size_t rows, size_t cols, const double* src,
+                                              uint16_t* hi, uint16_t* lo, float* inv) {
+  for (size_t r = 0; r < rows; ++r) {
+    const double* row = src + r * cols;
+    double mx = 0.0;
+    for (size_t k = 0; k < cols; ++k) mx = fmax(mx, fabs(row[k]));
+    int E = 0;
+    if (mx > 0.0) frexp(mx, &E);  // mx < 2^E: the scaled row max lies in [2^14, 2^15)
+    const int k2 = mx > 0.0 ? 15 - E : 0;
+    inv[r] = (float)ldexp(1.0, -k2);
+    for (size_t k = 0; k < cols; ++k) {
+      const double v = ldexp(row[k], k2);
+      const uint16_t h = f32_to_f16_rne((float)v);
+      hi[r * cols + k] = h;
+      lo[r * cols + k] = f32_to_f16_rne((float)(v - f16_to_double(h)));
+    }
+  }
+}
+
+extern "C" void jfg_split_f16_rows_host(int n, int nq, const double* ops, uint16_t* hi,
+                                        uint16_t* lo, float* inv) {
+  const size_t nn = (size_t)n * nq;
+  // (first element, rows, row length) of the four blocks the passes read
+  const size_t blk[4][3] = {{0, (size_t)2 * nq, (size_t)n},
+                            {2 * nn, (size_t)2 * nq, (size_t)n},
+                            {4 * nn, (size_t)2 * n, (size_t)nq},
+                            {6 * nn, (size_t)n, (size_t)2 * nq}};
+  size_t r_out = 0;
+  for (const auto& bk : blk) {
+    jfg_split_f16_rowscaled_host(bk[1], bk[2], ops + bk[0], hi + bk[0], lo + bk[0],
+                                 inv + r_out);
+    r_out += bk[1];
   }
 }
 

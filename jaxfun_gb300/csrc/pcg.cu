@@ -62,6 +62,38 @@ __global__ void __launch_bounds__(DOT_T)
   if (threadIdx.x == 0) part[b * NB + j] = s;
 }
 
+__device__ __forceinline__ float block_max(float v) {
+  __shared__ float red[32];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) red[w] = v;
+  __syncthreads();
+  const int nw = blockDim.x >> 5;
+  v = (threadIdx.x < nw) ? red[threadIdx.x] : 0.f;
+  if (w == 0)
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
+  __syncthreads();
+  return v;  // valid in thread 0
+}
+
+// slot[b] = max(slot[b], max |x[b]|) (float bits; non-negative floats order
+// like unsigned integers), listed problems or all
+template <typename T>
+__global__ void k_absmax(const T* __restrict__ x, long long N, unsigned* __restrict__ slot,
+                         const int* __restrict__ list, const int* count, int batch) {
+  const int b = active_problem(list, active_count(list, count, batch), batch, blockIdx.y);
+  if (b < 0) return;
+  float m = 0.f;
+  const T* xb = x + (long long)b * N;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N;
+       i += (long long)gridDim.x * blockDim.x)
+    m = fmaxf(m, fabsf((float)xb[i]));
+  m = block_max(m);
+  if (threadIdx.x == 0) atomicMax(slot + b, __float_as_uint(m));
+}
+
 template <typename T>
 __device__ __forceinline__ T sum_part(const T* part, int b) {
   T s = T(0);
@@ -76,16 +108,20 @@ __device__ __forceinline__ bool is_active(T rz, T rz0, double tol) {
 }
 
 // x += alpha p ; r -= alpha q ; alpha = rz / (p.q) while active
+// slots (optional, [4][batch]): the scaled split-FP16 apply's max slots of
+// this problem are cleared here, after the apply read them and before the
+// p update and the next apply's passes record new maxima
 template <typename T>
 __global__ void k_update_xr(T* __restrict__ x, T* __restrict__ r, const T* __restrict__ p,
                             const T* __restrict__ q, long long N, const T* __restrict__ pq_part,
                             const T* __restrict__ rz_prev, const T* __restrict__ rz0,
                             double tol, const int* __restrict__ list, const int* count,
-                            int batch) {
+                            int batch, unsigned* __restrict__ slots) {
   const int b = active_problem(list, active_count(list, count, batch), batch, blockIdx.y);
   if (b < 0) return;
   const T rz = sum_part(rz_prev, b);
   if (!is_active(rz, rz0[b], tol)) return;
+  if (slots && blockIdx.x == 0 && threadIdx.x < 4) slots[(long long)threadIdx.x * batch + b] = 0u;
   const T pq = sum_part(pq_part, b);
   const T alpha = rz / pq;
   const long long off = (long long)b * N;
@@ -97,11 +133,13 @@ __global__ void k_update_xr(T* __restrict__ x, T* __restrict__ r, const T* __res
 }
 
 // p = z + beta p ; beta = rz_new / rz_prev while active; counts iterations
+// pmax (optional): max |p| of each problem recorded for the next apply
 template <typename T>
 __global__ void k_update_p(T* __restrict__ p, const T* __restrict__ z, long long N,
                            const T* __restrict__ rz_new_part, const T* __restrict__ rz_prev_part,
                            const T* __restrict__ rz0, double tol, int* __restrict__ iters,
-                           const int* __restrict__ list, const int* count, int batch) {
+                           const int* __restrict__ list, const int* count, int batch,
+                           unsigned* __restrict__ pmax) {
   const int b = active_problem(list, active_count(list, count, batch), batch, blockIdx.y);
   if (b < 0) return;
   const T rzp = sum_part(rz_prev_part, b);
@@ -109,10 +147,18 @@ __global__ void k_update_p(T* __restrict__ p, const T* __restrict__ z, long long
   const T rzn = sum_part(rz_new_part, b);
   const T beta = rzn / rzp;
   const long long off = (long long)b * N;
+  float m = 0.f;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N;
-       i += (long long)gridDim.x * blockDim.x)
-    p[off + i] = z[off + i] + beta * p[off + i];
+       i += (long long)gridDim.x * blockDim.x) {
+    const T v = z[off + i] + beta * p[off + i];
+    p[off + i] = v;
+    m = fmaxf(m, fabsf((float)v));
+  }
   if (blockIdx.x == 0 && threadIdx.x == 0) iters[b] += 1;
+  if (pmax) {
+    m = block_max(m);
+    if (threadIdx.x == 0) atomicMax(pmax + b, __float_as_uint(m));
+  }
 }
 
 // Active list: keep the problems whose r.z is still above tol^2 r0.z0.  With
@@ -209,7 +255,8 @@ size_t pcg_ws(int ndim, int n, int nq, int batch) {
   const size_t vec = align_up((size_t)N * batch * sizeof(T), 256);
   const size_t scal = align_up((size_t)batch * NB * sizeof(T), 256);
   const size_t small = align_up((size_t)batch * sizeof(T), 256) +
-                       2 * align_up((size_t)batch * sizeof(int), 256) + 256;
+                       2 * align_up((size_t)batch * sizeof(int), 256) + 256 +
+                       align_up((size_t)4 * batch * sizeof(unsigned), 256);
   size_t inner = varcoef_ws(ndim, n, nq, batch, sizeof(T));
   const size_t f = fd_ws(ndim, n, batch, sizeof(T));
   if (f > inner) inner = f;
@@ -245,13 +292,30 @@ int pcg_run(const PcgProblem<T>& pb, T* x, int use_x0, double tol, int maxiter, 
   int* alist = (int*)(sm + align_up((size_t)batch * sizeof(T), 256) +
                       align_up((size_t)batch * sizeof(int), 256));
   int* nactive = (int*)((char*)alist + align_up((size_t)batch * sizeof(int), 256));
-  void* inner = (char*)nactive + 256;
+  unsigned* slots = (unsigned*)((char*)nactive + 256);
+  void* inner = (char*)slots + align_up((size_t)4 * batch * sizeof(unsigned), 256);
   const size_t inner_bytes = work_bytes - (size_t)((char*)inner - w);
 
   const Active all, act{alist, nactive};
+  const bool th = pb.engine == Engine::TH;
+  if (th && (ndim != 2 || !pb.ops_inv)) return JFG_ERR_ARG;
+  H16Ops h16;
+  h16.op_inv = pb.ops_inv;
+  h16.slots = th ? slots : nullptr;
+  unsigned* slot_p = th ? slots : nullptr;
   auto applyA = [&](const T* in, T* out, Active a) -> int {
     return varcoef_apply<T>(pb.engine, ndim, n, nq, batch, pb.ops, pb.kw, in, out, inner,
-                            inner_bytes, st, a);
+                            inner_bytes, st, a, th ? &h16 : nullptr);
+  };
+  // TH: clear the max slots and record max |v| of every problem in slot 0
+  // (the input of the next apply)
+  auto record_max = [&](const T* v) -> int {
+    if (!th) return JFG_OK;
+    JFG_CUDA_TRY(cudaMemsetAsync(slots, 0, sizeof(unsigned) * 4 * batch, st));
+    k_absmax<T><<<dim3(vec_blocks(N), batch), 256, 0, st>>>(v, N, slots, nullptr, nullptr,
+                                                            batch);
+    JFG_LAUNCHED();
+    return JFG_OK;
   };
   auto applyM = [&](const T* in, T* out, Active a) -> int {
     return fd_solve<T>(pb.m_engine, ndim, n, batch, pb.E, pb.W, pb.lam, nullptr, pb.fd_scale, in,
@@ -266,6 +330,7 @@ int pcg_run(const PcgProblem<T>& pb, T* x, int use_x0, double tol, int maxiter, 
   // ---- setup: r = rhs - A x (or x = 0, r = rhs); z = M^-1 r; p = z
   JFG_CUDA_TRY(cudaMemsetAsync(iters, 0, sizeof(int) * batch, st));
   if (use_x0) {
+    JFG_TRY(record_max(x));
     JFG_TRY(applyA(x, r, all));
     k_sub_from<T><<<vec_blocks(total), 256, 0, st>>>(pb.rhs, r, total);
     JFG_LAUNCHED();
@@ -294,6 +359,7 @@ int pcg_run(const PcgProblem<T>& pb, T* x, int use_x0, double tol, int maxiter, 
     JFG_LAUNCHED();
   }
   JFG_CUDA_TRY(cudaMemcpyAsync(p, z, sizeof(T) * total, cudaMemcpyDeviceToDevice, st));
+  JFG_TRY(record_max(p));
   // the problems that start active (r0.z0 > 0)
   k_compact<T><<<1, CMP_T, 0, st>>>(rz_part[1], rz0, tol, alist, nactive, batch, 1);
   JFG_LAUNCHED();
@@ -304,13 +370,13 @@ int pcg_run(const PcgProblem<T>& pb, T* x, int use_x0, double tol, int maxiter, 
     k_dot_part<T><<<dgrid, DOT_T, 0, st>>>(p, q, N, pq_part, alist, nactive, batch);
     JFG_LAUNCHED();
     k_update_xr<T><<<vgrid, 256, 0, st>>>(x, r, p, q, N, pq_part, rz_part[prev], rz0, tol, alist,
-                                          nactive, batch);
+                                          nactive, batch, slot_p);
     JFG_LAUNCHED();
     JFG_TRY(applyM(r, z, act));
     k_dot_part<T><<<dgrid, DOT_T, 0, st>>>(r, z, N, rz_part[cur], alist, nactive, batch);
     JFG_LAUNCHED();
     k_update_p<T><<<vgrid, 256, 0, st>>>(p, z, N, rz_part[cur], rz_part[prev], rz0, tol, iters,
-                                         alist, nactive, batch);
+                                         alist, nactive, batch, slot_p);
     JFG_LAUNCHED();
     k_compact<T><<<1, CMP_T, 0, st>>>(rz_part[cur], rz0, tol, alist, nactive, batch, 0);
     JFG_LAUNCHED();

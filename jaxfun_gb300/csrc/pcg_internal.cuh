@@ -13,7 +13,9 @@ struct PcgProblem {
   Engine m_engine = Engine::F64;   // engine of the preconditioner (E, W point at BF16
                                    // pairs when it is Engine::TB)
   int ndim = 2, n = 0, nq = 0, batch = 0;
-  OpRef<T> ops{nullptr, nullptr};  // packed variable-coefficient operators
+  OpRef<T> ops{nullptr, nullptr};  // packed variable-coefficient operators (FP16 pairs
+                                   // when engine is Engine::TH)
+  const float* ops_inv = nullptr;  // Engine::TH: inverse row scales of the operators
   const T* kw = nullptr;           // (batch, nq^ndim) kappa * quadrature weights
   OpRef<T> E{nullptr, nullptr};    // fast-diagonalisation forward (n x n)
   OpRef<T> W{nullptr, nullptr};    // fast-diagonalisation backward (n x n)

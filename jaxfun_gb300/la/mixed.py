@@ -30,6 +30,8 @@ class MixedPlan(C.Structure):
         ("precond_bf16", C.c_int),
         ("E_hi16", C.c_void_p), ("E_lo16", C.c_void_p), ("W_hi16", C.c_void_p),
         ("W_lo16", C.c_void_p),
+        ("apply_f16", C.c_int),
+        ("ops_hi16", C.c_void_p), ("ops_lo16", C.c_void_p), ("ops_inv16", C.c_void_p),
     ]
 
 
@@ -41,6 +43,21 @@ def split_bf16(a: np.ndarray) -> tuple[torch.Tensor, torch.Tensor]:
     lo = np.empty(a.shape, dtype=np.uint16)
     L.jfg_split_bf16_host(a.size, a.ctypes.data, hi.ctypes.data, lo.ctypes.data)
     return (as_device(hi.view(np.int16), torch.int16), as_device(lo.view(np.int16), torch.int16))
+
+
+def split_f16_rows(n: int, nq: int, ops: np.ndarray):
+    """2-D packed operators (FP64) -> FP16 (hi, lo) bit patterns as int16 device
+    tensors, each operator row scaled by a power of two, and the inverse row
+    scales (FP32 device tensor) for the scaled split-FP16 apply."""
+    L = _lib.lib()
+    a = np.ascontiguousarray(ops, dtype=np.float64)
+    hi = np.empty(a.shape, dtype=np.uint16)
+    lo = np.empty(a.shape, dtype=np.uint16)
+    inv = np.empty(L.jfg_varcoef_f16_rows(n, nq), dtype=np.float32)
+    L.jfg_split_f16_rows_host(n, nq, a.ctypes.data, hi.ctypes.data, lo.ctypes.data,
+                              inv.ctypes.data)
+    return (as_device(hi.view(np.int16), torch.int16), as_device(lo.view(np.int16), torch.int16),
+            as_device(inv, torch.float32))
 
 
 def split_tf32(a: np.ndarray) -> tuple[torch.Tensor, torch.Tensor]:
@@ -64,7 +81,7 @@ class MixedVarCoefSolver:
 
     def __init__(self, A: VarCoefMatrix, M: TPMatricesLUFactors | None = None,
                  residual: str = "df64", fp32_updates: bool | None = None,
-                 precond: str = "bf16x3"):
+                 precond: str = "bf16x3", apply: str = "f16x3"):
         """``residual``: arithmetic of the refinement residual r = b - A x,
         "df64" (double-FP32 on the FP32 units) or "f64" (FP64 FMAs).
         ``fp32_updates``: once ||r|| <= 1e-4 ||b||, update r -= ||r|| A d in FP32
@@ -73,11 +90,16 @@ class MixedVarCoefSolver:
         ``precond``: split-"bf16x3" (default) or split-"tf32" tensor-core passes
         for the inner fast-diagonalisation preconditioner; the preconditioner
         tolerates the BF16 pairs' ~2^-16 error (same iteration counts, ~7 %
-        faster at N = 256), the operator passes stay split-TF32.  Padded sizes
-        with nq % 8 != 0 use split-TF32 (the BF16 rows would not be 16-byte
-        multiples)."""
+        faster at N = 256).  Padded sizes with nq % 8 != 0 use split-TF32 (the
+        BF16 rows would not be 16-byte multiples).
+        ``apply``: the inner operator passes as scaled split-"f16x3" (default
+        in 2-D: FP16 hi/lo pairs with power-of-two scales per operator row and
+        per problem, the accuracy of split TF32 at twice its MMA rate) or
+        split-"tf32"; 3-D and nq % 8 != 0 use split-TF32."""
         if precond not in ("tf32", "bf16x3"):
             raise ValueError(f"precond must be 'tf32' or 'bf16x3', not {precond!r}")
+        if apply not in ("tf32", "f16x3"):
+            raise ValueError(f"apply must be 'tf32' or 'f16x3', not {apply!r}")
         if residual not in ("df64", "f64"):
             raise ValueError(f"residual must be 'df64' or 'f64', not {residual!r}")
         self.A = A
@@ -89,6 +111,9 @@ class MixedVarCoefSolver:
         D = s0.backward_matrix(None, 1)
         ops_pad = pack_varcoef_ops(nd, _pad(B, nq, nq), _pad(D, nq, nq))
         self.ops_hi, self.ops_lo = split_tf32(ops_pad)
+        af = apply == "f16x3" and nd == 2 and nq % 8 == 0
+        if af:
+            self.ops16 = split_f16_rows(nq, nq, ops_pad)
         self.ops32 = as_device(ops_pad, torch.float32)
         self.kw32 = A.kw.to(torch.float32).contiguous()
         fac = fd_preconditioner(A.T) if M is None else M
@@ -111,7 +136,11 @@ class MixedVarCoefSolver:
                               self.E16[0].data_ptr() if pb else None,
                               self.E16[1].data_ptr() if pb else None,
                               self.W16[0].data_ptr() if pb else None,
-                              self.W16[1].data_ptr() if pb else None)
+                              self.W16[1].data_ptr() if pb else None,
+                              1 if af else 0,
+                              self.ops16[0].data_ptr() if af else None,
+                              self.ops16[1].data_ptr() if af else None,
+                              self.ops16[2].data_ptr() if af else None)
 
     def workspace_bytes(self) -> int:
         A = self.A

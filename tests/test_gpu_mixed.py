@@ -15,9 +15,10 @@ def rel(a, b):
     return np.abs(a - b).max() / np.abs(b).max()
 
 
+@pytest.mark.parametrize("apply", ["f16x3", "tf32"])
 @pytest.mark.parametrize("precond", ["bf16x3", "tf32"])
 @pytest.mark.parametrize("ndim,N,batch", [(2, 32, 3), (2, 64, 2), (3, 16, 2)])
-def test_mixed_matches_fp64(ndim, N, batch, precond):
+def test_mixed_matches_fp64(ndim, N, batch, precond, apply):
     V = FunctionSpace(N, Legendre, bcs=DIRICHLET)
     T = TensorProduct(*([V] * ndim))
     rng = np.random.default_rng(N + ndim)
@@ -25,7 +26,7 @@ def test_mixed_matches_fp64(ndim, N, batch, precond):
     b = rng.standard_normal((batch,) + (N - 2,) * ndim)
     A = VarCoefMatrix(T, kap)
     xr, _ = pcg(A, b, tol=1e-14, maxiter=3000)
-    x, it_in, it_out = MixedVarCoefSolver(A, precond=precond).solve(b, tol=1e-12)
+    x, it_in, it_out = MixedVarCoefSolver(A, precond=precond, apply=apply).solve(b, tol=1e-12)
     xr, x = xr.cpu().numpy(), x.cpu().numpy()
     for i in range(batch):
         assert rel(x[i], xr[i]) < 1e-10, (i, it_in, it_out)

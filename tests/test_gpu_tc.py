@@ -176,3 +176,69 @@ def test_bounded_wait_times_out_and_context_stays_usable(variant):
     got = run_tc(op, x)
     ref = np.einsum("smk,bspk->bsmp", op, x.astype(np.float64))
     assert np.abs(got - ref).max() <= TC_TOL * np.abs(ref).max()
+
+
+def run_f16(op64, x32, epi=0, field=None, in_max_scale=1.0):
+    """jfg_contract_tc_f16x3: operator rows split on the host into scaled FP16
+    pairs, per-problem input scale from max |x[b]| (times in_max_scale, a
+    looser bound), out_max recorded.  Returns (out, out_max as floats)."""
+    L = _lib.lib()
+    S, M, K = op64.shape
+    B, S2, P, K2 = x32.shape
+    hi = np.empty((S, M, K), np.uint16)
+    lo = np.empty((S, M, K), np.uint16)
+    inv = np.empty(S * M, np.float32)
+    a = np.ascontiguousarray(op64, dtype=np.float64)
+    L.jfg_split_f16_rowscaled_host(S * M, K, a.ctypes.data, hi.ctypes.data, lo.ctypes.data,
+                                   inv.ctypes.data)
+    dev = lambda v: torch.as_tensor(np.ascontiguousarray(v), device="cuda")  # noqa: E731
+    t_hi, t_lo, t_inv = dev(hi.view(np.int16)), dev(lo.view(np.int16)), dev(inv)
+    t_x = dev(x32)
+    mx = (np.abs(x32.reshape(B, -1)).max(axis=1) * in_max_scale).astype(np.float32)
+    t_in = dev(mx.view(np.int32))
+    t_out_max = torch.zeros(B, dtype=torch.int32, device="cuda")
+    out = torch.zeros(B, S, M, P, dtype=torch.float32, device="cuda")
+    d = _lib.ContractDesc(batch=B, nseg=S, M=M, P=P, K=K, op_ld=K, op_seg=M * K, in_ld=K,
+                          in_seg=P * K, in_batch=S * P * K, out_ld=P, out_seg=M * P,
+                          out_batch=S * M * P, epilogue=epi, alpha=1.0, beta=0.0)
+    keep = []
+    if epi == 1:
+        f = dev(field.astype(np.float32))
+        keep.append(f)
+        d.field, d.field_ld, d.field_seg, d.field_batch = f.data_ptr(), P, M * P, S * M * P
+    st = L.jfg_contract_tc_f16x3(d, t_hi.data_ptr(), t_lo.data_ptr(), t_inv.data_ptr(), M,
+                                 t_in.data_ptr(), t_out_max.data_ptr(), t_x.data_ptr(),
+                                 out.data_ptr(), _lib.stream_handle())
+    assert st == 0, _lib.status_string(st)
+    torch.cuda.synchronize()
+    assert L.jfg_device_status() == 0
+    return (out.cpu().numpy().astype(np.float64),
+            t_out_max.cpu().numpy().view(np.float32).astype(np.float64))
+
+
+@pytest.mark.parametrize("S,M,P,K,epi", [(1, 512, 256, 256, 0), (2, 256, 200, 200, 1),
+                                         (1, 96, 130, 512, 0)])
+def test_f16x3_matches_fp64(S, M, P, K, epi):
+    """Scaled split-FP16 contraction against FP64 of the same FP32 inputs,
+    per problem (1e-5 of each problem's output maximum), with problems of
+    very different magnitudes, a zero problem, a loose input bound (2^9 too
+    large) and the recorded output maxima (exact float equality)."""
+    rng = np.random.default_rng(S * 1000 + M + P + K)
+    B = 4
+    op = rng.standard_normal((S, M, K)) * np.logspace(-3, 3, M)[None, :, None]
+    x = rng.standard_normal((B, S, P, K))
+    x *= np.array([1e-9, 1.0, 3e7, 0.0])[:, None, None, None]
+    x = x.astype(np.float32)
+    field = rng.uniform(0.1, 2.0, (B, S, M, P)) if epi == 1 else None
+    ref = np.einsum("smk,bspk->bsmp", op, x.astype(np.float64))
+    if epi == 1:
+        ref = ref * field.astype(np.float32).astype(np.float64)
+    for bound in (1.0, 512.0):
+        got, omax = run_f16(op, x, epi, field, in_max_scale=bound)
+        for b in range(B):
+            scale = np.abs(ref[b]).max()
+            if scale == 0:
+                assert np.all(got[b] == 0) and omax[b] == 0
+                continue
+            assert np.abs(got[b] - ref[b]).max() <= TC_TOL * scale, (b, bound)
+            assert omax[b] == np.abs(got[b]).max()

@@ -166,3 +166,47 @@ def test_xla_ffi_handlers_declared_and_build_is_optional():
     if importlib.util.find_spec("jax") is None and not os.environ.get("JFG_XLA_INCLUDE"):
         assert build.xla_include_dir() is None
         assert build.build_xla_ffi("nvcc", build.OUTDIR / build.LIBNAME) is None
+
+
+def test_f16_row_split_rounding_and_reconstruction():
+    """Host split of operator rows into scaled FP16 (hi, lo): hi is the
+    round-to-nearest-even FP16 of the scaled FP32 value (numpy's float16
+    conversion of the same FP32 value, subnormals and ties included), the
+    scaled row max lies in [2^14, 2^15), and hi + lo reproduces each row to
+    2^-22 of its maximum."""
+    import ctypes as C
+
+    import numpy as np
+
+    from jaxfun_gb300 import _lib
+
+    L = _lib.lib()
+    rng = np.random.default_rng(3)
+    rows, cols = 6, 300
+    a = rng.standard_normal((rows, cols)) * np.logspace(-12, 12, rows)[:, None]
+    a[1, :] *= np.exp(rng.uniform(-30, 0, cols))  # wide range inside a row
+    a[2] = 0.0
+    # row 3: no scaling (max in [2^14, 2^15)), FP16 edge values
+    edge = np.array([20000.0, 2.0 ** -25, 2.0 ** -25 * 1.0001, 2.0 ** -24, 3 * 2.0 ** -25,
+                     2.0 ** -14, 2.0 ** -14 * (1 - 2.0 ** -11), 1 + 2.0 ** -11, 1 + 3 * 2.0 ** -11,
+                     -1 - 2.0 ** -11, 5.96e-8, 6.1e-5, 1e-3, -1e-7])
+    a[3] = 0.0
+    a[3, : edge.size] = edge
+    hi = np.empty((rows, cols), np.uint16)
+    lo = np.empty((rows, cols), np.uint16)
+    inv = np.empty(rows, np.float32)
+    L.jfg_split_f16_rowscaled_host(rows, cols, a.ctypes.data, hi.ctypes.data, lo.ctypes.data,
+                                   inv.ctypes.data)
+    for r in range(rows):
+        s = 1.0 / float(inv[r])
+        v = a[r] * s
+        if np.abs(a[r]).max() > 0:
+            assert 2.0 ** 14 <= np.abs(v).max() < 2.0 ** 15
+        ref_hi = v.astype(np.float32).astype(np.float16).view(np.uint16)
+        assert np.array_equal(hi[r], ref_hi), r
+        rem = (v - hi[r].view(np.float16).astype(np.float64)).astype(np.float32)
+        assert np.array_equal(lo[r], rem.astype(np.float16).view(np.uint16)), r
+        back = (hi[r].view(np.float16).astype(np.float64)
+                + lo[r].view(np.float16).astype(np.float64)) * float(inv[r])
+        assert np.abs(back - a[r]).max() <= 2.0 ** -22 * max(np.abs(a[r]).max(), 1e-300)
+    assert inv[3] == 1.0
