@@ -175,6 +175,14 @@ int jfg_tc_set_variant(int operand_a_in_tmem);
  * stores where the output rows are 16-byte aligned (and beta == 0); 0 uses
  * plain coalesced stores everywhere. */
 int jfg_tc_set_store_path(int tma_store);
+/* Schedule of single-group launches with 16-bit operators (split BF16, scaled
+ * split FP16): 1 (default) operator-stationary -- each persistent CTA serves
+ * one (segment, operator chunk) slot, keeps that chunk for all K blocks in
+ * shared memory and streams only input tiles, used when the chunk fits
+ * beside >= 2 input stages (K <= 256 at 128 operator rows) and there are
+ * >= 2 tiles per CTA; 2 whenever the chunk fits; 0 streams operator and
+ * input tiles together. */
+int jfg_tc_set_op_resident(int on);
 /* Launch configuration of the tensor-core contraction. */
 typedef struct {
   int operand_a_in_tmem; /* 1: split input tile in TMEM; 0: in shared memory          */

@@ -87,6 +87,7 @@ SIGNATURES = {
     "jfg_split_bf16_host": (None, [_sz, _vp, _vp, _vp]),
     "jfg_tp_apply_tc_bf16x3": (_i, [_i, _vp, _vp, _i, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
     "jfg_tc_set_store_path": (_i, [_i]),
+    "jfg_tc_set_op_resident": (_i, [_i]),
     "jfg_banded_lu_size": (_sz, [_i, _i, _i, _i]),
     "jfg_banded_lu_factor_f64": (_i, [_i, _i, _i, _vp, _vp, _vp, _vp]),
     "jfg_banded_lu_solve_f64": (_i, [_i, _i, _i, _i, _vp, _vp, _vp, C.c_longlong,

@@ -53,6 +53,10 @@ static int g_operand_a_in_tmem = 1;
 // Epilogue output path: 1 TMA stores through shared memory where the layout
 // allows (default), 0 plain coalesced stores (jfg_tc_set_store_path).
 static int g_tma_store = 1;
+// Operator-stationary schedule for single-group 16-bit launches whose
+// operator chunk fits in shared memory: 0 off, 1 (default) when every CTA gets
+// >= 2 tiles, 2 whenever the chunk fits (jfg_tc_set_op_resident).
+static int g_op_resident = 1;
 
 namespace {
 
@@ -98,6 +102,12 @@ struct TcLaunch {
   int tmem_a;   // 1: split input tile (MMA operand A) kept in TMEM, not shared memory
   int mt_max;   // largest Mtile: sets the stage layout
   int out_stage; // 1 if any group stores through shared memory (8 x 4 KB after the stages)
+  // 1 (16-bit operators, one group): operator-stationary schedule.  CTA c
+  // serves the operator slot c % nslots, slot = s * mchunks + mc, loads that
+  // operator chunk (all K blocks, hi and lo) into shared memory once and
+  // streams only the input tiles of its (problem, p-tile) pairs.
+  int op_res;
+  int nslots;
 };
 
 // TMEM column map when operand A lives in TMEM: accumulator buffers at
@@ -350,10 +360,20 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   const int S = L.stages;
   const bool ta = B16 || L.tmem_a != 0;
+  const bool res = B16 && L.op_res != 0;
   const uint32_t omax = (uint32_t)L.mt_max * 128;  // Mtile rows of 128 B (hi or lo)
   const uint32_t xbuf = ta ? XB : 2 * XBYTES;  // X block (+ its lo part when in SMEM)
-  const uint32_t stage_bytes = xbuf + 2 * omax;
+  const uint32_t stage_bytes = res ? xbuf : xbuf + 2 * omax;
   const uint32_t acc_stride = ta ? ACC_STRIDE_TA : 256;
+  // operator-stationary schedule: this CTA's operator slot and tile stride
+  const int r_slot = res ? (int)(blockIdx.x % (unsigned)L.nslots) : 0;
+  const int r_mchunks = res ? (L.g[0].d.M + L.g[0].Mtile - 1) / L.g[0].Mtile : 1;
+  const int r_s = r_slot / r_mchunks, r_mc = r_slot - r_s * r_mchunks;
+  const long long r_j0 = res ? (long long)(blockIdx.x / (unsigned)L.nslots) : 0;
+  const long long r_step =
+      res ? (long long)((gridDim.x - (unsigned)r_slot + (unsigned)L.nslots - 1) / L.nslots) : 1;
+  const int r_nkb = res ? (L.g[0].d.K + KE - 1) / KE : 0;
+  const uint32_t res_bytes = res ? (uint32_t)r_nkb * 2 * omax : 0;
 
   if (threadIdx.x == 0) {
     long long acc = 0;
@@ -372,9 +392,13 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   __syncthreads();
   const unsigned long long budget = s_budget;
   const long long ntiles = tb[L.ngroups];
-  if ((long long)blockIdx.x >= ntiles) return;  // no tile for this CTA (uniform)
+  const int r_nptiles = (L.g[0].d.P + TILE_P - 1) / TILE_P;
+  const long long r_cnt = res ? (long long)nbs[0] * r_nptiles : 0;  // tiles of one slot
+  if (!res && (long long)blockIdx.x >= ntiles) return;  // no tile for this CTA (uniform)
+  if (res && r_j0 >= r_cnt) return;
 
-  uint8_t* ostage = smem + (size_t)S * stage_bytes;  // epilogue output boxes (if used)
+  uint8_t* sbase = smem + res_bytes;                   // input (and operator) stages
+  uint8_t* ostage = sbase + (size_t)S * stage_bytes;  // epilogue output boxes (if used)
   uint64_t* bars = (uint64_t*)(ostage + (L.out_stage ? 8 * STAGE_OUT : 0));
   uint64_t* full = bars;
   uint64_t* conv = bars + S;
@@ -383,7 +407,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   uint64_t* tempty = bars + 3 * S + 2;  // [2] accumulator drained
   uint64_t* hold = bars + 3 * S + 4;    // test hook: nothing arrives on it
   uint64_t* mma_done = bars + 3 * S + 5;  // MMA drain after a timeout
-  uint32_t* tmem_slot = (uint32_t*)(bars + 3 * S + 6);
+  uint64_t* opfull = bars + 3 * S + 6;    // resident operator chunk landed
+  uint32_t* tmem_slot = (uint32_t*)(bars + 3 * S + 7);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
@@ -399,6 +424,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     }
     mbar_init(hold, 1);
     mbar_init(mma_done, 1);
+    mbar_init(opfull, 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 1) {
@@ -413,10 +439,13 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
   const uint32_t tmem = *tmem_slot;
 
-  auto Xh = [&](int st) { return smem + (size_t)st * stage_bytes; };
-  auto Xl = [&](int st) { return smem + (size_t)st * stage_bytes + XBYTES; };
-  auto Oh = [&](int st) { return smem + (size_t)st * stage_bytes + xbuf; };
-  auto Ol = [&](int st) { return smem + (size_t)st * stage_bytes + xbuf + omax; };
+  auto Xh = [&](int st) { return sbase + (size_t)st * stage_bytes; };
+  auto Xl = [&](int st) { return sbase + (size_t)st * stage_bytes + XBYTES; };
+  auto Oh = [&](int st) { return sbase + (size_t)st * stage_bytes + xbuf; };
+  auto Ol = [&](int st) { return sbase + (size_t)st * stage_bytes + xbuf + omax; };
+  // resident operator chunk: K block kb of hi at 2 kb omax, lo right after it
+  auto OhR = [&](int kb) { return smem + (size_t)kb * 2 * omax; };
+  auto OlR = [&](int kb) { return smem + (size_t)kb * 2 * omax + omax; };
   // b = problem index (-1: an out-of-range list entry, computed but not stored)
   auto decode = [&](long long t, int& gi, int& pt, int& mc, int& b, int& s) {
     gi = 0;
@@ -442,15 +471,43 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     b = active_problem(q.d.batch_list, nbs[gi], q.d.batch, slot);
   };
   auto nkb_of = [&](int gi) { return (L.g[gi].d.K + KE - 1) / KE; };
+  // tile li of this CTA (false past the last one)
+  auto tile_of = [&](long long li, int& gi, int& pt, int& mc, int& b, int& s) -> bool {
+    if (!res) {
+      const long long t = (long long)blockIdx.x + li * (long long)gridDim.x;
+      if (t >= ntiles) return false;
+      decode(t, gi, pt, mc, b, s);
+      return true;
+    }
+    const long long j = r_j0 + li * r_step;
+    if (j >= r_cnt) return false;
+    const TcGroup& q = L.g[0];
+    gi = 0;
+    pt = (int)(j % r_nptiles);
+    b = active_problem(q.d.batch_list, nbs[0], q.d.batch, (int)(j / r_nptiles));
+    s = r_s;
+    mc = r_mc;
+    return true;
+  };
 
   if (warp == 0) {
     // ---------------- TMA producer ----------------
     if (lane == 0) {
       long long g = 0, issued = 0;
       bool ok = true;
-      for (long long t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
-        int gi, pt, mc, b, s;
-        decode(t, gi, pt, mc, b, s);
+      if (res) {
+        // the operator chunk of this CTA's slot, once: every K block, hi and lo
+        const TcGroup& q = L.g[0];
+        const uint32_t obytes = (uint32_t)q.Mtile * 128;
+        const int os = q.seg_op_map ? r_s : 0;
+        mbar_expect_tx(opfull, (uint32_t)r_nkb * 2 * obytes);
+        for (int kb = 0; kb < r_nkb; ++kb) {
+          tma_load_3d(OhR(kb), &L.maps[0][1], opfull, kb * KE, r_mc * q.Mtile, os);
+          tma_load_3d(OlR(kb), &L.maps[0][2], opfull, kb * KE, r_mc * q.Mtile, os);
+        }
+      }
+      int gi, pt, mc, b, s;
+      for (long long li = 0; ok && tile_of(li, gi, pt, mc, b, s); ++li) {
         const TcGroup& q = L.g[gi];
         const int cs = q.seg_in_map ? s : 0;
         const int cb = (q.bat_in_map && b > 0) ? b : 0;
@@ -464,19 +521,23 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             ok = false;
             break;
           }
-          mbar_expect_tx(&full[st], XB + 2 * obytes);
+          mbar_expect_tx(&full[st], res ? XB : XB + 2 * obytes);
           tma_load_4d(Xh(st), &L.maps[gi][0], &full[st], kb * KE, pt * TILE_P, cs, cb);
           if (B16)
             tma_load_4d(Xh(st) + XBYTES, &L.maps[gi][0], &full[st], kb * KE + KB,
                         pt * TILE_P, cs, cb);
-          tma_load_3d(Oh(st), &L.maps[gi][1], &full[st], kb * KE, mc * q.Mtile, os);
-          tma_load_3d(Ol(st), &L.maps[gi][2], &full[st], kb * KE, mc * q.Mtile, os);
+          if (!res) {
+            tma_load_3d(Oh(st), &L.maps[gi][1], &full[st], kb * KE, mc * q.Mtile, os);
+            tma_load_3d(Ol(st), &L.maps[gi][2], &full[st], kb * KE, mc * q.Mtile, os);
+          }
           issued = g + 1;
         }
       }
-      // drain: the latest use of every stage must have landed before exit
+      // drain: the latest use of every stage (and the resident operator) must
+      // have landed before exit
       for (long long q = (issued > S ? issued - S : 0); q < issued; ++q)
         mbar_wait(&full[q % S], (uint32_t)(q / S) & 1u, WAIT_NS);
+      if (res) mbar_wait(opfull, 0, WAIT_NS);
     }
   } else if (warp == 1) {
     // ---------------- MMA issuer ----------------
@@ -484,9 +545,9 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       long long g = 0;
       int li = 0;
       bool ok = true, issued_any = false;
-      for (long long t = blockIdx.x; t < ntiles && ok; t += gridDim.x, ++li) {
-        int gi, pt, mc, b, s;
-        decode(t, gi, pt, mc, b, s);
+      if (res && !mbar_wait(opfull, 0, budget)) ok = false;
+      int gi, pt, mc, b, s;
+      for (; ok && tile_of(li, gi, pt, mc, b, s); ++li) {
         const uint32_t idesc = H16   ? idesc_f16(TILE_P, L.g[gi].Mtile)
                                : B16 ? idesc_b16(TILE_P, L.g[gi].Mtile)
                                      : idesc_tf32(TILE_P, L.g[gi].Mtile);
@@ -507,7 +568,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           }
           issued_any = true;
           asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
-          const uint32_t oh = smem_u32(Oh(st)), ol = smem_u32(Ol(st));
+          const uint32_t oh = smem_u32(res ? OhR(kb) : Oh(st));
+          const uint32_t ol = smem_u32(res ? OlR(kb) : Ol(st));
           if (B16) {
             const uint32_t ah = tmem + (uint32_t)(A_COL0 + 64 * st), al = ah + 32;
 #pragma unroll
@@ -556,9 +618,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     const int row = 32 * (warp & 3) + lane;
     long long g = 0;
     bool ok = true;
-    for (long long t = blockIdx.x; t < ntiles && ok; t += gridDim.x) {
-      int gi, pt, mc, b, s;
-      decode(t, gi, pt, mc, b, s);
+    int gi, pt, mc, b, s;
+    for (long long li = 0; ok && tile_of(li, gi, pt, mc, b, s); ++li) {
       const int nkb = nkb_of(gi);
       float xsc = 1.f, xinv = 1.f;
       if (H16) h16_scale(L.g[gi].in_max, b, xsc, xinv);
@@ -668,9 +729,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     // test hook: a barrier nothing arrives on; its wait runs out (status set)
     // and this warp skips its tiles, so every other role's waits run out too
     const bool held = s_hold != 0 && !mbar_wait(hold, 0, budget);
-    for (long long t = blockIdx.x; t < ntiles && !held; t += gridDim.x, ++li) {
-      int gi, pt, mc, b, s;
-      decode(t, gi, pt, mc, b, s);
+    int gi, pt, mc, b, s;
+    for (; !held && tile_of(li, gi, pt, mc, b, s); ++li) {
       const TcGroup& q = L.g[gi];
       const jfg_contract_desc& d = q.d;
       const int Mt = q.Mtile;
@@ -984,10 +1044,41 @@ int launch_groups(int ng, const jfg_contract_desc* const* ds, const void* const*
     ostage |= L.g[i].tma_store;
   }
   if (tiles == 0) return JFG_OK;
+  int dev = 0, nsm = 0;
+  JFG_CUDA_TRY(cudaGetDevice(&dev));
+  JFG_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
+  int ctas = cfg.ctas > 0 && cfg.ctas < nsm ? cfg.ctas : nsm;
   const int ta = (b16 || cfg.operand_a_in_tmem) ? 1 : 0;
-  const size_t stage = (b16 ? 2 : ta ? 1 : 2) * (size_t)XBYTES + 2 * (size_t)mt_max * 128;
-  const size_t ob = ostage ? 8 * (size_t)STAGE_OUT : 0;
-  int stages = (int)((SMEM_MAX - 1024 - ob - 64 * 8) / stage);
+  // Operator-stationary schedule (16-bit operators, one group): each CTA keeps
+  // its operator chunk (every K block, hi and lo) in shared memory and streams
+  // only input tiles, halving the L2-to-SM traffic per tile.  Used when the
+  // chunk leaves room for >= 2 input stages and every slot gets >= 2 tiles
+  // per CTA.
+  bool res = false;
+  int nslots = 0;
+  size_t res_bytes = 0;
+  if (b16 && ng == 1 && g_op_resident) {
+    const TcGroup& q = L.g[0];
+    const int mch = (q.d.M + q.Mtile - 1) / q.Mtile;
+    nslots = q.d.nseg * mch;
+    res_bytes = (size_t)((q.d.K + 63) / 64) * 2 * (size_t)q.Mtile * 128;
+    const long long per_slot = (long long)((q.d.P + TILE_P - 1) / TILE_P) * q.d.batch;
+    const size_t room = (size_t)SMEM_MAX - 1024 - 64 * 8;
+    res = nslots <= ctas && (g_op_resident == 2 || per_slot * nslots >= 2LL * ctas) &&
+          res_bytes + 2 * (2 * (size_t)XBYTES) <= room;
+  }
+  const size_t stage = res ? 2 * (size_t)XBYTES
+                           : (b16 ? 2 : ta ? 1 : 2) * (size_t)XBYTES + 2 * (size_t)mt_max * 128;
+  size_t ob = ostage ? 8 * (size_t)STAGE_OUT : 0;
+  const size_t fixed = 1024 + (res ? res_bytes : 0) + 64 * 8;
+  int stages = (int)(((size_t)SMEM_MAX - fixed - ob) / stage);
+  if (res && stages < 3 && ostage && ((size_t)SMEM_MAX - fixed) / stage > (size_t)stages) {
+    // three input stages matter more than the TMA-store staging boxes
+    ostage = 0;
+    ob = 0;
+    L.g[0].tma_store = 0;
+    stages = (int)(((size_t)SMEM_MAX - fixed) / stage);
+  }
   if (stages > (ta ? 4 : 6)) stages = ta ? 4 : 6;
   if (cfg.stages >= 2 && cfg.stages < stages) stages = cfg.stages;
   if (stages < 2) return JFG_ERR_UNSUPPORTED;
@@ -996,13 +1087,14 @@ int launch_groups(int ng, const jfg_contract_desc* const* ds, const void* const*
   L.tmem_a = ta;
   L.mt_max = mt_max;
   L.out_stage = ostage;
-  const size_t smem = 1024 + stages * stage + ob + (3 * stages + 6) * 8 + 16;
+  L.op_res = res ? 1 : 0;
+  L.nslots = res ? nslots : 0;
+  const size_t smem = 1024 + res_bytes * (res ? 1 : 0) + stages * stage + ob +
+                      (3 * stages + 7) * 8 + 16;
   if (smem > (size_t)SMEM_MAX) return JFG_ERR_UNSUPPORTED;
-  int dev = 0, nsm = 0;
-  JFG_CUDA_TRY(cudaGetDevice(&dev));
-  JFG_CUDA_TRY(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev));
-  int ctas = cfg.ctas > 0 && cfg.ctas < nsm ? cfg.ctas : nsm;
-  dim3 grid((unsigned)(tiles < ctas ? tiles : ctas));
+  long long nct = tiles < ctas ? tiles : ctas;
+  if (res) nct = (long long)(ctas / nslots) * nslots;  // the same CTA count per slot
+  dim3 grid((unsigned)nct);
   JFG_TRY(setup_kernel_attr());
 #define JFG_LAUNCH(E)                                                          \
   do {                                                                         \
@@ -1202,6 +1294,12 @@ extern "C" int jfg_tc_set_wait_budget_ns(unsigned long long ns) {
 extern "C" int jfg_tc_test_hold(int on) {
   if (on != 0 && on != 1) return JFG_ERR_ARG;
   JFG_CUDA_TRY(cudaMemcpyToSymbol(jfg::g_tc_test_hold, &on, sizeof(on)));
+  return JFG_OK;
+}
+
+extern "C" int jfg_tc_set_op_resident(int on) {
+  if (on < 0 || on > 2) return JFG_ERR_ARG;
+  jfg::g_op_resident = on;
   return JFG_OK;
 }
 

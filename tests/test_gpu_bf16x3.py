@@ -13,6 +13,16 @@ pytestmark = pytest.mark.gpu
 B3_TOL = 6e-5
 
 
+@pytest.fixture(params=[1, 2, 0], ids=["sched-auto", "op-resident", "streaming"], autouse=True)
+def schedule(request):
+    """Operator-stationary schedule: automatic (what large launches get),
+    forced wherever the operator chunk fits, or off."""
+    L = _lib.lib()
+    assert L.jfg_tc_set_op_resident(request.param) == 0
+    yield request.param
+    L.jfg_tc_set_op_resident(1)
+
+
 def split16(op64):
     L = _lib.lib()
     a = np.ascontiguousarray(op64, dtype=np.float64)

@@ -15,10 +15,20 @@ def rel(a, b):
     return np.abs(a - b).max() / np.abs(b).max()
 
 
+@pytest.fixture(params=[1, 2], ids=["sched-auto", "op-resident"])
+def schedule(request):
+    from jaxfun_gb300 import _lib
+
+    L = _lib.lib()
+    assert L.jfg_tc_set_op_resident(request.param) == 0
+    yield request.param
+    L.jfg_tc_set_op_resident(1)
+
+
 @pytest.mark.parametrize("apply", ["f16x3", "tf32"])
 @pytest.mark.parametrize("precond", ["bf16x3", "tf32"])
 @pytest.mark.parametrize("ndim,N,batch", [(2, 32, 3), (2, 64, 2), (3, 16, 2)])
-def test_mixed_matches_fp64(ndim, N, batch, precond, apply):
+def test_mixed_matches_fp64(ndim, N, batch, precond, apply, schedule):
     V = FunctionSpace(N, Legendre, bcs=DIRICHLET)
     T = TensorProduct(*([V] * ndim))
     rng = np.random.default_rng(N + ndim)

@@ -216,9 +216,10 @@ def run_f16(op64, x32, epi=0, field=None, in_max_scale=1.0):
             t_out_max.cpu().numpy().view(np.float32).astype(np.float64))
 
 
+@pytest.mark.parametrize("sched", [1, 2, 0])
 @pytest.mark.parametrize("S,M,P,K,epi", [(1, 512, 256, 256, 0), (2, 256, 200, 200, 1),
-                                         (1, 96, 130, 512, 0)])
-def test_f16x3_matches_fp64(S, M, P, K, epi):
+                                         (1, 96, 130, 512, 0), (2, 64, 128, 512, 1)])
+def test_f16x3_matches_fp64(S, M, P, K, epi, sched):
     """Scaled split-FP16 contraction against FP64 of the same FP32 inputs,
     per problem (1e-5 of each problem's output maximum), with problems of
     very different magnitudes, a zero problem, a loose input bound (2^9 too
@@ -233,8 +234,13 @@ def test_f16x3_matches_fp64(S, M, P, K, epi):
     ref = np.einsum("smk,bspk->bsmp", op, x.astype(np.float64))
     if epi == 1:
         ref = ref * field.astype(np.float32).astype(np.float64)
-    for bound in (1.0, 512.0):
-        got, omax = run_f16(op, x, epi, field, in_max_scale=bound)
+    L = _lib.lib()
+    assert L.jfg_tc_set_op_resident(sched) == 0
+    try:
+        runs = [run_f16(op, x, epi, field, in_max_scale=bound) for bound in (1.0, 512.0)]
+    finally:
+        L.jfg_tc_set_op_resident(1)
+    for bound, (got, omax) in zip((1.0, 512.0), runs):
         for b in range(B):
             scale = np.abs(ref[b]).max()
             if scale == 0:
