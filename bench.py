@@ -938,8 +938,17 @@ def run_ours(args):
                                            it_out, mws.data_ptr(), mws.numel(), sh)
         _lib.check(st, "pcg_mixed")
 
+    tuned_txt = None
     with torch.cuda.stream(stream):
         prepare(kap, fgrid)
+        if not args.no_autotune:
+            # untimed: each distinct tensor-core pass of the inner solve gets its
+            # fastest launch configuration (kept for the process)
+            tuned = solver.autotune(mws)
+            tuned_txt = "; ".join(
+                f"{t['signature'].split(':', 1)[1]} -> {t['schedule']}, {t['stages'] or 'max'} "
+                f"stages, {t['store']} stores, mtile {t['mtile']} ({1e3 * t['ms']:.1f} us)"
+                for t in tuned)
         for _ in range(args.warmup):
             solve()
         torch.cuda.synchronize()
@@ -1138,6 +1147,7 @@ def run_ours(args):
                "fp64_pcg_iterations_mean": float(np.mean(it64[:])),
                "speedup_vs_fp64_pcg": value / fp64_value,
                "device_status": dev_status,
+               "autotuned_passes": tuned_txt,
                "l2": "inputs+workspace > L2 (129 MB) per step"}
         if mixed_zero is not None:
             cfg["mixed_zero_start_solves_per_s"] = mixed_zero["solves_per_s"]
@@ -1186,6 +1196,8 @@ def main():
     ap.add_argument("--maxiter", type=int, default=1000)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true",
+                    help="launch the inner solve's passes with the default configuration")
     ap.add_argument("--profile", action="store_true",
                     help="stop after the timed solves (for ncu launch lists of the headline)")
     ap.add_argument("--no-learned", action="store_true", help="mixed solve from a zero start")

@@ -191,6 +191,11 @@ typedef struct {
   int ctas;              /* persistent CTAs (0: one per SM)                          */
   int stages;            /* pipeline stages (0: as many as fit, else >= 2)           */
   int mtile;             /* operator rows per tile = MMA N (0: up to 128, else 64)   */
+  int schedule;          /* single-group 16-bit launches: 0 the process setting
+                            (jfg_tc_set_op_resident), 1 streaming, 2 operator-
+                            stationary where the chunk fits                       */
+  int store;             /* epilogue: 0 the process setting (jfg_tc_set_store_path),
+                            1 TMA bulk-tensor stores where allowed, 2 plain stores */
 } jfg_tc_config;
 /*
  * Grouped tensor-core contraction: ngroups independent contractions (each a
@@ -214,6 +219,24 @@ int jfg_contract_tc_grouped(int ngroups, const jfg_contract_desc* descs,
 int jfg_tc_autotune(int ngroups, const jfg_contract_desc* descs, const float* const* op_hi,
                     const float* const* op_lo, const float* const* in, float* const* out,
                     int reps, jfg_tc_config* best, float* best_ms, void* stream);
+/*
+ * Autotuning of single-group launches (jfg_contract_tc, _bf16x3, _f16x3 and
+ * the passes of the solvers built on them).  With on = 1, every launch whose
+ * signature (device, precision, batch, segments, M, P, K, epilogue, beta) has
+ * no tuned configuration yet and that is made outside stream capture first
+ * times the candidates -- pipeline depth (as many as fit, 3, 2) x schedule
+ * (streaming, operator-stationary for 16-bit operators) x epilogue store path
+ * (TMA, plain) x tile height (128, 64) x operand A placement (split TF32) --
+ * with CUDA events on its own operands (the launch runs, so out is written
+ * repeatedly), keeps the fastest for that signature and launches with it;
+ * tuned signatures always launch with their configuration.  Default 0.
+ */
+int jfg_tc_set_autotune(int on);
+/* Tuned single-group signatures: how many, and entry i (its signature as
+ * text, its configuration and its time in ms per launch). */
+int jfg_tc_tuned_count(void);
+int jfg_tc_tuned_entry(int i, char* signature, size_t signature_len, jfg_tc_config* cfg,
+                       float* ms);
 /* Split n FP64 values into TF32 hi (round to nearest) and FP32 lo = x - hi
  * (host arrays), the operator format jfg_contract_tc expects. */
 void jfg_split_tf32_host(size_t n, const double* src, float* hi, float* lo);
@@ -562,6 +585,13 @@ int jfg_pcg_varcoef_mixed_guess(const jfg_mixed_plan* plan, const double* rhs, d
                                 const double* guess, int use_x0, double tol, double inner_tol,
                                 int max_outer, int maxiter_inner, int* inner_iters,
                                 int* outer_iters, void* work, size_t work_bytes, void* stream);
+/* Autotune the tensor-core passes of this plan's inner solve (no counterpart
+ * in the reference): runs one operator apply and one preconditioner solve on
+ * the (zeroed) workspace with jfg_tc_set_autotune's tuning on, so each
+ * distinct pass signature keeps its fastest launch configuration for the
+ * process.  Synchronous; call before solving (outside stream capture). */
+int jfg_pcg_mixed_autotune(const jfg_mixed_plan* plan, void* work, size_t work_bytes,
+                           void* stream);
 
 #ifdef __cplusplus
 }

@@ -45,7 +45,8 @@ class NotConvergedError(JfgError):
 
 class TcConfig(C.Structure):
     _fields_ = [("operand_a_in_tmem", C.c_int), ("order", C.c_int), ("ctas", C.c_int),
-                ("stages", C.c_int), ("mtile", C.c_int)]
+                ("stages", C.c_int), ("mtile", C.c_int), ("schedule", C.c_int),
+                ("store", C.c_int)]
 
 
 class ContractDesc(C.Structure):
@@ -88,6 +89,9 @@ SIGNATURES = {
     "jfg_tp_apply_tc_bf16x3": (_i, [_i, _vp, _vp, _i, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
     "jfg_tc_set_store_path": (_i, [_i]),
     "jfg_tc_set_op_resident": (_i, [_i]),
+    "jfg_tc_set_autotune": (_i, [_i]),
+    "jfg_tc_tuned_count": (_i, []),
+    "jfg_tc_tuned_entry": (_i, [_i, C.c_char_p, _sz, _vp, _vp]),
     "jfg_banded_lu_size": (_sz, [_i, _i, _i, _i]),
     "jfg_banded_lu_factor_f64": (_i, [_i, _i, _i, _vp, _vp, _vp, _vp]),
     "jfg_banded_lu_solve_f64": (_i, [_i, _i, _i, _i, _vp, _vp, _vp, C.c_longlong,
@@ -136,6 +140,7 @@ SIGNATURES = {
     "jfg_varcoef_apply_f64": (_i, [_i, _i, _i, _i, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
     "jfg_varcoef_apply_f32": (_i, [_i, _i, _i, _i, _vp, _vp, _vp, _vp, _vp, _sz, _vp]),
     "jfg_pcg_mixed_workspace_size": (_sz, [_i, _i, _i, _i]),
+    "jfg_pcg_mixed_autotune": (_i, [_vp, _vp, _sz, _vp]),
     "jfg_pcg_varcoef_mixed": (_i, [_vp, _vp, _vp, _i, _d, _d, _i, _i, C.POINTER(_i),
                                    C.POINTER(_i), _vp, _sz, _vp]),
     "jfg_pcg_varcoef_mixed_guess": (_i, [_vp, _vp, _vp, _vp, _i, _d, _d, _i, _i, C.POINTER(_i),
@@ -242,3 +247,22 @@ SIGNATURES.update({
     "jfg_adam_step": (_i, [_ll, _vp, _vp, _vp, _vp, _f, _f, _f, _f, _i, _vp, _vp, _i, _i, _vp]),
     "jfg_sno_mse": (_i, [_ll, _vp, _ll, _vp, _vp, _vp, _vp, _vp]),
 })
+
+
+def tuned_configs() -> list[dict]:
+    """Single-group tensor-core launch configurations chosen by the autotuner
+    (jfg_tc_set_autotune / jfg_pcg_mixed_autotune), with their signatures and
+    times."""
+    L = lib()
+    out = []
+    buf = C.create_string_buffer(256)
+    for i in range(L.jfg_tc_tuned_count()):
+        cfg = TcConfig()
+        ms = C.c_float()
+        check(L.jfg_tc_tuned_entry(i, buf, 256, C.byref(cfg), C.byref(ms)), "jfg_tc_tuned_entry")
+        out.append({"signature": buf.value.decode(), "ms": ms.value,
+                    "operand_a_in_tmem": cfg.operand_a_in_tmem, "stages": cfg.stages,
+                    "mtile": cfg.mtile or 128,
+                    "schedule": {0: "default", 1: "streaming", 2: "operator-stationary"}[cfg.schedule],
+                    "store": {0: "default", 1: "tma", 2: "plain"}[cfg.store]})
+    return out

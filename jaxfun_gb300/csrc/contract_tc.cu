@@ -54,9 +54,10 @@ static int g_operand_a_in_tmem = 1;
 // allows (default), 0 plain coalesced stores (jfg_tc_set_store_path).
 static int g_tma_store = 1;
 // Operator-stationary schedule for single-group 16-bit launches whose
-// operator chunk fits in shared memory: 0 off, 1 (default) when every CTA gets
-// >= 2 tiles, 2 whenever the chunk fits (jfg_tc_set_op_resident).
-static int g_op_resident = 1;
+// operator chunk fits in shared memory: 0 (default) off, 1 when every CTA gets
+// >= 2 tiles, 2 whenever the chunk fits (jfg_tc_set_op_resident); a launch
+// configuration's schedule field overrides it.
+static int g_op_resident = 0;
 
 namespace {
 
@@ -1038,7 +1039,7 @@ int launch_groups(int ng, const jfg_contract_desc* const* ds, const void* const*
       L.g[i].op_inv = h16->op_inv;
       L.g[i].op_inv_seg = h16->op_inv_seg;
     }
-    if (!g_tma_store) L.g[i].tma_store = 0;
+    if (cfg.store == 2 || (cfg.store == 0 && !g_tma_store)) L.g[i].tma_store = 0;
     tiles += group_tiles(L.g[i]);
     if (L.g[i].Mtile > mt_max) mt_max = L.g[i].Mtile;
     ostage |= L.g[i].tma_store;
@@ -1057,14 +1058,15 @@ int launch_groups(int ng, const jfg_contract_desc* const* ds, const void* const*
   bool res = false;
   int nslots = 0;
   size_t res_bytes = 0;
-  if (b16 && ng == 1 && g_op_resident) {
+  const int sched = cfg.schedule == 1 ? 0 : cfg.schedule == 2 ? 2 : g_op_resident;
+  if (b16 && ng == 1 && sched) {
     const TcGroup& q = L.g[0];
     const int mch = (q.d.M + q.Mtile - 1) / q.Mtile;
     nslots = q.d.nseg * mch;
     res_bytes = (size_t)((q.d.K + 63) / 64) * 2 * (size_t)q.Mtile * 128;
     const long long per_slot = (long long)((q.d.P + TILE_P - 1) / TILE_P) * q.d.batch;
     const size_t room = (size_t)SMEM_MAX - 1024 - 64 * 8;
-    res = nslots <= ctas && (g_op_resident == 2 || per_slot * nslots >= 2LL * ctas) &&
+    res = nslots <= ctas && (sched == 2 || per_slot * nslots >= 2LL * ctas) &&
           res_bytes + 2 * (2 * (size_t)XBYTES) <= room;
   }
   const size_t stage = res ? 2 * (size_t)XBYTES
@@ -1147,25 +1149,130 @@ jfg_tc_config tc_default_config() {
   c.ctas = 0;
   c.stages = 0;
   c.mtile = 0;
+  c.schedule = 0;
+  c.store = 0;
   return c;
+}
+
+// ---- single-group launches: tuned configurations -------------------------
+
+struct SingleTuned {
+  jfg_tc_config cfg;
+  float ms;
+};
+std::mutex g_single_mu;
+std::map<std::string, SingleTuned> g_single;
+int g_tune_single = 0;
+
+std::string single_signature(int prec, const jfg_contract_desc& d) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  char buf[200];
+  snprintf(buf, sizeof buf, "d%d:p%d:b%d:s%d:M%d:P%d:K%d:e%d:beta%d", dev, prec, d.batch, d.nseg,
+           d.M, d.P, d.K, d.epilogue, d.beta != 0.0 ? 1 : 0);
+  return buf;
+}
+
+// Time every candidate configuration of this launch on its own operands and
+// keep the fastest for its signature.
+int tune_single(int prec, const jfg_contract_desc& d, const void* oh, const void* ol,
+                const float* in, float* out, const H16Aux* aux, cudaStream_t st,
+                const std::string& key, jfg_tc_config* best) {
+  const jfg_contract_desc* dp = &d;
+  std::vector<jfg_tc_config> cands;
+  for (int ta : {1, 0})
+    for (int sched : {1, 2})
+      for (int sg : {0, 3, 2})
+        for (int store : {1, 2})
+          for (int mt : {0, 64}) {
+            if ((prec != 0 && ta == 0) || (prec == 0 && sched == 2)) continue;
+            jfg_tc_config c = tc_default_config();
+            c.operand_a_in_tmem = ta;
+            c.schedule = sched;
+            c.stages = sg;
+            c.store = store;
+            c.mtile = mt;
+            cands.push_back(c);
+          }
+  cudaEvent_t e0, e1;
+  JFG_CUDA_TRY(cudaEventCreate(&e0));
+  JFG_CUDA_TRY(cudaEventCreate(&e1));
+  const int reps = 3;
+  float bt = -1.f;
+  jfg_tc_config bc = tc_default_config();
+  int status = JFG_OK;
+  for (const jfg_tc_config& c : cands) {
+    int s = launch_groups<1>(1, &dp, &oh, &ol, &in, &out, c, prec, st, aux);  // warm
+    if (s == JFG_ERR_UNSUPPORTED) continue;  // does not fit: not a candidate
+    if (s != JFG_OK) {
+      status = s;
+      break;
+    }
+    if (cudaEventRecord(e0, st) != cudaSuccess) {
+      status = JFG_ERR_CUDA;
+      break;
+    }
+    for (int r = 0; r < reps && s == JFG_OK; ++r)
+      s = launch_groups<1>(1, &dp, &oh, &ol, &in, &out, c, prec, st, aux);
+    float ms = 0.f;
+    if (s != JFG_OK || cudaEventRecord(e1, st) != cudaSuccess ||
+        cudaEventSynchronize(e1) != cudaSuccess || cudaEventElapsedTime(&ms, e0, e1) != cudaSuccess) {
+      status = s != JFG_OK ? s : JFG_ERR_CUDA;
+      break;
+    }
+    ms /= (float)reps;
+    if (bt < 0.f || ms < bt) {
+      bt = ms;
+      bc = c;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  if (status != JFG_OK) return status;
+  if (bt >= 0.f) {
+    std::lock_guard<std::mutex> lk(g_single_mu);
+    g_single[key] = SingleTuned{bc, bt};
+  }
+  *best = bc;
+  return JFG_OK;
+}
+
+// One single-group launch with the tuned configuration of its signature (or
+// the default); with autotuning on, an untuned signature launched outside
+// stream capture is tuned first.
+int launch_single(int prec, const jfg_contract_desc& d, const void* oh, const void* ol,
+                  const float* in, float* out, const H16Aux* aux, cudaStream_t st) {
+  const jfg_contract_desc* dp = &d;
+  jfg_tc_config cfg = tc_default_config();
+  const std::string key = single_signature(prec, d);
+  bool found = false;
+  {
+    std::lock_guard<std::mutex> lk(g_single_mu);
+    auto it = g_single.find(key);
+    if (it != g_single.end()) {
+      cfg = it->second.cfg;
+      found = true;
+    }
+  }
+  if (!found && g_tune_single) {
+    cudaStreamCaptureStatus cs = cudaStreamCaptureStatusNone;
+    JFG_CUDA_TRY(cudaStreamIsCapturing(st, &cs));
+    if (cs == cudaStreamCaptureStatusNone)
+      JFG_TRY(tune_single(prec, d, oh, ol, in, out, aux, st, key, &cfg));
+  }
+  return launch_groups<1>(1, &dp, &oh, &ol, &in, &out, cfg, prec, st, aux);
 }
 
 int contract_tc(const jfg_contract_desc& d, const float* op_hi, const float* op_lo,
                 const float* in, float* out, cudaStream_t st) {
   if (d.batch == 0 || d.M == 0 || d.P == 0) return validate_desc(d);
-  const jfg_contract_desc* dp = &d;
-  const void* oh = op_hi;
-  const void* ol = op_lo;
-  return launch_groups<1>(1, &dp, &oh, &ol, &in, &out, tc_default_config(), 0, st);
+  return launch_single(0, d, op_hi, op_lo, in, out, nullptr, st);
 }
 
 int contract_tc_b16(const jfg_contract_desc& d, const uint16_t* op_hi, const uint16_t* op_lo,
                     const float* in, float* out, cudaStream_t st) {
   if (d.batch == 0 || d.M == 0 || d.P == 0) return validate_desc(d);
-  const jfg_contract_desc* dp = &d;
-  const void* oh = op_hi;
-  const void* ol = op_lo;
-  return launch_groups<1>(1, &dp, &oh, &ol, &in, &out, tc_default_config(), 1, st);
+  return launch_single(1, d, op_hi, op_lo, in, out, nullptr, st);
 }
 
 int contract_tc_h16(const jfg_contract_desc& d, const uint16_t* op_hi, const uint16_t* op_lo,
@@ -1173,12 +1280,12 @@ int contract_tc_h16(const jfg_contract_desc& d, const uint16_t* op_hi, const uin
                     unsigned* out_max, const float* in, float* out, cudaStream_t st) {
   if (d.batch == 0 || d.M == 0 || d.P == 0) return validate_desc(d);
   if (!op_inv || !in_max) return JFG_ERR_ARG;
-  const jfg_contract_desc* dp = &d;
-  const void* oh = op_hi;
-  const void* ol = op_lo;
   const H16Aux aux{in_max, out_max, op_inv, op_inv_seg};
-  return launch_groups<1>(1, &dp, &oh, &ol, &in, &out, tc_default_config(), 2, st, &aux);
+  return launch_single(2, d, op_hi, op_lo, in, out, &aux, st);
 }
+
+void set_single_autotune(int on) { g_tune_single = on; }
+int single_autotune() { return g_tune_single; }
 
 int contract_tc_grouped(int ng, const jfg_contract_desc* ds, const float* const* op_hi,
                         const float* const* op_lo, const float* const* in, float* const* out,
@@ -1294,6 +1401,29 @@ extern "C" int jfg_tc_set_wait_budget_ns(unsigned long long ns) {
 extern "C" int jfg_tc_test_hold(int on) {
   if (on != 0 && on != 1) return JFG_ERR_ARG;
   JFG_CUDA_TRY(cudaMemcpyToSymbol(jfg::g_tc_test_hold, &on, sizeof(on)));
+  return JFG_OK;
+}
+
+extern "C" int jfg_tc_set_autotune(int on) {
+  if (on != 0 && on != 1) return JFG_ERR_ARG;
+  jfg::set_single_autotune(on);
+  return JFG_OK;
+}
+
+extern "C" int jfg_tc_tuned_count(void) {
+  std::lock_guard<std::mutex> lk(jfg::g_single_mu);
+  return (int)jfg::g_single.size();
+}
+
+extern "C" int jfg_tc_tuned_entry(int i, char* signature, size_t signature_len,
+                                  jfg_tc_config* cfg, float* ms) {
+  std::lock_guard<std::mutex> lk(jfg::g_single_mu);
+  if (i < 0 || i >= (int)jfg::g_single.size()) return JFG_ERR_ARG;
+  auto it = jfg::g_single.begin();
+  std::advance(it, i);
+  if (signature && signature_len > 0) snprintf(signature, signature_len, "%s", it->first.c_str());
+  if (cfg) *cfg = it->second.cfg;
+  if (ms) *ms = it->second.ms;
   return JFG_OK;
 }
 

@@ -98,6 +98,9 @@ int contract_tc_grouped(int ng, const jfg_contract_desc* ds, const float* const*
                         const float* const* op_lo, const float* const* in, float* const* out,
                         const jfg_tc_config& cfg, cudaStream_t st);
 jfg_tc_config tc_default_config();
+// Process-wide autotuning of single-group tensor-core launches (contract_tc.cu)
+void set_single_autotune(int on);
+int single_autotune();
 // One-time per-device setup of the tensor-core kernels (shared-memory opt-in,
 // tensor-map encoder); call before capturing their first launch into a graph.
 int tc_setup();

@@ -172,6 +172,59 @@ extern "C" int jfg_pcg_varcoef_mixed_guess(const jfg_mixed_plan* plan, const dou
                                            int* outer_iters, void* work, size_t work_bytes,
                                            void* stream);
 
+// Tune the tensor-core passes of the inner solve: one operator apply and one
+// preconditioner solve on zeroed workspace vectors with autotuning on, so
+// every distinct pass signature gets its fastest configuration (kept for the
+// process) before the solve captures its iteration graph.
+extern "C" int jfg_pcg_mixed_autotune(const jfg_mixed_plan* plan, void* work, size_t work_bytes,
+                                      void* stream) {
+  using namespace jfg;
+  if (!plan) return JFG_ERR_ARG;
+  const jfg_mixed_plan& P = *plan;
+  if ((P.ndim != 2 && P.ndim != 3) || P.n < 1 || P.nq < P.n || P.batch < 1 || !P.ops_hi ||
+      !P.ops_lo || !P.kw32 || !P.E_hi || !P.E_lo || !P.W_hi || !P.W_lo || !P.lam ||
+      (P.precond_bf16 && (!P.E_hi16 || !P.E_lo16 || !P.W_hi16 || !P.W_lo16)) ||
+      (P.apply_f16 && (P.ndim != 2 || (P.nq & 7) || !P.ops_hi16 || !P.ops_lo16 ||
+                       !P.ops_inv16)))
+    return JFG_ERR_ARG;
+  const int ndim = P.ndim, nq = P.nq, batch = P.batch;
+  const MixedLayout Lo = layout(ndim, P.n, nq, batch);
+  if (!work || work_bytes < Lo.total) return JFG_ERR_WORKSPACE;
+  cudaStream_t st = (cudaStream_t)stream;
+  char* w = (char*)work + Lo.vec64 + Lo.part + 2 * Lo.sc;
+  float* r32 = (float*)w;
+  float* d32 = (float*)(w + Lo.vec32);
+  char* wsin = w + 2 * Lo.vec32 + Lo.ws64;
+  unsigned* slots = (unsigned*)wsin;
+  const size_t sb = align_up((size_t)4 * batch * sizeof(unsigned), 256);
+  void* inner = wsin + sb;
+  const size_t inner_bytes = Lo.wsin - sb;
+  JFG_CUDA_TRY(cudaMemsetAsync(r32, 0, Lo.vec32, st));
+  JFG_CUDA_TRY(cudaMemsetAsync(slots, 0, sb, st));
+  H16Ops h16;
+  h16.op_inv = P.ops_inv16;
+  h16.slots = slots;
+  const bool th = P.apply_f16 != 0;
+  const bool pbf = P.precond_bf16 != 0;
+  const OpRef<float> ops = th ? OpRef<float>{(const float*)P.ops_hi16, (const float*)P.ops_lo16}
+                              : OpRef<float>{P.ops_hi, P.ops_lo};
+  const OpRef<float> E = pbf ? OpRef<float>{(const float*)P.E_hi16, (const float*)P.E_lo16}
+                             : OpRef<float>{P.E_hi, P.E_lo};
+  const OpRef<float> W = pbf ? OpRef<float>{(const float*)P.W_hi16, (const float*)P.W_lo16}
+                             : OpRef<float>{P.W_hi, P.W_lo};
+  const int prev = single_autotune();
+  set_single_autotune(1);
+  int s = varcoef_apply<float>(th ? Engine::TH : Engine::TC, ndim, nq, nq, batch, ops, P.kw32,
+                               r32, d32, inner, inner_bytes, st, Active(), th ? &h16 : nullptr);
+  if (s == JFG_OK)
+    s = fd_solve<float>(pbf ? Engine::TB : Engine::TC, ndim, nq, batch, E, W, P.lam, nullptr,
+                        P.fd_scale, r32, d32, inner, inner_bytes, st);
+  set_single_autotune(prev);
+  if (s != JFG_OK) return s;
+  JFG_CUDA_TRY(cudaStreamSynchronize(st));
+  return JFG_OK;
+}
+
 extern "C" int jfg_pcg_varcoef_mixed(const jfg_mixed_plan* plan, const double* rhs, double* x,
                                      int use_x0, double tol, double inner_tol, int max_outer,
                                      int maxiter_inner, int* inner_iters, int* outer_iters,

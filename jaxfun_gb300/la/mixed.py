@@ -142,6 +142,17 @@ class MixedVarCoefSolver:
                               self.ops16[1].data_ptr() if af else None,
                               self.ops16[2].data_ptr() if af else None)
 
+    def autotune(self, ws=None) -> list[dict]:
+        """Tune the tensor-core passes of the inner solve once (each distinct
+        pass signature keeps its fastest launch configuration for the
+        process); returns the tuned configurations."""
+        L = _lib.lib()
+        if ws is None:
+            ws = workspace(self.workspace_bytes(), slot=1)
+        _lib.check(L.jfg_pcg_mixed_autotune(C.byref(self.plan), ws.data_ptr(), ws.numel(),
+                                            _lib.stream_handle()), "jfg_pcg_mixed_autotune")
+        return _lib.tuned_configs()
+
     def workspace_bytes(self) -> int:
         A = self.A
         return int(_lib.lib().jfg_pcg_mixed_workspace_size(A.ndim, A.n, A.nq, A.batch))

@@ -71,3 +71,24 @@ def test_mixed_with_initial_guess_and_converged_problem():
     x, it_in, it_out = MixedVarCoefSolver(A).solve(b, x0=x0, tol=1e-12)
     assert it_out[0] == 0 and it_out[1] >= 1
     assert rel(x.cpu().numpy()[1], xr.cpu().numpy()[1]) < 1e-10
+
+
+def test_mixed_after_autotune():
+    """The solver's autotune tunes every distinct tensor-core pass of its inner
+    solve; the solve with the tuned configurations still reaches 1e-10."""
+    N, batch = 64, 3
+    V = FunctionSpace(N, Legendre, bcs=DIRICHLET)
+    T = TensorProduct(V, V)
+    rng = np.random.default_rng(77)
+    kap = np.exp(rng.standard_normal((batch, N, N)))
+    b = rng.standard_normal((batch, N - 2, N - 2))
+    A = VarCoefMatrix(T, kap)
+    S = MixedVarCoefSolver(A)
+    tuned = S.autotune()
+    sigs = [t["signature"] for t in tuned]
+    assert any(":p2:b3:" in s for s in sigs) and any(":p1:b3:" in s for s in sigs), sigs
+    xr, _ = pcg(A, b, tol=1e-14, maxiter=3000)
+    x, _, _ = S.solve(b, tol=1e-12)
+    xr, x = xr.cpu().numpy(), x.cpu().numpy()
+    for i in range(batch):
+        assert rel(x[i], xr[i]) < 1e-10
