@@ -253,20 +253,20 @@ def test_f16x3_matches_fp64(S, M, P, K, epi, sched):
 def test_autotuned_launch_is_correct_and_recorded():
     """With autotuning on, the first launch of a signature times its candidate
     configurations (including the operator-stationary schedule and plain
-    stores), records the winner, and the result is still correct; the next
-    launch of that signature uses the recorded configuration."""
+    stores) and records the winner (a signature tuned earlier in the process
+    keeps its entry); the result is correct, and so is the next launch of that
+    signature, which uses the recorded configuration."""
     L = _lib.lib()
     rng = np.random.default_rng(33)
     op = rng.standard_normal((1, 256, 256))
     x = rng.standard_normal((6, 1, 256, 256)).astype(np.float32)
     ref = np.einsum("smk,bspk->bsmp", op, x.astype(np.float64))
-    n0 = L.jfg_tc_tuned_count()
     assert L.jfg_tc_set_autotune(1) == 0
     try:
         got, _ = run_f16(op, x)
     finally:
         L.jfg_tc_set_autotune(0)
-    assert L.jfg_tc_tuned_count() >= n0 + 1
+    assert L.jfg_tc_tuned_count() >= 1
     entries = _lib.tuned_configs()
     assert any("p2:b6:s1:M256:P256:K256" in e["signature"] for e in entries)
     assert np.abs(got - ref).max() <= TC_TOL * np.abs(ref).max()
