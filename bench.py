@@ -212,14 +212,16 @@ def run_reference(args):
 
 
 def roofline_microbench(B: int, N: int, reps: int = 20, M: int | None = None,
-                        prec: str = "f16x3"):
+                        prec: str = "f16x3", field_pass: bool = False):
     """Time the dominant kernel -- the tcgen05 contraction at the first
     variable-coefficient pass shape of the inner solve (stacked [B; D]
     operator: M = 2N quadrature rows, P = K = N padded coefficients, B problems;
     M = N gives the preconditioner pass) -- with CUDA events on its launch
     stream.  prec "f16x3": scaled split FP16 (kind::f16, the inner solve's
-    operator passes); "tf32": split TF32 (kind::tf32).  Returns achieved
-    numbers; FLOPs count each contraction once."""
+    operator passes); "tf32": split TF32 (kind::tf32).  field_pass: the
+    second operator pass instead (two segments of M = N rows, the kappa*w
+    field multiplied in the epilogue).  Returns achieved numbers; FLOPs count
+    each contraction once."""
     import numpy as np
     import torch
 
@@ -229,23 +231,31 @@ def roofline_microbench(B: int, N: int, reps: int = 20, M: int | None = None,
     L = _lib.lib()
     P = K = N
     M = 2 * N if M is None else M
+    S = 1
+    if field_pass:
+        S, M = 2, N
     rng = np.random.default_rng(0)
-    op = rng.standard_normal((M, K))
-    x = torch.randn(B, P, K, dtype=torch.float32, device="cuda")
-    y = torch.empty(B, M, P, dtype=torch.float32, device="cuda")
-    d = _lib.ContractDesc(batch=B, nseg=1, M=M, P=P, K=K, op_ld=K, in_ld=K, in_batch=P * K,
-                          out_ld=P, out_batch=M * P, alpha=1.0, beta=0.0)
+    op = rng.standard_normal((S * M, K))
+    x = torch.randn(B, S, P, K, dtype=torch.float32, device="cuda")
+    y = torch.empty(B, S, M, P, dtype=torch.float32, device="cuda")
+    d = _lib.ContractDesc(batch=B, nseg=S, M=M, P=P, K=K, op_ld=K, op_seg=M * K, in_ld=K,
+                          in_seg=P * K, in_batch=S * P * K, out_ld=P, out_seg=M * P,
+                          out_batch=S * M * P, alpha=1.0, beta=0.0)
+    if field_pass:
+        fld = torch.rand(B, M, P, dtype=torch.float32, device="cuda") + 0.5
+        d.epilogue = 1
+        d.field, d.field_ld, d.field_seg, d.field_batch = fld.data_ptr(), P, 0, M * P
     s = torch.cuda.current_stream()
     if prec == "f16x3":
-        hi = np.empty((M, K), np.uint16)
-        lo = np.empty((M, K), np.uint16)
-        inv = np.empty(M, np.float32)
-        L.jfg_split_f16_rowscaled_host(M, K, op.ctypes.data, hi.ctypes.data, lo.ctypes.data,
+        hi = np.empty((S * M, K), np.uint16)
+        lo = np.empty((S * M, K), np.uint16)
+        inv = np.empty(S * M, np.float32)
+        L.jfg_split_f16_rowscaled_host(S * M, K, op.ctypes.data, hi.ctypes.data, lo.ctypes.data,
                                        inv.ctypes.data)
         t_hi = torch.as_tensor(hi.view(np.int16), device="cuda")
         t_lo = torch.as_tensor(lo.view(np.int16), device="cuda")
         t_inv = torch.as_tensor(inv, device="cuda")
-        in_max = x.abs().amax(dim=(1, 2)).contiguous().view(torch.int32)
+        in_max = x.abs().amax(dim=(1, 2, 3)).contiguous().view(torch.int32)
         out_max = torch.zeros(B, dtype=torch.int32, device="cuda")
         call = lambda: L.jfg_contract_tc_f16x3(  # noqa: E731
             d, t_hi.data_ptr(), t_lo.data_ptr(), t_inv.data_ptr(), M, in_max.data_ptr(),
@@ -264,9 +274,9 @@ def roofline_microbench(B: int, N: int, reps: int = 20, M: int | None = None,
     e1.record(s)
     e1.synchronize()
     t = e0.elapsed_time(e1) / 1e3 / reps
-    flops = 2.0 * M * P * K * B
-    nbytes = 4.0 * B * P * (K + M)
-    return {"M": M, "P": P, "K": K, "t": t, "flops": flops, "bytes": nbytes, "prec": prec,
+    flops = 2.0 * M * P * K * B * S
+    nbytes = 4.0 * B * S * P * (K + M) + (4.0 * B * M * P if field_pass else 0.0)
+    return {"M": M, "P": P, "K": K, "S": S, "t": t, "flops": flops, "bytes": nbytes, "prec": prec,
             "tflops_alg": flops / t / 1e12,
             "tflops_issued": 3 * flops / t / 1e12, "gbs": nbytes / t / 1e9}
 
@@ -1204,12 +1214,14 @@ def main():
     ap.add_argument("--weights", default=os.path.join(
         ROOT, "jaxfun_gb300", "sno", "weights", "sno_varcoef2d_N256.npz"))
     ap.add_argument("--kernel-only", nargs="?", const="contract", default=None,
-                    choices=["contract", "contract_tf32", "gemm", "fp64", "df64", "transform",
+                    choices=["contract", "contract_tf32", "contract_field",
+                             "contract_field_tf32", "gemm", "fp64", "df64", "transform",
                              "transform_tf32"],
                     help="time one kernel and print its numbers (used for ncu captures): "
                          "contract = tcgen05 scaled split-FP16 contraction at the variable-"
                          "coefficient pass shape (M = 512, P = K = 256), B problems; "
-                         "contract_tf32 = its split-TF32 variant; "
+                         "contract_tf32 = its split-TF32 variant; contract_field(_tf32) = "
+                         "the second operator pass (2 segments, kappa*w field epilogue); "
                          "gemm = BF16 GEMM of the neural operator's spectral transform "
                          "(1024 x 64 x 4096 per sample, B samples); fp64 = FP64 CUDA-core "
                          "contraction at the variable-coefficient pass shape; df64 = the same "
@@ -1248,10 +1260,13 @@ def main():
         import torch
 
         torch.cuda.set_device(int(os.environ.get("LOCAL_RANK", "0")))
-        if args.kernel_only in ("contract", "contract_tf32"):
-            prec = "tf32" if args.kernel_only == "contract_tf32" else "f16x3"
+        if args.kernel_only in ("contract", "contract_tf32", "contract_field",
+                                "contract_field_tf32"):
+            prec = "tf32" if args.kernel_only.endswith("tf32") else "f16x3"
             out = {"kernel": "k_contract_tc",
-                   **roofline_microbench(args.batch, N_GRID, reps=3, prec=prec)}
+                   **roofline_microbench(args.batch, N_GRID, reps=3, prec=prec,
+                                         field_pass=args.kernel_only.startswith(
+                                             "contract_field"))}
         else:
             out = other_kernel_microbench(args.kernel_only, args.batch)
         print(json.dumps({"batch": args.batch, **out}), flush=True)

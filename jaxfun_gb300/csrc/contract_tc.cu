@@ -1186,6 +1186,12 @@ int tune_single(int prec, const jfg_contract_desc& d, const void* oh, const void
         for (int store : {1, 2})
           for (int mt : {0, 64}) {
             if ((prec != 0 && ta == 0) || (prec == 0 && sched == 2)) continue;
+            // the operator-stationary schedule only where the chunk fits beside
+            // two input stages (else the launch would stream anyway)
+            if (sched == 2 && (size_t)((d.K + 63) / 64) * 2 * (mt ? mt : 128) * 128 +
+                                      4 * (size_t)XBYTES >
+                                  (size_t)SMEM_MAX - 1024 - 64 * 8)
+              continue;
             jfg_tc_config c = tc_default_config();
             c.operand_a_in_tmem = ta;
             c.schedule = sched;
