@@ -308,6 +308,17 @@ __device__ __forceinline__ void tmem_st32(uint32_t taddr, const uint32_t* v) {
       : "memory");
 }
 
+// Store 16 consecutive 32-bit columns of this thread's TMEM lane.
+__device__ __forceinline__ void tmem_st16(uint32_t taddr, const uint32_t* v) {
+  asm volatile(
+      "tcgen05.st.sync.aligned.32x32b.x16.b32 [%0], "
+      "{%1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, %15, %16};" ::"r"(taddr),
+      "r"(v[0]), "r"(v[1]), "r"(v[2]), "r"(v[3]), "r"(v[4]), "r"(v[5]), "r"(v[6]), "r"(v[7]),
+      "r"(v[8]), "r"(v[9]), "r"(v[10]), "r"(v[11]), "r"(v[12]), "r"(v[13]), "r"(v[14]),
+      "r"(v[15])
+      : "memory");
+}
+
 __device__ __forceinline__ void mma_commit(uint64_t* bar) {
   asm volatile(
       "tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(
@@ -631,54 +642,55 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           break;
         }
         if (H16) {
-          // 64 FP32 of this row, scaled by 2^k, -> FP16 hi / lo pairs
-          uint32_t h[32], l[32];
+          // 64 FP32 of this row, scaled by 2^k, -> FP16 hi / lo pairs; one
+          // 32-element half at a time (16 hi and 16 lo columns) keeps the
+          // live registers low
+          const uint32_t tbase = tmem + ((uint32_t)(32 * (warp & 3)) << 16) +
+                                 (uint32_t)(A_COL0 + 64 * st);
 #pragma unroll
           for (int half = 0; half < 2; ++half) {
+            uint32_t h[16], l[16];
             const float4* xr = (const float4*)(Xh(st) + half * XBYTES + row * 128);
 #pragma unroll
             for (int c = 0; c < 8; ++c) {
               const float4 v = xr[c ^ (row & 7)];
               const float a0 = v.x * xsc, a1 = v.y * xsc, a2 = v.z * xsc, a3 = v.w * xsc;
-              const int w = 16 * half + 2 * c;
               const uint32_t h0 = pack_f16x2(a0, a1), h1 = pack_f16x2(a2, a3);
               const float2 f0 = unpack_f16x2(h0), f1 = unpack_f16x2(h1);
-              h[w] = h0;
-              h[w + 1] = h1;
-              l[w] = pack_f16x2(a0 - f0.x, a1 - f0.y);
-              l[w + 1] = pack_f16x2(a2 - f1.x, a3 - f1.y);
+              h[2 * c] = h0;
+              h[2 * c + 1] = h1;
+              l[2 * c] = pack_f16x2(a0 - f0.x, a1 - f0.y);
+              l[2 * c + 1] = pack_f16x2(a2 - f1.x, a3 - f1.y);
             }
+            tmem_st16(tbase + 16 * half, h);
+            tmem_st16(tbase + 32 + 16 * half, l);
           }
-          const uint32_t tbase = tmem + ((uint32_t)(32 * (warp & 3)) << 16) +
-                                 (uint32_t)(A_COL0 + 64 * st);
-          tmem_st32(tbase, h);
-          tmem_st32(tbase + 32, l);
           asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
           asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
         } else if (B16) {
           // 64 FP32 of this row (two swizzled 128-byte rows) -> BF16 hi / lo,
-          // packed in pairs (lower k in the lower half) into 32 TMEM columns each
-          uint32_t h[32], l[32];
+          // packed in pairs (lower k in the lower half) into 32 TMEM columns
+          // each, one 32-element half (16 + 16 columns) at a time
+          const uint32_t tbase = tmem + ((uint32_t)(32 * (warp & 3)) << 16) +
+                                 (uint32_t)(A_COL0 + 64 * st);
 #pragma unroll
           for (int half = 0; half < 2; ++half) {
+            uint32_t h[16], l[16];
             const float4* xr = (const float4*)(Xh(st) + half * XBYTES + row * 128);
 #pragma unroll
             for (int c = 0; c < 8; ++c) {
               const float4 v = xr[c ^ (row & 7)];
-              const int w = 16 * half + 2 * c;
               const uint32_t h0 = pack_bf16x2(v.x, v.y), h1 = pack_bf16x2(v.z, v.w);
-              h[w] = h0;
-              h[w + 1] = h1;
-              l[w] = pack_bf16x2(v.x - __uint_as_float(h0 << 16),
-                                 v.y - __uint_as_float(h0 & 0xFFFF0000u));
-              l[w + 1] = pack_bf16x2(v.z - __uint_as_float(h1 << 16),
-                                     v.w - __uint_as_float(h1 & 0xFFFF0000u));
+              h[2 * c] = h0;
+              h[2 * c + 1] = h1;
+              l[2 * c] = pack_bf16x2(v.x - __uint_as_float(h0 << 16),
+                                     v.y - __uint_as_float(h0 & 0xFFFF0000u));
+              l[2 * c + 1] = pack_bf16x2(v.z - __uint_as_float(h1 << 16),
+                                         v.w - __uint_as_float(h1 & 0xFFFF0000u));
             }
+            tmem_st16(tbase + 16 * half, h);
+            tmem_st16(tbase + 32 + 16 * half, l);
           }
-          const uint32_t tbase = tmem + ((uint32_t)(32 * (warp & 3)) << 16) +
-                                 (uint32_t)(A_COL0 + 64 * st);
-          tmem_st32(tbase, h);
-          tmem_st32(tbase + 32, l);
           asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
           asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
         } else if (ta) {
@@ -761,75 +773,84 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       }
       const uint32_t tacc = tmem + ((uint32_t)(32 * q4) << 16) + (uint32_t)buf * acc_stride;
       for (int c = half * 2; c < Mt / 16; c += 4) {
-        // columns [c*16, c*16+32): two 16-column TMEM loads
+        // columns [c*16, c*16+32), in two halves of 16 (one 16-column TMEM
+        // load each, so only 16-wide arrays are live)
         const int mb = mc * Mt + c * 16;
         const int nj = (c + 1 < Mt / 16) ? 32 : 16;
-        float aux[32], prev[32], osc[32];
-        if (pin) {
-#pragma unroll
-          for (int j = 0; j < 32; ++j) {
-            const int m = mb + j;
-            const bool ok = j < nj && m < d.M;
-            if (EPI == JFG_EPI_MUL_FIELD)
-              aux[j] = ok ? __ldg(fld + (long long)m * d.field_ld + p) : 0.f;
-            else if (EPI == JFG_EPI_DIV_EIG)
-              aux[j] = ok ? __ldg(lam_m + m) : 1.f;
-            if (H16) {
-              // output scale (operator row and input scale) folded into aux
-              // where the epilogue allows
-              const float sc = ok ? __ldg(oinv + m) * xinv : 0.f;
-              if (EPI == JFG_EPI_DIV_EIG)
-                osc[j] = sc;
-              else if (EPI == JFG_EPI_MUL_FIELD)
-                aux[j] *= sc;
-              else
-                aux[j] = sc;
-            }
-            if (BETA) prev[j] = ok ? outS[(long long)m * d.out_ld + p] : 0.f;
-          }
-        }
-        float v[32];
-        tmem_ld16(tacc + (uint32_t)(c * 16), v);
-        if (nj == 32) tmem_ld16(tacc + (uint32_t)(c * 16 + 16), v + 16);
-        if (!BETA && q.tma_store) {
+        const bool tstore = !BETA && q.tma_store;
+        float* box = (float*)(ostage + (size_t)(warp - 6) * STAGE_OUT);
+        if (tstore) {
           // stage this warp's 32 (p) x 32 (m) box in shared memory, [m][p] with p
           // contiguous, and store it with one bulk tensor copy (out-of-range rows
           // and columns are clipped by the copy)
-          float* box = (float*)(ostage + (size_t)(warp - 6) * STAGE_OUT);
           if (lane == 0) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
           __syncwarp();
+        }
+        for (int hh = 0; hh < nj / 16; ++hh) {
+          const int mh = mb + 16 * hh;
+          float aux[16], prev[16], osc[16];
+          if (pin) {
 #pragma unroll
-          for (int j = 0; j < 32; ++j) {
-            float r = v[j];  // rows outside the problem are clipped by the store
-            if (H16 && EPI == JFG_EPI_NONE) r *= pin ? aux[j] : 0.f;
-            if (H16 && EPI == JFG_EPI_DIV_EIG) r *= pin ? osc[j] : 0.f;
-            if (EPI == JFG_EPI_MUL_FIELD) r *= pin ? aux[j] : 0.f;
-            if (EPI == JFG_EPI_DIV_EIG) r = __fdividef(r, c0 + c1 * ((pin ? aux[j] : 1.f) + lp));
-            r *= alpha;
-            if (H16) omax = fmaxf(omax, fabsf(r));
-            box[j * 32 + lane] = r;
+            for (int j = 0; j < 16; ++j) {
+              const int m = mh + j;
+              const bool ok = m < d.M;
+              if (EPI == JFG_EPI_MUL_FIELD)
+                aux[j] = ok ? __ldg(fld + (long long)m * d.field_ld + p) : 0.f;
+              else if (EPI == JFG_EPI_DIV_EIG)
+                aux[j] = ok ? __ldg(lam_m + m) : 1.f;
+              if (H16) {
+                // output scale (operator row and input scale) folded into aux
+                // where the epilogue allows
+                const float sc = ok ? __ldg(oinv + m) * xinv : 0.f;
+                if (EPI == JFG_EPI_DIV_EIG)
+                  osc[j] = sc;
+                else if (EPI == JFG_EPI_MUL_FIELD)
+                  aux[j] *= sc;
+                else
+                  aux[j] = sc;
+              }
+              if (BETA) prev[j] = ok ? outS[(long long)m * d.out_ld + p] : 0.f;
+            }
           }
+          float v[16];
+          tmem_ld16(tacc + (uint32_t)(c * 16 + 16 * hh), v);
+          if (tstore) {
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+              float r = v[j];  // rows outside the problem are clipped by the store
+              if (H16 && EPI == JFG_EPI_NONE) r *= pin ? aux[j] : 0.f;
+              if (H16 && EPI == JFG_EPI_DIV_EIG) r *= pin ? osc[j] : 0.f;
+              if (EPI == JFG_EPI_MUL_FIELD) r *= pin ? aux[j] : 0.f;
+              if (EPI == JFG_EPI_DIV_EIG)
+                r = __fdividef(r, c0 + c1 * ((pin ? aux[j] : 1.f) + lp));
+              r *= alpha;
+              if (H16) omax = fmaxf(omax, fabsf(r));
+              box[(16 * hh + j) * 32 + lane] = r;
+            }
+          } else if (pin) {
+#pragma unroll
+            for (int j = 0; j < 16; ++j) {
+              const int m = mh + j;
+              if (m < d.M) {
+                float r = v[j];
+                if (H16 && EPI == JFG_EPI_NONE) r *= aux[j];
+                if (H16 && EPI == JFG_EPI_DIV_EIG) r *= osc[j];
+                if (EPI == JFG_EPI_MUL_FIELD) r *= aux[j];
+                if (EPI == JFG_EPI_DIV_EIG) r = __fdividef(r, c0 + c1 * (aux[j] + lp));
+                r *= alpha;
+                if (BETA) r += beta * prev[j];
+                if (H16) omax = fmaxf(omax, fabsf(r));
+                outS[(long long)m * d.out_ld + p] = r;
+              }
+            }
+          }
+        }
+        if (tstore) {
           asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
           __syncwarp();
           if (lane == 0 && b >= 0)
             tma_store_4d(&L.maps[gi][3], box, pt * TILE_P + 32 * q4, mb, s, b);
           if (lane == 0) asm volatile("cp.async.bulk.commit_group;" ::: "memory");
-        } else if (pin) {
-#pragma unroll
-          for (int j = 0; j < 32; ++j) {
-            const int m = mb + j;
-            if (j < nj && m < d.M) {
-              float r = v[j];
-              if (H16 && EPI == JFG_EPI_NONE) r *= aux[j];
-              if (H16 && EPI == JFG_EPI_DIV_EIG) r *= osc[j];
-              if (EPI == JFG_EPI_MUL_FIELD) r *= aux[j];
-              if (EPI == JFG_EPI_DIV_EIG) r = __fdividef(r, c0 + c1 * (aux[j] + lp));
-              r *= alpha;
-              if (BETA) r += beta * prev[j];
-              if (H16) omax = fmaxf(omax, fabsf(r));
-              outS[(long long)m * d.out_ld + p] = r;
-            }
-          }
         }
       }
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
