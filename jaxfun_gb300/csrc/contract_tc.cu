@@ -749,8 +749,6 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       const int Mt = q.Mtile;
       const float alpha = (float)d.alpha, beta = (float)d.beta;
       const int buf = li & 1;
-      if (!mbar_wait(&tfull[buf], (uint32_t)(li >> 1) & 1u, budget)) break;
-      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       const int p = pt * TILE_P + row;
       const bool pin = p < d.P && b >= 0;
       const int bb = b < 0 ? 0 : b;
@@ -771,86 +769,95 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         h16_scale(q.in_max, b, xsc, xinv);
         oinv = q.op_inv + (long long)s * q.op_inv_seg;
       }
+      // This warp's 16-column blocks of the tile: cb(k) = 2 half + 4 (k / 2) +
+      // k % 2 (pairs form the 32 x 32 boxes of the TMA stores).  The per-column
+      // factors of block k+1 (field values, eigenvalues, operator scales) are
+      // loaded while block k is processed, and those of block 0 before the
+      // accumulator wait, so their latency overlaps the main loop.
+      const int ncb = Mt / 16;
+      auto cb_of = [&](int k) { return half * 2 + 4 * (k >> 1) + (k & 1); };
+      auto load_aux = [&](int cbk, float* a) {
+        const int m0 = mc * Mt + cbk * 16;
+#pragma unroll
+        for (int j = 0; j < 16; ++j) {
+          const int m = m0 + j;
+          const bool ok = pin && m < d.M;
+          float v = 1.f;
+          if (EPI == JFG_EPI_MUL_FIELD) v = ok ? __ldg(fld + (long long)m * d.field_ld + p) : 0.f;
+          if (EPI == JFG_EPI_DIV_EIG) v = ok ? __ldg(lam_m + m) : 1.f;
+          if (H16 && EPI != JFG_EPI_DIV_EIG) v *= ok ? __ldg(oinv + m) * xinv : 0.f;
+          a[j] = v;
+        }
+      };
+      float aux[16], nxt[16];
+      if (cb_of(0) < ncb) load_aux(cb_of(0), aux);
+      if (!mbar_wait(&tfull[buf], (uint32_t)(li >> 1) & 1u, budget)) break;
+      asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       const uint32_t tacc = tmem + ((uint32_t)(32 * q4) << 16) + (uint32_t)buf * acc_stride;
-      for (int c = half * 2; c < Mt / 16; c += 4) {
-        // columns [c*16, c*16+32), in two halves of 16 (one 16-column TMEM
-        // load each, so only 16-wide arrays are live)
-        const int mb = mc * Mt + c * 16;
-        const int nj = (c + 1 < Mt / 16) ? 32 : 16;
-        const bool tstore = !BETA && q.tma_store;
-        float* box = (float*)(ostage + (size_t)(warp - 6) * STAGE_OUT);
-        if (tstore) {
-          // stage this warp's 32 (p) x 32 (m) box in shared memory, [m][p] with p
-          // contiguous, and store it with one bulk tensor copy (out-of-range rows
-          // and columns are clipped by the copy)
-          if (lane == 0) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
-          __syncwarp();
-        }
-        for (int hh = 0; hh < nj / 16; ++hh) {
-          const int mh = mb + 16 * hh;
-          float aux[16], prev[16], osc[16];
-          if (pin) {
+      const bool tstore = !BETA && q.tma_store;
+      float* box = (float*)(ostage + (size_t)(warp - 6) * STAGE_OUT);
+      for (int k = 0; cb_of(k) < ncb; ++k) {
+        const int cb = cb_of(k);
+        const bool more = cb_of(k + 1) < ncb;
+        if (more) load_aux(cb_of(k + 1), nxt);
+        const int mh = mc * Mt + cb * 16;
+        float osc[16], prev[16];
+        if (pin) {
 #pragma unroll
-            for (int j = 0; j < 16; ++j) {
-              const int m = mh + j;
-              const bool ok = m < d.M;
-              if (EPI == JFG_EPI_MUL_FIELD)
-                aux[j] = ok ? __ldg(fld + (long long)m * d.field_ld + p) : 0.f;
-              else if (EPI == JFG_EPI_DIV_EIG)
-                aux[j] = ok ? __ldg(lam_m + m) : 1.f;
-              if (H16) {
-                // output scale (operator row and input scale) folded into aux
-                // where the epilogue allows
-                const float sc = ok ? __ldg(oinv + m) * xinv : 0.f;
-                if (EPI == JFG_EPI_DIV_EIG)
-                  osc[j] = sc;
-                else if (EPI == JFG_EPI_MUL_FIELD)
-                  aux[j] *= sc;
-                else
-                  aux[j] = sc;
-              }
-              if (BETA) prev[j] = ok ? outS[(long long)m * d.out_ld + p] : 0.f;
-            }
+          for (int j = 0; j < 16; ++j) {
+            const int m = mh + j;
+            const bool ok = m < d.M;
+            if (H16 && EPI == JFG_EPI_DIV_EIG) osc[j] = ok ? __ldg(oinv + m) * xinv : 0.f;
+            if (BETA) prev[j] = ok ? outS[(long long)m * d.out_ld + p] : 0.f;
           }
-          float v[16];
-          tmem_ld16(tacc + (uint32_t)(c * 16 + 16 * hh), v);
-          if (tstore) {
+        }
+        float v[16];
+        tmem_ld16(tacc + (uint32_t)(cb * 16), v);
+        if (tstore) {
+          // stage this warp's 32 (p) x 32 (m) box in shared memory, [m][p] with
+          // p contiguous, and store it with one bulk tensor copy (out-of-range
+          // rows and columns are clipped by the copy)
+          if ((k & 1) == 0) {
+            if (lane == 0) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+            __syncwarp();
+          }
 #pragma unroll
-            for (int j = 0; j < 16; ++j) {
-              float r = v[j];  // rows outside the problem are clipped by the store
-              if (H16 && EPI == JFG_EPI_NONE) r *= pin ? aux[j] : 0.f;
-              if (H16 && EPI == JFG_EPI_DIV_EIG) r *= pin ? osc[j] : 0.f;
-              if (EPI == JFG_EPI_MUL_FIELD) r *= pin ? aux[j] : 0.f;
-              if (EPI == JFG_EPI_DIV_EIG)
-                r = __fdividef(r, c0 + c1 * ((pin ? aux[j] : 1.f) + lp));
+          for (int j = 0; j < 16; ++j) {
+            float r = v[j];  // rows outside the problem are clipped by the store
+            if (EPI != JFG_EPI_NONE || H16) r *= (EPI == JFG_EPI_DIV_EIG) ? 1.f : (pin ? aux[j] : 0.f);
+            if (H16 && EPI == JFG_EPI_DIV_EIG) r *= pin ? osc[j] : 0.f;
+            if (EPI == JFG_EPI_DIV_EIG) r = __fdividef(r, c0 + c1 * ((pin ? aux[j] : 1.f) + lp));
+            r *= alpha;
+            if (H16) omax = fmaxf(omax, fabsf(r));
+            box[(16 * (k & 1) + j) * 32 + lane] = r;
+          }
+          if ((k & 1) == 1 || !more || cb_of(k + 1) != cb + 1) {
+            asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+            __syncwarp();
+            if (lane == 0 && b >= 0)
+              tma_store_4d(&L.maps[gi][3], box, pt * TILE_P + 32 * q4, mc * Mt + (cb & ~1) * 16,
+                           s, b);
+            if (lane == 0) asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+          }
+        } else if (pin) {
+#pragma unroll
+          for (int j = 0; j < 16; ++j) {
+            const int m = mh + j;
+            if (m < d.M) {
+              float r = v[j];
+              if (EPI != JFG_EPI_NONE || H16) r *= (EPI == JFG_EPI_DIV_EIG) ? 1.f : aux[j];
+              if (H16 && EPI == JFG_EPI_DIV_EIG) r *= osc[j];
+              if (EPI == JFG_EPI_DIV_EIG) r = __fdividef(r, c0 + c1 * (aux[j] + lp));
               r *= alpha;
+              if (BETA) r += beta * prev[j];
               if (H16) omax = fmaxf(omax, fabsf(r));
-              box[(16 * hh + j) * 32 + lane] = r;
-            }
-          } else if (pin) {
-#pragma unroll
-            for (int j = 0; j < 16; ++j) {
-              const int m = mh + j;
-              if (m < d.M) {
-                float r = v[j];
-                if (H16 && EPI == JFG_EPI_NONE) r *= aux[j];
-                if (H16 && EPI == JFG_EPI_DIV_EIG) r *= osc[j];
-                if (EPI == JFG_EPI_MUL_FIELD) r *= aux[j];
-                if (EPI == JFG_EPI_DIV_EIG) r = __fdividef(r, c0 + c1 * (aux[j] + lp));
-                r *= alpha;
-                if (BETA) r += beta * prev[j];
-                if (H16) omax = fmaxf(omax, fabsf(r));
-                outS[(long long)m * d.out_ld + p] = r;
-              }
+              outS[(long long)m * d.out_ld + p] = r;
             }
           }
         }
-        if (tstore) {
-          asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
-          __syncwarp();
-          if (lane == 0 && b >= 0)
-            tma_store_4d(&L.maps[gi][3], box, pt * TILE_P + 32 * q4, mb, s, b);
-          if (lane == 0) asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+        if (more) {
+#pragma unroll
+          for (int j = 0; j < 16; ++j) aux[j] = nxt[j];
         }
       }
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
