@@ -87,6 +87,11 @@ struct TcGroup {
   unsigned* out_max;
   const float* op_inv;  // op_inv[s * op_inv_seg + m]
   long long op_inv_seg;
+  // field-multiply epilogue of a single-group launch: the field's 32 x 32
+  // boxes are fetched by TMA (L.fmap) into the warp's output staging box
+  int tma_field;
+  int fld_seg;  // the field map has a segment dimension (field_seg != 0)
+  int fld_bat;  // the field map has a batch dimension (field_batch != 0)
 };
 
 // Kernel parameter block (__grid_constant__): groups and their tensor maps
@@ -96,6 +101,7 @@ constexpr int SMEM_MAX = 227 * 1024 - 1024;   // dynamic shared memory (static u
 template <int G>
 struct TcLaunch {
   CUtensorMap maps[G][4];
+  CUtensorMap fmap;  // field of group 0 (TcGroup::tma_field)
   TcGroup g[G];
   int ngroups;
   int stages;
@@ -420,7 +426,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   uint64_t* hold = bars + 3 * S + 4;    // test hook: nothing arrives on it
   uint64_t* mma_done = bars + 3 * S + 5;  // MMA drain after a timeout
   uint64_t* opfull = bars + 3 * S + 6;    // resident operator chunk landed
-  uint32_t* tmem_slot = (uint32_t*)(bars + 3 * S + 7);
+  uint64_t* fbar = bars + 3 * S + 7;      // [8] field box landed (one per epilogue warp)
+  uint32_t* tmem_slot = (uint32_t*)(bars + 3 * S + 15);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
@@ -437,6 +444,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     mbar_init(hold, 1);
     mbar_init(mma_done, 1);
     mbar_init(opfull, 1);
+    for (int i = 0; i < 8; ++i) mbar_init(&fbar[i], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 1) {
@@ -742,8 +750,12 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     // test hook: a barrier nothing arrives on; its wait runs out (status set)
     // and this warp skips its tiles, so every other role's waits run out too
     const bool held = s_hold != 0 && !mbar_wait(hold, 0, budget);
+    const int ew = warp - 6;   // this warp's staging box and field barrier
+    uint32_t fph = 0;          // phase of fbar[ew]
+    bool fpend = false;        // a field box load is in flight
+    bool fok = true;
     int gi, pt, mc, b, s;
-    for (; !held && tile_of(li, gi, pt, mc, b, s); ++li) {
+    for (; !held && fok && tile_of(li, gi, pt, mc, b, s); ++li) {
       const TcGroup& q = L.g[gi];
       const jfg_contract_desc& d = q.d;
       const int Mt = q.Mtile;
@@ -776,6 +788,20 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       // accumulator wait, so their latency overlaps the main loop.
       const int ncb = Mt / 16;
       auto cb_of = [&](int k) { return half * 2 + 4 * (k >> 1) + (k & 1); };
+      // field-multiply epilogue with TMA: the field's 32 x 32 box of each
+      // output box is fetched into the staging box by one bulk tensor copy
+      const bool tfld = EPI == JFG_EPI_MUL_FIELD && !BETA && q.tma_store && q.tma_field;
+      float* box = (float*)(ostage + (size_t)ew * STAGE_OUT);
+      auto issue_field = [&](int cbk) {
+        if (lane == 0) {
+          asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");  // box free
+          mbar_expect_tx(&fbar[ew], STAGE_OUT);
+          tma_load_4d(box, &L.fmap, &fbar[ew], pt * TILE_P + 32 * q4, mc * Mt + (cbk & ~1) * 16,
+                      q.fld_seg ? s : 0, q.fld_bat ? bb : 0);
+        }
+        __syncwarp();
+        fpend = true;
+      };
       auto load_aux = [&](int cbk, float* a) {
         const int m0 = mc * Mt + cbk * 16;
 #pragma unroll
@@ -783,19 +809,22 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           const int m = m0 + j;
           const bool ok = pin && m < d.M;
           float v = 1.f;
-          if (EPI == JFG_EPI_MUL_FIELD) v = ok ? __ldg(fld + (long long)m * d.field_ld + p) : 0.f;
+          if (EPI == JFG_EPI_MUL_FIELD && !tfld)
+            v = ok ? __ldg(fld + (long long)m * d.field_ld + p) : 0.f;
           if (EPI == JFG_EPI_DIV_EIG) v = ok ? __ldg(lam_m + m) : 1.f;
           if (H16 && EPI != JFG_EPI_DIV_EIG) v *= ok ? __ldg(oinv + m) * xinv : 0.f;
           a[j] = v;
         }
       };
       float aux[16], nxt[16];
-      if (cb_of(0) < ncb) load_aux(cb_of(0), aux);
+      if (cb_of(0) < ncb) {
+        load_aux(cb_of(0), aux);
+        if (tfld) issue_field(cb_of(0));
+      }
       if (!mbar_wait(&tfull[buf], (uint32_t)(li >> 1) & 1u, budget)) break;
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
       const uint32_t tacc = tmem + ((uint32_t)(32 * q4) << 16) + (uint32_t)buf * acc_stride;
       const bool tstore = !BETA && q.tma_store;
-      float* box = (float*)(ostage + (size_t)(warp - 6) * STAGE_OUT);
       for (int k = 0; cb_of(k) < ncb; ++k) {
         const int cb = cb_of(k);
         const bool more = cb_of(k + 1) < ncb;
@@ -818,13 +847,24 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           // p contiguous, and store it with one bulk tensor copy (out-of-range
           // rows and columns are clipped by the copy)
           if ((k & 1) == 0) {
-            if (lane == 0) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
-            __syncwarp();
+            if (tfld) {
+              if (k > 0) issue_field(cb);
+              if (!mbar_wait(&fbar[ew], fph, budget)) {
+                fok = false;
+                break;
+              }
+              fph ^= 1u;
+              fpend = false;
+            } else {
+              if (lane == 0) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+              __syncwarp();
+            }
           }
 #pragma unroll
           for (int j = 0; j < 16; ++j) {
             float r = v[j];  // rows outside the problem are clipped by the store
             if (EPI != JFG_EPI_NONE || H16) r *= (EPI == JFG_EPI_DIV_EIG) ? 1.f : (pin ? aux[j] : 0.f);
+            if (tfld) r *= box[(16 * (k & 1) + j) * 32 + lane];
             if (H16 && EPI == JFG_EPI_DIV_EIG) r *= pin ? osc[j] : 0.f;
             if (EPI == JFG_EPI_DIV_EIG) r = __fdividef(r, c0 + c1 * ((pin ? aux[j] : 1.f) + lp));
             r *= alpha;
@@ -871,6 +911,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         if (lane == 0 && b >= 0) atomicMax(q.out_max + b, __float_as_uint(omax));
       }
     }
+    // a field box load still in flight (after a timeout) lands before exit
+    if (fpend) mbar_wait(&fbar[ew], fph, WAIT_NS);
     // bulk tensor stores of this warp complete before the kernel ends
     if (lane == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
   }
@@ -1068,6 +1110,32 @@ int launch_groups(int ng, const jfg_contract_desc* const* ds, const void* const*
       L.g[i].op_inv_seg = h16->op_inv_seg;
     }
     if (cfg.store == 2 || (cfg.store == 0 && !g_tma_store)) L.g[i].tma_store = 0;
+    // single-group field-multiply launches fetch the field's 32 x 32 boxes
+    // by TMA into the epilogue's staging boxes (16-byte aligned rows needed)
+    TcGroup& q = L.g[i];
+    const jfg_contract_desc& d = *ds[i];
+    if (G == 1 && ng == 1 && d.epilogue == JFG_EPI_MUL_FIELD && q.tma_store && d.field &&
+        ((uintptr_t)d.field & 15u) == 0 && (d.field_ld & 3) == 0 && (d.field_seg & 3) == 0 &&
+        (d.field_batch & 3) == 0) {
+      q.fld_seg = (d.nseg > 1 && d.field_seg != 0) ? 1 : 0;
+      q.fld_bat = (d.batch > 1 && d.field_batch != 0) ? 1 : 0;
+      const cuuint64_t plane = (cuuint64_t)d.field_ld * d.M;
+      cuuint64_t dims[4] = {(cuuint64_t)d.P, (cuuint64_t)d.M,
+                            (cuuint64_t)(q.fld_seg ? d.nseg : 1),
+                            (cuuint64_t)(q.fld_bat ? d.batch : 1)};
+      cuuint64_t str[3] = {(cuuint64_t)d.field_ld * 4,
+                           (q.fld_seg ? (cuuint64_t)d.field_seg : plane) * 4,
+                           (q.fld_bat ? (cuuint64_t)d.field_batch : plane) * 4};
+      cuuint32_t box[4] = {32, 32, 1, 1};
+      cuuint32_t estr[4] = {1, 1, 1, 1};
+      EncodeTiledFn fn = encode_fn();
+      q.tma_field = (fn && fn(&L.fmap, CU_TENSOR_MAP_DATA_TYPE_FLOAT32, 4, (void*)d.field, dims,
+                              str, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                              CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                              CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) == CUDA_SUCCESS)
+                         ? 1
+                         : 0;
+    }
     tiles += group_tiles(L.g[i]);
     if (L.g[i].Mtile > mt_max) mt_max = L.g[i].Mtile;
     ostage |= L.g[i].tma_store;
@@ -1120,7 +1188,7 @@ int launch_groups(int ng, const jfg_contract_desc* const* ds, const void* const*
   L.op_res = res ? 1 : 0;
   L.nslots = res ? nslots : 0;
   const size_t smem = 1024 + res_bytes * (res ? 1 : 0) + stages * stage + ob +
-                      (3 * stages + 7) * 8 + 16;
+                      (3 * stages + 15) * 8 + 16;
   if (smem > (size_t)SMEM_MAX) return JFG_ERR_UNSUPPORTED;
   long long nct = tiles < ctas ? tiles : ctas;
   if (res) nct = (long long)(ctas / nslots) * nslots;  // the same CTA count per slot
