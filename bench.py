@@ -1197,7 +1197,11 @@ def main():
     # stopping rules calibrated on seeded problems so that each path ends at
     # <= 1e-10 max relative error against a tight FP64 solve (checked below)
     ap.add_argument("--tol", type=float, default=1e-11, help="outer relative residual")
-    ap.add_argument("--inner-tol", type=float, default=1e-5)
+    # inner tolerance: the residual is updated in FP32 after the first correction,
+    # and its error scales with the residual left by that correction; 5e-6 keeps
+    # the answer at <= 6e-11 error with the scaled split-FP16 operator (1e-5 gave
+    # 1.2e-10, and tightening the outer rule alone did not help)
+    ap.add_argument("--inner-tol", type=float, default=5e-6)
     ap.add_argument("--fp64-tol", type=float, default=5e-12)
     ap.add_argument("--fp64-batch", type=int, default=128)
     ap.add_argument("--fp64-steps", type=int, default=1)

@@ -157,7 +157,7 @@ class MixedVarCoefSolver:
         A = self.A
         return int(_lib.lib().jfg_pcg_mixed_workspace_size(A.ndim, A.n, A.nq, A.batch))
 
-    def solve(self, b, x0=None, tol: float = 1e-10, inner_tol: float = 1e-5,
+    def solve(self, b, x0=None, tol: float = 1e-10, inner_tol: float = 5e-6,
               max_outer: int = 10, maxiter_inner: int = 1000, out=None, ws=None, guess=None):
         """Returns (x, inner_iterations, outer_iterations) per problem.
 

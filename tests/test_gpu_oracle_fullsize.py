@@ -78,9 +78,9 @@ def test_headline_config3_against_oracle():
         return max(float(np.abs(x[i] - ref[i]).max() / np.abs(ref[i]).max())
                    for i in range(len(seeds)))
 
-    # the headline path and its stopping rules (outer relres 1e-11, inner 1e-5)
-    x_l, _, _ = S.solve(b, tol=1e-11, inner_tol=1e-5, guess=guess)
-    x_z, _, _ = S.solve(b, tol=1e-11, inner_tol=1e-5)
+    # the headline path and its stopping rules (outer relres 1e-11, inner 5e-6)
+    x_l, _, _ = S.solve(b, tol=1e-11, inner_tol=5e-6, guess=guess)
+    x_z, _, _ = S.solve(b, tol=1e-11, inner_tol=5e-6)
     assert err(x_l) <= 1e-10, err(x_l)
     assert err(x_z) <= 1e-10, err(x_z)
     # the plain FP64 GPU path, run tight, agrees with the oracle to 1e-12
