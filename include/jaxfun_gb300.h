@@ -559,6 +559,11 @@ typedef struct {
   const uint16_t* ops_lo16;  /* FP16 lo                                             */
   const float* ops_inv16;    /* inverse row scales, jfg_varcoef_f16_rows(n, nq) of them:
                                 [B;D] 2nq | D, B 2nq | B^T, D^T 2n | [D^T|B^T] n     */
+  int fused_dots;        /* inner PCG scalars from the contraction epilogues instead of
+                            separate dot kernels: bit 0 p.Ap = sum kappa w |grad p|^2 in
+                            the operator's field pass; bit 1 r.M^-1 r = sum (E r)^2 / D
+                            in the preconditioner's divide pass (valid only when
+                            E = W^T, the symmetric (Legendre) factorisation)            */
 } jfg_mixed_plan;
 
 /* Rows of the 2-D packed operator set (jfg_varcoef_pack_ops_host(2, n, nq))

@@ -92,6 +92,9 @@ struct TcGroup {
   int tma_field;
   int fld_seg;  // the field map has a segment dimension (field_seg != 0)
   int fld_bat;  // the field map has a batch dimension (field_batch != 0)
+  // fused dot (field / divide epilogues): partials of sum(acc * out) per
+  // problem at dot_part[b * DOT_NBMAX + tile-of-problem * 8 + epilogue warp]
+  float* dot_part;
 };
 
 // Kernel parameter block (__grid_constant__): groups and their tensor maps
@@ -775,12 +778,13 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       const float* __restrict__ fld = nullptr;
       if (EPI == JFG_EPI_MUL_FIELD)
         fld = (const float*)d.field + (long long)bb * d.field_batch + (long long)s * d.field_seg;
-      float xsc = 1.f, xinv = 1.f, omax = 0.f;
+      float xsc = 1.f, xinv = 1.f, omax = 0.f, dsum = 0.f;
       const float* __restrict__ oinv = nullptr;
       if (H16) {
         h16_scale(q.in_max, b, xsc, xinv);
         oinv = q.op_inv + (long long)s * q.op_inv_seg;
       }
+      const bool fdot = EPI != JFG_EPI_NONE && q.dot_part != nullptr;
       // This warp's 16-column blocks of the tile: cb(k) = 2 half + 4 (k / 2) +
       // k % 2 (pairs form the 32 x 32 boxes of the TMA stores).  The per-column
       // factors of block k+1 (field values, eigenvalues, operator scales) are
@@ -863,11 +867,19 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 #pragma unroll
           for (int j = 0; j < 16; ++j) {
             float r = v[j];  // rows outside the problem are clipped by the store
+            // a = the contraction before the epilogue factor (operator and
+            // input scales applied), for the fused dot sum(a * out)
+            float a = r;
             if (EPI != JFG_EPI_NONE || H16) r *= (EPI == JFG_EPI_DIV_EIG) ? 1.f : (pin ? aux[j] : 0.f);
+            if (tfld) a = r;  // aux held only the scales; the field comes next
             if (tfld) r *= box[(16 * (k & 1) + j) * 32 + lane];
             if (H16 && EPI == JFG_EPI_DIV_EIG) r *= pin ? osc[j] : 0.f;
-            if (EPI == JFG_EPI_DIV_EIG) r = __fdividef(r, c0 + c1 * ((pin ? aux[j] : 1.f) + lp));
+            if (EPI == JFG_EPI_DIV_EIG) {
+              a = r;
+              r = __fdividef(r, c0 + c1 * ((pin ? aux[j] : 1.f) + lp));
+            }
             r *= alpha;
+            if (fdot) dsum = fmaf(a, r, dsum);
             if (H16) omax = fmaxf(omax, fabsf(r));
             box[(16 * (k & 1) + j) * 32 + lane] = r;
           }
@@ -885,10 +897,15 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             const int m = mh + j;
             if (m < d.M) {
               float r = v[j];
+              float a = r;  // (split FP16 with the field in aux fuses no dot)
               if (EPI != JFG_EPI_NONE || H16) r *= (EPI == JFG_EPI_DIV_EIG) ? 1.f : aux[j];
               if (H16 && EPI == JFG_EPI_DIV_EIG) r *= osc[j];
-              if (EPI == JFG_EPI_DIV_EIG) r = __fdividef(r, c0 + c1 * (aux[j] + lp));
+              if (EPI == JFG_EPI_DIV_EIG) {
+                a = r;
+                r = __fdividef(r, c0 + c1 * (aux[j] + lp));
+              }
               r *= alpha;
+              if (fdot) dsum = fmaf(a, r, dsum);
               if (BETA) r += beta * prev[j];
               if (H16) omax = fmaxf(omax, fabsf(r));
               outS[(long long)m * d.out_ld + p] = r;
@@ -903,6 +920,14 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
       __syncwarp();
       if (lane == 0) mbar_arrive(&tempty[buf]);
+      if (fdot) {
+        // this warp's partial of the tile, one deterministic slot each
+#pragma unroll
+        for (int o = 16; o > 0; o >>= 1) dsum += __shfl_xor_sync(0xffffffffu, dsum, o);
+        const int mch = (d.M + Mt - 1) / Mt, npt = (d.P + TILE_P - 1) / TILE_P;
+        if (lane == 0 && b >= 0)
+          q.dot_part[(long long)b * DOT_NBMAX + ((s * mch + mc) * npt + pt) * 8 + ew] = dsum;
+      }
       if (H16 && q.out_max != nullptr) {
         // max |output| of this tile for the next pass's input scale (float
         // bits of non-negative values order like unsigned integers)
@@ -1088,7 +1113,8 @@ template <int G>
 int launch_groups(int ng, const jfg_contract_desc* const* ds, const void* const* op_hi,
                   const void* const* op_lo, const float* const* in, float* const* out,
                   const jfg_tc_config& cfg, int prec, cudaStream_t st,
-                  const H16Aux* h16 = nullptr) {
+                  const H16Aux* h16 = nullptr, const DotOut* dot = nullptr) {
+  if (dot && dot->nb) *dot->nb = 0;
   const bool b16 = prec != 0;
   if (prec == 2 && (G != 1 || ng != 1 || !h16 || !h16->op_inv)) return JFG_ERR_ARG;
   static_assert(sizeof(TcLaunch<G>) <= 32000, "kernel parameter block too large");
@@ -1187,6 +1213,20 @@ int launch_groups(int ng, const jfg_contract_desc* const* ds, const void* const*
   L.out_stage = ostage;
   L.op_res = res ? 1 : 0;
   L.nslots = res ? nslots : 0;
+  if (dot && dot->part && ng == 1) {
+    // fused dot: field or divide epilogue, <= DOT_NBMAX partials per problem;
+    // split FP16 with the field loaded per element keeps the factors folded
+    // and fuses none
+    TcGroup& q = L.g[0];
+    const int e = q.d.epilogue;
+    const long long nb = (long long)q.d.nseg * ((q.d.M + q.Mtile - 1) / q.Mtile) *
+                         ((q.d.P + TILE_P - 1) / TILE_P) * 8;
+    if ((e == JFG_EPI_DIV_EIG || (e == JFG_EPI_MUL_FIELD && (prec != 2 || q.tma_field))) &&
+        q.d.beta == 0.0 && nb <= DOT_NBMAX) {
+      q.dot_part = dot->part;
+      if (dot->nb) *dot->nb = (int)nb;
+    }
+  }
   const size_t smem = 1024 + res_bytes * (res ? 1 : 0) + stages * stage + ob +
                       (3 * stages + 15) * 8 + 16;
   if (smem > (size_t)SMEM_MAX) return JFG_ERR_UNSUPPORTED;
@@ -1343,7 +1383,8 @@ int tune_single(int prec, const jfg_contract_desc& d, const void* oh, const void
 // the default); with autotuning on, an untuned signature launched outside
 // stream capture is tuned first.
 int launch_single(int prec, const jfg_contract_desc& d, const void* oh, const void* ol,
-                  const float* in, float* out, const H16Aux* aux, cudaStream_t st) {
+                  const float* in, float* out, const H16Aux* aux, cudaStream_t st,
+                  const DotOut* dot = nullptr) {
   const jfg_contract_desc* dp = &d;
   jfg_tc_config cfg = tc_default_config();
   const std::string key = single_signature(prec, d);
@@ -1362,28 +1403,32 @@ int launch_single(int prec, const jfg_contract_desc& d, const void* oh, const vo
     if (cs == cudaStreamCaptureStatusNone)
       JFG_TRY(tune_single(prec, d, oh, ol, in, out, aux, st, key, &cfg));
   }
-  return launch_groups<1>(1, &dp, &oh, &ol, &in, &out, cfg, prec, st, aux);
+  return launch_groups<1>(1, &dp, &oh, &ol, &in, &out, cfg, prec, st, aux, dot);
 }
 
 int contract_tc(const jfg_contract_desc& d, const float* op_hi, const float* op_lo,
-                const float* in, float* out, cudaStream_t st) {
+                const float* in, float* out, cudaStream_t st, const DotOut* dot) {
+  if (dot && dot->nb) *dot->nb = 0;
   if (d.batch == 0 || d.M == 0 || d.P == 0) return validate_desc(d);
-  return launch_single(0, d, op_hi, op_lo, in, out, nullptr, st);
+  return launch_single(0, d, op_hi, op_lo, in, out, nullptr, st, dot);
 }
 
 int contract_tc_b16(const jfg_contract_desc& d, const uint16_t* op_hi, const uint16_t* op_lo,
-                    const float* in, float* out, cudaStream_t st) {
+                    const float* in, float* out, cudaStream_t st, const DotOut* dot) {
+  if (dot && dot->nb) *dot->nb = 0;
   if (d.batch == 0 || d.M == 0 || d.P == 0) return validate_desc(d);
-  return launch_single(1, d, op_hi, op_lo, in, out, nullptr, st);
+  return launch_single(1, d, op_hi, op_lo, in, out, nullptr, st, dot);
 }
 
 int contract_tc_h16(const jfg_contract_desc& d, const uint16_t* op_hi, const uint16_t* op_lo,
                     const float* op_inv, long long op_inv_seg, const unsigned* in_max,
-                    unsigned* out_max, const float* in, float* out, cudaStream_t st) {
+                    unsigned* out_max, const float* in, float* out, cudaStream_t st,
+                    const DotOut* dot) {
+  if (dot && dot->nb) *dot->nb = 0;
   if (d.batch == 0 || d.M == 0 || d.P == 0) return validate_desc(d);
   if (!op_inv || !in_max) return JFG_ERR_ARG;
   const H16Aux aux{in_max, out_max, op_inv, op_inv_seg};
-  return launch_single(2, d, op_hi, op_lo, in, out, &aux, st);
+  return launch_single(2, d, op_hi, op_lo, in, out, &aux, st, dot);
 }
 
 void set_single_autotune(int on) { g_tune_single = on; }

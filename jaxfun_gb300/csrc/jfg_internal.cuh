@@ -72,6 +72,19 @@ struct H16Ops {
   unsigned* slots = nullptr;
 };
 
+// Fused dot product of a field-multiply or eigenvalue-divide pass: the
+// epilogue writes, per problem b, partials part[b * DOT_NBMAX + i], i < *nb,
+// of sum(acc * out) (acc the contraction before the epilogue factor, out the
+// written value) -- p.Ap of the variable-coefficient operator in its field
+// pass, r.M^-1 r of the fast diagonalisation in its divide pass.  The launch
+// sets *nb (its tiles per problem x 8 epilogue warps), or 0 when the pass
+// cannot produce it (then the caller computes the dot itself).
+constexpr int DOT_NBMAX = 64;
+struct DotOut {
+  float* part = nullptr;
+  int* nb = nullptr;
+};
+
 int contract_f64(const jfg_contract_desc& d, const double* op, const double* in, double* out,
                  cudaStream_t st);
 int contract_f32(const jfg_contract_desc& d, const float* op, const float* in, float* out,
@@ -82,17 +95,18 @@ int contract_df64(const jfg_contract_desc& d, const double* op, const float2* op
 // dst[i] = (hi, lo) FP32 split of src[i] (the DF engine's pre-split operator)
 int split_pairs_f64(const double* src, float2* dst, long long n, cudaStream_t st);
 int contract_tc(const jfg_contract_desc& d, const float* op_hi, const float* op_lo,
-                const float* in, float* out, cudaStream_t st);
+                const float* in, float* out, cudaStream_t st, const DotOut* dot = nullptr);
 // the same contraction with the operator as BF16 (hi, lo): three BF16 MMAs per product
 int contract_tc_b16(const jfg_contract_desc& d, const uint16_t* op_hi, const uint16_t* op_lo,
-                    const float* in, float* out, cudaStream_t st);
+                    const float* in, float* out, cudaStream_t st, const DotOut* dot = nullptr);
 // the same contraction in scaled split FP16: operator (hi, lo) FP16 scaled per
 // row with inverse scales op_inv[s * op_inv_seg + m]; the input of problem b
 // is scaled by a power of two from in_max[b] (float bits of an upper bound on
 // max |in[b]|); out_max[b] (optional, atomicMax) receives max |out[b]|
 int contract_tc_h16(const jfg_contract_desc& d, const uint16_t* op_hi, const uint16_t* op_lo,
                     const float* op_inv, long long op_inv_seg, const unsigned* in_max,
-                    unsigned* out_max, const float* in, float* out, cudaStream_t st);
+                    unsigned* out_max, const float* in, float* out, cudaStream_t st,
+                    const DotOut* dot = nullptr);
 // ngroups contractions in persistent grouped launches (contract_tc.cu)
 int contract_tc_grouped(int ng, const jfg_contract_desc* ds, const float* const* op_hi,
                         const float* const* op_lo, const float* const* in, float* const* out,
@@ -113,10 +127,11 @@ inline int contract(Engine e, const jfg_contract_desc& d, OpRef<double> op, cons
   return contract_f64(d, op.hi, in, out, st);
 }
 inline int contract(Engine e, const jfg_contract_desc& d, OpRef<float> op, const float* in,
-                    float* out, cudaStream_t st) {
-  if (e == Engine::TC) return contract_tc(d, op.hi, op.lo, in, out, st);
+                    float* out, cudaStream_t st, const DotOut* dot = nullptr) {
+  if (e == Engine::TC) return contract_tc(d, op.hi, op.lo, in, out, st, dot);
   if (e == Engine::TB)
-    return contract_tc_b16(d, (const uint16_t*)op.hi, (const uint16_t*)op.lo, in, out, st);
+    return contract_tc_b16(d, (const uint16_t*)op.hi, (const uint16_t*)op.lo, in, out, st, dot);
+  if (dot && dot->nb) *dot->nb = 0;  // CUDA-core engines do not fuse the dot
   return contract_f32(d, op.hi, in, out, st);
 }
 
@@ -171,11 +186,12 @@ int tp_apply(Engine e, int ndim, const int* rows, const int* cols, int batch,
 template <typename T>
 int fd_solve(Engine e, int ndim, int n, int batch, OpRef<T> E, OpRef<T> W, const T* lam,
              const T* c0, const T* c1, const T* rhs, T* out, void* work, size_t work_bytes,
-             cudaStream_t st, Active act = Active());
+             cudaStream_t st, Active act = Active(), const DotOut* dot = nullptr);
 template <typename T>
 int varcoef_apply(Engine e, int ndim, int n, int nq, int batch, OpRef<T> ops, const T* kw,
                   const T* u, T* v, void* work, size_t work_bytes, cudaStream_t st,
-                  Active act = Active(), const H16Ops* h16 = nullptr);
+                  Active act = Active(), const H16Ops* h16 = nullptr,
+                  const DotOut* dot = nullptr);
 // number of inverse row scales of the 2-D packed operators (TH engine)
 inline long long varcoef_h16_rows(int n, int nq) { return 4LL * nq + 3LL * n; }
 

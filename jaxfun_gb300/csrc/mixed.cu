@@ -289,6 +289,7 @@ extern "C" int jfg_pcg_varcoef_mixed_guess(const jfg_mixed_plan* plan, const dou
   pb.ops = P.apply_f16 ? OpRef<float>{(const float*)P.ops_hi16, (const float*)P.ops_lo16}
                        : OpRef<float>{P.ops_hi, P.ops_lo};
   pb.ops_inv = P.apply_f16 ? P.ops_inv16 : nullptr;
+  pb.fuse_dots = P.fused_dots & 3;
   pb.kw = P.kw32;
   pb.E = pbf ? OpRef<float>{(const float*)P.E_hi16, (const float*)P.E_lo16}
              : OpRef<float>{P.E_hi, P.E_lo};

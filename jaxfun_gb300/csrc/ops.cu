@@ -143,7 +143,8 @@ size_t fd_ws(int ndim, int n, int batch, int eb) {
 template <typename T>
 int fd_solve(Engine e, int ndim, int n, int batch, OpRef<T> E, OpRef<T> W, const T* lam,
              const T* c0, const T* c1, const T* rhs, T* out, void* work, size_t work_bytes,
-             cudaStream_t st, Active act) {
+             cudaStream_t st, Active act, const DotOut* dot) {
+  if (dot && dot->nb) *dot->nb = 0;
   if ((ndim != 2 && ndim != 3) || n < 1 || batch < 0 || !E.hi || !W.hi || !lam || !rhs ||
       !out)
     return JFG_ERR_ARG;
@@ -173,7 +174,12 @@ int fd_solve(Engine e, int ndim, int n, int batch, OpRef<T> E, OpRef<T> W, const
       d.c1 = c1;
     }
     T* dst = (t == 2 * ndim - 1) ? out : buf[b];
-    JFG_TRY(contract(e, d, t < ndim ? E : W, src, dst, st));
+    if constexpr (std::is_same<T, float>::value) {
+      // the divide pass can fuse r.M^-1 r (sum of acc * out)
+      JFG_TRY(contract(e, d, t < ndim ? E : W, src, dst, st, t == ndim - 1 ? dot : nullptr));
+    } else {
+      JFG_TRY(contract(e, d, t < ndim ? E : W, src, dst, st));
+    }
     src = dst;
     b ^= 1;
   }
@@ -203,7 +209,8 @@ size_t varcoef_ws(int ndim, int n, int nq, int batch, int eb) {
 template <typename T>
 int varcoef_apply(Engine e, int ndim, int n, int nq, int batch, OpRef<T> ops, const T* kw,
                   const T* u, T* v, void* work, size_t work_bytes, cudaStream_t st,
-                  Active act, const H16Ops* h16) {
+                  Active act, const H16Ops* h16, const DotOut* dot) {
+  if (dot && dot->nb) *dot->nb = 0;
   if ((ndim != 2 && ndim != 3) || n < 1 || nq < 1 || batch < 0 || !ops.hi || !kw || !u || !v)
     return JFG_ERR_ARG;
   const size_t need = varcoef_ws(ndim, n, nq, batch, (int)sizeof(T));
@@ -260,8 +267,10 @@ int varcoef_apply(Engine e, int ndim, int n, int nq, int batch, OpRef<T> ops, co
         d2.field_ld = nq;
         d2.field_seg = 0;
         d2.field_batch = (long long)nq * nq;
+        // the field pass can fuse p.Ap = sum over both gradient components of
+        // kappa w (grad p)^2 (sum of acc * out)
         JFG_TRY(contract_tc_h16(d2, oh + 2 * nn, ol + 2 * nn, inv + 2LL * nq, nq, sl + B,
-                                sl + 2 * B, bufA, bufB, st));
+                                sl + 2 * B, bufA, bufB, st, dot));
         jfg_contract_desc d3 = make_desc(batch, n, nq, nq, act);
         d3.nseg = 2;
         d3.op_seg = nn;
@@ -451,16 +460,16 @@ template int tp_apply<float>(Engine, int, const int*, const int*, int, const OpR
                              const float*, float*, void*, size_t, cudaStream_t, const float*);
 template int fd_solve<double>(Engine, int, int, int, OpRef<double>, OpRef<double>,
                               const double*, const double*, const double*, const double*,
-                              double*, void*, size_t, cudaStream_t, Active);
+                              double*, void*, size_t, cudaStream_t, Active, const DotOut*);
 template int fd_solve<float>(Engine, int, int, int, OpRef<float>, OpRef<float>, const float*,
                              const float*, const float*, const float*, float*, void*, size_t,
-                             cudaStream_t, Active);
+                             cudaStream_t, Active, const DotOut*);
 template int varcoef_apply<double>(Engine, int, int, int, int, OpRef<double>, const double*,
                                    const double*, double*, void*, size_t, cudaStream_t, Active,
-                                   const H16Ops*);
+                                   const H16Ops*, const DotOut*);
 template int varcoef_apply<float>(Engine, int, int, int, int, OpRef<float>, const float*,
                                   const float*, float*, void*, size_t, cudaStream_t, Active,
-                                  const H16Ops*);
+                                  const H16Ops*, const DotOut*);
 
 }  // namespace jfg
 

@@ -13,6 +13,8 @@
 #include <math.h>
 #include <string.h>
 
+#include <type_traits>
+
 #include "jfg_internal.cuh"
 #include "pcg_internal.cuh"
 
@@ -20,7 +22,8 @@ namespace jfg {
 
 namespace {
 
-constexpr int NB = 16;    // partial sums per problem
+constexpr int NB = 16;    // partial sums per problem of the explicit dot kernel
+constexpr int PS = DOT_NBMAX;  // partial-sum slots per problem (fused dots use up to PS)
 constexpr int DOT_T = 256;
 
 template <typename T>
@@ -44,7 +47,7 @@ __device__ __forceinline__ T block_sum(T v) {
   return v;  // valid in thread 0
 }
 
-// part[b*NB + j] = sum over chunk j of x[b]*y[b]  (listed problems, or all)
+// part[b*PS + j] = sum over chunk j < NB of x[b]*y[b]  (listed problems, or all)
 template <typename T>
 __global__ void __launch_bounds__(DOT_T)
     k_dot_part(const T* __restrict__ x, const T* __restrict__ y, long long N,
@@ -59,7 +62,7 @@ __global__ void __launch_bounds__(DOT_T)
   T s = T(0);
   for (long long i = lo + threadIdx.x; i < hi; i += DOT_T) s += xb[i] * yb[i];
   s = block_sum(s);
-  if (threadIdx.x == 0) part[b * NB + j] = s;
+  if (threadIdx.x == 0) part[b * PS + j] = s;
 }
 
 __device__ __forceinline__ float block_max(float v) {
@@ -95,10 +98,10 @@ __global__ void k_absmax(const T* __restrict__ x, long long N, unsigned* __restr
 }
 
 template <typename T>
-__device__ __forceinline__ T sum_part(const T* part, int b) {
+__device__ __forceinline__ T sum_part(const T* part, int b, int nb) {
   T s = T(0);
 #pragma unroll
-  for (int j = 0; j < NB; ++j) s += part[b * NB + j];
+  for (int j = 0; j < nb; ++j) s += part[b * PS + j];
   return s;
 }
 
@@ -116,13 +119,13 @@ __global__ void k_update_xr(T* __restrict__ x, T* __restrict__ r, const T* __res
                             const T* __restrict__ q, long long N, const T* __restrict__ pq_part,
                             const T* __restrict__ rz_prev, const T* __restrict__ rz0,
                             double tol, const int* __restrict__ list, const int* count,
-                            int batch, unsigned* __restrict__ slots) {
+                            int batch, unsigned* __restrict__ slots, int nb_pq, int nb_rz) {
   const int b = active_problem(list, active_count(list, count, batch), batch, blockIdx.y);
   if (b < 0) return;
-  const T rz = sum_part(rz_prev, b);
+  const T rz = sum_part(rz_prev, b, nb_rz);
   if (!is_active(rz, rz0[b], tol)) return;
   if (slots && blockIdx.x == 0 && threadIdx.x < 4) slots[(long long)threadIdx.x * batch + b] = 0u;
-  const T pq = sum_part(pq_part, b);
+  const T pq = sum_part(pq_part, b, nb_pq);
   const T alpha = rz / pq;
   const long long off = (long long)b * N;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N;
@@ -139,12 +142,12 @@ __global__ void k_update_p(T* __restrict__ p, const T* __restrict__ z, long long
                            const T* __restrict__ rz_new_part, const T* __restrict__ rz_prev_part,
                            const T* __restrict__ rz0, double tol, int* __restrict__ iters,
                            const int* __restrict__ list, const int* count, int batch,
-                           unsigned* __restrict__ pmax) {
+                           unsigned* __restrict__ pmax, int nb_rz) {
   const int b = active_problem(list, active_count(list, count, batch), batch, blockIdx.y);
   if (b < 0) return;
-  const T rzp = sum_part(rz_prev_part, b);
+  const T rzp = sum_part(rz_prev_part, b, nb_rz);
   if (!is_active(rzp, rz0[b], tol)) return;
-  const T rzn = sum_part(rz_new_part, b);
+  const T rzn = sum_part(rz_new_part, b, nb_rz);
   const T beta = rzn / rzp;
   const long long off = (long long)b * N;
   float m = 0.f;
@@ -169,7 +172,7 @@ constexpr int CMP_T = 256;
 template <typename T>
 __global__ void __launch_bounds__(CMP_T)
     k_compact(const T* __restrict__ rz_part, const T* __restrict__ rz0, double tol,
-              int* __restrict__ list, int* __restrict__ count, int batch, int init) {
+              int* __restrict__ list, int* __restrict__ count, int batch, int init, int nb_rz) {
   __shared__ int wcnt[CMP_T / 32];
   __shared__ int base;
   const int n = init ? batch : active_count(list, count, batch);
@@ -180,7 +183,8 @@ __global__ void __launch_bounds__(CMP_T)
     const int j = j0 + threadIdx.x;
     int b = -1;
     if (j < n) b = init ? j : list[j];
-    const bool keep = b >= 0 && b < batch && is_active(sum_part(rz_part, b), rz0[b], tol);
+    const bool keep =
+        b >= 0 && b < batch && is_active(sum_part(rz_part, b, nb_rz), rz0[b], tol);
     const unsigned m = __ballot_sync(0xffffffffu, keep);
     if (lane == 0) wcnt[w] = __popc(m);
     __syncthreads();  // every list[j] of this chunk has been read
@@ -199,9 +203,9 @@ __global__ void __launch_bounds__(CMP_T)
 }
 
 template <typename T>
-__global__ void k_set_rz0(const T* __restrict__ part, T* __restrict__ rz0, int batch) {
+__global__ void k_set_rz0(const T* __restrict__ part, T* __restrict__ rz0, int batch, int nb) {
   const int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b < batch) rz0[b] = sum_part(part, b);
+  if (b < batch) rz0[b] = sum_part(part, b, nb);
 }
 
 // Per problem: if the guess residual is not better than the zero start
@@ -209,9 +213,10 @@ __global__ void k_set_rz0(const T* __restrict__ part, T* __restrict__ rz0, int b
 template <typename T>
 __global__ void k_judge_guess(T* __restrict__ x, T* __restrict__ r, T* __restrict__ z,
                               const T* __restrict__ b, const T* __restrict__ zb, long long N,
-                              const T* __restrict__ rz_part, const T* __restrict__ bz_part) {
+                              const T* __restrict__ rz_part, const T* __restrict__ bz_part,
+                              int nb) {
   const int bi = blockIdx.y;
-  if (sum_part(rz_part, bi) < sum_part(bz_part, bi)) return;
+  if (sum_part(rz_part, bi, nb) < sum_part(bz_part, bi, nb)) return;
   const long long off = (long long)bi * N;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N;
        i += (long long)gridDim.x * blockDim.x) {
@@ -223,11 +228,12 @@ __global__ void k_judge_guess(T* __restrict__ x, T* __restrict__ r, T* __restric
 
 // rz partials of problems that fell back to the zero start become b.M^-1 b
 template <typename T>
-__global__ void k_fix_rz(T* __restrict__ rz_part, const T* __restrict__ bz_part, int batch) {
+__global__ void k_fix_rz(T* __restrict__ rz_part, const T* __restrict__ bz_part, int batch,
+                         int nb) {
   const int bi = blockIdx.x * blockDim.x + threadIdx.x;
   if (bi >= batch) return;
-  if (sum_part(rz_part, bi) >= sum_part(bz_part, bi))
-    for (int j = 0; j < NB; ++j) rz_part[bi * NB + j] = bz_part[bi * NB + j];
+  if (sum_part(rz_part, bi, nb) >= sum_part(bz_part, bi, nb))
+    for (int j = 0; j < nb; ++j) rz_part[bi * PS + j] = bz_part[bi * PS + j];
 }
 
 // y = a - y  (r = rhs - A x)
@@ -253,7 +259,7 @@ size_t pcg_ws(int ndim, int n, int nq, int batch) {
   long long N = 1;
   for (int i = 0; i < ndim; ++i) N *= n;
   const size_t vec = align_up((size_t)N * batch * sizeof(T), 256);
-  const size_t scal = align_up((size_t)batch * NB * sizeof(T), 256);
+  const size_t scal = align_up((size_t)batch * PS * sizeof(T), 256);
   const size_t small = align_up((size_t)batch * sizeof(T), 256) +
                        2 * align_up((size_t)batch * sizeof(int), 256) + 256 +
                        align_up((size_t)4 * batch * sizeof(unsigned), 256);
@@ -278,7 +284,7 @@ int pcg_run(const PcgProblem<T>& pb, T* x, int use_x0, double tol, int maxiter, 
   long long N = 1;
   for (int i = 0; i < ndim; ++i) N *= n;
   const size_t vec = align_up((size_t)N * batch * sizeof(T), 256);
-  const size_t scal = align_up((size_t)batch * NB * sizeof(T), 256);
+  const size_t scal = align_up((size_t)batch * PS * sizeof(T), 256);
   char* w = (char*)work;
   T* r = (T*)w;
   T* z = (T*)(w + vec);
@@ -303,9 +309,17 @@ int pcg_run(const PcgProblem<T>& pb, T* x, int use_x0, double tol, int maxiter, 
   h16.op_inv = pb.ops_inv;
   h16.slots = th ? slots : nullptr;
   unsigned* slot_p = th ? slots : nullptr;
-  auto applyA = [&](const T* in, T* out, Active a) -> int {
+  // Fused dots (FP32 tensor-core engines): p.Ap from the operator's field
+  // pass and r.M^-1 r from the preconditioner's divide pass; each launch
+  // reports its partial count (0: not fused, then explicit dot kernels).
+  const bool fuse_pq = std::is_same<T, float>::value && pb.engine != Engine::F32 &&
+                       ndim == 2 && (pb.fuse_dots & 1);
+  const bool fuse = std::is_same<T, float>::value && pb.m_engine != Engine::F32 &&
+                    (pb.fuse_dots & 2);
+  int nb_pq = NB, nb_rz = NB;
+  auto applyA = [&](const T* in, T* out, Active a, DotOut* dot = nullptr) -> int {
     return varcoef_apply<T>(pb.engine, ndim, n, nq, batch, pb.ops, pb.kw, in, out, inner,
-                            inner_bytes, st, a, th ? &h16 : nullptr);
+                            inner_bytes, st, a, th ? &h16 : nullptr, dot);
   };
   // TH: clear the max slots and record max |v| of every problem in slot 0
   // (the input of the next apply)
@@ -317,9 +331,25 @@ int pcg_run(const PcgProblem<T>& pb, T* x, int use_x0, double tol, int maxiter, 
     JFG_LAUNCHED();
     return JFG_OK;
   };
-  auto applyM = [&](const T* in, T* out, Active a) -> int {
+  auto applyM = [&](const T* in, T* out, Active a, DotOut* dot = nullptr) -> int {
     return fd_solve<T>(pb.m_engine, ndim, n, batch, pb.E, pb.W, pb.lam, nullptr, pb.fd_scale, in,
-                       out, inner, inner_bytes, st, a);
+                       out, inner, inner_bytes, st, a, dot);
+  };
+  // out . M^-1 in into part: fused into the preconditioner when possible
+  auto applyM_dot = [&](const T* in, T* out, Active a, T* part, int& nb) -> int {
+    int got = 0;
+    DotOut d;
+    d.part = fuse ? (float*)part : nullptr;
+    d.nb = &got;
+    JFG_TRY(applyM(in, out, a, fuse ? &d : nullptr));
+    if (got > 0) {
+      nb = got;
+      return JFG_OK;
+    }
+    nb = NB;
+    k_dot_part<T><<<dim3(NB, batch), DOT_T, 0, st>>>(in, out, N, part, a.list, a.count, batch);
+    JFG_LAUNCHED();
+    return JFG_OK;
   };
 
   const int vb = vec_blocks(N);
@@ -338,47 +368,56 @@ int pcg_run(const PcgProblem<T>& pb, T* x, int use_x0, double tol, int maxiter, 
     JFG_CUDA_TRY(cudaMemsetAsync(x, 0, sizeof(T) * total, st));
     JFG_CUDA_TRY(cudaMemcpyAsync(r, pb.rhs, sizeof(T) * total, cudaMemcpyDeviceToDevice, st));
   }
-  JFG_TRY(applyM(r, z, all));
-  k_dot_part<T><<<dgrid, DOT_T, 0, st>>>(r, z, N, rz_part[1], nullptr, nullptr, batch);
-  JFG_LAUNCHED();
+  JFG_TRY(applyM_dot(r, z, all, rz_part[1], nb_rz));
   if (use_x0 && pb.judge_x0) {
     // Judge the initial guess against the zero start: keep it only where its
     // preconditioned residual is smaller than that of the right-hand side,
     // and measure convergence relative to the right-hand side either way.
-    JFG_TRY(applyM(pb.rhs, q, all));
-    k_dot_part<T><<<dgrid, DOT_T, 0, st>>>(pb.rhs, q, N, pq_part, nullptr, nullptr, batch);
+    int nb_bz = NB;
+    JFG_TRY(applyM_dot(pb.rhs, q, all, pq_part, nb_bz));
+    if (nb_bz != nb_rz) return JFG_ERR_UNSUPPORTED;  // same launch signature: cannot differ
+    k_judge_guess<T><<<vgrid, 256, 0, st>>>(x, r, z, pb.rhs, q, N, rz_part[1], pq_part, nb_rz);
     JFG_LAUNCHED();
-    k_judge_guess<T><<<vgrid, 256, 0, st>>>(x, r, z, pb.rhs, q, N, rz_part[1], pq_part);
+    k_set_rz0<T><<<(batch + 127) / 128, 128, 0, st>>>(pq_part, rz0, batch, nb_rz);
     JFG_LAUNCHED();
-    k_set_rz0<T><<<(batch + 127) / 128, 128, 0, st>>>(pq_part, rz0, batch);
-    JFG_LAUNCHED();
-    k_fix_rz<T><<<(batch + 127) / 128, 128, 0, st>>>(rz_part[1], pq_part, batch);
+    k_fix_rz<T><<<(batch + 127) / 128, 128, 0, st>>>(rz_part[1], pq_part, batch, nb_rz);
     JFG_LAUNCHED();
   } else {
-    k_set_rz0<T><<<(batch + 127) / 128, 128, 0, st>>>(rz_part[1], rz0, batch);
+    k_set_rz0<T><<<(batch + 127) / 128, 128, 0, st>>>(rz_part[1], rz0, batch, nb_rz);
     JFG_LAUNCHED();
   }
   JFG_CUDA_TRY(cudaMemcpyAsync(p, z, sizeof(T) * total, cudaMemcpyDeviceToDevice, st));
   JFG_TRY(record_max(p));
   // the problems that start active (r0.z0 > 0)
-  k_compact<T><<<1, CMP_T, 0, st>>>(rz_part[1], rz0, tol, alist, nactive, batch, 1);
+  k_compact<T><<<1, CMP_T, 0, st>>>(rz_part[1], rz0, tol, alist, nactive, batch, 1, nb_rz);
   JFG_LAUNCHED();
 
   auto iteration = [&](int it) -> int {
     const int prev = (it + 1) & 1, cur = it & 1;
-    JFG_TRY(applyA(p, q, act));
-    k_dot_part<T><<<dgrid, DOT_T, 0, st>>>(p, q, N, pq_part, alist, nactive, batch);
-    JFG_LAUNCHED();
+    {
+      int got = 0;
+      DotOut d;
+      d.part = fuse_pq ? (float*)pq_part : nullptr;
+      d.nb = &got;
+      JFG_TRY(applyA(p, q, act, fuse_pq ? &d : nullptr));
+      if (got > 0) {
+        nb_pq = got;
+      } else {
+        nb_pq = NB;
+        k_dot_part<T><<<dgrid, DOT_T, 0, st>>>(p, q, N, pq_part, alist, nactive, batch);
+        JFG_LAUNCHED();
+      }
+    }
     k_update_xr<T><<<vgrid, 256, 0, st>>>(x, r, p, q, N, pq_part, rz_part[prev], rz0, tol, alist,
-                                          nactive, batch, slot_p);
+                                          nactive, batch, slot_p, nb_pq, nb_rz);
     JFG_LAUNCHED();
-    JFG_TRY(applyM(r, z, act));
-    k_dot_part<T><<<dgrid, DOT_T, 0, st>>>(r, z, N, rz_part[cur], alist, nactive, batch);
-    JFG_LAUNCHED();
+    int nb_new = NB;
+    JFG_TRY(applyM_dot(r, z, act, rz_part[cur], nb_new));
+    if (nb_new != nb_rz) return JFG_ERR_UNSUPPORTED;  // same launch signature: cannot differ
     k_update_p<T><<<vgrid, 256, 0, st>>>(p, z, N, rz_part[cur], rz_part[prev], rz0, tol, iters,
-                                         alist, nactive, batch, slot_p);
+                                         alist, nactive, batch, slot_p, nb_rz);
     JFG_LAUNCHED();
-    k_compact<T><<<1, CMP_T, 0, st>>>(rz_part[cur], rz0, tol, alist, nactive, batch, 0);
+    k_compact<T><<<1, CMP_T, 0, st>>>(rz_part[cur], rz0, tol, alist, nactive, batch, 0, nb_rz);
     JFG_LAUNCHED();
     return JFG_OK;
   };

@@ -25,6 +25,10 @@ struct PcgProblem {
   // with an initial guess: keep it per problem only if its preconditioned
   // residual beats the zero start, and stop relative to the right-hand side
   bool judge_x0 = false;
+  // fused dots (FP32 tensor-core engines): bit 0 p.Ap from the operator's
+  // field pass, bit 1 r.M^-1 r from the preconditioner's divide pass (only
+  // when its forward factor is the transpose of its backward factor)
+  int fuse_dots = 0;
 };
 
 template <typename T>

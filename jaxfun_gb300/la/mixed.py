@@ -32,6 +32,7 @@ class MixedPlan(C.Structure):
         ("W_lo16", C.c_void_p),
         ("apply_f16", C.c_int),
         ("ops_hi16", C.c_void_p), ("ops_lo16", C.c_void_p), ("ops_inv16", C.c_void_p),
+        ("fused_dots", C.c_int),
     ]
 
 
@@ -81,7 +82,7 @@ class MixedVarCoefSolver:
 
     def __init__(self, A: VarCoefMatrix, M: TPMatricesLUFactors | None = None,
                  residual: str = "df64", fp32_updates: bool | None = None,
-                 precond: str = "bf16x3", apply: str = "f16x3"):
+                 precond: str = "bf16x3", apply: str = "f16x3", fused_dots: bool = True):
         """``residual``: arithmetic of the refinement residual r = b - A x,
         "df64" (double-FP32 on the FP32 units) or "f64" (FP64 FMAs).
         ``fp32_updates``: once ||r|| <= 1e-4 ||b||, update r -= ||r|| A d in FP32
@@ -95,7 +96,10 @@ class MixedVarCoefSolver:
         ``apply``: the inner operator passes as scaled split-"f16x3" (default
         in 2-D: FP16 hi/lo pairs with power-of-two scales per operator row and
         per problem, the accuracy of split TF32 at twice its MMA rate) or
-        split-"tf32"; 3-D and nq % 8 != 0 use split-TF32."""
+        split-"tf32"; 3-D and nq % 8 != 0 use split-TF32.
+        ``fused_dots``: take the inner PCG's p.Ap and r.M^-1 r from the
+        contraction epilogues (the field pass and the divide pass) instead of
+        separate dot kernels; r.M^-1 r only for a symmetric factorisation."""
         if precond not in ("tf32", "bf16x3"):
             raise ValueError(f"precond must be 'tf32' or 'bf16x3', not {precond!r}")
         if apply not in ("tf32", "f16x3"):
@@ -126,6 +130,11 @@ class MixedVarCoefSolver:
             self.W16 = split_bf16(_pad(fac.W_host, nq, nq))
         lam = np.ones(nq)
         lam[:n] = fac.lam_host
+        # PCG scalars from the epilogues: p.Ap always (the operator is
+        # symmetric by construction), r.M^-1 r when E = W^T
+        fused = 1 | (2 if (fused_dots and np.array_equal(fac.E_host, fac.W_host.T)) else 0)
+        if not fused_dots:
+            fused = 0
         self.lam = as_device(lam, torch.float32)
         self.plan = MixedPlan(nd, n, nq, A.batch, A.ops.data_ptr(), A.kw.data_ptr(),
                               self.ops_hi.data_ptr(), self.ops_lo.data_ptr(),
@@ -140,7 +149,8 @@ class MixedVarCoefSolver:
                               1 if af else 0,
                               self.ops16[0].data_ptr() if af else None,
                               self.ops16[1].data_ptr() if af else None,
-                              self.ops16[2].data_ptr() if af else None)
+                              self.ops16[2].data_ptr() if af else None,
+                              fused)
 
     def autotune(self, ws=None) -> list[dict]:
         """Tune the tensor-core passes of the inner solve once (each distinct
