@@ -13,7 +13,9 @@
 #include <math.h>
 #include <string.h>
 
+#include <mutex>
 #include <type_traits>
+#include <vector>
 
 #include "jfg_internal.cuh"
 #include "pcg_internal.cuh"
@@ -118,10 +120,12 @@ template <typename T>
 __global__ void k_update_xr(T* __restrict__ x, T* __restrict__ r, const T* __restrict__ p,
                             const T* __restrict__ q, long long N, const T* __restrict__ pq_part,
                             const T* __restrict__ rz_prev, const T* __restrict__ rz0,
-                            double tol, const int* __restrict__ list, const int* count,
-                            int batch, unsigned* __restrict__ slots, int nb_pq, int nb_rz) {
+                            const double* __restrict__ tolp, const int* __restrict__ list,
+                            const int* count, int batch, unsigned* __restrict__ slots, int nb_pq,
+                            int nb_rz) {
   const int b = active_problem(list, active_count(list, count, batch), batch, blockIdx.y);
   if (b < 0) return;
+  const double tol = *tolp;
   const T rz = sum_part(rz_prev, b, nb_rz);
   if (!is_active(rz, rz0[b], tol)) return;
   if (slots && blockIdx.x == 0 && threadIdx.x < 4) slots[(long long)threadIdx.x * batch + b] = 0u;
@@ -140,11 +144,12 @@ __global__ void k_update_xr(T* __restrict__ x, T* __restrict__ r, const T* __res
 template <typename T>
 __global__ void k_update_p(T* __restrict__ p, const T* __restrict__ z, long long N,
                            const T* __restrict__ rz_new_part, const T* __restrict__ rz_prev_part,
-                           const T* __restrict__ rz0, double tol, int* __restrict__ iters,
-                           const int* __restrict__ list, const int* count, int batch,
-                           unsigned* __restrict__ pmax, int nb_rz) {
+                           const T* __restrict__ rz0, const double* __restrict__ tolp,
+                           int* __restrict__ iters, const int* __restrict__ list,
+                           const int* count, int batch, unsigned* __restrict__ pmax, int nb_rz) {
   const int b = active_problem(list, active_count(list, count, batch), batch, blockIdx.y);
   if (b < 0) return;
+  const double tol = *tolp;
   const T rzp = sum_part(rz_prev_part, b, nb_rz);
   if (!is_active(rzp, rz0[b], tol)) return;
   const T rzn = sum_part(rz_new_part, b, nb_rz);
@@ -171,8 +176,10 @@ __global__ void k_update_p(T* __restrict__ p, const T* __restrict__ z, long long
 constexpr int CMP_T = 256;
 template <typename T>
 __global__ void __launch_bounds__(CMP_T)
-    k_compact(const T* __restrict__ rz_part, const T* __restrict__ rz0, double tol,
-              int* __restrict__ list, int* __restrict__ count, int batch, int init, int nb_rz) {
+    k_compact(const T* __restrict__ rz_part, const T* __restrict__ rz0,
+              const double* __restrict__ tolp, int* __restrict__ list, int* __restrict__ count,
+              int batch, int init, int nb_rz) {
+  const double tol = *tolp;
   __shared__ int wcnt[CMP_T / 32];
   __shared__ int base;
   const int n = init ? batch : active_count(list, count, batch);
@@ -201,6 +208,10 @@ __global__ void __launch_bounds__(CMP_T)
   }
   if (threadIdx.x == 0) *count = base;
 }
+
+// the convergence tolerance of this solve, read by the (graph-replayed)
+// iteration kernels from device memory
+__global__ void k_set_tol(double* __restrict__ tolp, double tol) { *tolp = tol; }
 
 template <typename T>
 __global__ void k_set_rz0(const T* __restrict__ part, T* __restrict__ rz0, int batch, int nb) {
@@ -254,6 +265,49 @@ inline int vec_blocks(long long N) {
 
 // ---------------------------------------------------------------------------
 
+// ---- cache of instantiated iteration graphs -------------------------------
+
+struct GraphKey {
+  std::vector<long long> ints;
+  std::vector<const void*> ptrs;
+  bool operator==(const GraphKey& o) const { return ints == o.ints && ptrs == o.ptrs; }
+};
+struct GraphEntry {
+  GraphKey key;
+  cudaGraphExec_t exec;
+  long long kernels;
+  unsigned long long used;
+};
+std::mutex g_graph_mu;
+std::vector<GraphEntry> g_graphs;
+unsigned long long g_graph_clock = 0;
+constexpr size_t GRAPH_CACHE_MAX = 16;
+
+void graph_cache_find(const GraphKey& k, cudaGraphExec_t* exec, long long* kernels) {
+  std::lock_guard<std::mutex> lk(g_graph_mu);
+  for (GraphEntry& e : g_graphs)
+    if (e.key == k) {
+      e.used = ++g_graph_clock;
+      *exec = e.exec;
+      *kernels = e.kernels;
+      return;
+    }
+}
+
+// Keep a new graph; the least recently used one goes when the cache is full
+// (its earlier launches are already ordered on their streams).
+void graph_cache_put(const GraphKey& k, cudaGraphExec_t exec, long long kernels) {
+  std::lock_guard<std::mutex> lk(g_graph_mu);
+  if (g_graphs.size() >= GRAPH_CACHE_MAX) {
+    size_t lru = 0;
+    for (size_t i = 1; i < g_graphs.size(); ++i)
+      if (g_graphs[i].used < g_graphs[lru].used) lru = i;
+    cudaGraphExecDestroy(g_graphs[lru].exec);
+    g_graphs.erase(g_graphs.begin() + lru);
+  }
+  g_graphs.push_back(GraphEntry{k, exec, kernels, ++g_graph_clock});
+}
+
 template <typename T>
 size_t pcg_ws(int ndim, int n, int nq, int batch) {
   long long N = 1;
@@ -298,6 +352,7 @@ int pcg_run(const PcgProblem<T>& pb, T* x, int use_x0, double tol, int maxiter, 
   int* alist = (int*)(sm + align_up((size_t)batch * sizeof(T), 256) +
                       align_up((size_t)batch * sizeof(int), 256));
   int* nactive = (int*)((char*)alist + align_up((size_t)batch * sizeof(int), 256));
+  double* tol_dev = (double*)((char*)nactive + 8);  // inside nactive's 256-byte block
   unsigned* slots = (unsigned*)((char*)nactive + 256);
   void* inner = (char*)slots + align_up((size_t)4 * batch * sizeof(unsigned), 256);
   const size_t inner_bytes = work_bytes - (size_t)((char*)inner - w);
@@ -389,7 +444,9 @@ int pcg_run(const PcgProblem<T>& pb, T* x, int use_x0, double tol, int maxiter, 
   JFG_CUDA_TRY(cudaMemcpyAsync(p, z, sizeof(T) * total, cudaMemcpyDeviceToDevice, st));
   JFG_TRY(record_max(p));
   // the problems that start active (r0.z0 > 0)
-  k_compact<T><<<1, CMP_T, 0, st>>>(rz_part[1], rz0, tol, alist, nactive, batch, 1, nb_rz);
+  k_set_tol<<<1, 1, 0, st>>>(tol_dev, tol);
+  JFG_LAUNCHED();
+  k_compact<T><<<1, CMP_T, 0, st>>>(rz_part[1], rz0, tol_dev, alist, nactive, batch, 1, nb_rz);
   JFG_LAUNCHED();
 
   auto iteration = [&](int it) -> int {
@@ -408,16 +465,17 @@ int pcg_run(const PcgProblem<T>& pb, T* x, int use_x0, double tol, int maxiter, 
         JFG_LAUNCHED();
       }
     }
-    k_update_xr<T><<<vgrid, 256, 0, st>>>(x, r, p, q, N, pq_part, rz_part[prev], rz0, tol, alist,
-                                          nactive, batch, slot_p, nb_pq, nb_rz);
+    k_update_xr<T><<<vgrid, 256, 0, st>>>(x, r, p, q, N, pq_part, rz_part[prev], rz0, tol_dev,
+                                          alist, nactive, batch, slot_p, nb_pq, nb_rz);
     JFG_LAUNCHED();
     int nb_new = NB;
     JFG_TRY(applyM_dot(r, z, act, rz_part[cur], nb_new));
     if (nb_new != nb_rz) return JFG_ERR_UNSUPPORTED;  // same launch signature: cannot differ
-    k_update_p<T><<<vgrid, 256, 0, st>>>(p, z, N, rz_part[cur], rz_part[prev], rz0, tol, iters,
-                                         alist, nactive, batch, slot_p, nb_rz);
+    k_update_p<T><<<vgrid, 256, 0, st>>>(p, z, N, rz_part[cur], rz_part[prev], rz0, tol_dev,
+                                         iters, alist, nactive, batch, slot_p, nb_rz);
     JFG_LAUNCHED();
-    k_compact<T><<<1, CMP_T, 0, st>>>(rz_part[cur], rz0, tol, alist, nactive, batch, 0, nb_rz);
+    k_compact<T><<<1, CMP_T, 0, st>>>(rz_part[cur], rz0, tol_dev, alist, nactive, batch, 0,
+                                      nb_rz);
     JFG_LAUNCHED();
     return JFG_OK;
   };
@@ -428,7 +486,23 @@ int pcg_run(const PcgProblem<T>& pb, T* x, int use_x0, double tol, int maxiter, 
   const bool use_graph = (st != 0) && (maxiter >= CH);
   cudaGraphExec_t exec = nullptr;
   long long graph_kernels = 0;
+  // The chunk of CH iterations depends only on the buffers, operators, sizes
+  // and engines (the tolerance is read from device memory), so its
+  // instantiated graph is kept and replayed by later calls with the same key.
+  GraphKey key;
   if (use_graph) {
+    int dev = 0;
+    JFG_CUDA_TRY(cudaGetDevice(&dev));
+    const long long v[] = {dev, (long long)sizeof(T), (long long)pb.engine,
+                           (long long)pb.m_engine, ndim, n, nq, batch, pb.fuse_dots, nb_rz,
+                           (long long)work_bytes};
+    const void* ptrs[] = {x, work, pb.ops.hi, pb.ops.lo, pb.ops_inv, pb.kw, pb.E.hi, pb.E.lo,
+                          pb.W.hi, pb.W.lo, pb.lam, pb.fd_scale};
+    key.ints.assign(v, v + sizeof(v) / sizeof(v[0]));
+    key.ptrs.assign(ptrs, ptrs + sizeof(ptrs) / sizeof(ptrs[0]));
+    graph_cache_find(key, &exec, &graph_kernels);
+  }
+  if (use_graph && !exec) {
     cudaGraph_t graph = nullptr;
     JFG_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     set_capturing(true);
@@ -456,6 +530,7 @@ int pcg_run(const PcgProblem<T>& pb, T* x, int use_x0, double tol, int maxiter, 
     cudaError_t ei = cudaGraphInstantiate(&exec, graph, 0);
     cudaGraphDestroy(graph);
     JFG_CUDA_TRY(ei);
+    graph_cache_put(key, exec, graph_kernels);
   }
   int done_iters = 0;
   int status = JFG_OK;
@@ -486,7 +561,6 @@ int pcg_run(const PcgProblem<T>& pb, T* x, int use_x0, double tol, int maxiter, 
     }
     if (h_active == 0) break;
   }
-  if (exec) cudaGraphExecDestroy(exec);
   if (status != JFG_OK) return status;
   if (iters_host) {
     JFG_CUDA_TRY(cudaMemcpyAsync(iters_host, iters, sizeof(int) * batch,
