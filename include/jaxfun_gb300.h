@@ -564,6 +564,12 @@ typedef struct {
                             the operator's field pass; bit 1 r.M^-1 r = sum (E r)^2 / D
                             in the preconditioner's divide pass (valid only when
                             E = W^T, the symmetric (Legendre) factorisation)            */
+  int schedule;          /* 0: every outer step waits for all problems' inner solves;
+                            1: each problem takes its outer steps on its own (its
+                            converged inner solve leaves for a ready list that takes
+                            its outer step at the next 10-iteration boundary and
+                            restarts while the others iterate), so the batch runs
+                            about its slowest problem's total iteration count       */
 } jfg_mixed_plan;
 
 /* Rows of the 2-D packed operator set (jfg_varcoef_pack_ops_host(2, n, nq))

@@ -79,7 +79,7 @@ struct H16Ops {
 // pass, r.M^-1 r of the fast diagonalisation in its divide pass.  The launch
 // sets *nb (its tiles per problem x 8 epilogue warps), or 0 when the pass
 // cannot produce it (then the caller computes the dot itself).
-constexpr int DOT_NBMAX = 64;
+constexpr int DOT_NBMAX = 128;
 struct DotOut {
   float* part = nullptr;
   int* nb = nullptr;

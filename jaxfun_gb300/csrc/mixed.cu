@@ -21,9 +21,14 @@ namespace {
 
 constexpr int NBS = 16;
 
-__global__ void k_sq_part(const double* __restrict__ x, long long N, double* __restrict__ part) {
+__global__ void k_sq_part(const double* __restrict__ x, long long N, double* __restrict__ part,
+                          const int* __restrict__ list = nullptr, const int* count = nullptr,
+                          int batch = 0) {
   __shared__ double red[32];
-  const int b = blockIdx.y, j = blockIdx.x;
+  const int b = list ? active_problem(list, active_count(list, count, batch), batch, blockIdx.y)
+                     : (int)blockIdx.y;
+  if (b < 0) return;
+  const int j = blockIdx.x;
   const long long chunk = (N + NBS - 1) / NBS;
   const long long lo = j * chunk, hi = min(N, lo + chunk);
   const double* xb = x + (long long)b * N;
@@ -44,8 +49,11 @@ __global__ void k_sq_part(const double* __restrict__ x, long long N, double* __r
 // out32[b][padded] = in64[b][unpadded] * scale[b] (zero in the padding)
 __global__ void k_pad_scale(int ndim, int n, int nq, long long Npad, long long Nun,
                             const double* __restrict__ in, const double* __restrict__ scale,
-                            float* __restrict__ out) {
-  const int b = blockIdx.y;
+                            float* __restrict__ out, const int* __restrict__ list = nullptr,
+                            const int* count = nullptr, int batch = 0) {
+  const int b = list ? active_problem(list, active_count(list, count, batch), batch, blockIdx.y)
+                     : (int)blockIdx.y;
+  if (b < 0) return;
   const double sc = scale[b];
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < Npad;
        i += (long long)gridDim.x * blockDim.x) {
@@ -65,8 +73,12 @@ __global__ void k_pad_scale(int ndim, int n, int nq, long long Npad, long long N
 // x64[b][unpadded] += sign * s[b] * d32[b][padded]
 __global__ void k_unpad_axpy(int ndim, int n, int nq, long long Npad, long long Nun,
                              const float* __restrict__ d, const double* __restrict__ s,
-                             double* __restrict__ x, double sign) {
-  const int b = blockIdx.y;
+                             double* __restrict__ x, double sign,
+                             const int* __restrict__ list = nullptr, const int* count = nullptr,
+                             int batch = 0) {
+  const int b = list ? active_problem(list, active_count(list, count, batch), batch, blockIdx.y)
+                     : (int)blockIdx.y;
+  if (b < 0) return;
   const double sc = sign * s[b];
   if (sc == 0.0) return;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < Nun;
@@ -88,6 +100,141 @@ __global__ void k_sub_from64(const double* __restrict__ a, double* __restrict__ 
     y[i] = a[i] - y[i];
 }
 
+// y[b] = a[b] - y[b] for the listed problems (length N each)
+__global__ void k_sub_from64_list(const double* __restrict__ a, double* __restrict__ y,
+                                  long long N, const int* __restrict__ list, const int* count,
+                                  int batch) {
+  const int b = active_problem(list, active_count(list, count, batch), batch, blockIdx.y);
+  if (b < 0) return;
+  const long long off = (long long)b * N;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N;
+       i += (long long)gridDim.x * blockDim.x)
+    y[off + i] = a[off + i] - y[off + i];
+}
+
+// ---- per-problem outer steps (the flat schedule) -------------------------
+
+// bn[b] = ||rhs_b|| from its partial sums
+__global__ void k_norms_from(const double* __restrict__ part, double* __restrict__ out,
+                             int batch) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= batch) return;
+  double s = 0.0;
+  for (int j = 0; j < NBS; ++j) s += part[b * NBS + j];
+  out[b] = sqrt(s);
+}
+
+constexpr int OT = 256;
+
+// Outer decision for the listed problems (all with list NULL) from the norms
+// of their new residuals: a problem above tol ||rhs_b|| with outer steps left
+// restarts its inner solve (scales 1/||r|| and ||r||, inner tolerance
+// max(inner_tol, min(0.1, 0.3 tol / relres)), residual kind of its next outer
+// step: FP32 update once relres <= 1e-4 when allowed); the others stop
+// (state 2 converged, 3 out of outer steps).  The restart list keeps the
+// order.  One block.
+__global__ void __launch_bounds__(OT)
+    k_outer_decide(const double* __restrict__ part, const double* __restrict__ bn, double tol,
+                   double inner_tol, int max_outer, int fp32_ok, const int* __restrict__ list,
+                   const int* count, int batch, double* __restrict__ sc_in,
+                   double* __restrict__ sc_out, double* __restrict__ tolv,
+                   int* __restrict__ outer_cnt, int* __restrict__ res_mode,
+                   int* __restrict__ state, int* __restrict__ rlist, int* __restrict__ nr) {
+  __shared__ int wcnt[OT / 32];
+  __shared__ int base;
+  const int n = active_count(list, count, batch);
+  if (threadIdx.x == 0) base = 0;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int j0 = 0; j0 < n; j0 += OT) {
+    const int j = j0 + threadIdx.x;
+    const int b = j < n ? (list ? list[j] : j) : -1;
+    bool act = false;
+    if (b >= 0 && b < batch) {
+      double s = 0.0;
+      for (int k = 0; k < NBS; ++k) s += part[b * NBS + k];
+      const double rn = sqrt(s), bb = bn[b];
+      const double relres = bb > 0.0 ? rn / bb : 0.0;
+      act = rn > tol * bb && outer_cnt[b] < max_outer;
+      if (act) {
+        sc_in[b] = 1.0 / rn;
+        sc_out[b] = rn;
+        double tk = inner_tol;
+        const double need = relres > 0.0 ? 0.3 * tol / relres : 0.1;
+        if (need > tk) tk = need < 0.1 ? need : 0.1;
+        tolv[b] = tk;
+        res_mode[b] = (fp32_ok && relres <= 1e-4) ? 1 : 0;
+        outer_cnt[b] += 1;
+        state[b] = 1;
+      } else {
+        sc_in[b] = 0.0;
+        sc_out[b] = 0.0;
+        state[b] = rn <= tol * bb ? 2 : 3;
+      }
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, act);
+    if (lane == 0) wcnt[w] = __popc(m);
+    __syncthreads();
+    int off = base + __popc(m & ((1u << lane) - 1u));
+    for (int i = 0; i < w; ++i) off += wcnt[i];
+    if (act) rlist[off] = b;
+    __syncthreads();
+    if (threadIdx.x == 0)
+      for (int i = 0; i < OT / 32; ++i) base += wcnt[i];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) *nr = base;
+}
+
+// The ready problems (inner solve over) into all / recompute-residual /
+// FP32-update lists; the ready count is cleared.  One block.
+__global__ void __launch_bounds__(OT)
+    k_split_ready(const int* __restrict__ ready, int* __restrict__ nready,
+                  const int* __restrict__ res_mode, int batch, int* __restrict__ rall,
+                  int* __restrict__ ctrl /* [0] all, [1] recompute, [2] update */,
+                  int* __restrict__ rdf, int* __restrict__ rup) {
+  __shared__ int wa[OT / 32], wb[OT / 32];
+  __shared__ int ba, bb2;
+  const int n = min(max(*nready, 0), batch);
+  if (threadIdx.x == 0) ba = bb2 = 0;
+  __syncthreads();
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int j0 = 0; j0 < n; j0 += OT) {
+    const int j = j0 + threadIdx.x;
+    const int b = j < n ? ready[j] : -1;
+    const bool valid = b >= 0 && b < batch;
+    if (valid) rall[j] = b;
+    const bool up = valid && res_mode[b] == 1;
+    const bool df = valid && !up;
+    const unsigned mu = __ballot_sync(0xffffffffu, up), md = __ballot_sync(0xffffffffu, df);
+    if (lane == 0) {
+      wa[w] = __popc(md);
+      wb[w] = __popc(mu);
+    }
+    __syncthreads();
+    int od = ba + __popc(md & ((1u << lane) - 1u)), ou = bb2 + __popc(mu & ((1u << lane) - 1u));
+    for (int i = 0; i < w; ++i) {
+      od += wa[i];
+      ou += wb[i];
+    }
+    if (df) rdf[od] = b;
+    if (up) rup[ou] = b;
+    __syncthreads();
+    if (threadIdx.x == 0)
+      for (int i = 0; i < OT / 32; ++i) {
+        ba += wa[i];
+        bb2 += wb[i];
+      }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    ctrl[0] = n;
+    ctrl[1] = ba;
+    ctrl[2] = bb2;
+    *nready = 0;
+  }
+}
+
 inline int blocks_for(long long n, int cap) {
   long long b = (n + 255) / 256;
   if (b > cap) b = cap;
@@ -96,7 +243,7 @@ inline int blocks_for(long long n, int cap) {
 
 struct MixedLayout {
   long long Nun, Npad;
-  size_t vec64, part, sc, vec32, ws64, wsin, opdf, total;
+  size_t vec64, part, sc, vec32, ws64, wsin, opdf, outer, total;
 };
 
 MixedLayout layout(int ndim, int n, int nq, int batch) {
@@ -113,7 +260,10 @@ MixedLayout layout(int ndim, int n, int nq, int batch) {
   // the FP64 operator split once per solve into (hi, lo) pairs for the
   // double-FP32 residual passes
   L.opdf = align_up((size_t)8 * n * nq * sizeof(float2), 256);
-  L.total = L.vec64 + L.part + 2 * L.sc + 2 * L.vec32 + L.ws64 + L.wsin + L.opdf;
+  // per-problem outer state: ||rhs||, outer count, state, residual kind, four
+  // lists and a control block
+  L.outer = align_up((size_t)batch * 8, 256) + 7 * align_up((size_t)batch * 4, 256) + 256;
+  L.total = L.vec64 + L.part + 2 * L.sc + 2 * L.vec32 + L.ws64 + L.wsin + L.opdf + L.outer;
   return L;
 }
 
@@ -252,7 +402,8 @@ extern "C" int jfg_pcg_varcoef_mixed_guess(const jfg_mixed_plan* plan, const dou
       (P.precond_bf16 && (!P.E_hi16 || !P.E_lo16 || !P.W_hi16 || !P.W_lo16)) ||
       (P.apply_f16 != 0 && P.apply_f16 != 1) ||
       (P.apply_f16 && (P.ndim != 2 || (P.nq & 7) || !P.ops_hi16 || !P.ops_lo16 ||
-                       !P.ops_inv16)))
+                       !P.ops_inv16)) ||
+      (P.schedule != 0 && P.schedule != 1))
     return JFG_ERR_ARG;
   const int ndim = P.ndim, n = P.n, nq = P.nq, batch = P.batch;
   const MixedLayout Lo = layout(ndim, n, nq, batch);
@@ -338,6 +489,130 @@ extern "C" int jfg_pcg_varcoef_mixed_guess(const jfg_mixed_plan* plan, const dou
     JFG_LAUNCHED();
     return JFG_OK;
   };
+
+  if (P.schedule == 1) {
+    // ---- flat schedule: every problem takes its outer steps on its own ----
+    // A problem whose inner solve has converged (or hit maxiter_inner) leaves
+    // the active list for the ready list; at the next chunk boundary the
+    // ready problems take their outer step together (x += ||r|| d, the new
+    // residual -- recomputed in FP64-class arithmetic or updated in FP32 --
+    // its norm and the decision) and restart, while the others keep
+    // iterating.  The batch then runs about as many inner iterations as its
+    // slowest problem needs in total, not the sum of the slowest per step.
+    char* ob = (char*)opdf + Lo.opdf;
+    const size_t ib = align_up((size_t)batch * 4, 256);
+    double* bnd = (double*)ob;
+    ob += align_up((size_t)batch * 8, 256);
+    int* outer_cnt = (int*)ob;
+    int* state = (int*)(ob + ib);
+    int* res_mode = (int*)(ob + 2 * ib);
+    int* rall = (int*)(ob + 3 * ib);
+    int* rdf = (int*)(ob + 4 * ib);
+    int* rup = (int*)(ob + 5 * ib);
+    int* rlist = (int*)(ob + 6 * ib);
+    int* ctrl = (int*)(ob + 7 * ib);  // [0] ready, [1] recompute, [2] update, [3] restart
+    JFG_CUDA_TRY(cudaMemsetAsync(outer_cnt, 0, 3 * ib, st));
+    JFG_CUDA_TRY(cudaMemsetAsync(ctrl, 0, 256, st));
+    PcgCtx<float> c;
+    c.maxit = maxiter_inner;
+    c.track_ready = true;
+    JFG_TRY(c.init(pb, d32, wsin, Lo.wsin, st));
+    const int fp32_ok = P.ops32 ? 1 : 0;
+    const dim3 lgrid(NBS, batch);
+    // ||rhs_b||, the first residual and the first decision (all problems)
+    k_sq_part<<<lgrid, 256, 0, st>>>(rhs, Lo.Nun, part);
+    JFG_LAUNCHED();
+    k_norms_from<<<(batch + 127) / 128, 128, 0, st>>>(part, bnd, batch);
+    JFG_LAUNCHED();
+    if (use_x0) {
+      JFG_TRY(residual());
+    } else {
+      JFG_CUDA_TRY(cudaMemsetAsync(x, 0, sizeof(double) * tot64, st));
+      JFG_CUDA_TRY(
+          cudaMemcpyAsync(r64, rhs, sizeof(double) * tot64, cudaMemcpyDeviceToDevice, st));
+    }
+    k_sq_part<<<lgrid, 256, 0, st>>>(r64, Lo.Nun, part);
+    JFG_LAUNCHED();
+    k_outer_decide<<<1, OT, 0, st>>>(part, bnd, tol, inner_tol, max_outer, fp32_ok, nullptr,
+                                     nullptr, batch, sc_in, sc_out, c.tolv, outer_cnt, res_mode,
+                                     state, rlist, ctrl + 3);
+    JFG_LAUNCHED();
+    k_pad_scale<<<pgrid, 256, 0, st>>>(ndim, n, nq, Lo.Npad, Lo.Nun, r64, sc_in, r32, rlist,
+                                       ctrl + 3, batch);
+    JFG_LAUNCHED();
+    const bool from_guess = guess != nullptr && !use_x0;
+    if (from_guess) {
+      // the learned guess starts each first inner solve, judged per problem
+      k_pad_scale<<<pgrid, 256, 0, st>>>(ndim, n, nq, Lo.Npad, Lo.Nun, guess, sc_in, d32, rlist,
+                                         ctrl + 3, batch);
+      JFG_LAUNCHED();
+    }
+    JFG_TRY(c.start(rlist, ctrl + 3, from_guess ? 1 : 0, from_guess));
+    const long long guard =
+        (long long)(max_outer + 1) * (maxiter_inner / PcgCtx<float>::CH + 2) + 8;
+    int hc[2] = {0, 0};
+    int status = JFG_OK;
+    for (long long loops = 0;; ++loops) {
+      JFG_CUDA_TRY(cudaMemcpyAsync(hc, c.nactive, 2 * sizeof(int), cudaMemcpyDeviceToHost, st));
+      JFG_CUDA_TRY(cudaStreamSynchronize(st));
+      if (hc[0] == 0 && hc[1] == 0) break;
+      if (loops > guard) {
+        status = JFG_ERR_NOT_CONVERGED;
+        break;
+      }
+      if (hc[1] > 0) {
+        // outer step of the ready problems
+        k_split_ready<<<1, OT, 0, st>>>(c.ready, c.nready, res_mode, batch, rall, ctrl, rdf, rup);
+        JFG_LAUNCHED();
+        k_unpad_axpy<<<ugrid, 256, 0, st>>>(ndim, n, nq, Lo.Npad, Lo.Nun, d32, sc_out, x, 1.0,
+                                            rall, ctrl, batch);
+        JFG_LAUNCHED();
+        // recomputed residuals r = rhs - A x
+        JFG_TRY(varcoef_apply<double>(
+            P.residual == 1 ? Engine::DF : Engine::F64, ndim, n, nq, batch,
+            OpRef<double>{P.ops64, P.residual == 1 ? (const double*)opdf : nullptr}, P.kw64, x,
+            r64, ws64, Lo.ws64, st, Active{rdf, ctrl + 1}));
+        k_sub_from64_list<<<ugrid, 256, 0, st>>>(rhs, r64, Lo.Nun, rdf, ctrl + 1, batch);
+        JFG_LAUNCHED();
+        // updated residuals r -= ||r|| A32 d (the apply's scratch is the inner
+        // solve's pass scratch, free between chunks)
+        if (fp32_ok) {
+          JFG_TRY(varcoef_apply<float>(Engine::F32, ndim, nq, nq, batch,
+                                       OpRef<float>{P.ops32, nullptr}, P.kw32, d32, r32, c.inner,
+                                       c.inner_bytes, st, Active{rup, ctrl + 2}));
+          k_unpad_axpy<<<ugrid, 256, 0, st>>>(ndim, n, nq, Lo.Npad, Lo.Nun, r32, sc_out, r64,
+                                              -1.0, rup, ctrl + 2, batch);
+          JFG_LAUNCHED();
+        }
+        k_sq_part<<<lgrid, 256, 0, st>>>(r64, Lo.Nun, part, rall, ctrl, batch);
+        JFG_LAUNCHED();
+        k_outer_decide<<<1, OT, 0, st>>>(part, bnd, tol, inner_tol, max_outer, fp32_ok, rall,
+                                         ctrl, batch, sc_in, sc_out, c.tolv, outer_cnt, res_mode,
+                                         state, rlist, ctrl + 3);
+        JFG_LAUNCHED();
+        k_pad_scale<<<pgrid, 256, 0, st>>>(ndim, n, nq, Lo.Npad, Lo.Nun, r64, sc_in, r32, rlist,
+                                           ctrl + 3, batch);
+        JFG_LAUNCHED();
+        JFG_TRY(c.start(rlist, ctrl + 3, 0, false));
+        continue;
+      }
+      JFG_TRY(c.chunk());
+    }
+    std::vector<int> hst(batch);
+    JFG_CUDA_TRY(cudaMemcpyAsync(hst.data(), state, sizeof(int) * batch, cudaMemcpyDeviceToHost,
+                                 st));
+    if (inner_iters)
+      JFG_CUDA_TRY(cudaMemcpyAsync(inner_iters, c.iters, sizeof(int) * batch,
+                                   cudaMemcpyDeviceToHost, st));
+    if (outer_iters)
+      JFG_CUDA_TRY(cudaMemcpyAsync(outer_iters, outer_cnt, sizeof(int) * batch,
+                                   cudaMemcpyDeviceToHost, st));
+    JFG_CUDA_TRY(cudaStreamSynchronize(st));
+    if (status != JFG_OK) return status;
+    for (int b = 0; b < batch; ++b)
+      if (hst[b] != 2) return JFG_ERR_NOT_CONVERGED;
+    return JFG_OK;
+  }
 
   JFG_TRY(norms(rhs, bn));
   if (use_x0) {

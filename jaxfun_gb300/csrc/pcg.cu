@@ -125,7 +125,7 @@ __global__ void k_update_xr(T* __restrict__ x, T* __restrict__ r, const T* __res
                             int nb_rz) {
   const int b = active_problem(list, active_count(list, count, batch), batch, blockIdx.y);
   if (b < 0) return;
-  const double tol = *tolp;
+  const double tol = tolp[b];
   const T rz = sum_part(rz_prev, b, nb_rz);
   if (!is_active(rz, rz0[b], tol)) return;
   if (slots && blockIdx.x == 0 && threadIdx.x < 4) slots[(long long)threadIdx.x * batch + b] = 0u;
@@ -146,10 +146,11 @@ __global__ void k_update_p(T* __restrict__ p, const T* __restrict__ z, long long
                            const T* __restrict__ rz_new_part, const T* __restrict__ rz_prev_part,
                            const T* __restrict__ rz0, const double* __restrict__ tolp,
                            int* __restrict__ iters, const int* __restrict__ list,
-                           const int* count, int batch, unsigned* __restrict__ pmax, int nb_rz) {
+                           const int* count, int batch, unsigned* __restrict__ pmax, int nb_rz,
+                           int* __restrict__ inner_it) {
   const int b = active_problem(list, active_count(list, count, batch), batch, blockIdx.y);
   if (b < 0) return;
-  const double tol = *tolp;
+  const double tol = tolp[b];
   const T rzp = sum_part(rz_prev_part, b, nb_rz);
   if (!is_active(rzp, rz0[b], tol)) return;
   const T rzn = sum_part(rz_new_part, b, nb_rz);
@@ -162,61 +163,201 @@ __global__ void k_update_p(T* __restrict__ p, const T* __restrict__ z, long long
     p[off + i] = v;
     m = fmaxf(m, fabsf((float)v));
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0) iters[b] += 1;
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    iters[b] += 1;
+    if (inner_it) inner_it[b] += 1;
+  }
   if (pmax) {
     m = block_max(m);
     if (threadIdx.x == 0) atomicMax(pmax + b, __float_as_uint(m));
   }
 }
 
-// Active list: keep the problems whose r.z is still above tol^2 r0.z0.  With
-// init the candidates are 0..batch-1, else the current list (filtered in
+// Active list: keep the problems whose r.z is still above tol_b^2 r0.z0 (and,
+// with inner_it, that have run fewer than maxit iterations since their start).
+// With init the candidates are 0..batch-1, else the current list (filtered in
 // place: an entry moves only to a lower slot, after its chunk has been read).
-// One block; the order of the problems is kept.
+// ready (optional): the problems dropped here are appended to ready[*nready]
+// (their inner solve is over).  One block; the order of the problems is kept.
 constexpr int CMP_T = 256;
 template <typename T>
 __global__ void __launch_bounds__(CMP_T)
     k_compact(const T* __restrict__ rz_part, const T* __restrict__ rz0,
               const double* __restrict__ tolp, int* __restrict__ list, int* __restrict__ count,
-              int batch, int init, int nb_rz) {
-  const double tol = *tolp;
-  __shared__ int wcnt[CMP_T / 32];
-  __shared__ int base;
+              int batch, int init, int nb_rz, const int* __restrict__ inner_it, int maxit,
+              int* __restrict__ ready, int* __restrict__ nready) {
+  __shared__ int wcnt[CMP_T / 32], wdrop[CMP_T / 32];
+  __shared__ int base, dbase;
   const int n = init ? batch : active_count(list, count, batch);
-  if (threadIdx.x == 0) base = 0;
+  if (threadIdx.x == 0) {
+    base = 0;
+    dbase = ready ? *nready : 0;
+  }
   __syncthreads();
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   for (int j0 = 0; j0 < n; j0 += CMP_T) {
     const int j = j0 + threadIdx.x;
     int b = -1;
     if (j < n) b = init ? j : list[j];
-    const bool keep =
-        b >= 0 && b < batch && is_active(sum_part(rz_part, b, nb_rz), rz0[b], tol);
+    const bool valid = b >= 0 && b < batch;
+    const bool keep = valid && is_active(sum_part(rz_part, b, nb_rz), rz0[b], tolp[b]) &&
+                      !(inner_it && maxit > 0 && inner_it[b] >= maxit);
+    const bool drop = valid && !keep && ready != nullptr;
     const unsigned m = __ballot_sync(0xffffffffu, keep);
-    if (lane == 0) wcnt[w] = __popc(m);
+    const unsigned md = __ballot_sync(0xffffffffu, drop);
+    if (lane == 0) {
+      wcnt[w] = __popc(m);
+      wdrop[w] = __popc(md);
+    }
     __syncthreads();  // every list[j] of this chunk has been read
     int off = base + __popc(m & ((1u << lane) - 1u));
-    for (int i = 0; i < w; ++i) off += wcnt[i];
+    int doff = dbase + __popc(md & ((1u << lane) - 1u));
+    for (int i = 0; i < w; ++i) {
+      off += wcnt[i];
+      doff += wdrop[i];
+    }
     if (keep) list[off] = b;
+    if (drop) ready[doff] = b;
     __syncthreads();
     if (threadIdx.x == 0) {
-      int t = 0;
-      for (int i = 0; i < CMP_T / 32; ++i) t += wcnt[i];
+      int t = 0, td = 0;
+      for (int i = 0; i < CMP_T / 32; ++i) {
+        t += wcnt[i];
+        td += wdrop[i];
+      }
       base += t;
+      dbase += td;
     }
     __syncthreads();
   }
-  if (threadIdx.x == 0) *count = base;
+  if (threadIdx.x == 0) {
+    *count = base;
+    if (ready) *nready = dbase;
+  }
 }
 
-// the convergence tolerance of this solve, read by the (graph-replayed)
+// the convergence tolerance of every problem, read by the (graph-replayed)
 // iteration kernels from device memory
-__global__ void k_set_tol(double* __restrict__ tolp, double tol) { *tolp = tol; }
+__global__ void k_set_tol(double* __restrict__ tolp, double tol, int batch) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b < batch) tolp[b] = tol;
+}
+
+// ---- restarts of listed problems (the flat mixed-precision schedule) ----
+
+// x = 0 (unless keep_x), r = rhs for the listed problems
+template <typename T>
+__global__ void k_restart_vec(T* __restrict__ x, T* __restrict__ r, const T* __restrict__ rhs,
+                              long long N, int keep_x, const int* __restrict__ list,
+                              const int* count, int batch) {
+  const int b = active_problem(list, active_count(list, count, batch), batch, blockIdx.y);
+  if (b < 0) return;
+  const long long off = (long long)b * N;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N;
+       i += (long long)gridDim.x * blockDim.x) {
+    if (!keep_x) x[off + i] = T(0);
+    r[off + i] = rhs[off + i];
+  }
+}
+
+// y = a - y for the listed problems
+template <typename T>
+__global__ void k_sub_from_list(const T* __restrict__ a, T* __restrict__ y, long long N,
+                                const int* __restrict__ list, const int* count, int batch) {
+  const int b = active_problem(list, active_count(list, count, batch), batch, blockIdx.y);
+  if (b < 0) return;
+  const long long off = (long long)b * N;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N;
+       i += (long long)gridDim.x * blockDim.x)
+    y[off + i] = a[off + i] - y[off + i];
+}
+
+// dst = src for the listed problems
+template <typename T>
+__global__ void k_copy_list(T* __restrict__ dst, const T* __restrict__ src, long long N,
+                            const int* __restrict__ list, const int* count, int batch) {
+  const int b = active_problem(list, active_count(list, count, batch), batch, blockIdx.y);
+  if (b < 0) return;
+  const long long off = (long long)b * N;
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N;
+       i += (long long)gridDim.x * blockDim.x)
+    dst[off + i] = src[off + i];
+}
+
+// per listed problem: clear its four max slots and its iteration count since
+// the start (one thread each)
+__global__ void k_restart_scalars(unsigned* __restrict__ slots, int* __restrict__ inner_it,
+                                  const int* __restrict__ list, const int* count, int batch) {
+  const int n = active_count(list, count, batch);
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
+    const int b = list ? list[j] : j;
+    if (b < 0 || b >= batch) continue;
+    if (slots)
+      for (int k = 0; k < 4; ++k) slots[(long long)k * batch + b] = 0u;
+    if (inner_it) inner_it[b] = 0;
+  }
+}
+
+// Append the listed problems whose r.z is above tol_b^2 r0.z0 to the active
+// list, the others to the ready list (one block; order kept).
+template <typename T>
+__global__ void __launch_bounds__(CMP_T)
+    k_append_active(const T* __restrict__ rz_part, const T* __restrict__ rz0,
+                    const double* __restrict__ tolp, int nb_rz, const int* __restrict__ list,
+                    const int* count, int batch, int* __restrict__ alist,
+                    int* __restrict__ nactive, int* __restrict__ ready,
+                    int* __restrict__ nready) {
+  __shared__ int wcnt[CMP_T / 32], wdrop[CMP_T / 32];
+  __shared__ int base, dbase;
+  const int n = active_count(list, count, batch);
+  if (threadIdx.x == 0) {
+    base = *nactive;
+    dbase = ready ? *nready : 0;
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  for (int j0 = 0; j0 < n; j0 += CMP_T) {
+    const int j = j0 + threadIdx.x;
+    const int b = j < n ? (list ? list[j] : j) : -1;
+    const bool valid = b >= 0 && b < batch;
+    const bool keep = valid && is_active(sum_part(rz_part, b, nb_rz), rz0[b], tolp[b]);
+    const bool drop = valid && !keep && ready != nullptr;
+    const unsigned m = __ballot_sync(0xffffffffu, keep);
+    const unsigned md = __ballot_sync(0xffffffffu, drop);
+    if (lane == 0) {
+      wcnt[w] = __popc(m);
+      wdrop[w] = __popc(md);
+    }
+    __syncthreads();
+    int off = base + __popc(m & ((1u << lane) - 1u));
+    int doff = dbase + __popc(md & ((1u << lane) - 1u));
+    for (int i = 0; i < w; ++i) {
+      off += wcnt[i];
+      doff += wdrop[i];
+    }
+    if (keep) alist[off] = b;
+    if (drop) ready[doff] = b;
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      for (int i = 0; i < CMP_T / 32; ++i) {
+        base += wcnt[i];
+        dbase += wdrop[i];
+      }
+    }
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    *nactive = base;
+    if (ready) *nready = dbase;
+  }
+}
 
 template <typename T>
-__global__ void k_set_rz0(const T* __restrict__ part, T* __restrict__ rz0, int batch, int nb) {
-  const int b = blockIdx.x * blockDim.x + threadIdx.x;
-  if (b < batch) rz0[b] = sum_part(part, b, nb);
+__global__ void k_set_rz0(const T* __restrict__ part, T* __restrict__ rz0, int batch, int nb,
+                          const int* __restrict__ list = nullptr, const int* count = nullptr) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int b = active_problem(list, active_count(list, count, batch), batch, j);
+  if (b >= 0) rz0[b] = sum_part(part, b, nb);
 }
 
 // Per problem: if the guess residual is not better than the zero start
@@ -225,8 +366,11 @@ template <typename T>
 __global__ void k_judge_guess(T* __restrict__ x, T* __restrict__ r, T* __restrict__ z,
                               const T* __restrict__ b, const T* __restrict__ zb, long long N,
                               const T* __restrict__ rz_part, const T* __restrict__ bz_part,
-                              int nb) {
-  const int bi = blockIdx.y;
+                              int nb, const int* __restrict__ list = nullptr,
+                              const int* count = nullptr, int batch = 0) {
+  const int bi = list ? active_problem(list, active_count(list, count, batch), batch, blockIdx.y)
+                      : (int)blockIdx.y;
+  if (bi < 0) return;
   if (sum_part(rz_part, bi, nb) < sum_part(bz_part, bi, nb)) return;
   const long long off = (long long)bi * N;
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N;
@@ -240,9 +384,11 @@ __global__ void k_judge_guess(T* __restrict__ x, T* __restrict__ r, T* __restric
 // rz partials of problems that fell back to the zero start become b.M^-1 b
 template <typename T>
 __global__ void k_fix_rz(T* __restrict__ rz_part, const T* __restrict__ bz_part, int batch,
-                         int nb) {
-  const int bi = blockIdx.x * blockDim.x + threadIdx.x;
-  if (bi >= batch) return;
+                         int nb, const int* __restrict__ list = nullptr,
+                         const int* count = nullptr) {
+  const int j = blockIdx.x * blockDim.x + threadIdx.x;
+  const int bi = active_problem(list, active_count(list, count, batch), batch, j);
+  if (bi < 0) return;
   if (sum_part(rz_part, bi, nb) >= sum_part(bz_part, bi, nb))
     for (int j = 0; j < nb; ++j) rz_part[bi * PS + j] = bz_part[bi * PS + j];
 }
@@ -315,7 +461,8 @@ size_t pcg_ws(int ndim, int n, int nq, int batch) {
   const size_t vec = align_up((size_t)N * batch * sizeof(T), 256);
   const size_t scal = align_up((size_t)batch * PS * sizeof(T), 256);
   const size_t small = align_up((size_t)batch * sizeof(T), 256) +
-                       2 * align_up((size_t)batch * sizeof(int), 256) + 256 +
+                       4 * align_up((size_t)batch * sizeof(int), 256) + 256 +
+                       align_up((size_t)batch * sizeof(double), 256) +
                        align_up((size_t)4 * batch * sizeof(unsigned), 256);
   size_t inner = varcoef_ws(ndim, n, nq, batch, sizeof(T));
   const size_t f = fd_ws(ndim, n, batch, sizeof(T));
@@ -326,183 +473,217 @@ size_t pcg_ws(int ndim, int n, int nq, int batch) {
 template size_t pcg_ws<double>(int, int, int, int);
 template size_t pcg_ws<float>(int, int, int, int);
 
+// ---- the batched PCG context -----------------------------------------------
+
 template <typename T>
-int pcg_run(const PcgProblem<T>& pb, T* x, int use_x0, double tol, int maxiter, int* iters_host,
-            void* work, size_t work_bytes, cudaStream_t st) {
-  const int ndim = pb.ndim, n = pb.n, nq = pb.nq, batch = pb.batch;
-  if ((ndim != 2 && ndim != 3) || n < 1 || nq < n || batch < 1 || !pb.rhs || !x ||
-      !(tol > 0.0) || maxiter < 0)
+int PcgCtx<T>::init(const PcgProblem<T>& problem, T* x_, void* work, size_t work_bytes,
+                    cudaStream_t stream) {
+  pb = problem;
+  st = stream;
+  x = x_;
+  ndim = pb.ndim;
+  n = pb.n;
+  nq = pb.nq;
+  batch = pb.batch;
+  if ((ndim != 2 && ndim != 3) || n < 1 || nq < n || batch < 1 || !pb.rhs || !x)
     return JFG_ERR_ARG;
   const size_t need = pcg_ws<T>(ndim, n, nq, batch);
   if (!work || work_bytes < need) return JFG_ERR_WORKSPACE;
-  long long N = 1;
+  N = 1;
   for (int i = 0; i < ndim; ++i) N *= n;
   const size_t vec = align_up((size_t)N * batch * sizeof(T), 256);
   const size_t scal = align_up((size_t)batch * PS * sizeof(T), 256);
+  const size_t ib = align_up((size_t)batch * sizeof(int), 256);
   char* w = (char*)work;
-  T* r = (T*)w;
-  T* z = (T*)(w + vec);
-  T* p = (T*)(w + 2 * vec);
-  T* q = (T*)(w + 3 * vec);
-  T* pq_part = (T*)(w + 4 * vec);
-  T* rz_part[2] = {(T*)(w + 4 * vec + scal), (T*)(w + 4 * vec + 2 * scal)};
+  r = (T*)w;
+  z = (T*)(w + vec);
+  p = (T*)(w + 2 * vec);
+  q = (T*)(w + 3 * vec);
+  pq_part = (T*)(w + 4 * vec);
+  rz_part[0] = (T*)(w + 4 * vec + scal);
+  rz_part[1] = (T*)(w + 4 * vec + 2 * scal);
   char* sm = w + 4 * vec + 3 * scal;
-  T* rz0 = (T*)sm;
-  int* iters = (int*)(sm + align_up((size_t)batch * sizeof(T), 256));
-  int* alist = (int*)(sm + align_up((size_t)batch * sizeof(T), 256) +
-                      align_up((size_t)batch * sizeof(int), 256));
-  int* nactive = (int*)((char*)alist + align_up((size_t)batch * sizeof(int), 256));
-  double* tol_dev = (double*)((char*)nactive + 8);  // inside nactive's 256-byte block
-  unsigned* slots = (unsigned*)((char*)nactive + 256);
-  void* inner = (char*)slots + align_up((size_t)4 * batch * sizeof(unsigned), 256);
-  const size_t inner_bytes = work_bytes - (size_t)((char*)inner - w);
-
-  const Active all, act{alist, nactive};
-  const bool th = pb.engine == Engine::TH;
+  rz0 = (T*)sm;
+  sm += align_up((size_t)batch * sizeof(T), 256);
+  iters = (int*)sm;
+  sm += ib;
+  alist = (int*)sm;
+  sm += ib;
+  nactive = (int*)sm;  // the control block: active count, then ready count
+  nready = nactive + 1;
+  sm += 256;
+  tolv = (double*)sm;
+  sm += align_up((size_t)batch * sizeof(double), 256);
+  inner_it = (int*)sm;
+  sm += ib;
+  ready = (int*)sm;
+  sm += ib;
+  slots = (unsigned*)sm;
+  sm += align_up((size_t)4 * batch * sizeof(unsigned), 256);
+  inner = sm;
+  inner_bytes = work_bytes - (size_t)(sm - w);
+  work_ptr = work;
+  work_size = work_bytes;
+  th = pb.engine == Engine::TH;
   if (th && (ndim != 2 || !pb.ops_inv)) return JFG_ERR_ARG;
-  H16Ops h16;
   h16.op_inv = pb.ops_inv;
   h16.slots = th ? slots : nullptr;
-  unsigned* slot_p = th ? slots : nullptr;
   // Fused dots (FP32 tensor-core engines): p.Ap from the operator's field
   // pass and r.M^-1 r from the preconditioner's divide pass; each launch
   // reports its partial count (0: not fused, then explicit dot kernels).
-  const bool fuse_pq = std::is_same<T, float>::value && pb.engine != Engine::F32 &&
-                       ndim == 2 && (pb.fuse_dots & 1);
-  const bool fuse = std::is_same<T, float>::value && pb.m_engine != Engine::F32 &&
-                    (pb.fuse_dots & 2);
-  int nb_pq = NB, nb_rz = NB;
-  auto applyA = [&](const T* in, T* out, Active a, DotOut* dot = nullptr) -> int {
-    return varcoef_apply<T>(pb.engine, ndim, n, nq, batch, pb.ops, pb.kw, in, out, inner,
-                            inner_bytes, st, a, th ? &h16 : nullptr, dot);
-  };
-  // TH: clear the max slots and record max |v| of every problem in slot 0
-  // (the input of the next apply)
-  auto record_max = [&](const T* v) -> int {
-    if (!th) return JFG_OK;
-    JFG_CUDA_TRY(cudaMemsetAsync(slots, 0, sizeof(unsigned) * 4 * batch, st));
-    k_absmax<T><<<dim3(vec_blocks(N), batch), 256, 0, st>>>(v, N, slots, nullptr, nullptr,
-                                                            batch);
-    JFG_LAUNCHED();
-    return JFG_OK;
-  };
-  auto applyM = [&](const T* in, T* out, Active a, DotOut* dot = nullptr) -> int {
-    return fd_solve<T>(pb.m_engine, ndim, n, batch, pb.E, pb.W, pb.lam, nullptr, pb.fd_scale, in,
-                       out, inner, inner_bytes, st, a, dot);
-  };
-  // out . M^-1 in into part: fused into the preconditioner when possible
-  auto applyM_dot = [&](const T* in, T* out, Active a, T* part, int& nb) -> int {
-    int got = 0;
-    DotOut d;
-    d.part = fuse ? (float*)part : nullptr;
-    d.nb = &got;
-    JFG_TRY(applyM(in, out, a, fuse ? &d : nullptr));
-    if (got > 0) {
-      nb = got;
-      return JFG_OK;
-    }
-    nb = NB;
-    k_dot_part<T><<<dim3(NB, batch), DOT_T, 0, st>>>(in, out, N, part, a.list, a.count, batch);
-    JFG_LAUNCHED();
-    return JFG_OK;
-  };
-
-  const int vb = vec_blocks(N);
-  const dim3 vgrid(vb, batch);
-  const dim3 dgrid(NB, batch);
-  const long long total = N * batch;
-
-  // ---- setup: r = rhs - A x (or x = 0, r = rhs); z = M^-1 r; p = z
+  fuse_pq = std::is_same<T, float>::value && pb.engine != Engine::F32 && ndim == 2 &&
+            (pb.fuse_dots & 1);
+  fuse_rz = std::is_same<T, float>::value && pb.m_engine != Engine::F32 && (pb.fuse_dots & 2);
+  nb_pq = NB;
+  nb_rz = NB;
+  vb = vec_blocks(N);
+  JFG_CUDA_TRY(cudaMemsetAsync(nactive, 0, 2 * sizeof(int), st));
   JFG_CUDA_TRY(cudaMemsetAsync(iters, 0, sizeof(int) * batch, st));
-  if (use_x0) {
-    JFG_TRY(record_max(x));
-    JFG_TRY(applyA(x, r, all));
-    k_sub_from<T><<<vec_blocks(total), 256, 0, st>>>(pb.rhs, r, total);
-    JFG_LAUNCHED();
-  } else {
-    JFG_CUDA_TRY(cudaMemsetAsync(x, 0, sizeof(T) * total, st));
-    JFG_CUDA_TRY(cudaMemcpyAsync(r, pb.rhs, sizeof(T) * total, cudaMemcpyDeviceToDevice, st));
+  return JFG_OK;
+}
+
+template <typename T>
+int PcgCtx<T>::applyA(const T* in, T* out, Active a, DotOut* dot) {
+  return varcoef_apply<T>(pb.engine, ndim, n, nq, batch, pb.ops, pb.kw, in, out, inner,
+                          inner_bytes, st, a, th ? &h16 : nullptr, dot);
+}
+
+template <typename T>
+int PcgCtx<T>::applyM(const T* in, T* out, Active a, DotOut* dot) {
+  return fd_solve<T>(pb.m_engine, ndim, n, batch, pb.E, pb.W, pb.lam, nullptr, pb.fd_scale, in,
+                     out, inner, inner_bytes, st, a, dot);
+}
+
+// out . M^-1 in into part: fused into the preconditioner when possible
+template <typename T>
+int PcgCtx<T>::applyM_dot(const T* in, T* out, Active a, T* part, int& nb) {
+  int got = 0;
+  DotOut d;
+  d.part = fuse_rz ? (float*)part : nullptr;
+  d.nb = &got;
+  JFG_TRY(applyM(in, out, a, fuse_rz ? &d : nullptr));
+  if (got > 0) {
+    nb = got;
+    return JFG_OK;
   }
-  JFG_TRY(applyM_dot(r, z, all, rz_part[1], nb_rz));
-  if (use_x0 && pb.judge_x0) {
+  nb = NB;
+  k_dot_part<T><<<dim3(NB, batch), DOT_T, 0, st>>>(in, out, N, part, a.list, a.count, batch);
+  JFG_LAUNCHED();
+  return JFG_OK;
+}
+
+// TH: clear the listed problems' max slots and record max |v| in slot 0 (the
+// input of the next apply)
+template <typename T>
+int PcgCtx<T>::record_max(const T* v, Active a) {
+  if (!th) return JFG_OK;
+  k_restart_scalars<<<(batch + 255) / 256, 256, 0, st>>>(slots, nullptr, a.list, a.count, batch);
+  JFG_LAUNCHED();
+  k_absmax<T><<<dim3(vb, batch), 256, 0, st>>>(v, N, slots, a.list, a.count, batch);
+  JFG_LAUNCHED();
+  return JFG_OK;
+}
+
+template <typename T>
+int PcgCtx<T>::start(const int* list, const int* count, int use_x0, bool judge) {
+  const Active a{list, count};
+  const dim3 vgrid(vb, batch);
+  // r = rhs - A x (or x = 0, r = rhs); z = M^-1 r; p = z
+  k_restart_vec<T><<<vgrid, 256, 0, st>>>(x, r, pb.rhs, N, use_x0, list, count, batch);
+  JFG_LAUNCHED();
+  k_restart_scalars<<<(batch + 255) / 256, 256, 0, st>>>(nullptr, inner_it, list, count, batch);
+  JFG_LAUNCHED();
+  if (use_x0) {
+    JFG_TRY(record_max(x, a));
+    JFG_TRY(applyA(x, r, a));
+    k_sub_from_list<T><<<vgrid, 256, 0, st>>>(pb.rhs, r, N, list, count, batch);
+    JFG_LAUNCHED();
+  }
+  JFG_TRY(applyM_dot(r, z, a, rz_part[1], nb_rz));
+  const int sb = (batch + 127) / 128;
+  if (use_x0 && judge) {
     // Judge the initial guess against the zero start: keep it only where its
     // preconditioned residual is smaller than that of the right-hand side,
     // and measure convergence relative to the right-hand side either way.
     int nb_bz = NB;
-    JFG_TRY(applyM_dot(pb.rhs, q, all, pq_part, nb_bz));
+    JFG_TRY(applyM_dot(pb.rhs, q, a, pq_part, nb_bz));
     if (nb_bz != nb_rz) return JFG_ERR_UNSUPPORTED;  // same launch signature: cannot differ
-    k_judge_guess<T><<<vgrid, 256, 0, st>>>(x, r, z, pb.rhs, q, N, rz_part[1], pq_part, nb_rz);
+    k_judge_guess<T><<<vgrid, 256, 0, st>>>(x, r, z, pb.rhs, q, N, rz_part[1], pq_part, nb_rz,
+                                            list, count, batch);
     JFG_LAUNCHED();
-    k_set_rz0<T><<<(batch + 127) / 128, 128, 0, st>>>(pq_part, rz0, batch, nb_rz);
+    k_set_rz0<T><<<sb, 128, 0, st>>>(pq_part, rz0, batch, nb_rz, list, count);
     JFG_LAUNCHED();
-    k_fix_rz<T><<<(batch + 127) / 128, 128, 0, st>>>(rz_part[1], pq_part, batch, nb_rz);
+    k_fix_rz<T><<<sb, 128, 0, st>>>(rz_part[1], pq_part, batch, nb_rz, list, count);
     JFG_LAUNCHED();
   } else {
-    k_set_rz0<T><<<(batch + 127) / 128, 128, 0, st>>>(rz_part[1], rz0, batch, nb_rz);
+    k_set_rz0<T><<<sb, 128, 0, st>>>(rz_part[1], rz0, batch, nb_rz, list, count);
     JFG_LAUNCHED();
   }
-  JFG_CUDA_TRY(cudaMemcpyAsync(p, z, sizeof(T) * total, cudaMemcpyDeviceToDevice, st));
-  JFG_TRY(record_max(p));
-  // the problems that start active (r0.z0 > 0)
-  k_set_tol<<<1, 1, 0, st>>>(tol_dev, tol);
+  k_copy_list<T><<<vgrid, 256, 0, st>>>(p, z, N, list, count, batch);
   JFG_LAUNCHED();
-  k_compact<T><<<1, CMP_T, 0, st>>>(rz_part[1], rz0, tol_dev, alist, nactive, batch, 1, nb_rz);
+  JFG_TRY(record_max(p, a));
+  // the listed problems that start active (r0.z0 > 0) join the active list;
+  // with ready tracking the others are ready at once
+  k_append_active<T><<<1, CMP_T, 0, st>>>(rz_part[1], rz0, tolv, nb_rz, list, count, batch,
+                                          alist, nactive, track_ready ? ready : nullptr, nready);
   JFG_LAUNCHED();
+  return JFG_OK;
+}
 
-  auto iteration = [&](int it) -> int {
-    const int prev = (it + 1) & 1, cur = it & 1;
-    {
-      int got = 0;
-      DotOut d;
-      d.part = fuse_pq ? (float*)pq_part : nullptr;
-      d.nb = &got;
-      JFG_TRY(applyA(p, q, act, fuse_pq ? &d : nullptr));
-      if (got > 0) {
-        nb_pq = got;
-      } else {
-        nb_pq = NB;
-        k_dot_part<T><<<dgrid, DOT_T, 0, st>>>(p, q, N, pq_part, alist, nactive, batch);
-        JFG_LAUNCHED();
-      }
+template <typename T>
+int PcgCtx<T>::iteration(int it) {
+  const int prev = (it + 1) & 1, cur = it & 1;
+  const Active act{alist, nactive};
+  const dim3 vgrid(vb, batch);
+  unsigned* slot_p = th ? slots : nullptr;
+  {
+    int got = 0;
+    DotOut d;
+    d.part = fuse_pq ? (float*)pq_part : nullptr;
+    d.nb = &got;
+    JFG_TRY(applyA(p, q, act, fuse_pq ? &d : nullptr));
+    if (got > 0) {
+      nb_pq = got;
+    } else {
+      nb_pq = NB;
+      k_dot_part<T><<<dim3(NB, batch), DOT_T, 0, st>>>(p, q, N, pq_part, alist, nactive, batch);
+      JFG_LAUNCHED();
     }
-    k_update_xr<T><<<vgrid, 256, 0, st>>>(x, r, p, q, N, pq_part, rz_part[prev], rz0, tol_dev,
-                                          alist, nactive, batch, slot_p, nb_pq, nb_rz);
-    JFG_LAUNCHED();
-    int nb_new = NB;
-    JFG_TRY(applyM_dot(r, z, act, rz_part[cur], nb_new));
-    if (nb_new != nb_rz) return JFG_ERR_UNSUPPORTED;  // same launch signature: cannot differ
-    k_update_p<T><<<vgrid, 256, 0, st>>>(p, z, N, rz_part[cur], rz_part[prev], rz0, tol_dev,
-                                         iters, alist, nactive, batch, slot_p, nb_rz);
-    JFG_LAUNCHED();
-    k_compact<T><<<1, CMP_T, 0, st>>>(rz_part[cur], rz0, tol_dev, alist, nactive, batch, 0,
-                                      nb_rz);
-    JFG_LAUNCHED();
-    return JFG_OK;
-  };
-
-  // ---- iterate in chunks of CH iterations (CH even: the partial-sum
-  // ping-pong then lines up with the captured graph)
-  const int CH = 10;
-  const bool use_graph = (st != 0) && (maxiter >= CH);
-  cudaGraphExec_t exec = nullptr;
-  long long graph_kernels = 0;
-  // The chunk of CH iterations depends only on the buffers, operators, sizes
-  // and engines (the tolerance is read from device memory), so its
-  // instantiated graph is kept and replayed by later calls with the same key.
-  GraphKey key;
-  if (use_graph) {
-    int dev = 0;
-    JFG_CUDA_TRY(cudaGetDevice(&dev));
-    const long long v[] = {dev, (long long)sizeof(T), (long long)pb.engine,
-                           (long long)pb.m_engine, ndim, n, nq, batch, pb.fuse_dots, nb_rz,
-                           (long long)work_bytes};
-    const void* ptrs[] = {x, work, pb.ops.hi, pb.ops.lo, pb.ops_inv, pb.kw, pb.E.hi, pb.E.lo,
-                          pb.W.hi, pb.W.lo, pb.lam, pb.fd_scale};
-    key.ints.assign(v, v + sizeof(v) / sizeof(v[0]));
-    key.ptrs.assign(ptrs, ptrs + sizeof(ptrs) / sizeof(ptrs[0]));
-    graph_cache_find(key, &exec, &graph_kernels);
   }
-  if (use_graph && !exec) {
+  k_update_xr<T><<<vgrid, 256, 0, st>>>(x, r, p, q, N, pq_part, rz_part[prev], rz0, tolv, alist,
+                                        nactive, batch, slot_p, nb_pq, nb_rz);
+  JFG_LAUNCHED();
+  int nb_new = NB;
+  JFG_TRY(applyM_dot(r, z, act, rz_part[cur], nb_new));
+  if (nb_new != nb_rz) return JFG_ERR_UNSUPPORTED;  // same launch signature: cannot differ
+  k_update_p<T><<<vgrid, 256, 0, st>>>(p, z, N, rz_part[cur], rz_part[prev], rz0, tolv, iters,
+                                       alist, nactive, batch, slot_p, nb_rz, inner_it);
+  JFG_LAUNCHED();
+  k_compact<T><<<1, CMP_T, 0, st>>>(rz_part[cur], rz0, tolv, alist, nactive, batch, 0, nb_rz,
+                                    inner_it, maxit, track_ready ? ready : nullptr, nready);
+  JFG_LAUNCHED();
+  return JFG_OK;
+}
+
+// CH iterations: the cached graph of this context (captured on first use).
+// The chunk depends only on the buffers, operators, sizes, engines and the
+// per-problem iteration cap (the tolerances are read from device memory).
+template <typename T>
+int PcgCtx<T>::chunk() {
+  cudaGraphExec_t exec = nullptr;
+  long long kernels = 0;
+  int dev = 0;
+  JFG_CUDA_TRY(cudaGetDevice(&dev));
+  GraphKey key;
+  const long long v[] = {dev, (long long)sizeof(T), (long long)pb.engine, (long long)pb.m_engine,
+                         ndim, n, nq, batch, pb.fuse_dots, nb_rz, (long long)work_size, maxit,
+                         track_ready ? 1 : 0, CH};
+  const void* ptrs[] = {x, work_ptr, pb.ops.hi, pb.ops.lo, pb.ops_inv, pb.kw, pb.E.hi, pb.E.lo,
+                        pb.W.hi, pb.W.lo, pb.lam, pb.fd_scale};
+  key.ints.assign(v, v + sizeof(v) / sizeof(v[0]));
+  key.ptrs.assign(ptrs, ptrs + sizeof(ptrs) / sizeof(ptrs[0]));
+  graph_cache_find(key, &exec, &kernels);
+  if (!exec) {
     cudaGraph_t graph = nullptr;
     JFG_CUDA_TRY(cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal));
     set_capturing(true);
@@ -518,41 +699,57 @@ int pcg_run(const PcgProblem<T>& pb, T* x, int use_x0, double tol, int maxiter, 
     size_t nn = 0;
     cudaGraphGetNodes(graph, nullptr, &nn);
     if (nn > 0) {
-      cudaGraphNode_t nodes[4096];
-      if (nn > 4096) nn = 4096;
-      cudaGraphGetNodes(graph, nodes, &nn);
+      std::vector<cudaGraphNode_t> nodes(nn);
+      cudaGraphGetNodes(graph, nodes.data(), &nn);
       for (size_t i = 0; i < nn; ++i) {
         cudaGraphNodeType t;
         if (cudaGraphNodeGetType(nodes[i], &t) == cudaSuccess && t == cudaGraphNodeTypeKernel)
-          ++graph_kernels;
+          ++kernels;
       }
     }
     cudaError_t ei = cudaGraphInstantiate(&exec, graph, 0);
     cudaGraphDestroy(graph);
     JFG_CUDA_TRY(ei);
-    graph_cache_put(key, exec, graph_kernels);
+    graph_cache_put(key, exec, kernels);
   }
+  cudaError_t e = cudaGraphLaunch(exec, st);
+  if (e != cudaSuccess) {
+    set_last_cuda_error(e);
+    return JFG_ERR_CUDA;
+  }
+  count_launches(kernels);
+  return JFG_OK;
+}
+
+template <typename T>
+int pcg_run(const PcgProblem<T>& pb, T* x, int use_x0, double tol, int maxiter, int* iters_host,
+            void* work, size_t work_bytes, cudaStream_t st) {
+  if (!(tol > 0.0) || maxiter < 0) return JFG_ERR_ARG;
+  PcgCtx<T> c;
+  JFG_TRY(c.init(pb, x, work, work_bytes, st));
+  k_set_tol<<<(pb.batch + 127) / 128, 128, 0, st>>>(c.tolv, tol, pb.batch);
+  JFG_LAUNCHED();
+  JFG_TRY(c.start(nullptr, nullptr, use_x0, pb.judge_x0));
+  // iterate in chunks of CH iterations (CH even: the partial-sum ping-pong
+  // then lines up with the captured graph); a default stream or fewer than
+  // CH iterations left run without the graph
+  const bool use_graph = (st != 0) && (maxiter >= PcgCtx<T>::CH);
   int done_iters = 0;
   int status = JFG_OK;
   int h_active = 1;
   while (done_iters < maxiter) {
-    if (use_graph && maxiter - done_iters >= CH) {
-      cudaError_t e = cudaGraphLaunch(exec, st);
-      if (e != cudaSuccess) {
-        set_last_cuda_error(e);
-        status = JFG_ERR_CUDA;
-        break;
-      }
-      count_launches(graph_kernels);
-      done_iters += CH;
+    if (use_graph && maxiter - done_iters >= PcgCtx<T>::CH) {
+      status = c.chunk();
+      if (status != JFG_OK) break;
+      done_iters += PcgCtx<T>::CH;
     } else {
-      const int todo = (maxiter - done_iters < CH) ? maxiter - done_iters : CH;
-      for (int i = 0; i < todo && status == JFG_OK; ++i)
-        status = iteration(done_iters + i);
+      const int todo = (maxiter - done_iters < PcgCtx<T>::CH) ? maxiter - done_iters
+                                                               : PcgCtx<T>::CH;
+      for (int i = 0; i < todo && status == JFG_OK; ++i) status = c.iteration(done_iters + i);
       if (status != JFG_OK) break;
       done_iters += todo;
     }
-    cudaError_t e = cudaMemcpyAsync(&h_active, nactive, sizeof(int), cudaMemcpyDeviceToHost, st);
+    cudaError_t e = cudaMemcpyAsync(&h_active, c.nactive, sizeof(int), cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) {
       set_last_cuda_error(e);
@@ -563,13 +760,15 @@ int pcg_run(const PcgProblem<T>& pb, T* x, int use_x0, double tol, int maxiter, 
   }
   if (status != JFG_OK) return status;
   if (iters_host) {
-    JFG_CUDA_TRY(cudaMemcpyAsync(iters_host, iters, sizeof(int) * batch,
+    JFG_CUDA_TRY(cudaMemcpyAsync(iters_host, c.iters, sizeof(int) * pb.batch,
                                  cudaMemcpyDeviceToHost, st));
     JFG_CUDA_TRY(cudaStreamSynchronize(st));
   }
   return h_active == 0 ? JFG_OK : JFG_ERR_NOT_CONVERGED;
 }
 
+template struct PcgCtx<float>;
+template struct PcgCtx<double>;
 template int pcg_run<double>(const PcgProblem<double>&, double*, int, double, int, int*, void*,
                              size_t, cudaStream_t);
 template int pcg_run<float>(const PcgProblem<float>&, float*, int, double, int, int*, void*,

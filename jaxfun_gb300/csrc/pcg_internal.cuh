@@ -3,6 +3,8 @@
 
 #include <vector>
 
+#include <cuda_runtime.h>
+
 #include "jfg_internal.cuh"
 
 namespace jfg {
@@ -48,5 +50,46 @@ int batch_norms(long long N, int batch, const double* x, double* part_dev,
 template <typename T>
 int pcg_run(const PcgProblem<T>& pb, T* x, int use_x0, double tol, int maxiter,
             int* iters_host, void* work, size_t work_bytes, cudaStream_t st);
+
+// The batched PCG as reusable steps on a workspace (pcg_ws bytes): problems
+// can (re)start one list at a time and leave through the ready list, so
+// different problems may be at different points of their solves.
+template <typename T>
+struct PcgCtx {
+  static constexpr int CH = 10;  // iterations per captured chunk
+  PcgProblem<T> pb;
+  cudaStream_t st = 0;
+  int ndim = 2, n = 0, nq = 0, batch = 0, vb = 1;
+  long long N = 0;
+  T *x = nullptr, *r = nullptr, *z = nullptr, *p = nullptr, *q = nullptr;
+  T *pq_part = nullptr, *rz_part[2] = {nullptr, nullptr}, *rz0 = nullptr;
+  int *iters = nullptr, *alist = nullptr, *nactive = nullptr, *nready = nullptr;
+  int *inner_it = nullptr, *ready = nullptr;
+  double* tolv = nullptr;   // per-problem tolerance (device)
+  unsigned* slots = nullptr;
+  void* inner = nullptr;
+  size_t inner_bytes = 0;
+  void* work_ptr = nullptr;
+  size_t work_size = 0;
+  bool th = false, fuse_pq = false, fuse_rz = false;
+  int nb_pq = 16, nb_rz = 16;
+  H16Ops h16;
+  int maxit = 0;             // per-problem iteration cap since its start (0: none)
+  bool track_ready = false;  // problems leaving the active list go to the ready list
+
+  // x: the (batch, n^ndim) iterate; pb.rhs the right-hand sides; clears the
+  // active and ready counts and the iteration counts
+  int init(const PcgProblem<T>& problem, T* x, void* work, size_t work_bytes, cudaStream_t st);
+  // (re)start the listed problems (list NULL: all) from x = 0, or from x with
+  // use_x0 (judged against the zero start with judge); tolv must be set
+  int start(const int* list, const int* count, int use_x0, bool judge);
+  int iteration(int it);
+  int chunk();  // CH iterations through the cached graph (st must not be the legacy stream)
+
+  int applyA(const T* in, T* out, Active a, DotOut* dot = nullptr);
+  int applyM(const T* in, T* out, Active a, DotOut* dot = nullptr);
+  int applyM_dot(const T* in, T* out, Active a, T* part, int& nb);
+  int record_max(const T* v, Active a);
+};
 
 }  // namespace jfg

@@ -33,6 +33,7 @@ class MixedPlan(C.Structure):
         ("apply_f16", C.c_int),
         ("ops_hi16", C.c_void_p), ("ops_lo16", C.c_void_p), ("ops_inv16", C.c_void_p),
         ("fused_dots", C.c_int),
+        ("schedule", C.c_int),
     ]
 
 
@@ -82,7 +83,8 @@ class MixedVarCoefSolver:
 
     def __init__(self, A: VarCoefMatrix, M: TPMatricesLUFactors | None = None,
                  residual: str = "df64", fp32_updates: bool | None = None,
-                 precond: str = "bf16x3", apply: str = "f16x3", fused_dots: bool = True):
+                 precond: str = "bf16x3", apply: str = "f16x3", fused_dots: bool = True,
+                 schedule: str = "flat"):
         """``residual``: arithmetic of the refinement residual r = b - A x,
         "df64" (double-FP32 on the FP32 units) or "f64" (FP64 FMAs).
         ``fp32_updates``: once ||r|| <= 1e-4 ||b||, update r -= ||r|| A d in FP32
@@ -99,7 +101,13 @@ class MixedVarCoefSolver:
         split-"tf32"; 3-D and nq % 8 != 0 use split-TF32.
         ``fused_dots``: take the inner PCG's p.Ap and r.M^-1 r from the
         contraction epilogues (the field pass and the divide pass) instead of
-        separate dot kernels; r.M^-1 r only for a symmetric factorisation."""
+        separate dot kernels; r.M^-1 r only for a symmetric factorisation.
+        ``schedule``: "flat" (default) -- each problem takes its refinement
+        steps on its own, restarting its inner solve at the next 10-iteration
+        boundary after it converges while the others keep iterating -- or
+        "sync" (every refinement step waits for all inner solves)."""
+        if schedule not in ("flat", "sync"):
+            raise ValueError(f"schedule must be 'flat' or 'sync', not {schedule!r}")
         if precond not in ("tf32", "bf16x3"):
             raise ValueError(f"precond must be 'tf32' or 'bf16x3', not {precond!r}")
         if apply not in ("tf32", "f16x3"):
@@ -150,7 +158,7 @@ class MixedVarCoefSolver:
                               self.ops16[0].data_ptr() if af else None,
                               self.ops16[1].data_ptr() if af else None,
                               self.ops16[2].data_ptr() if af else None,
-                              fused)
+                              fused, 1 if schedule == "flat" else 0)
 
     def autotune(self, ws=None) -> list[dict]:
         """Tune the tensor-core passes of the inner solve once (each distinct

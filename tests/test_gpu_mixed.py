@@ -119,3 +119,61 @@ def test_fused_dots_match_explicit(precond):
             assert rel(x[i], xr[i]) < 1e-10, (fused, i)
         its[fused] = it_in.astype(float)
     assert np.all(np.abs(its[True] - its[False]) <= 0.1 * its[False] + 2), its
+
+
+@pytest.mark.parametrize("ndim,N,batch", [(2, 48, 6), (3, 16, 3)])
+def test_flat_schedule_matches_sync_and_fp64(ndim, N, batch):
+    """Per-problem refinement steps (the flat schedule) reach the same
+    <= 1e-10 answers as the synchronised schedule; a problem with a zero
+    right-hand side converges at once; with a perturbed start and with a
+    guess for the first inner solve as well."""
+    V = FunctionSpace(N, Legendre, bcs=DIRICHLET)
+    T = TensorProduct(*([V] * ndim))
+    rng = np.random.default_rng(17 + ndim)
+    kap = np.exp(rng.standard_normal((batch,) + (N,) * ndim) * np.linspace(0.2, 1.5, batch)
+                 .reshape((batch,) + (1,) * ndim))
+    b = rng.standard_normal((batch,) + (N - 2,) * ndim)
+    b[1] = 0.0
+    A = VarCoefMatrix(T, kap)
+    xr, _ = pcg(A, b, tol=1e-14, maxiter=4000)
+    xr = xr.cpu().numpy()
+    res = {}
+    for sched in ("flat", "sync"):
+        S = MixedVarCoefSolver(A, schedule=sched)
+        x, it_in, it_out = S.solve(b, tol=1e-12)
+        x = x.cpu().numpy()
+        assert np.all(x[1] == 0.0) and it_out[1] == 0
+        for i in range(batch):
+            if i != 1:
+                assert rel(x[i], xr[i]) < 1e-10, (sched, i, it_in, it_out)
+        res[sched] = it_in
+        # from an FP64 starting iterate and from a guess
+        x0 = xr + 1e-3 * rng.standard_normal(xr.shape) * np.abs(xr).max()
+        x0[1] = 0.0
+        x, _, _ = S.solve(b, x0=x0, tol=1e-12)
+        x = x.cpu().numpy()
+        g, _, _ = S.solve(b, tol=1e-12, guess=x0)
+        g = g.cpu().numpy()
+        for i in range(batch):
+            if i != 1:
+                assert rel(x[i], xr[i]) < 1e-10, (sched, "x0", i)
+                assert rel(g[i], xr[i]) < 1e-10, (sched, "guess", i)
+    # the same inner work per problem, within the chunk granularity
+    assert np.all(np.abs(res["flat"] - res["sync"]) <= 0.25 * res["sync"] + 12), res
+
+
+def test_flat_schedule_outer_budget_exhausted():
+    """With one outer step allowed and a tight tolerance the flat schedule
+    stops and reports non-convergence instead of looping."""
+    from jaxfun_gb300 import _lib
+
+    N = 32
+    V = FunctionSpace(N, Legendre, bcs=DIRICHLET)
+    T = TensorProduct(V, V)
+    rng = np.random.default_rng(3)
+    kap = np.exp(rng.standard_normal((2, N, N)))
+    b = rng.standard_normal((2, N - 2, N - 2))
+    S = MixedVarCoefSolver(VarCoefMatrix(T, kap), schedule="flat")
+    with pytest.raises(_lib.JfgError) as e:
+        S.solve(b, tol=1e-13, max_outer=1)
+    assert e.value.status == _lib.JFG_ERR_NOT_CONVERGED
