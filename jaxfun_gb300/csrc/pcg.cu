@@ -670,6 +670,11 @@ int PcgCtx<T>::iteration(int it) {
 // per-problem iteration cap (the tolerances are read from device memory).
 template <typename T>
 int PcgCtx<T>::chunk() {
+  if (st == 0) {
+    // the legacy default stream cannot be captured: launch the iterations
+    for (int i = 0; i < CH; ++i) JFG_TRY(iteration(i));
+    return JFG_OK;
+  }
   cudaGraphExec_t exec = nullptr;
   long long kernels = 0;
   int dev = 0;

@@ -84,7 +84,8 @@ struct PcgCtx {
   // use_x0 (judged against the zero start with judge); tolv must be set
   int start(const int* list, const int* count, int use_x0, bool judge);
   int iteration(int it);
-  int chunk();  // CH iterations through the cached graph (st must not be the legacy stream)
+  int chunk();  // CH iterations through the cached graph (launched directly on the
+                // legacy default stream, which cannot be captured)
 
   int applyA(const T* in, T* out, Active a, DotOut* dot = nullptr);
   int applyM(const T* in, T* out, Active a, DotOut* dot = nullptr);
