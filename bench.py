@@ -902,7 +902,8 @@ def run_ours(args):
         kap = torch.as_tensor(kap_h, device="cuda")
         fgrid = torch.as_tensor(f_h, device="cuda")
         A = VarCoefMatrix(T, kap)                 # FP64 operator (kw = kappa w (x) w)
-        solver = MixedVarCoefSolver(A, fused_dots=not args.no_fused_dots)
+        solver = MixedVarCoefSolver(A, fused_dots=not args.no_fused_dots,
+                                    schedule=args.schedule)
         SP = torch.as_tensor(D.scalar_product_matrix(), device="cuda")
         rhs = torch.empty(B, n, n, dtype=torch.float64, device="cuda")
         x = torch.empty(B, n, n, dtype=torch.float64, device="cuda")
@@ -1210,6 +1211,8 @@ def main():
     ap.add_argument("--maxiter", type=int, default=1000)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--skip-cpu", action="store_true")
+    ap.add_argument("--schedule", default="flat", choices=["flat", "sync"],
+                    help="refinement steps per problem (flat) or for the whole batch (sync)")
     ap.add_argument("--no-fused-dots", action="store_true",
                     help="inner PCG dots as separate kernels (not from the epilogues)")
     ap.add_argument("--no-autotune", action="store_true",
