@@ -1211,7 +1211,7 @@ def main():
     ap.add_argument("--maxiter", type=int, default=1000)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--skip-cpu", action="store_true")
-    ap.add_argument("--schedule", default="flat", choices=["flat", "sync"],
+    ap.add_argument("--schedule", default="sync", choices=["flat", "sync"],
                     help="refinement steps per problem (flat) or for the whole batch (sync)")
     ap.add_argument("--no-fused-dots", action="store_true",
                     help="inner PCG dots as separate kernels (not from the epilogues)")
