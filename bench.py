@@ -34,7 +34,7 @@ N_GRID = 256
 # DRAM bytes (read + write) of one scaled split-FP16 k_contract_tc launch at
 # M = 512, P = K = 256, 128 problems, from ncu (dram__bytes_read.sum +
 # dram__bytes_write.sum); None until captured.
-TC_TRAFFIC_PER_LAUNCH_B128 = None
+TC_TRAFFIC_PER_LAUNCH_B128 = 34.173440e6 + 8.172288e6
 
 
 def peaks():
@@ -941,8 +941,10 @@ def run_ours(args):
                                        f_d.data_ptr(), rhs.data_ptr(), tp_ws.data_ptr(),
                                        tp_ws.numel(), sh), "scalar_product")
 
-    def solve(use_model=True):
+    def solve(use_model=True, given=None):
         g = learned_guess() if (use_model and model is not None) else None
+        if given is not None:
+            g = given
         st = L.jfg_pcg_varcoef_mixed_guess(_lib.C.byref(solver.plan), rhs.data_ptr(),
                                            x.data_ptr(), None if g is None else g.data_ptr(), 0,
                                            args.tol, args.inner_tol, 10, args.maxiter, it_in,
@@ -1052,6 +1054,28 @@ def run_ours(args):
         err_mixed = float(rel(x[:nf]).max())
         err_fp64 = float(rel(x64).max())
         xt_cpu0 = xt[0].cpu().numpy()
+        # What the guess can gain at this refinement schedule: the network's
+        # guess error, and the same timed solve started from the tight FP64
+        # solution itself (a perfect guess; the inner solve sees it rounded to
+        # FP32) -- the ceiling of any learned start.
+        guess_info = {}
+        if model is not None and nf == B:
+            gq = learned_guess()
+            guess_info["learned_guess_rel_l2_mean"] = float(
+                ((gq - xt).norm(dim=(1, 2)) / xt.norm(dim=(1, 2))).mean())
+            pg = xt.clone()
+            solve(use_model=False, given=pg)
+            torch.cuda.synchronize()
+            e0.record(stream)
+            for _ in range(max(1, args.steps)):
+                solve(use_model=False, given=pg)
+            e1.record(stream)
+            e1.synchronize()
+            tp = e0.elapsed_time(e1) / 1e3 / max(1, args.steps)
+            guess_info["perfect_guess_solves_per_s"] = world * B / tp
+            guess_info["perfect_guess_inner_iterations_mean"] = float(np.mean(it_in[:]))
+            guess_info["perfect_guess_max_rel_err"] = float(rel(x).max())
+            x.copy_(x_learned)
         if mixed_zero is not None:
             mixed_zero["max_rel_err"] = float(rel(x_zero[:nf]).max())
         x_cpu0 = x[0].cpu().numpy()
@@ -1168,6 +1192,7 @@ def run_ours(args):
             cfg["learned_vs_zero_start_speedup"] = value / mixed_zero["solves_per_s"]
         if tr is not None:
             cfg.update(tr)
+        cfg.update(guess_info)
         line = {
             "metric": METRIC, "value": value, "unit": "solves/s", "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * t / args.steps,
