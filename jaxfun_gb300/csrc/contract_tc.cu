@@ -111,7 +111,9 @@ struct TcLaunch {
   int tmem_cols;
   int tmem_a;   // 1: split input tile (MMA operand A) kept in TMEM, not shared memory
   int mt_max;   // largest Mtile: sets the stage layout
-  int out_stage; // 1 if any group stores through shared memory (8 x 4 KB after the stages)
+  int out_stage; // 32 x 32 staging boxes per epilogue warp after the stages: 0, 1 (TMA
+                 // stores) or 2 (field-multiply launches: both of a warp's field boxes
+                 // of a tile are fetched ahead and stored from separate boxes)
   // 1 (16-bit operators, one group): operator-stationary schedule.  CTA c
   // serves the operator slot c % nslots, slot = s * mchunks + mc, loads that
   // operator chunk (all K blocks, hi and lo) into shared memory once and
@@ -420,7 +422,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
 
   uint8_t* sbase = smem + res_bytes;                   // input (and operator) stages
   uint8_t* ostage = sbase + (size_t)S * stage_bytes;  // epilogue output boxes (if used)
-  uint64_t* bars = (uint64_t*)(ostage + (L.out_stage ? 8 * STAGE_OUT : 0));
+  uint64_t* bars = (uint64_t*)(ostage + (size_t)8 * STAGE_OUT * L.out_stage);
   uint64_t* full = bars;
   uint64_t* conv = bars + S;
   uint64_t* empty = bars + 2 * S;
@@ -429,8 +431,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   uint64_t* hold = bars + 3 * S + 4;    // test hook: nothing arrives on it
   uint64_t* mma_done = bars + 3 * S + 5;  // MMA drain after a timeout
   uint64_t* opfull = bars + 3 * S + 6;    // resident operator chunk landed
-  uint64_t* fbar = bars + 3 * S + 7;      // [8] field box landed (one per epilogue warp)
-  uint32_t* tmem_slot = (uint32_t*)(bars + 3 * S + 15);
+  uint64_t* fbar = bars + 3 * S + 7;      // [16] field box landed (two per epilogue warp)
+  uint32_t* tmem_slot = (uint32_t*)(bars + 3 * S + 23);
 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
 
@@ -447,7 +449,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     mbar_init(hold, 1);
     mbar_init(mma_done, 1);
     mbar_init(opfull, 1);
-    for (int i = 0; i < 8; ++i) mbar_init(&fbar[i], 1);
+    for (int i = 0; i < 16; ++i) mbar_init(&fbar[i], 1);
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
   if (warp == 1) {
@@ -753,10 +755,14 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     // test hook: a barrier nothing arrives on; its wait runs out (status set)
     // and this warp skips its tiles, so every other role's waits run out too
     const bool held = s_hold != 0 && !mbar_wait(hold, 0, budget);
-    const int ew = warp - 6;   // this warp's staging box and field barrier
-    uint32_t fph = 0;          // phase of fbar[ew]
-    bool fpend = false;        // a field box load is in flight
+    const int ew = warp - 6;   // this warp's staging boxes and field barriers
+    uint32_t fph = 0;          // phase bit j of fbar[2 ew + j]
+    uint32_t fpend = 0;        // bit j: a field box load into box j is in flight
     bool fok = true;
+    const int nbox = L.out_stage > 0 ? L.out_stage : 1;
+    auto box_of = [&](int j) {
+      return (float*)(ostage + ((size_t)ew * nbox + (j < nbox ? j : 0)) * STAGE_OUT);
+    };
     int gi, pt, mc, b, s;
     for (; !held && fok && tile_of(li, gi, pt, mc, b, s); ++li) {
       const TcGroup& q = L.g[gi];
@@ -795,16 +801,15 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       // field-multiply epilogue with TMA: the field's 32 x 32 box of each
       // output box is fetched into the staging box by one bulk tensor copy
       const bool tfld = EPI == JFG_EPI_MUL_FIELD && !BETA && q.tma_store && q.tma_field;
-      float* box = (float*)(ostage + (size_t)ew * STAGE_OUT);
-      auto issue_field = [&](int cbk) {
+      const bool dbl = tfld && nbox == 2;
+      // field box of output box j (blocks k = 2j, 2j+1) into staging box j
+      auto issue_field = [&](int j, int cbk) {
         if (lane == 0) {
-          asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");  // box free
-          mbar_expect_tx(&fbar[ew], STAGE_OUT);
-          tma_load_4d(box, &L.fmap, &fbar[ew], pt * TILE_P + 32 * q4, mc * Mt + (cbk & ~1) * 16,
-                      q.fld_seg ? s : 0, q.fld_bat ? bb : 0);
+          mbar_expect_tx(&fbar[2 * ew + j], STAGE_OUT);
+          tma_load_4d(box_of(j), &L.fmap, &fbar[2 * ew + j], pt * TILE_P + 32 * q4,
+                      mc * Mt + (cbk & ~1) * 16, q.fld_seg ? s : 0, q.fld_bat ? bb : 0);
         }
-        __syncwarp();
-        fpend = true;
+        fpend |= 1u << j;
       };
       auto load_aux = [&](int cbk, float* a) {
         const int m0 = mc * Mt + cbk * 16;
@@ -823,7 +828,13 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       float aux[16], nxt[16];
       if (cb_of(0) < ncb) {
         load_aux(cb_of(0), aux);
-        if (tfld) issue_field(cb_of(0));
+        if (tfld) {
+          // the staging boxes are free once the previous stores have read them
+          if (lane == 0) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+          __syncwarp();
+          issue_field(0, cb_of(0));
+          if (dbl && cb_of(2) < ncb) issue_field(1, cb_of(2));
+        }
       }
       if (!mbar_wait(&tfull[buf], (uint32_t)(li >> 1) & 1u, budget)) break;
       asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
@@ -846,19 +857,25 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         }
         float v[16];
         tmem_ld16(tacc + (uint32_t)(cb * 16), v);
+        float* cbox = box_of(dbl ? (k >> 1) : 0);  // this output box's staging box
         if (tstore) {
           // stage this warp's 32 (p) x 32 (m) box in shared memory, [m][p] with
           // p contiguous, and store it with one bulk tensor copy (out-of-range
           // rows and columns are clipped by the copy)
           if ((k & 1) == 0) {
             if (tfld) {
-              if (k > 0) issue_field(cb);
-              if (!mbar_wait(&fbar[ew], fph, budget)) {
+              const int j = dbl ? (k >> 1) : 0;
+              if (!dbl && k > 0) {
+                if (lane == 0) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+                __syncwarp();
+                issue_field(0, cb);
+              }
+              if (!mbar_wait(&fbar[2 * ew + j], (fph >> j) & 1u, budget)) {
                 fok = false;
                 break;
               }
-              fph ^= 1u;
-              fpend = false;
+              fph ^= 1u << j;
+              fpend &= ~(1u << j);
             } else {
               if (lane == 0) asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
               __syncwarp();
@@ -872,7 +889,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             float a = r;
             if (EPI != JFG_EPI_NONE || H16) r *= (EPI == JFG_EPI_DIV_EIG) ? 1.f : (pin ? aux[j] : 0.f);
             if (tfld) a = r;  // aux held only the scales; the field comes next
-            if (tfld) r *= box[(16 * (k & 1) + j) * 32 + lane];
+            if (tfld) r *= cbox[(16 * (k & 1) + j) * 32 + lane];
             if (H16 && EPI == JFG_EPI_DIV_EIG) r *= pin ? osc[j] : 0.f;
             if (EPI == JFG_EPI_DIV_EIG) {
               a = r;
@@ -881,13 +898,13 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             r *= alpha;
             if (fdot) dsum = fmaf(a, r, dsum);
             if (H16) omax = fmaxf(omax, fabsf(r));
-            box[(16 * (k & 1) + j) * 32 + lane] = r;
+            cbox[(16 * (k & 1) + j) * 32 + lane] = r;
           }
           if ((k & 1) == 1 || !more || cb_of(k + 1) != cb + 1) {
             asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
             __syncwarp();
             if (lane == 0 && b >= 0)
-              tma_store_4d(&L.maps[gi][3], box, pt * TILE_P + 32 * q4, mc * Mt + (cb & ~1) * 16,
+              tma_store_4d(&L.maps[gi][3], cbox, pt * TILE_P + 32 * q4, mc * Mt + (cb & ~1) * 16,
                            s, b);
             if (lane == 0) asm volatile("cp.async.bulk.commit_group;" ::: "memory");
           }
@@ -936,8 +953,9 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         if (lane == 0 && b >= 0) atomicMax(q.out_max + b, __float_as_uint(omax));
       }
     }
-    // a field box load still in flight (after a timeout) lands before exit
-    if (fpend) mbar_wait(&fbar[ew], fph, WAIT_NS);
+    // field box loads still in flight (after a timeout) land before exit
+    for (int j = 0; j < 2; ++j)
+      if (fpend & (1u << j)) mbar_wait(&fbar[2 * ew + j], (fph >> j) & 1u, WAIT_NS);
     // bulk tensor stores of this warp complete before the kernel ends
     if (lane == 0) asm volatile("cp.async.bulk.wait_group 0;" ::: "memory");
   }
@@ -1193,12 +1211,19 @@ int launch_groups(int ng, const jfg_contract_desc* const* ds, const void* const*
   }
   const size_t stage = res ? 2 * (size_t)XBYTES
                            : (b16 ? 2 : ta ? 1 : 2) * (size_t)XBYTES + 2 * (size_t)mt_max * 128;
-  size_t ob = ostage ? 8 * (size_t)STAGE_OUT : 0;
+  // field-multiply launches stage both of a warp's boxes of a tile (the
+  // field of each fetched ahead), when two pipeline stages still fit
+  int nbuf = ostage ? 1 : 0;
+  if (!res && ng == 1 && L.g[0].tma_field &&
+      (size_t)SMEM_MAX - 1024 - 64 * 8 - 16 * (size_t)STAGE_OUT >= 2 * stage)
+    nbuf = 2;
+  size_t ob = 8 * (size_t)STAGE_OUT * nbuf;
   const size_t fixed = 1024 + (res ? res_bytes : 0) + 64 * 8;
   int stages = (int)(((size_t)SMEM_MAX - fixed - ob) / stage);
   if (res && stages < 3 && ostage && ((size_t)SMEM_MAX - fixed) / stage > (size_t)stages) {
     // three input stages matter more than the TMA-store staging boxes
     ostage = 0;
+    nbuf = 0;
     ob = 0;
     L.g[0].tma_store = 0;
     stages = (int)(((size_t)SMEM_MAX - fixed) / stage);
@@ -1210,7 +1235,7 @@ int launch_groups(int ng, const jfg_contract_desc* const* ds, const void* const*
   L.tmem_cols = 512;  // two accumulator buffers (+ operand A stages in TMEM mode)
   L.tmem_a = ta;
   L.mt_max = mt_max;
-  L.out_stage = ostage;
+  L.out_stage = nbuf;
   L.op_res = res ? 1 : 0;
   L.nslots = res ? nslots : 0;
   if (dot && dot->part && ng == 1) {
@@ -1228,7 +1253,7 @@ int launch_groups(int ng, const jfg_contract_desc* const* ds, const void* const*
     }
   }
   const size_t smem = 1024 + res_bytes * (res ? 1 : 0) + stages * stage + ob +
-                      (3 * stages + 15) * 8 + 16;
+                      (3 * stages + 23) * 8 + 16;
   if (smem > (size_t)SMEM_MAX) return JFG_ERR_UNSUPPORTED;
   long long nct = tiles < ctas ? tiles : ctas;
   if (res) nct = (long long)(ctas / nslots) * nslots;  // the same CTA count per slot
