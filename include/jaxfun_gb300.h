@@ -176,12 +176,12 @@ int jfg_tc_set_variant(int operand_a_in_tmem);
  * plain coalesced stores everywhere. */
 int jfg_tc_set_store_path(int tma_store);
 /* Schedule of single-group launches with 16-bit operators (split BF16, scaled
- * split FP16): 1 (default) operator-stationary -- each persistent CTA serves
- * one (segment, operator chunk) slot, keeps that chunk for all K blocks in
- * shared memory and streams only input tiles, used when the chunk fits
- * beside >= 2 input stages (K <= 256 at 128 operator rows) and there are
- * >= 2 tiles per CTA; 2 whenever the chunk fits; 0 streams operator and
- * input tiles together. */
+ * split FP16): 0 (default) streams operator and input tiles together; 1
+ * operator-stationary -- each persistent CTA serves one (segment, operator
+ * chunk) slot, keeps that chunk for all K blocks in shared memory and streams
+ * only input tiles, used when the chunk fits beside >= 2 input stages
+ * (K <= 256 at 128 operator rows) and there are >= 2 tiles per CTA; 2
+ * whenever the chunk fits.  The autotuner tries both where the chunk fits. */
 int jfg_tc_set_op_resident(int on);
 /* Launch configuration of the tensor-core contraction. */
 typedef struct {
