@@ -34,8 +34,21 @@ N_FINE = 256
 class GridMaps:
     """Per-axis FP64 operators between the solver's space and the network grid."""
 
-    def __init__(self, N: int = N_FINE, n: int = 64, guess_modes: int = 32, ndim: int = 2):
+    # Dirichlet modes per axis the learned guess keeps.  Beyond them the
+    # network's prediction is mostly noise relative to the solution's small
+    # content there, and noise in high modes costs PCG iterations.  2-D, 128
+    # problems of N = 256 solved to 1e-11: 107.9 mean inner iterations from
+    # zero, 100.6 from the guess cut at 32 modes, 97.4 at 6, 95.0 at 8, 94.6
+    # at 10 (smooth tapers did no better than a cut).  3-D, 32 problems of
+    # N = 128: cutting below 16 modes gained nothing.
+    GUESS_MODES = {2: 10, 3: 16}
+
+    def __init__(self, N: int = N_FINE, n: int = 64, guess_modes: int | None = None,
+                 ndim: int = 2):
+        if guess_modes is None:
+            guess_modes = self.GUESS_MODES[ndim]
         self.N, self.n, self.ndim = N, n, ndim
+        self.guess_modes = guess_modes
         Lo, lo = Legendre(N), Legendre(n)
         # fine-grid field -> first n Legendre modes -> values on the n-point grid
         self.to_net = lo.backward_matrix() @ Lo.forward_matrix()[:n, :]
@@ -44,9 +57,8 @@ class GridMaps:
         self.coef_to_net = D.backward_matrix(n)
         d = FunctionSpace(n, Legendre, bcs=DIRICHLET)
         # network-grid values -> Dirichlet coefficients (the basis functions
-        # phi_k = L_k - L_{k+2} do not depend on N), padded to N-2.  Only the
-        # first guess_modes are kept: the network resolves 32 Legendre modes
-        # per axis and its higher-mode content is noise in the energy norm.
+        # phi_k = L_k - L_{k+2} do not depend on N), padded to N-2; only the
+        # first guess_modes are kept.
         G = np.zeros((N - 2, n))
         m = min(guess_modes, n - 2)
         G[:m] = d.forward_matrix()[:m]
@@ -280,9 +292,11 @@ def main():
     ap.add_argument("--width", type=int, default=64)
     ap.add_argument("--chunk", type=int, default=128, help="problems per generating solve")
     ap.add_argument("--gain-problems", type=int, default=128)
+    ap.add_argument("--guess-modes", type=int, default=None,
+                    help="Dirichlet modes per axis kept in the learned guess")
     args = ap.parse_args()
     torch.cuda.set_device(0)
-    maps = GridMaps(N=args.N, n=args.n, guess_modes=args.modes, ndim=args.ndim)
+    maps = GridMaps(N=args.N, n=args.n, guess_modes=args.guess_modes, ndim=args.ndim)
     s = torch.cuda.Stream()
     with torch.cuda.stream(s):
         tr = generate(args.train, seed=1, maps=maps, chunk=args.chunk)

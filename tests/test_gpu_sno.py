@@ -228,7 +228,7 @@ def test_learned_guess_saves_iterations_3d():
 
     path = os.path.join(os.path.dirname(T.__file__), "weights", "sno_varcoef3d_N128.npz")
     model = T.load(path, batch=8)
-    maps = T.GridMaps(N=128, n=model.cfg.n, guess_modes=model.cfg.modes, ndim=3)
+    maps = T.GridMaps(N=128, n=model.cfg.n, ndim=3)
     data = T.generate(8, seed=11, maps=maps, chunk=8, keep_fine=True, log=lambda *_: None)
     kap, f, b, _ = data["fine"][0]
     A = VarCoefMatrix(maps.T, kap)
