@@ -9,7 +9,9 @@
 // converged gets a zero inner right-hand side, so its inner PCG is inactive
 // from the first iteration and its x is left untouched.
 #include <math.h>
+#include <string.h>
 
+#include <mutex>
 #include <vector>
 
 #include "jfg_internal.cuh"
@@ -235,6 +237,43 @@ __global__ void __launch_bounds__(OT)
   }
 }
 
+// ---- control of the solve loop inside one CUDA graph ----------------------
+// ctrl[8] body iterations, ctrl[9] outer steps taken, ctrl[10] chunks run,
+// ctrl[11] set when the iteration guard ended the loop.
+constexpr int CT_LOOPS = 8, CT_READY = 9, CT_CHUNKS = 10, CT_GUARD = 11;
+
+// Before the loop: it runs while some problem is active or ready.
+__global__ void k_loop_init(cudaGraphConditionalHandle h_loop, const int* __restrict__ pcg_ctl) {
+  if (threadIdx.x == 0 && blockIdx.x == 0)
+    cudaGraphSetConditional(h_loop, (pcg_ctl[0] > 0 || pcg_ctl[1] > 0) ? 1u : 0u);
+}
+
+// Head of each loop body: the ready problems take their outer step now
+// (schedule 1: whenever some are ready; schedule 0: once no problem is still
+// iterating), else the active ones run a chunk of iterations.
+__global__ void k_loop_branch(cudaGraphConditionalHandle h_ready, const int* __restrict__ pcg_ctl,
+                              int flat, int* __restrict__ ctrl) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const int na = pcg_ctl[0], nr = pcg_ctl[1];
+  const bool ready = nr > 0 && (flat || na <= 0);
+  cudaGraphSetConditional(h_ready, ready ? 1u : 0u);
+  ctrl[ready ? CT_READY : CT_CHUNKS] += 1;
+}
+
+// Tail of each loop body: go on while problems are active or ready, at most
+// guard times.
+__global__ void k_loop_next(cudaGraphConditionalHandle h_loop, const int* __restrict__ pcg_ctl,
+                            int* __restrict__ ctrl, int guard) {
+  if (threadIdx.x != 0 || blockIdx.x != 0) return;
+  const int loops = ++ctrl[CT_LOOPS];
+  bool more = pcg_ctl[0] > 0 || pcg_ctl[1] > 0;
+  if (more && loops >= guard) {
+    ctrl[CT_GUARD] = 1;
+    more = false;
+  }
+  cudaGraphSetConditional(h_loop, more ? 1u : 0u);
+}
+
 inline int blocks_for(long long n, int cap) {
   long long b = (n + 255) / 256;
   if (b > cap) b = cap;
@@ -265,6 +304,94 @@ MixedLayout layout(int ndim, int n, int nq, int batch) {
   L.outer = align_up((size_t)batch * 8, 256) + 7 * align_up((size_t)batch * 4, 256) + 256;
   L.total = L.vec64 + L.part + 2 * L.sc + 2 * L.vec32 + L.ws64 + L.wsin + L.opdf + L.outer;
   return L;
+}
+
+// ---- cache of instantiated solve graphs ------------------------------------
+// A solve graph: the prologue, then a loop (conditional WHILE node) whose body
+// picks (conditional IF/ELSE node) the outer step of the ready problems or a
+// chunk of inner iterations.  Kernel nodes per part, for the launch count.
+struct SolveGraph {
+  GraphKey key;
+  cudaGraphExec_t exec = nullptr;
+  long long k_top = 0, k_ready = 0, k_chunk = 0, k_body = 0;
+  unsigned long long used = 0;
+};
+std::mutex g_solve_mu;
+std::vector<SolveGraph> g_solves;
+unsigned long long g_solve_clock = 0;
+constexpr size_t SOLVE_CACHE_MAX = 8;
+
+bool solve_cache_find(const GraphKey& k, SolveGraph* out) {
+  std::lock_guard<std::mutex> lk(g_solve_mu);
+  for (SolveGraph& e : g_solves)
+    if (e.key == k) {
+      e.used = ++g_solve_clock;
+      *out = e;
+      return true;
+    }
+  return false;
+}
+
+void solve_cache_put(const SolveGraph& g) {
+  std::lock_guard<std::mutex> lk(g_solve_mu);
+  if (g_solves.size() >= SOLVE_CACHE_MAX) {
+    size_t lru = 0;
+    for (size_t i = 1; i < g_solves.size(); ++i)
+      if (g_solves[i].used < g_solves[lru].used) lru = i;
+    cudaGraphExecDestroy(g_solves[lru].exec);
+    g_solves.erase(g_solves.begin() + lru);
+  }
+  g_solves.push_back(g);
+  g_solves.back().used = ++g_solve_clock;
+}
+
+long long kernel_nodes(cudaGraph_t g) {
+  size_t nn = 0;
+  if (cudaGraphGetNodes(g, nullptr, &nn) != cudaSuccess || nn == 0) return 0;
+  std::vector<cudaGraphNode_t> nodes(nn);
+  if (cudaGraphGetNodes(g, nodes.data(), &nn) != cudaSuccess) return 0;
+  long long k = 0;
+  for (size_t i = 0; i < nn; ++i) {
+    cudaGraphNodeType t;
+    if (cudaGraphNodeGetType(nodes[i], &t) == cudaSuccess && t == cudaGraphNodeTypeKernel) ++k;
+  }
+  return k;
+}
+
+// Add a conditional node after everything captured so far on st (which keeps
+// capturing after it); its body graphs are returned in bodies.
+int add_conditional(cudaStream_t st, cudaGraph_t g, cudaGraphConditionalHandle h,
+                    cudaGraphConditionalNodeType type, unsigned size, cudaGraph_t* bodies) {
+  cudaStreamCaptureStatus cs;
+  const cudaGraphNode_t* deps = nullptr;
+  size_t nd = 0;
+  JFG_CUDA_TRY(cudaStreamGetCaptureInfo(st, &cs, nullptr, nullptr, &deps, nullptr, &nd));
+  if (cs != cudaStreamCaptureStatusActive) return JFG_ERR_CUDA;
+  cudaGraphNodeParams np = {};  // every reserved and unused byte zero
+  np.type = cudaGraphNodeTypeConditional;
+  np.conditional.handle = h;
+  np.conditional.type = type;
+  np.conditional.size = size;
+  cudaGraphNode_t node;
+  JFG_CUDA_TRY(cudaGraphAddNode(&node, g, deps, nullptr, nd, &np));
+  for (unsigned i = 0; i < size; ++i) bodies[i] = np.conditional.phGraph_out[i];
+  JFG_CUDA_TRY(cudaStreamUpdateCaptureDependencies(st, &node, nullptr, 1,
+                                                   cudaStreamSetCaptureDependencies));
+  return JFG_OK;
+}
+
+// Capture fill() into graph g on st; on failure the capture is ended and the
+// error returned.
+template <typename F>
+int capture_into(cudaStream_t st, cudaGraph_t g, F&& fill) {
+  JFG_CUDA_TRY(cudaStreamBeginCaptureToGraph(st, g, nullptr, nullptr, 0,
+                                             cudaStreamCaptureModeThreadLocal));
+  const int s = fill();
+  cudaGraph_t out = nullptr;
+  const cudaError_t e = cudaStreamEndCapture(st, &out);
+  if (s != JFG_OK) return s;
+  JFG_CUDA_TRY(e);
+  return JFG_OK;
 }
 
 }  // namespace
@@ -454,22 +581,6 @@ extern "C" int jfg_pcg_varcoef_mixed_guess(const jfg_mixed_plan* plan, const dou
   const dim3 pgrid(blocks_for(Lo.Npad, 256), batch);
   const dim3 ugrid(blocks_for(Lo.Nun, 256), batch);
   const dim3 sgrid(NBS, batch);
-  std::vector<double> hp((size_t)batch * NBS), bn(batch), rn(batch), hs_in(batch), hs_out(batch);
-  std::vector<int> it_tmp(batch), acc_in(batch, 0), acc_out(batch, 0);
-
-  auto norms = [&](const double* v, std::vector<double>& out) -> int {
-    k_sq_part<<<sgrid, 256, 0, st>>>(v, Lo.Nun, part);
-    JFG_LAUNCHED();
-    JFG_CUDA_TRY(cudaMemcpyAsync(hp.data(), part, sizeof(double) * batch * NBS,
-                                 cudaMemcpyDeviceToHost, st));
-    JFG_CUDA_TRY(cudaStreamSynchronize(st));
-    for (int b = 0; b < batch; ++b) {
-      double s = 0.0;
-      for (int j = 0; j < NBS; ++j) s += hp[(size_t)b * NBS + j];
-      out[b] = sqrt(s);
-    }
-    return JFG_OK;
-  };
   auto residual = [&]() -> int {
     JFG_TRY(varcoef_apply<double>(
         P.residual == 1 ? Engine::DF : Engine::F64, ndim, n, nq, batch,
@@ -480,46 +591,50 @@ extern "C" int jfg_pcg_varcoef_mixed_guess(const jfg_mixed_plan* plan, const dou
     return JFG_OK;
   };
 
-  // r -= s_b * A32 d (FP32 CUDA-core apply of the inner correction, padded layout)
-  auto residual_update = [&]() -> int {
-    JFG_TRY(varcoef_apply<float>(Engine::F32, ndim, nq, nq, batch,
-                                 OpRef<float>{P.ops32, nullptr}, P.kw32, d32, r32, wsin,
-                                 Lo.wsin, st));
-    k_unpad_axpy<<<ugrid, 256, 0, st>>>(ndim, n, nq, Lo.Npad, Lo.Nun, r32, sc_out, r64, -1.0);
-    JFG_LAUNCHED();
-    return JFG_OK;
-  };
+  // ---- per-problem outer steps, decided on the device ----
+  // A problem whose inner solve has converged (or hit maxiter_inner) leaves
+  // the active list for the ready list.  The ready problems then take their
+  // outer step together -- x += ||r|| d, the new residual (recomputed in
+  // FP64-class arithmetic, or updated in FP32 once it is small), its norm and
+  // the decision -- and restart.  Schedule 0 takes that step once no problem
+  // is still iterating (the batch's outer steps stay in step); schedule 1 at
+  // the next chunk boundary while the others keep iterating.  On a stream
+  // that can be captured the whole solve is ONE cached CUDA graph: the
+  // prologue, then a conditional WHILE node whose body chooses (conditional
+  // IF/ELSE node, set by a one-thread kernel) between the outer step and a
+  // chunk of inner iterations; the host waits once, at the end.
+  char* ob = (char*)opdf + Lo.opdf;
+  const size_t ib = align_up((size_t)batch * 4, 256);
+  double* bnd = (double*)ob;
+  ob += align_up((size_t)batch * 8, 256);
+  int* outer_cnt = (int*)ob;
+  int* state = (int*)(ob + ib);
+  int* res_mode = (int*)(ob + 2 * ib);
+  int* rall = (int*)(ob + 3 * ib);
+  int* rdf = (int*)(ob + 4 * ib);
+  int* rup = (int*)(ob + 5 * ib);
+  int* rlist = (int*)(ob + 6 * ib);
+  // [0] ready, [1] recompute, [2] update, [3] restart, [CT_*] loop control
+  int* ctrl = (int*)(ob + 7 * ib);
+  PcgCtx<float> c;
+  c.maxit = maxiter_inner;
+  c.track_ready = true;
+  JFG_TRY(c.init(pb, d32, wsin, Lo.wsin, st));
+  const int fp32_ok = P.ops32 ? 1 : 0;
+  const int flat = P.schedule == 1 ? 1 : 0;
+  const dim3 lgrid(NBS, batch);
+  const bool from_guess = guess != nullptr && !use_x0;
+  const long long guard_ll =
+      (long long)(max_outer + 1) * (maxiter_inner / PcgCtx<float>::CH + 2) + 8;
+  const int guard = guard_ll > (1LL << 30) ? (1 << 30) : (int)guard_ll;
 
-  if (P.schedule == 1) {
-    // ---- flat schedule: every problem takes its outer steps on its own ----
-    // A problem whose inner solve has converged (or hit maxiter_inner) leaves
-    // the active list for the ready list; at the next chunk boundary the
-    // ready problems take their outer step together (x += ||r|| d, the new
-    // residual -- recomputed in FP64-class arithmetic or updated in FP32 --
-    // its norm and the decision) and restart, while the others keep
-    // iterating.  The batch then runs about as many inner iterations as its
-    // slowest problem needs in total, not the sum of the slowest per step.
-    char* ob = (char*)opdf + Lo.opdf;
-    const size_t ib = align_up((size_t)batch * 4, 256);
-    double* bnd = (double*)ob;
-    ob += align_up((size_t)batch * 8, 256);
-    int* outer_cnt = (int*)ob;
-    int* state = (int*)(ob + ib);
-    int* res_mode = (int*)(ob + 2 * ib);
-    int* rall = (int*)(ob + 3 * ib);
-    int* rdf = (int*)(ob + 4 * ib);
-    int* rup = (int*)(ob + 5 * ib);
-    int* rlist = (int*)(ob + 6 * ib);
-    int* ctrl = (int*)(ob + 7 * ib);  // [0] ready, [1] recompute, [2] update, [3] restart
+  // ||rhs_b||, the first residual, the first decision (all problems) and the
+  // start of the first inner solves
+  auto prologue = [&]() -> int {
+    JFG_CUDA_TRY(cudaMemsetAsync(c.nactive, 0, 2 * sizeof(int), st));
+    JFG_CUDA_TRY(cudaMemsetAsync(c.iters, 0, sizeof(int) * batch, st));
     JFG_CUDA_TRY(cudaMemsetAsync(outer_cnt, 0, 3 * ib, st));
     JFG_CUDA_TRY(cudaMemsetAsync(ctrl, 0, 256, st));
-    PcgCtx<float> c;
-    c.maxit = maxiter_inner;
-    c.track_ready = true;
-    JFG_TRY(c.init(pb, d32, wsin, Lo.wsin, st));
-    const int fp32_ok = P.ops32 ? 1 : 0;
-    const dim3 lgrid(NBS, batch);
-    // ||rhs_b||, the first residual and the first decision (all problems)
     k_sq_part<<<lgrid, 256, 0, st>>>(rhs, Lo.Nun, part);
     JFG_LAUNCHED();
     k_norms_from<<<(batch + 127) / 128, 128, 0, st>>>(part, bnd, batch);
@@ -540,147 +655,183 @@ extern "C" int jfg_pcg_varcoef_mixed_guess(const jfg_mixed_plan* plan, const dou
     k_pad_scale<<<pgrid, 256, 0, st>>>(ndim, n, nq, Lo.Npad, Lo.Nun, r64, sc_in, r32, rlist,
                                        ctrl + 3, batch);
     JFG_LAUNCHED();
-    const bool from_guess = guess != nullptr && !use_x0;
     if (from_guess) {
       // the learned guess starts each first inner solve, judged per problem
       k_pad_scale<<<pgrid, 256, 0, st>>>(ndim, n, nq, Lo.Npad, Lo.Nun, guess, sc_in, d32, rlist,
                                          ctrl + 3, batch);
       JFG_LAUNCHED();
     }
-    JFG_TRY(c.start(rlist, ctrl + 3, from_guess ? 1 : 0, from_guess));
-    const long long guard =
-        (long long)(max_outer + 1) * (maxiter_inner / PcgCtx<float>::CH + 2) + 8;
+    return c.start(rlist, ctrl + 3, from_guess ? 1 : 0, from_guess);
+  };
+
+  // the outer step of the ready problems, then their restart
+  auto ready_step = [&]() -> int {
+    k_split_ready<<<1, OT, 0, st>>>(c.ready, c.nready, res_mode, batch, rall, ctrl, rdf, rup);
+    JFG_LAUNCHED();
+    k_unpad_axpy<<<ugrid, 256, 0, st>>>(ndim, n, nq, Lo.Npad, Lo.Nun, d32, sc_out, x, 1.0, rall,
+                                        ctrl, batch);
+    JFG_LAUNCHED();
+    // recomputed residuals r = rhs - A x
+    JFG_TRY(varcoef_apply<double>(
+        P.residual == 1 ? Engine::DF : Engine::F64, ndim, n, nq, batch,
+        OpRef<double>{P.ops64, P.residual == 1 ? (const double*)opdf : nullptr}, P.kw64, x, r64,
+        ws64, Lo.ws64, st, Active{rdf, ctrl + 1}));
+    k_sub_from64_list<<<ugrid, 256, 0, st>>>(rhs, r64, Lo.Nun, rdf, ctrl + 1, batch);
+    JFG_LAUNCHED();
+    // updated residuals r -= ||r|| A32 d (the apply's scratch is the inner
+    // solve's pass scratch, free between chunks)
+    if (fp32_ok) {
+      JFG_TRY(varcoef_apply<float>(Engine::F32, ndim, nq, nq, batch,
+                                   OpRef<float>{P.ops32, nullptr}, P.kw32, d32, r32, c.inner,
+                                   c.inner_bytes, st, Active{rup, ctrl + 2}));
+      k_unpad_axpy<<<ugrid, 256, 0, st>>>(ndim, n, nq, Lo.Npad, Lo.Nun, r32, sc_out, r64, -1.0,
+                                          rup, ctrl + 2, batch);
+      JFG_LAUNCHED();
+    }
+    k_sq_part<<<lgrid, 256, 0, st>>>(r64, Lo.Nun, part, rall, ctrl, batch);
+    JFG_LAUNCHED();
+    k_outer_decide<<<1, OT, 0, st>>>(part, bnd, tol, inner_tol, max_outer, fp32_ok, rall, ctrl,
+                                     batch, sc_in, sc_out, c.tolv, outer_cnt, res_mode, state,
+                                     rlist, ctrl + 3);
+    JFG_LAUNCHED();
+    k_pad_scale<<<pgrid, 256, 0, st>>>(ndim, n, nq, Lo.Npad, Lo.Nun, r64, sc_in, r32, rlist,
+                                       ctrl + 3, batch);
+    JFG_LAUNCHED();
+    return c.start(rlist, ctrl + 3, 0, false);
+  };
+
+  int status = JFG_OK;
+  int hctl[4] = {0, 0, 0, 0};  // body iterations, outer steps, chunks, guard hit
+  SolveGraph sg;
+  const bool graphed = st != 0;
+  if (!graphed) {
+    // the legacy default stream cannot be captured: the host drives the loop
+    JFG_TRY(prologue());
     int hc[2] = {0, 0};
-    int status = JFG_OK;
     for (long long loops = 0;; ++loops) {
       JFG_CUDA_TRY(cudaMemcpyAsync(hc, c.nactive, 2 * sizeof(int), cudaMemcpyDeviceToHost, st));
       JFG_CUDA_TRY(cudaStreamSynchronize(st));
-      if (hc[0] == 0 && hc[1] == 0) break;
-      if (loops > guard) {
+      if (hc[0] <= 0 && hc[1] <= 0) break;
+      if (loops >= guard) {
         status = JFG_ERR_NOT_CONVERGED;
         break;
       }
-      if (hc[1] > 0) {
-        // outer step of the ready problems
-        k_split_ready<<<1, OT, 0, st>>>(c.ready, c.nready, res_mode, batch, rall, ctrl, rdf, rup);
-        JFG_LAUNCHED();
-        k_unpad_axpy<<<ugrid, 256, 0, st>>>(ndim, n, nq, Lo.Npad, Lo.Nun, d32, sc_out, x, 1.0,
-                                            rall, ctrl, batch);
-        JFG_LAUNCHED();
-        // recomputed residuals r = rhs - A x
-        JFG_TRY(varcoef_apply<double>(
-            P.residual == 1 ? Engine::DF : Engine::F64, ndim, n, nq, batch,
-            OpRef<double>{P.ops64, P.residual == 1 ? (const double*)opdf : nullptr}, P.kw64, x,
-            r64, ws64, Lo.ws64, st, Active{rdf, ctrl + 1}));
-        k_sub_from64_list<<<ugrid, 256, 0, st>>>(rhs, r64, Lo.Nun, rdf, ctrl + 1, batch);
-        JFG_LAUNCHED();
-        // updated residuals r -= ||r|| A32 d (the apply's scratch is the inner
-        // solve's pass scratch, free between chunks)
-        if (fp32_ok) {
-          JFG_TRY(varcoef_apply<float>(Engine::F32, ndim, nq, nq, batch,
-                                       OpRef<float>{P.ops32, nullptr}, P.kw32, d32, r32, c.inner,
-                                       c.inner_bytes, st, Active{rup, ctrl + 2}));
-          k_unpad_axpy<<<ugrid, 256, 0, st>>>(ndim, n, nq, Lo.Npad, Lo.Nun, r32, sc_out, r64,
-                                              -1.0, rup, ctrl + 2, batch);
-          JFG_LAUNCHED();
-        }
-        k_sq_part<<<lgrid, 256, 0, st>>>(r64, Lo.Nun, part, rall, ctrl, batch);
-        JFG_LAUNCHED();
-        k_outer_decide<<<1, OT, 0, st>>>(part, bnd, tol, inner_tol, max_outer, fp32_ok, rall,
-                                         ctrl, batch, sc_in, sc_out, c.tolv, outer_cnt, res_mode,
-                                         state, rlist, ctrl + 3);
-        JFG_LAUNCHED();
-        k_pad_scale<<<pgrid, 256, 0, st>>>(ndim, n, nq, Lo.Npad, Lo.Nun, r64, sc_in, r32, rlist,
-                                           ctrl + 3, batch);
-        JFG_LAUNCHED();
-        JFG_TRY(c.start(rlist, ctrl + 3, 0, false));
-        continue;
+      if (hc[1] > 0 && (flat || hc[0] <= 0)) {
+        JFG_TRY(ready_step());
+      } else {
+        JFG_TRY(c.chunk());
       }
-      JFG_TRY(c.chunk());
     }
-    std::vector<int> hst(batch);
-    JFG_CUDA_TRY(cudaMemcpyAsync(hst.data(), state, sizeof(int) * batch, cudaMemcpyDeviceToHost,
-                                 st));
-    if (inner_iters)
-      JFG_CUDA_TRY(cudaMemcpyAsync(inner_iters, c.iters, sizeof(int) * batch,
-                                   cudaMemcpyDeviceToHost, st));
-    if (outer_iters)
-      JFG_CUDA_TRY(cudaMemcpyAsync(outer_iters, outer_cnt, sizeof(int) * batch,
-                                   cudaMemcpyDeviceToHost, st));
-    JFG_CUDA_TRY(cudaStreamSynchronize(st));
-    if (status != JFG_OK) return status;
-    for (int b = 0; b < batch; ++b)
-      if (hst[b] != 2) return JFG_ERR_NOT_CONVERGED;
-    return JFG_OK;
-  }
-
-  JFG_TRY(norms(rhs, bn));
-  if (use_x0) {
-    JFG_TRY(residual());
   } else {
-    JFG_CUDA_TRY(cudaMemsetAsync(x, 0, sizeof(double) * tot64, st));
-    JFG_CUDA_TRY(cudaMemcpyAsync(r64, rhs, sizeof(double) * tot64, cudaMemcpyDeviceToDevice, st));
+    int dev = 0;
+    JFG_CUDA_TRY(cudaGetDevice(&dev));
+    GraphKey key;
+    long long tb[2];
+    const double tv[2] = {tol, inner_tol};
+    memcpy(tb, tv, sizeof(tb));
+    const long long v[] = {dev,
+                           ndim,
+                           n,
+                           nq,
+                           batch,
+                           use_x0,
+                           from_guess ? 1 : 0,
+                           max_outer,
+                           maxiter_inner,
+                           flat,
+                           P.residual,
+                           P.precond_bf16,
+                           P.apply_f16,
+                           P.fused_dots,
+                           fp32_ok,
+                           (long long)work_bytes,
+                           tb[0],
+                           tb[1]};
+    key.ints.assign(v, v + sizeof(v) / sizeof(v[0]));
+    const void* ptrs[] = {rhs,        x,         guess,      work,      P.ops64,   P.kw64,
+                          P.ops32,    P.kw32,    P.ops_hi,   P.ops_lo,  P.ops_hi16, P.ops_lo16,
+                          P.ops_inv16, P.E_hi,   P.E_lo,     P.W_hi,    P.W_lo,    P.E_hi16,
+                          P.E_lo16,   P.W_hi16,  P.W_lo16,   P.lam,     P.fd_scale};
+    key.ptrs.assign(ptrs, ptrs + sizeof(ptrs) / sizeof(ptrs[0]));
+    if (!solve_cache_find(key, &sg)) {
+      sg.key = key;
+      cudaGraph_t g = nullptr, body = nullptr, br[2] = {nullptr, nullptr};
+      JFG_CUDA_TRY(cudaGraphCreate(&g, 0));
+      cudaGraphConditionalHandle h_loop = 0, h_ready = 0;
+      set_capturing(true);
+      int s = JFG_OK;
+      // the loop condition starts at 0 on every launch; only k_loop_init and
+      // k_loop_next (bounded by the guard) set it
+      if (cudaGraphConditionalHandleCreate(&h_loop, g, 0, cudaGraphCondAssignDefault) !=
+          cudaSuccess)
+        s = JFG_ERR_CUDA;
+      if (s == JFG_OK)
+        s = capture_into(st, g, [&]() -> int {
+          JFG_TRY(prologue());
+          k_loop_init<<<1, 32, 0, st>>>(h_loop, c.nactive);
+          JFG_CHECK_LAUNCH();
+          return add_conditional(st, g, h_loop, cudaGraphCondTypeWhile, 1, &body);
+        });
+      if (s == JFG_OK && cudaGraphConditionalHandleCreate(&h_ready, body, 0, 0) != cudaSuccess)
+        s = JFG_ERR_CUDA;
+      if (s == JFG_OK)
+        s = capture_into(st, body, [&]() -> int {
+          k_loop_branch<<<1, 32, 0, st>>>(h_ready, c.nactive, flat, ctrl);
+          JFG_CHECK_LAUNCH();
+          JFG_TRY(add_conditional(st, body, h_ready, cudaGraphCondTypeIf, 2, br));
+          k_loop_next<<<1, 32, 0, st>>>(h_loop, c.nactive, ctrl, guard);
+          JFG_CHECK_LAUNCH();
+          return JFG_OK;
+        });
+      if (s == JFG_OK) s = capture_into(st, br[0], ready_step);
+      if (s == JFG_OK)
+        s = capture_into(st, br[1], [&]() -> int {
+          for (int i = 0; i < PcgCtx<float>::CH; ++i) JFG_TRY(c.iteration(i));
+          return JFG_OK;
+        });
+      set_capturing(false);
+      if (s == JFG_OK) {
+        sg.k_top = kernel_nodes(g);
+        sg.k_body = kernel_nodes(body);
+        sg.k_ready = kernel_nodes(br[0]);
+        sg.k_chunk = kernel_nodes(br[1]);
+        const cudaError_t ei = cudaGraphInstantiate(&sg.exec, g, 0);
+        if (ei != cudaSuccess) {
+          set_last_cuda_error(ei);
+          s = JFG_ERR_CUDA;
+        }
+      }
+      cudaGraphDestroy(g);
+      if (s != JFG_OK) return s;
+      solve_cache_put(sg);
+    }
+    const cudaError_t e = cudaGraphLaunch(sg.exec, st);
+    if (e != cudaSuccess) {
+      set_last_cuda_error(e);
+      return JFG_ERR_CUDA;
+    }
+    JFG_CUDA_TRY(
+        cudaMemcpyAsync(hctl, ctrl + CT_LOOPS, sizeof(hctl), cudaMemcpyDeviceToHost, st));
   }
-  const bool start_from_guess = guess != nullptr && !use_x0;
-  bool all_done = false;
-  for (int outer = 0; outer <= max_outer; ++outer) {
-    JFG_TRY(norms(r64, rn));
-    int active = 0;
-    double worst = 0.0;  // largest relative residual among active problems
-    for (int b = 0; b < batch; ++b) {
-      const bool act = rn[b] > tol * bn[b];
-      hs_in[b] = act ? 1.0 / rn[b] : 0.0;
-      hs_out[b] = act ? rn[b] : 0.0;
-      active += act ? 1 : 0;
-      if (act && bn[b] > 0.0 && rn[b] / bn[b] > worst) worst = rn[b] / bn[b];
-    }
-    if (active == 0) {
-      all_done = true;
-      break;
-    }
-    if (outer == max_outer) break;
-    for (int b = 0; b < batch; ++b) acc_out[b] += hs_out[b] != 0.0 ? 1 : 0;
-    JFG_CUDA_TRY(cudaMemcpyAsync(sc_in, hs_in.data(), sizeof(double) * batch,
-                                 cudaMemcpyHostToDevice, st));
-    JFG_CUDA_TRY(cudaMemcpyAsync(sc_out, hs_out.data(), sizeof(double) * batch,
-                                 cudaMemcpyHostToDevice, st));
-    k_pad_scale<<<pgrid, 256, 0, st>>>(ndim, n, nq, Lo.Npad, Lo.Nun, r64, sc_in, r32);
-    JFG_LAUNCHED();
-    // The inner solve only has to shrink the residual by about tol / relres:
-    // close to convergence a loose inner tolerance suffices (at most 0.1).
-    double tol_k = inner_tol;
-    if (worst > 0.0) {
-      const double need = 0.3 * tol / worst;
-      if (need > tol_k) tol_k = need < 0.1 ? need : 0.1;
-    }
-    // First inner solve from the learned guess (scaled like the inner
-    // right-hand side b / ||b||), judged per problem against the zero start.
-    const bool from_guess = start_from_guess && outer == 0;
-    if (from_guess) {
-      k_pad_scale<<<pgrid, 256, 0, st>>>(ndim, n, nq, Lo.Npad, Lo.Nun, guess, sc_in, d32);
-      JFG_LAUNCHED();
-    }
-    pb.judge_x0 = from_guess;
-    const int s = pcg_run<float>(pb, d32, from_guess ? 1 : 0, tol_k, maxiter_inner,
-                                 it_tmp.data(), wsin, Lo.wsin, st);
-    pb.judge_x0 = false;
-    if (s != JFG_OK && s != JFG_ERR_NOT_CONVERGED) return s;
-    for (int b = 0; b < batch; ++b) acc_in[b] += it_tmp[b];
-    k_unpad_axpy<<<ugrid, 256, 0, st>>>(ndim, n, nq, Lo.Npad, Lo.Nun, d32, sc_out, x, 1.0);
-    JFG_LAUNCHED();
-    // Residual of the new iterate.  While the residual is large it is
-    // recomputed in FP64 (r = b - A x).  Once it is below 1e-4 ||b|| the
-    // correction d is small, and r -= ||r|| A d in FP32 is accurate to about
-    // 1e-7 ||r|| <= 1e-11 ||b||.
-    if (P.ops32 && worst <= 1e-4) {
-      JFG_TRY(residual_update());
-    } else {
-      JFG_TRY(residual());
-    }
-  }
+  std::vector<int> hst(batch);
+  JFG_CUDA_TRY(cudaMemcpyAsync(hst.data(), state, sizeof(int) * batch, cudaMemcpyDeviceToHost,
+                               st));
   if (inner_iters)
-    for (int b = 0; b < batch; ++b) inner_iters[b] = acc_in[b];
+    JFG_CUDA_TRY(cudaMemcpyAsync(inner_iters, c.iters, sizeof(int) * batch,
+                                 cudaMemcpyDeviceToHost, st));
   if (outer_iters)
-    for (int b = 0; b < batch; ++b) outer_iters[b] = acc_out[b];
-  return all_done ? JFG_OK : JFG_ERR_NOT_CONVERGED;
+    JFG_CUDA_TRY(cudaMemcpyAsync(outer_iters, outer_cnt, sizeof(int) * batch,
+                                 cudaMemcpyDeviceToHost, st));
+  JFG_CUDA_TRY(cudaStreamSynchronize(st));
+  if (graphed) {
+    // kernels the graph ran: its top level, and per body iteration the two
+    // control kernels plus the chosen branch
+    count_launches(sg.k_top + (long long)hctl[0] * sg.k_body +
+                   (long long)hctl[1] * sg.k_ready + (long long)hctl[2] * sg.k_chunk);
+    if (hctl[3]) status = JFG_ERR_NOT_CONVERGED;
+  }
+  if (status != JFG_OK) return status;
+  for (int b = 0; b < batch; ++b)
+    if (hst[b] != 2) return JFG_ERR_NOT_CONVERGED;
+  return JFG_OK;
 }

@@ -413,11 +413,6 @@ inline int vec_blocks(long long N) {
 
 // ---- cache of instantiated iteration graphs -------------------------------
 
-struct GraphKey {
-  std::vector<long long> ints;
-  std::vector<const void*> ptrs;
-  bool operator==(const GraphKey& o) const { return ints == o.ints && ptrs == o.ptrs; }
-};
 struct GraphEntry {
   GraphKey key;
   cudaGraphExec_t exec;

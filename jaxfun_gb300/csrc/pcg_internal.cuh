@@ -51,6 +51,14 @@ template <typename T>
 int pcg_run(const PcgProblem<T>& pb, T* x, int use_x0, double tol, int maxiter,
             int* iters_host, void* work, size_t work_bytes, cudaStream_t st);
 
+// Key of a cached instantiated graph: the sizes, switches and scalars it was
+// captured with, and every pointer its kernels use.
+struct GraphKey {
+  std::vector<long long> ints;
+  std::vector<const void*> ptrs;
+  bool operator==(const GraphKey& o) const { return ints == o.ints && ptrs == o.ptrs; }
+};
+
 // The batched PCG as reusable steps on a workspace (pcg_ws bytes): problems
 // can (re)start one list at a time and leave through the ready list, so
 // different problems may be at different points of their solves.

@@ -22,7 +22,7 @@ def schedule(request):
     L = _lib.lib()
     assert L.jfg_tc_set_op_resident(request.param) == 0
     yield request.param
-    L.jfg_tc_set_op_resident(1)
+    L.jfg_tc_set_op_resident(0)
 
 
 @pytest.mark.parametrize("apply", ["f16x3", "tf32"])
@@ -176,4 +176,54 @@ def test_flat_schedule_outer_budget_exhausted():
     S = MixedVarCoefSolver(VarCoefMatrix(T, kap), schedule="flat")
     with pytest.raises(_lib.JfgError) as e:
         S.solve(b, tol=1e-13, max_outer=1)
+    assert e.value.status == _lib.JFG_ERR_NOT_CONVERGED
+
+
+@pytest.mark.parametrize("sched", ["sync", "flat"])
+def test_whole_solve_graph_matches_host_loop(sched):
+    """On a stream that can be captured the whole refinement loop is one CUDA
+    graph (a conditional WHILE node around an IF/ELSE choice of outer step or
+    inner chunk).  It gives bit-identical answers and iteration counts to the
+    host-driven loop on the legacy default stream -- from zero, from a
+    starting iterate and from a guess, with a problem whose right-hand side
+    is zero -- also when the cached graph is replayed on new data; an
+    exhausted outer budget still reports non-convergence."""
+    import torch
+
+    from jaxfun_gb300 import _lib
+
+    N, batch = 48, 5
+    V = FunctionSpace(N, Legendre, bcs=DIRICHLET)
+    T = TensorProduct(V, V)
+    rng = np.random.default_rng(29)
+    kap = np.exp(rng.standard_normal((batch, N, N)))
+    A = VarCoefMatrix(T, kap)
+    S = MixedVarCoefSolver(A, schedule=sched)
+    bs = [rng.standard_normal((batch, N - 2, N - 2)) for _ in range(2)]
+    for b in bs:
+        b[2] = 0.0
+    x0 = 1e-3 * rng.standard_normal(bs[0].shape)
+    x0[2] = 0.0
+    side = torch.cuda.Stream()
+
+    def run(b, stream, **kw):
+        bt = torch.as_tensor(b, device="cuda")
+        with torch.cuda.stream(stream):
+            x, it_in, it_out = S.solve(bt, tol=1e-12, **kw)
+            x = x.clone()
+        torch.cuda.synchronize()
+        return x.cpu().numpy(), np.array(it_in), np.array(it_out)
+
+    legacy = torch.cuda.default_stream()
+    for kw in ({}, {"x0": x0}, {"guess": x0}):
+        for b in bs:  # the second right-hand side replays the cached graph
+            xh, ih, oh = run(b, legacy, **kw)
+            xg, ig, og = run(b, side, **kw)
+            assert np.array_equal(xh, xg), (kw.keys(), np.abs(xh - xg).max())
+            assert np.array_equal(ih, ig) and np.array_equal(oh, og), (ih, ig, oh, og)
+            assert np.all(xg[2] == 0.0) and og[2] == 0
+    with pytest.raises(_lib.JfgError) as e:
+        with torch.cuda.stream(side):
+            S.solve(torch.as_tensor(bs[0], device="cuda"), tol=1e-13, max_outer=1)
+        torch.cuda.synchronize()
     assert e.value.status == _lib.JFG_ERR_NOT_CONVERGED
