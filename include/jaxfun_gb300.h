@@ -110,6 +110,24 @@ int jfg_weighted_field_f64(int ndim, int nq, int batch, const double* kappa, con
 int jfg_exp_weighted_field_f64(int ndim, int nq, int batch, const double* g,
                                const double* scale, const double* shift, const double* w,
                                double* kappa, double* kw, float* kw32, void* stream);
+/* The same coefficient from the ORTHOGONAL-basis coefficients of g
+ * ((batch, n, ..., n), a JAXFunction's coefficients) in one sequence: the
+ * backward transform (V: the (nq, n) backward matrix of the orthogonal
+ * space, every axis) whose last pass evaluates exp and the weights in its
+ * epilogue, so g never crosses HBM on its own -- evaluate_jaxfunction_expr_quad
+ * for exp(g) (src/jaxfun/galerkin/arguments.py:928-990) fused into the
+ * backward transform of the coefficients (src/jaxfun/galerkin/
+ * tensorproductspace.py:330-346).  standardize = 1: g is shifted and scaled
+ * to mean 0 and population standard deviation 1 per problem; the last pass
+ * then writes g with per-tile moments (count, mean, sum of squared
+ * deviations, combined pairwise) and one more pass applies exp and the
+ * weights.  kappa and kw32 may be NULL.  Workspace:
+ * jfg_exp_weighted_backward_workspace_size. */
+size_t jfg_exp_weighted_backward_workspace_size(int ndim, int n, int nq, int batch);
+int jfg_exp_weighted_backward_f64(int ndim, int n, int nq, int batch, const double* V,
+                                  const double* g_coef, int standardize, const double* w,
+                                  double* kappa, double* kw, float* kw32, void* work,
+                                  size_t work_bytes, void* stream);
 /* Per problem: mean of g and 1 / population standard deviation (FP64, two
  * passes), for standardising g before exp (shift = mean, scale = 1 / std). */
 int jfg_field_moments_f64(int ndim, int nq, int batch, const double* g, double* mean,
@@ -195,7 +213,10 @@ typedef struct {
                             (jfg_tc_set_op_resident), 1 streaming, 2 operator-
                             stationary where the chunk fits                       */
   int store;             /* epilogue: 0 the process setting (jfg_tc_set_store_path),
-                            1 TMA bulk-tensor stores where allowed, 2 plain stores */
+                            1 TMA bulk-tensor stores where allowed (field-multiply
+                            launches stage two boxes per epilogue warp where two
+                            pipeline stages still fit), 2 plain stores, 3 TMA
+                            stores with one staging box per epilogue warp       */
 } jfg_tc_config;
 /*
  * Grouped tensor-core contraction: ngroups independent contractions (each a

@@ -80,6 +80,9 @@ SIGNATURES = {
     "jfg_weighted_field_f64": (_i, [_i, _i, _i, _vp, _vp, _vp, _vp, _vp]),
     "jfg_exp_weighted_field_f64": (_i, [_i, _i, _i, _vp, _vp, _vp, _vp, _vp, _vp, _vp, _vp]),
     "jfg_field_moments_f64": (_i, [_i, _i, _i, _vp, _vp, _vp, _vp]),
+    "jfg_exp_weighted_backward_workspace_size": (_sz, [_i, _i, _i, _i]),
+    "jfg_exp_weighted_backward_f64": (_i, [_i, _i, _i, _i, _vp, _vp, _i, _vp, _vp, _vp, _vp,
+                                           _vp, _sz, _vp]),
     "jfg_contract_f64": (_i, [C.POINTER(ContractDesc), _vp, _vp, _vp, _vp]),
     "jfg_contract_f32": (_i, [C.POINTER(ContractDesc), _vp, _vp, _vp, _vp]),
     "jfg_contract_df64": (_i, [C.POINTER(ContractDesc), _vp, _vp, _vp, _vp]),
@@ -264,5 +267,5 @@ def tuned_configs() -> list[dict]:
                     "operand_a_in_tmem": cfg.operand_a_in_tmem, "stages": cfg.stages,
                     "mtile": cfg.mtile or 128,
                     "schedule": {0: "default", 1: "streaming", 2: "operator-stationary"}[cfg.schedule],
-                    "store": {0: "default", 1: "tma", 2: "plain"}[cfg.store]})
+                    "store": {0: "default", 1: "tma", 2: "plain", 3: "tma-one-box"}[cfg.store]})
     return out

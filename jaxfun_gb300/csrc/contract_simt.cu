@@ -22,10 +22,24 @@ constexpr int NT = 256;  // threads: 16 x 16, each R x R outputs
 // Tile (16 R) x (16 R): R = 4 (64 x 64) for large launches; small launches
 // take R = 2 or 1 so that they still spread over the SMs (on GB300 one SM
 // issues only about 2 DFMA per clock, so a lone 64 x 64 FP64 tile is slow).
+// block sum over the NT threads (every thread gets the total)
+__device__ __forceinline__ double block_sum_nt(double v, double* red) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  __syncthreads();
+  if ((threadIdx.x & 31) == 0) red[threadIdx.x >> 5] = v;
+  __syncthreads();
+  double t = 0.0;
+#pragma unroll
+  for (int i = 0; i < NT / 32; ++i) t += red[i];
+  return t;
+}
+
 template <typename T, int EPI, int R>
 __global__ void __launch_bounds__(NT)
     k_contract_simt(const jfg_contract_desc d, const T* __restrict__ op,
-                    const T* __restrict__ in, T* __restrict__ out) {
+                    const T* __restrict__ in, T* __restrict__ out, T* __restrict__ aux = nullptr,
+                    float* __restrict__ aux32 = nullptr, double* __restrict__ part = nullptr) {
   constexpr int TM = 16 * R;  // rows of the operator per CTA
   constexpr int TP = 16 * R;  // columns (p) per CTA
   __shared__ T As[TK][TM + 4];
@@ -82,6 +96,77 @@ __global__ void __launch_bounds__(NT)
   T* outS = out + (long long)b * d.out_batch + (long long)s * d.out_seg;
   const T alpha = T(d.alpha);
   const T beta = T(d.beta);
+  if (EPI == EPI_EXP_WEIGHT) {
+    // kappa = exp(scale (v - shift)), kw = kappa wm[m] wp[p] (FP64, optional
+    // FP32 copy at the field strides); kappa itself into aux when given
+    const T sh = d.c0 ? ((const T*)d.c0)[b] : T(0);
+    const T sc = d.c1 ? ((const T*)d.c1)[b] : T(1);
+    T* auxS = aux ? aux + (long long)b * d.out_batch + (long long)s * d.out_seg : nullptr;
+    float* a32 = aux32 ? aux32 + (long long)b * d.field_batch + (long long)s * d.field_seg
+                       : nullptr;
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+      const int m = m0 + ty * R + i;
+      if (m >= d.M) continue;
+      const T wm = ((const T*)d.lam_m)[m];
+#pragma unroll
+      for (int j = 0; j < R; ++j) {
+        const int p = p0 + tx * R + j;
+        if (p >= d.P) continue;
+        const T k = exp(sc * (alpha * acc[i][j] - sh));
+        const T v = k * wm * ((const T*)d.lam_p)[p];
+        outS[(long long)m * d.out_ld + p] = v;
+        if (auxS) auxS[(long long)m * d.out_ld + p] = k;
+        if (a32) a32[(long long)m * d.field_ld + p] = (float)v;
+      }
+    }
+    return;
+  }
+  if (EPI == EPI_MOMENTS) {
+    // out = alpha v, and this tile's count, mean and sum of squared
+    // deviations (two passes over the registers) at part[b][tile][3]
+    __shared__ double red[NT / 32];
+    double cnt = 0.0, sum = 0.0;
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+      const int m = m0 + ty * R + i;
+#pragma unroll
+      for (int j = 0; j < R; ++j) {
+        const int p = p0 + tx * R + j;
+        if (m < d.M && p < d.P) {
+          const T v = alpha * acc[i][j];
+          outS[(long long)m * d.out_ld + p] = v;
+          cnt += 1.0;
+          sum += (double)v;
+        }
+      }
+    }
+    const double n_t = block_sum_nt(cnt, red);
+    const double mu = n_t > 0.0 ? block_sum_nt(sum, red) / n_t : 0.0;
+    double q = 0.0;
+#pragma unroll
+    for (int i = 0; i < R; ++i) {
+      const int m = m0 + ty * R + i;
+#pragma unroll
+      for (int j = 0; j < R; ++j) {
+        const int p = p0 + tx * R + j;
+        if (m < d.M && p < d.P) {
+          const double dv = (double)(alpha * acc[i][j]) - mu;
+          q = fma(dv, dv, q);
+        }
+      }
+    }
+    const double m2 = block_sum_nt(q, red);
+    if (threadIdx.x == 0) {
+      const long long tiles = (long long)gridDim.x * gridDim.y * d.nseg;
+      const long long t = ((long long)s * gridDim.y + blockIdx.y) * gridDim.x + blockIdx.x;
+      double* pt = part + ((long long)b * tiles + t) * 3;
+      pt[0] = n_t;
+      pt[1] = mu;
+      pt[2] = m2;
+    }
+    return;
+  }
 #pragma unroll
   for (int i = 0; i < R; ++i) {
     const int m = m0 + ty * R + i;
@@ -175,6 +260,39 @@ int launch_simt(const jfg_contract_desc& d, const T* op, const T* in, T* out,
 }
 
 }  // namespace
+
+// Last pass of a backward transform with a coefficient epilogue (FP64,
+// internal: not reachable through jfg_contract_*).  EPI_EXP_WEIGHT: out = kw
+// (lam_m, lam_p the per-row and per-column quadrature weights, c0 / c1 the
+// per-problem shift / scale), aux = kappa, aux32 = FP32 kw.  EPI_MOMENTS: out
+// = the values, part = (count, mean, M2) per tile; *tiles = tiles per problem.
+int contract_f64_coef(const jfg_contract_desc& d, int kind, const double* op, const double* in,
+                      double* out, double* aux, float* aux32, double* part, long long* tiles,
+                      cudaStream_t st) {
+  if ((kind != EPI_EXP_WEIGHT && kind != EPI_MOMENTS) || !op || !in || !out) return JFG_ERR_ARG;
+  if (d.batch < 0 || d.nseg < 1 || d.M < 0 || d.P < 0 || d.K < 1 || d.op_ld < d.K ||
+      d.in_ld < d.K || d.out_ld < d.P || d.batch_list || d.beta != 0.0)
+    return JFG_ERR_ARG;
+  if (kind == EPI_EXP_WEIGHT && (!d.lam_m || !d.lam_p || (aux32 && d.field_ld < d.P)))
+    return JFG_ERR_ARG;
+  if (kind == EPI_MOMENTS && !part) return JFG_ERR_ARG;
+  const long long gz = (long long)d.batch * d.nseg;
+  if (gz > 65535) return JFG_ERR_ARG;
+  constexpr int tile = 64;  // R = 4
+  const dim3 grid((d.P + tile - 1) / tile, (d.M + tile - 1) / tile, (unsigned)gz);
+  if (grid.y > 65535) return JFG_ERR_ARG;
+  if (tiles) *tiles = (long long)grid.x * grid.y * d.nseg;
+  if (gz == 0 || d.M == 0 || d.P == 0) return JFG_OK;
+  if (kind == EPI_EXP_WEIGHT)
+    k_contract_simt<double, EPI_EXP_WEIGHT, 4><<<grid, NT, 0, st>>>(d, op, in, out, aux, aux32,
+                                                                     nullptr);
+  else
+    k_contract_simt<double, EPI_MOMENTS, 4><<<grid, NT, 0, st>>>(d, op, in, out, nullptr,
+                                                                  nullptr, part);
+  JFG_CHECK_LAUNCH();
+  count_launches(1);
+  return JFG_OK;
+}
 
 int validate_desc(const jfg_contract_desc& d) {
   if (d.batch < 0 || d.nseg < 1 || d.M < 0 || d.P < 0 || d.K < 1) return JFG_ERR_ARG;

@@ -135,6 +135,15 @@ inline int contract(Engine e, const jfg_contract_desc& d, OpRef<float> op, const
   return contract_f32(d, op.hi, in, out, st);
 }
 
+// Internal epilogues of the FP64 CUDA-core contraction (not part of the C
+// ABI's jfg_contract_desc.epilogue values): the coefficient of a
+// variable-coefficient form from the last pass of its backward transform.
+constexpr int EPI_EXP_WEIGHT = 8;  // kw = exp(c1[b] (v - c0[b])) lam_m[m] lam_p[p]
+constexpr int EPI_MOMENTS = 9;     // v, plus (count, mean, M2) per tile
+int contract_f64_coef(const jfg_contract_desc& d, int kind, const double* op, const double* in,
+                      double* out, double* aux, float* aux32, double* part, long long* tiles,
+                      cudaStream_t st);
+
 // Optional device-side active subset of a batch (jfg_contract_desc.batch_list).
 struct Active {
   const int* list = nullptr;

@@ -453,6 +453,43 @@ __global__ void k_exp_weighted_field(int ndim, int nq, long long per, long long 
   }
 }
 
+// per-column weights of the last backward pass: wp[i] = prod of w over the
+// base-nq digits of i (ndim - 1 of them)
+__global__ void k_digit_weights(int digits, int nq, long long total, const double* __restrict__ w,
+                                double* __restrict__ wp) {
+  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
+       i += (long long)gridDim.x * blockDim.x) {
+    long long r = i;
+    double v = 1.0;
+    for (int a = 0; a < digits; ++a) {
+      v *= w[r % nq];
+      r /= nq;
+    }
+    wp[i] = v;
+  }
+}
+
+// per problem: shift = mean, scale = 1 / population std from the tiles'
+// (count, mean, M2) of the backward's last pass (Chan's pairwise update)
+__global__ void k_moments_combine(const double* __restrict__ part, long long tiles, int batch,
+                                  double* __restrict__ shift, double* __restrict__ scale) {
+  const int b = blockIdx.x * blockDim.x + threadIdx.x;
+  if (b >= batch) return;
+  const double* pt = part + (long long)b * tiles * 3;
+  double n = 0.0, mu = 0.0, m2 = 0.0;
+  for (long long t = 0; t < tiles; ++t) {
+    const double nb = pt[3 * t], mb = pt[3 * t + 1], qb = pt[3 * t + 2];
+    if (nb <= 0.0) continue;
+    const double nn = n + nb, dl = mb - mu;
+    mu += dl * (nb / nn);
+    m2 += qb + dl * dl * (n * nb / nn);
+    n = nn;
+  }
+  const double var = n > 0.0 ? m2 / n : 0.0;
+  shift[b] = mu;
+  scale[b] = var > 0.0 ? 1.0 / sqrt(var) : 1.0;
+}
+
 template int tp_apply<double>(Engine, int, const int*, const int*, int, const OpRef<double>*,
                               const double*, double*, void*, size_t, cudaStream_t,
                               const double*);
@@ -523,6 +560,97 @@ extern "C" int jfg_exp_weighted_field_f64(int ndim, int nq, int batch, const dou
       ndim, nq, per, total, g, scale, shift, w, kappa, kw, kw32);
   JFG_CHECK_LAUNCH();
   jfg::count_launches(1);
+  return JFG_OK;
+}
+
+// ---- coefficient from its expansion: backward transform + exp + weights ----
+
+namespace {
+struct ExpBackwardLayout {
+  size_t inter, wp, part, mom, total;
+};
+ExpBackwardLayout exp_backward_layout(int ndim, int n, int nq, int batch) {
+  ExpBackwardLayout L;
+  const int rows[3] = {nq, nq, nq}, cols[3] = {n, n, n};
+  L.inter = ndim > 1 ? jfg::align_up(jfg::tp_apply_ws(ndim, rows, cols, batch, 8), 256) : 0;
+  long long P = 1;
+  for (int i = 1; i < ndim; ++i) P *= nq;
+  L.wp = jfg::align_up((size_t)P * 8, 256);
+  const long long tiles = ((P + 63) / 64) * ((nq + 63) / 64);
+  L.part = jfg::align_up((size_t)batch * tiles * 3 * 8, 256);
+  L.mom = jfg::align_up((size_t)batch * 2 * 8, 256);
+  L.total = L.inter + L.wp + L.part + L.mom;
+  return L;
+}
+}  // namespace
+
+extern "C" size_t jfg_exp_weighted_backward_workspace_size(int ndim, int n, int nq, int batch) {
+  if (ndim < 1 || ndim > 3 || n < 1 || nq < 1 || batch < 0) return 0;
+  return exp_backward_layout(ndim, n, nq, batch).total;
+}
+
+extern "C" int jfg_exp_weighted_backward_f64(int ndim, int n, int nq, int batch, const double* V,
+                                             const double* g_coef, int standardize,
+                                             const double* w, double* kappa, double* kw,
+                                             float* kw32, void* work, size_t work_bytes,
+                                             void* stream) {
+  using namespace jfg;
+  if (ndim < 1 || ndim > 3 || n < 1 || nq < 1 || batch < 0 || !V || !g_coef || !w || !kw ||
+      (standardize != 0 && standardize != 1))
+    return JFG_ERR_ARG;
+  const ExpBackwardLayout L = exp_backward_layout(ndim, n, nq, batch);
+  if (!work || work_bytes < L.total) return JFG_ERR_WORKSPACE;
+  if (batch == 0) return JFG_OK;
+  cudaStream_t st = (cudaStream_t)stream;
+  char* wk = (char*)work;
+  double* wp = (double*)(wk + L.inter);
+  double* part = (double*)(wk + L.inter + L.wp);
+  double* shift = (double*)(wk + L.inter + L.wp + L.part);
+  double* scale = shift + batch;
+  long long P = 1;
+  for (int i = 1; i < ndim; ++i) P *= nq;
+  {
+    long long blocks = (P + 255) / 256;
+    if (blocks > 1024) blocks = 1024;
+    k_digit_weights<<<(int)blocks, 256, 0, st>>>(ndim - 1, nq, P, w, wp);
+    JFG_LAUNCHED();
+  }
+  // passes 1 .. ndim-1: the plain backward contraction (tp_apply's order:
+  // contract the last axis, rotate it to the front)
+  const int rows[3] = {nq, nq, nq}, cols[3] = {n, n, n};
+  const size_t inter = ndim > 1 ? tp_inter_bytes(ndim, rows, cols, batch, 8) : 0;
+  double* buf[2] = {(double*)wk, (double*)(wk + inter)};
+  const double* src = g_coef;
+  long long Pt = 1;
+  for (int i = 0; i < ndim - 1; ++i) Pt *= n;  // leading axes still in coefficients
+  for (int t = 0; t < ndim - 1; ++t) {
+    jfg_contract_desc d = make_desc(batch, nq, (int)Pt, n);
+    double* dst = buf[t & 1];
+    JFG_TRY(contract_f64(d, V, src, dst, st));
+    Pt = Pt / n * nq;
+    src = dst;
+  }
+  // last pass: M = nq (axis 0 comes to the front), P = nq^(ndim-1)
+  jfg_contract_desc d = make_desc(batch, nq, (int)P, n);
+  if (!standardize) {
+    d.lam_m = w;
+    d.lam_p = wp;
+    d.field_ld = P;
+    d.field_batch = (long long)nq * P;
+    return contract_f64_coef(d, EPI_EXP_WEIGHT, V, src, kw, kappa, kw32, nullptr, nullptr, st);
+  }
+  // standardised: g into kw with per-tile moments, then exp and weights in
+  // place (each element is read before it is overwritten, by its own thread)
+  long long tiles = 0;
+  JFG_TRY(contract_f64_coef(d, EPI_MOMENTS, V, src, kw, nullptr, nullptr, part, &tiles, st));
+  k_moments_combine<<<(batch + 127) / 128, 128, 0, st>>>(part, tiles, batch, shift, scale);
+  JFG_LAUNCHED();
+  const long long total = (long long)nq * P * batch;
+  long long blocks = (total + 255) / 256;
+  if (blocks > 8 * 152) blocks = 8 * 152;
+  k_exp_weighted_field<<<(int)blocks, 256, 0, st>>>(ndim, nq, (long long)nq * P, total, kw,
+                                                     scale, shift, w, kappa, kw, kw32);
+  JFG_LAUNCHED();
   return JFG_OK;
 }
 

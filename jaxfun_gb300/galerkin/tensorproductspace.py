@@ -184,6 +184,23 @@ def tp_apply_affine(mats: list[np.ndarray], x, shift: np.ndarray, cache: bool = 
     return out
 
 
+_SPB_CACHE: dict = {}
+
+
+def _sp_backward_matrix(test, source) -> np.ndarray:
+    """SP_test B_source at the test space's quadrature rule: (dim_test x
+    dim_source), the scalar product of a source-space expansion."""
+    key = (id(test), id(source))
+    hit = _SPB_CACHE.get(key)
+    if hit is not None and hit[0] is test and hit[1] is source:
+        return hit[2]
+    nq = test.num_quad_points
+    M = test.scalar_product_matrix(nq) @ source.backward_matrix(nq)
+    M.setflags(write=False)
+    _SPB_CACHE[key] = (test, source, M)
+    return M
+
+
 def _apply_1d(mat: np.ndarray, x) -> torch.Tensor:
     return tp_apply([mat], x)
 
@@ -278,6 +295,22 @@ class TensorProductSpace:
         shp = tuple(u.shape[-nd:])
         mats = [s.scalar_product_matrix(shp[i]) for i, s in enumerate(self.basespaces)]
         return self._apply(mats, u, precision)
+
+    def scalar_product_expansion(self, coef, source: "TensorProductSpace | None" = None,
+                                 precision: str = "f64") -> torch.Tensor:
+        """(f, v) for every test function v of this space, with f given by its
+        coefficients in ``source`` (default: this space's orthogonal space) --
+        inner(f*v) of a JAXFunction f (inner.py:914-984 on the values that
+        evaluate_jaxfunction_expr_quad, arguments.py:928-990, produces).  The
+        backward transform of f and the scalar product are fused per axis into
+        one operator, SP_ax B_ax (FP64 host product, cached), so the whole
+        right-hand side is ONE tensor-product apply: half the passes of
+        backward then scalar_product, and f's grid values never exist."""
+        src = self.get_orthogonal() if source is None else source
+        if len(src) != len(self):
+            raise ValueError("source space has a different dimension")
+        mats = [_sp_backward_matrix(s, t) for s, t in zip(self.basespaces, src.basespaces)]
+        return self._apply(mats, coef, precision)
 
     def backward_derivative(self, c, k: tuple[int, ...]) -> torch.Tensor:
         """d^k u / dx^k on the quadrature grid (per-axis derivative orders)."""

@@ -110,8 +110,41 @@ class VarCoefMatrix:
                        ) -> "VarCoefMatrix":
         """A(exp(g)) for g given by its orthogonal-basis coefficients (a
         JAXFunction's coefficients, ``(*batch, N, ..., N)``): the backward
-        transform to the quadrature grid, then ``from_log``."""
-        return cls.from_log(T, T.get_orthogonal().backward(g_coef), standardize=standardize)
+        transform to the quadrature grid with exp and the quadrature weighting
+        in the epilogue of its last pass (``jfg_exp_weighted_backward_f64``;
+        with ``standardize`` that pass records per-tile moments instead and
+        one more pass applies exp and the weights)."""
+        obj = cls.__new__(cls)
+        s0 = T.basespaces[0]
+        if any(s != s0 for s in T.basespaces):
+            raise ValueError("VarCoefMatrix needs the same 1-D space on every axis")
+        obj.T = T
+        obj.ndim = nd = len(T)
+        obj.n = s0.dim
+        obj.nq = nq = s0.num_quad_points
+        To = T.get_orthogonal()
+        o0 = To.basespaces[0]
+        no = o0.dim
+        g_coef = as_device(g_coef).contiguous()
+        if tuple(g_coef.shape[g_coef.ndim - nd:]) != (no,) * nd:
+            raise ValueError(f"g_coef must end in {(no,) * nd}")
+        obj.batch_shape = tuple(g_coef.shape[: g_coef.ndim - nd])
+        batch = obj.batch
+        V = as_device(np.ascontiguousarray(o0.backward_matrix(nq)))
+        if tuple(V.shape) != (nq, no):
+            raise ValueError("the orthogonal space's backward matrix is not (nq, N)")
+        w = as_device(np.array(s0.quad_points_and_weights()[1]))
+        shp = obj.batch_shape + (nq,) * nd
+        kappa = torch.empty(shp, dtype=torch.float64, device=g_coef.device)
+        kw = torch.empty_like(kappa)
+        L = _lib.lib()
+        ws = workspace(L.jfg_exp_weighted_backward_workspace_size(nd, no, nq, batch))
+        _lib.check(L.jfg_exp_weighted_backward_f64(
+            nd, no, nq, batch, V.data_ptr(), g_coef.data_ptr(), 1 if standardize else 0,
+            w.data_ptr(), kappa.data_ptr(), kw.data_ptr(), None, ws.data_ptr(), ws.numel(),
+            _lib.stream_handle()), "exp_weighted_backward")
+        obj._finish(kappa, kw)
+        return obj
 
     @property
     def batch(self) -> int:
