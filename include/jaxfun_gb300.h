@@ -213,10 +213,7 @@ typedef struct {
                             (jfg_tc_set_op_resident), 1 streaming, 2 operator-
                             stationary where the chunk fits                       */
   int store;             /* epilogue: 0 the process setting (jfg_tc_set_store_path),
-                            1 TMA bulk-tensor stores where allowed (field-multiply
-                            launches stage two boxes per epilogue warp where two
-                            pipeline stages still fit), 2 plain stores, 3 TMA
-                            stores with one staging box per epilogue warp       */
+                            1 TMA bulk-tensor stores where allowed, 2 plain stores */
 } jfg_tc_config;
 /*
  * Grouped tensor-core contraction: ngroups independent contractions (each a

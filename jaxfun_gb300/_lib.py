@@ -267,5 +267,5 @@ def tuned_configs() -> list[dict]:
                     "operand_a_in_tmem": cfg.operand_a_in_tmem, "stages": cfg.stages,
                     "mtile": cfg.mtile or 128,
                     "schedule": {0: "default", 1: "streaming", 2: "operator-stationary"}[cfg.schedule],
-                    "store": {0: "default", 1: "tma", 2: "plain", 3: "tma-one-box"}[cfg.store]})
+                    "store": {0: "default", 1: "tma", 2: "plain"}[cfg.store]})
     return out
