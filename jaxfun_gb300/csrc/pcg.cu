@@ -112,60 +112,140 @@ __device__ __forceinline__ bool is_active(T rz, T rz0, double tol) {
   return rz0 > T(0) && rz > T(0) && (double)rz > tol * tol * (double)rz0;
 }
 
-// x += alpha p ; r -= alpha q ; alpha = rz / (p.q) while active
+// 16-byte vectors of T for the per-iteration updates
+template <typename T>
+struct Vec16;
+template <>
+struct Vec16<float> {
+  using type = float4;
+  static constexpr int n = 4;
+};
+template <>
+struct Vec16<double> {
+  using type = double2;
+  static constexpr int n = 2;
+};
+template <typename V>
+__device__ __forceinline__ float vabsmax(const V& v);
+template <>
+__device__ __forceinline__ float vabsmax(const float4& v) {
+  return fmaxf(fmaxf(fabsf(v.x), fabsf(v.y)), fmaxf(fabsf(v.z), fabsf(v.w)));
+}
+template <>
+__device__ __forceinline__ float vabsmax(const double2& v) {
+  return fmaxf(fabsf((float)v.x), fabsf((float)v.y));
+}
+__device__ __forceinline__ float4 vaxpy(float a, const float4& x, const float4& y) {
+  return make_float4(fmaf(a, x.x, y.x), fmaf(a, x.y, y.y), fmaf(a, x.z, y.z), fmaf(a, x.w, y.w));
+}
+__device__ __forceinline__ double2 vaxpy(double a, const double2& x, const double2& y) {
+  return make_double2(fma(a, x.x, y.x), fma(a, x.y, y.y));
+}
+
+__device__ __forceinline__ bool al16(const void* ptr) {
+  return ((uintptr_t)ptr & 15u) == 0;
+}
+
+// The per-problem scalars of an update are computed once per block (thread
+// 0, the same partial-sum order everywhere) and shared: every thread doing
+// them cost more than the vector traffic (the FP64 tolerance test alone).
+// Vector part: 16-byte accesses when N is a multiple of the vector width,
+// else element by element.
+
+// r -= alpha q ; alpha = rz / (p.q) while active (x takes its alpha p in
+// k_update_xp, which reads p anyway)
 // slots (optional, [4][batch]): the scaled split-FP16 apply's max slots of
 // this problem are cleared here, after the apply read them and before the
 // p update and the next apply's passes record new maxima
 template <typename T>
-__global__ void k_update_xr(T* __restrict__ x, T* __restrict__ r, const T* __restrict__ p,
-                            const T* __restrict__ q, long long N, const T* __restrict__ pq_part,
-                            const T* __restrict__ rz_prev, const T* __restrict__ rz0,
-                            const double* __restrict__ tolp, const int* __restrict__ list,
-                            const int* count, int batch, unsigned* __restrict__ slots, int nb_pq,
-                            int nb_rz) {
+__global__ void k_update_r(T* __restrict__ r, const T* __restrict__ q, long long N,
+                           const T* __restrict__ pq_part, const T* __restrict__ rz_prev,
+                           const T* __restrict__ rz0, const double* __restrict__ tolp,
+                           const int* __restrict__ list, const int* count, int batch,
+                           unsigned* __restrict__ slots, int nb_pq, int nb_rz) {
+  __shared__ T s_alpha;
+  __shared__ int s_act;
   const int b = active_problem(list, active_count(list, count, batch), batch, blockIdx.y);
   if (b < 0) return;
-  const double tol = tolp[b];
-  const T rz = sum_part(rz_prev, b, nb_rz);
-  if (!is_active(rz, rz0[b], tol)) return;
-  if (slots && blockIdx.x == 0 && threadIdx.x < 4) slots[(long long)threadIdx.x * batch + b] = 0u;
-  const T pq = sum_part(pq_part, b, nb_pq);
-  const T alpha = rz / pq;
+  if (threadIdx.x == 0) {
+    const T rz = sum_part(rz_prev, b, nb_rz);
+    s_act = is_active(rz, rz0[b], tolp[b]) ? 1 : 0;
+    s_alpha = s_act ? rz / sum_part(pq_part, b, nb_pq) : T(0);
+    if (s_act && slots && blockIdx.x == 0)
+      for (int k = 0; k < 4; ++k) slots[(long long)k * batch + b] = 0u;
+  }
+  __syncthreads();
+  if (!s_act) return;
+  const T alpha = -s_alpha;
   const long long off = (long long)b * N;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N;
-       i += (long long)gridDim.x * blockDim.x) {
-    x[off + i] += alpha * p[off + i];
-    r[off + i] -= alpha * q[off + i];
+  using V = typename Vec16<T>::type;
+  constexpr int VN = Vec16<T>::n;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  const long long t0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (N % VN == 0 && al16(r + off) && al16(q + off)) {
+    V* rv = reinterpret_cast<V*>(r + off);
+    const V* qv = reinterpret_cast<const V*>(q + off);
+    for (long long i = t0; i < N / VN; i += stride) rv[i] = vaxpy(alpha, qv[i], rv[i]);
+  } else {
+    for (long long i = t0; i < N; i += stride) r[off + i] = fma(alpha, q[off + i], r[off + i]);
   }
 }
 
-// p = z + beta p ; beta = rz_new / rz_prev while active; counts iterations
-// pmax (optional): max |p| of each problem recorded for the next apply
+// x += alpha p ; p = z + beta p ; alpha = rz_prev / (p.q), beta = rz_new /
+// rz_prev while active; counts iterations.  pmax (optional): max |p| of each
+// problem recorded for the next apply
 template <typename T>
-__global__ void k_update_p(T* __restrict__ p, const T* __restrict__ z, long long N,
-                           const T* __restrict__ rz_new_part, const T* __restrict__ rz_prev_part,
-                           const T* __restrict__ rz0, const double* __restrict__ tolp,
-                           int* __restrict__ iters, const int* __restrict__ list,
-                           const int* count, int batch, unsigned* __restrict__ pmax, int nb_rz,
-                           int* __restrict__ inner_it) {
+__global__ void k_update_xp(T* __restrict__ x, T* __restrict__ p, const T* __restrict__ z,
+                            long long N, const T* __restrict__ pq_part,
+                            const T* __restrict__ rz_new_part, const T* __restrict__ rz_prev_part,
+                            const T* __restrict__ rz0, const double* __restrict__ tolp,
+                            int* __restrict__ iters, const int* __restrict__ list,
+                            const int* count, int batch, unsigned* __restrict__ pmax, int nb_pq,
+                            int nb_rz, int* __restrict__ inner_it) {
+  __shared__ T s_alpha, s_beta;
+  __shared__ int s_act;
   const int b = active_problem(list, active_count(list, count, batch), batch, blockIdx.y);
   if (b < 0) return;
-  const double tol = tolp[b];
-  const T rzp = sum_part(rz_prev_part, b, nb_rz);
-  if (!is_active(rzp, rz0[b], tol)) return;
-  const T rzn = sum_part(rz_new_part, b, nb_rz);
-  const T beta = rzn / rzp;
-  const long long off = (long long)b * N;
-  float m = 0.f;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < N;
-       i += (long long)gridDim.x * blockDim.x) {
-    const T v = z[off + i] + beta * p[off + i];
-    p[off + i] = v;
-    m = fmaxf(m, fabsf((float)v));
+  if (threadIdx.x == 0) {
+    const T rzp = sum_part(rz_prev_part, b, nb_rz);
+    s_act = is_active(rzp, rz0[b], tolp[b]) ? 1 : 0;
+    if (s_act) {
+      s_alpha = rzp / sum_part(pq_part, b, nb_pq);
+      s_beta = sum_part(rz_new_part, b, nb_rz) / rzp;
+      if (blockIdx.x == 0) {
+        iters[b] += 1;
+        if (inner_it) inner_it[b] += 1;
+      }
+    }
   }
-  if (blockIdx.x == 0 && threadIdx.x == 0) {
-    iters[b] += 1;
-    if (inner_it) inner_it[b] += 1;
+  __syncthreads();
+  if (!s_act) return;
+  const T alpha = s_alpha, beta = s_beta;
+  const long long off = (long long)b * N;
+  using V = typename Vec16<T>::type;
+  constexpr int VN = Vec16<T>::n;
+  const long long stride = (long long)gridDim.x * blockDim.x;
+  const long long t0 = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  float m = 0.f;
+  if (N % VN == 0 && al16(x + off) && al16(p + off) && al16(z + off)) {
+    V* xv = reinterpret_cast<V*>(x + off);
+    V* pv = reinterpret_cast<V*>(p + off);
+    const V* zv = reinterpret_cast<const V*>(z + off);
+    for (long long i = t0; i < N / VN; i += stride) {
+      const V po = pv[i];
+      xv[i] = vaxpy(alpha, po, xv[i]);
+      const V pn = vaxpy(beta, po, zv[i]);
+      pv[i] = pn;
+      m = fmaxf(m, vabsmax(pn));
+    }
+  } else {
+    for (long long i = t0; i < N; i += stride) {
+      const T po = p[off + i];
+      x[off + i] = fma(alpha, po, x[off + i]);
+      const T v = fma(beta, po, z[off + i]);
+      p[off + i] = v;
+      m = fmaxf(m, fabsf((float)v));
+    }
   }
   if (pmax) {
     m = block_max(m);
@@ -399,6 +479,14 @@ __global__ void k_sub_from(const T* __restrict__ a, T* __restrict__ y, long long
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < n;
        i += (long long)gridDim.x * blockDim.x)
     y[i] = a[i] - y[i];
+}
+
+// blocks per problem of the per-iteration updates: ~16 vector elements per
+// thread
+inline int upd_blocks(long long N) {
+  long long b = (N + 256 * 16 - 1) / (256 * 16);
+  if (b > 64) b = 64;
+  return (int)(b < 1 ? 1 : b);
 }
 
 inline int vec_blocks(long long N) {
@@ -645,14 +733,16 @@ int PcgCtx<T>::iteration(int it) {
       JFG_LAUNCHED();
     }
   }
-  k_update_xr<T><<<vgrid, 256, 0, st>>>(x, r, p, q, N, pq_part, rz_part[prev], rz0, tolv, alist,
-                                        nactive, batch, slot_p, nb_pq, nb_rz);
+  const dim3 ugrid(upd_blocks(N), batch);
+  k_update_r<T><<<ugrid, 256, 0, st>>>(r, q, N, pq_part, rz_part[prev], rz0, tolv, alist,
+                                       nactive, batch, slot_p, nb_pq, nb_rz);
   JFG_LAUNCHED();
   int nb_new = NB;
   JFG_TRY(applyM_dot(r, z, act, rz_part[cur], nb_new));
   if (nb_new != nb_rz) return JFG_ERR_UNSUPPORTED;  // same launch signature: cannot differ
-  k_update_p<T><<<vgrid, 256, 0, st>>>(p, z, N, rz_part[cur], rz_part[prev], rz0, tolv, iters,
-                                       alist, nactive, batch, slot_p, nb_rz, inner_it);
+  k_update_xp<T><<<ugrid, 256, 0, st>>>(x, p, z, N, pq_part, rz_part[cur], rz_part[prev], rz0,
+                                        tolv, iters, alist, nactive, batch, slot_p, nb_pq, nb_rz,
+                                        inner_it);
   JFG_LAUNCHED();
   k_compact<T><<<1, CMP_T, 0, st>>>(rz_part[cur], rz0, tolv, alist, nactive, batch, 0, nb_rz,
                                     inner_it, maxit, track_ready ? ready : nullptr, nready);
