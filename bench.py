@@ -894,8 +894,11 @@ def run_ours(args):
     D = FunctionSpace(N, Legendre, bcs=DIRICHLET)
     T = TensorProduct(D, D)
     kap_h, f_h = make_problems(B, N, seed0=replicas.seed_base(rank))  # own problems per rank
-    stream = torch.cuda.Stream()
-    sh = stream.cuda_stream
+    # --host-loop (profiling aid): the legacy default stream, which cannot be
+    # captured, so the refinement loop is host-driven and every kernel of the
+    # solve is a separate launch in a profiler's list
+    stream = torch.cuda.default_stream() if args.host_loop else torch.cuda.Stream()
+    sh = 0 if args.host_loop else stream.cuda_stream
     with torch.cuda.stream(stream):
         # ---- resident inputs and plans (untimed setup)
         w = torch.as_tensor(np.array(D.quad_points_and_weights()[1]), device="cuda")
@@ -1251,6 +1254,9 @@ def main():
                     help="inner PCG dots as separate kernels (not from the epilogues)")
     ap.add_argument("--no-autotune", action="store_true",
                     help="launch the inner solve's passes with the default configuration")
+    ap.add_argument("--host-loop", action="store_true",
+                    help="solve on the legacy default stream (host-driven loop, no whole-solve "
+                         "graph): every kernel a separate launch for profilers")
     ap.add_argument("--profile", action="store_true",
                     help="stop after the timed solves (for ncu launch lists of the headline)")
     ap.add_argument("--no-learned", action="store_true", help="mixed solve from a zero start")
