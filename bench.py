@@ -67,7 +67,7 @@ class Clocks:
         try:
             self.proc = subprocess.Popen(
                 ["nvidia-smi", "-i", str(self.gpu), f"--query-gpu={self.Q}",
-                 "--format=csv,noheader,nounits", "-lms", "200"],
+                 "--format=csv,noheader,nounits", "-lms", "50"],
                 stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
         except Exception:
             self.proc = None
@@ -907,7 +907,7 @@ def run_ours(args):
         A = VarCoefMatrix(T, kap)                 # FP64 operator (kw = kappa w (x) w)
         solver = MixedVarCoefSolver(A, fused_dots=not args.no_fused_dots,
                                     schedule=args.schedule)
-        SP = torch.as_tensor(D.scalar_product_matrix(), device="cuda")
+        SP = torch.as_tensor(np.array(D.scalar_product_matrix()), device="cuda")
         rhs = torch.empty(B, n, n, dtype=torch.float64, device="cuda")
         x = torch.empty(B, n, n, dtype=torch.float64, device="cuda")
         rows, cols = _lib.int_array([n, n]), _lib.int_array([N, N])
@@ -1229,7 +1229,7 @@ def run_ours(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=3)
+    ap.add_argument("--steps", type=int, default=10)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--batch", type=int, default=128)
     # stopping rules calibrated on seeded problems so that each path ends at

@@ -250,6 +250,10 @@ int jfg_tc_autotune(int ngroups, const jfg_contract_desc* descs, const float* co
  * tuned signatures always launch with their configuration.  Default 0.
  */
 int jfg_tc_set_autotune(int on);
+/* One configuration for every single-group tensor-core launch of the
+ * process (NULL: back to the tuned or default one) -- for tests and tuning
+ * studies; no counterpart in the reference. */
+int jfg_tc_force_config(const jfg_tc_config* cfg);
 /* Tuned single-group signatures: how many, and entry i (its signature as
  * text, its configuration and its time in ms per launch). */
 int jfg_tc_tuned_count(void);

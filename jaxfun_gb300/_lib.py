@@ -93,6 +93,7 @@ SIGNATURES = {
     "jfg_tc_set_store_path": (_i, [_i]),
     "jfg_tc_set_op_resident": (_i, [_i]),
     "jfg_tc_set_autotune": (_i, [_i]),
+    "jfg_tc_force_config": (_i, [_vp]),
     "jfg_tc_tuned_count": (_i, []),
     "jfg_tc_tuned_entry": (_i, [_i, C.c_char_p, _sz, _vp, _vp]),
     "jfg_banded_lu_size": (_sz, [_i, _i, _i, _i]),

@@ -1407,6 +1407,11 @@ int tune_single(int prec, const jfg_contract_desc& d, const void* oh, const void
 // One single-group launch with the tuned configuration of its signature (or
 // the default); with autotuning on, an untuned signature launched outside
 // stream capture is tuned first.
+// jfg_tc_force_config: one configuration for every single-group launch
+// (tests and tuning studies), instead of the tuned or default one
+bool g_force_on = false;
+jfg_tc_config g_force_cfg;
+
 int launch_single(int prec, const jfg_contract_desc& d, const void* oh, const void* ol,
                   const float* in, float* out, const H16Aux* aux, cudaStream_t st,
                   const DotOut* dot = nullptr) {
@@ -1416,10 +1421,15 @@ int launch_single(int prec, const jfg_contract_desc& d, const void* oh, const vo
   bool found = false;
   {
     std::lock_guard<std::mutex> lk(g_single_mu);
-    auto it = g_single.find(key);
-    if (it != g_single.end()) {
-      cfg = it->second.cfg;
+    if (g_force_on) {
+      cfg = g_force_cfg;
       found = true;
+    } else {
+      auto it = g_single.find(key);
+      if (it != g_single.end()) {
+        cfg = it->second.cfg;
+        found = true;
+      }
     }
   }
   if (!found && g_tune_single) {
@@ -1573,6 +1583,13 @@ extern "C" int jfg_tc_set_wait_budget_ns(unsigned long long ns) {
 extern "C" int jfg_tc_test_hold(int on) {
   if (on != 0 && on != 1) return JFG_ERR_ARG;
   JFG_CUDA_TRY(cudaMemcpyToSymbol(jfg::g_tc_test_hold, &on, sizeof(on)));
+  return JFG_OK;
+}
+
+extern "C" int jfg_tc_force_config(const jfg_tc_config* cfg) {
+  std::lock_guard<std::mutex> lk(jfg::g_single_mu);
+  jfg::g_force_on = cfg != nullptr;
+  if (cfg) jfg::g_force_cfg = *cfg;
   return JFG_OK;
 }
 

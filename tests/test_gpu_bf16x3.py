@@ -20,7 +20,7 @@ def schedule(request):
     L = _lib.lib()
     assert L.jfg_tc_set_op_resident(request.param) == 0
     yield request.param
-    L.jfg_tc_set_op_resident(1)
+    L.jfg_tc_set_op_resident(0)
 
 
 def split16(op64):

@@ -239,7 +239,7 @@ def test_f16x3_matches_fp64(S, M, P, K, epi, sched):
     try:
         runs = [run_f16(op, x, epi, field, in_max_scale=bound) for bound in (1.0, 512.0)]
     finally:
-        L.jfg_tc_set_op_resident(1)
+        L.jfg_tc_set_op_resident(0)
     for bound, (got, omax) in zip((1.0, 512.0), runs):
         for b in range(B):
             scale = np.abs(ref[b]).max()
@@ -272,3 +272,30 @@ def test_autotuned_launch_is_correct_and_recorded():
     assert np.abs(got - ref).max() <= TC_TOL * np.abs(ref).max()
     got2, _ = run_f16(op, x)
     assert np.abs(got2 - ref).max() <= TC_TOL * np.abs(ref).max()
+
+
+@pytest.mark.parametrize("mtile", [0, 64])
+@pytest.mark.parametrize("S,M,P,K", [(2, 256, 200, 200), (2, 256, 256, 256), (1, 130, 96, 512)])
+def test_f16x3_field_forced_configs(S, M, P, K, mtile):
+    """The scaled split-FP16 field-multiply pass under forced launch
+    configurations (jfg_tc_force_config): TMA stores with the field fetched
+    into the staging boxes, and plain stores with the field loaded per
+    element, at both tile heights, against FP64 of the same FP32 inputs."""
+    L = _lib.lib()
+    rng = np.random.default_rng(S * 1000 + P + mtile)
+    B = 9
+    op = rng.standard_normal((S, M, K))
+    x = rng.standard_normal((B, S, P, K)).astype(np.float32)
+    field = rng.uniform(0.5, 2.0, (B, S, M, P))
+    ref = np.einsum("smk,bspk->bsmp", op, x.astype(np.float64)) * field.astype(np.float32)
+    scale = np.abs(ref).max()
+    try:
+        for store in (1, 2):
+            for stages in (0, 2):
+                cfg = _lib.TcConfig(operand_a_in_tmem=1, order=0, ctas=0, stages=stages,
+                                    mtile=mtile, schedule=1, store=store)
+                assert L.jfg_tc_force_config(_lib.C.byref(cfg)) == 0
+                got, _ = run_f16(op, x, epi=1, field=field)
+                assert np.abs(got - ref).max() <= TC_TOL * scale, (store, stages)
+    finally:
+        assert L.jfg_tc_force_config(None) == 0
