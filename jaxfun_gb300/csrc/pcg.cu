@@ -201,7 +201,8 @@ __global__ void k_update_xp(T* __restrict__ x, T* __restrict__ p, const T* __res
                             const T* __restrict__ rz0, const double* __restrict__ tolp,
                             int* __restrict__ iters, const int* __restrict__ list,
                             const int* count, int batch, unsigned* __restrict__ pmax, int nb_pq,
-                            int nb_rz, int* __restrict__ inner_it) {
+                            int nb_rz, int* __restrict__ inner_it, int maxit,
+                            int* __restrict__ keep) {
   __shared__ T s_alpha, s_beta;
   __shared__ int s_act;
   const int b = active_problem(list, active_count(list, count, batch), batch, blockIdx.y);
@@ -209,14 +210,23 @@ __global__ void k_update_xp(T* __restrict__ x, T* __restrict__ p, const T* __res
   if (threadIdx.x == 0) {
     const T rzp = sum_part(rz_prev_part, b, nb_rz);
     s_act = is_active(rzp, rz0[b], tolp[b]) ? 1 : 0;
+    int kp = 0;
     if (s_act) {
+      const T rzn = sum_part(rz_new_part, b, nb_rz);
       s_alpha = rzp / sum_part(pq_part, b, nb_pq);
-      s_beta = sum_part(rz_new_part, b, nb_rz) / rzp;
+      s_beta = rzn / rzp;
+      // whether the problem stays in the active list (read by k_compact)
+      kp = is_active(rzn, rz0[b], tolp[b]) ? 1 : 0;
       if (blockIdx.x == 0) {
         iters[b] += 1;
-        if (inner_it) inner_it[b] += 1;
+        if (inner_it) {
+          const int it = inner_it[b] + 1;
+          inner_it[b] = it;
+          if (maxit > 0 && it >= maxit) kp = 0;
+        }
       }
     }
+    if (blockIdx.x == 0) keep[b] = kp;
   }
   __syncthreads();
   if (!s_act) return;
@@ -253,22 +263,19 @@ __global__ void k_update_xp(T* __restrict__ x, T* __restrict__ p, const T* __res
   }
 }
 
-// Active list: keep the problems whose r.z is still above tol_b^2 r0.z0 (and,
-// with inner_it, that have run fewer than maxit iterations since their start).
-// With init the candidates are 0..batch-1, else the current list (filtered in
-// place: an entry moves only to a lower slot, after its chunk has been read).
-// ready (optional): the problems dropped here are appended to ready[*nready]
-// (their inner solve is over).  One block; the order of the problems is kept.
+// Active list: keep the problems k_update_xp flagged (r.z still above
+// tol_b^2 r0.z0 and, with an iteration cap, fewer than maxit iterations since
+// their start).  The list is filtered in place: an entry moves only to a lower
+// slot, after its chunk has been read.  ready (optional): the problems dropped
+// here are appended to ready[*nready] (their inner solve is over).  One block;
+// the order of the problems is kept.
 constexpr int CMP_T = 256;
-template <typename T>
 __global__ void __launch_bounds__(CMP_T)
-    k_compact(const T* __restrict__ rz_part, const T* __restrict__ rz0,
-              const double* __restrict__ tolp, int* __restrict__ list, int* __restrict__ count,
-              int batch, int init, int nb_rz, const int* __restrict__ inner_it, int maxit,
-              int* __restrict__ ready, int* __restrict__ nready) {
+    k_compact(const int* __restrict__ keep, int* __restrict__ list, int* __restrict__ count,
+              int batch, int* __restrict__ ready, int* __restrict__ nready) {
   __shared__ int wcnt[CMP_T / 32], wdrop[CMP_T / 32];
   __shared__ int base, dbase;
-  const int n = init ? batch : active_count(list, count, batch);
+  const int n = active_count(list, count, batch);
   if (threadIdx.x == 0) {
     base = 0;
     dbase = ready ? *nready : 0;
@@ -278,12 +285,11 @@ __global__ void __launch_bounds__(CMP_T)
   for (int j0 = 0; j0 < n; j0 += CMP_T) {
     const int j = j0 + threadIdx.x;
     int b = -1;
-    if (j < n) b = init ? j : list[j];
+    if (j < n) b = list[j];
     const bool valid = b >= 0 && b < batch;
-    const bool keep = valid && is_active(sum_part(rz_part, b, nb_rz), rz0[b], tolp[b]) &&
-                      !(inner_it && maxit > 0 && inner_it[b] >= maxit);
-    const bool drop = valid && !keep && ready != nullptr;
-    const unsigned m = __ballot_sync(0xffffffffu, keep);
+    const bool kp = valid && keep[b] != 0;
+    const bool drop = valid && !kp && ready != nullptr;
+    const unsigned m = __ballot_sync(0xffffffffu, kp);
     const unsigned md = __ballot_sync(0xffffffffu, drop);
     if (lane == 0) {
       wcnt[w] = __popc(m);
@@ -296,7 +302,7 @@ __global__ void __launch_bounds__(CMP_T)
       off += wcnt[i];
       doff += wdrop[i];
     }
-    if (keep) list[off] = b;
+    if (kp) list[off] = b;
     if (drop) ready[doff] = b;
     __syncthreads();
     if (threadIdx.x == 0) {
@@ -544,7 +550,7 @@ size_t pcg_ws(int ndim, int n, int nq, int batch) {
   const size_t vec = align_up((size_t)N * batch * sizeof(T), 256);
   const size_t scal = align_up((size_t)batch * PS * sizeof(T), 256);
   const size_t small = align_up((size_t)batch * sizeof(T), 256) +
-                       4 * align_up((size_t)batch * sizeof(int), 256) + 256 +
+                       5 * align_up((size_t)batch * sizeof(int), 256) + 256 +
                        align_up((size_t)batch * sizeof(double), 256) +
                        align_up((size_t)4 * batch * sizeof(unsigned), 256);
   size_t inner = varcoef_ws(ndim, n, nq, batch, sizeof(T));
@@ -600,6 +606,8 @@ int PcgCtx<T>::init(const PcgProblem<T>& problem, T* x_, void* work, size_t work
   inner_it = (int*)sm;
   sm += ib;
   ready = (int*)sm;
+  sm += ib;
+  keep = (int*)sm;
   sm += ib;
   slots = (unsigned*)sm;
   sm += align_up((size_t)4 * batch * sizeof(unsigned), 256);
@@ -742,10 +750,10 @@ int PcgCtx<T>::iteration(int it) {
   if (nb_new != nb_rz) return JFG_ERR_UNSUPPORTED;  // same launch signature: cannot differ
   k_update_xp<T><<<ugrid, 256, 0, st>>>(x, p, z, N, pq_part, rz_part[cur], rz_part[prev], rz0,
                                         tolv, iters, alist, nactive, batch, slot_p, nb_pq, nb_rz,
-                                        inner_it);
+                                        inner_it, maxit, keep);
   JFG_LAUNCHED();
-  k_compact<T><<<1, CMP_T, 0, st>>>(rz_part[cur], rz0, tolv, alist, nactive, batch, 0, nb_rz,
-                                    inner_it, maxit, track_ready ? ready : nullptr, nready);
+  k_compact<<<1, CMP_T, 0, st>>>(keep, alist, nactive, batch, track_ready ? ready : nullptr,
+                                 nready);
   JFG_LAUNCHED();
   return JFG_OK;
 }

@@ -73,6 +73,7 @@ struct PcgCtx {
   T *pq_part = nullptr, *rz_part[2] = {nullptr, nullptr}, *rz0 = nullptr;
   int *iters = nullptr, *alist = nullptr, *nactive = nullptr, *nready = nullptr;
   int *inner_it = nullptr, *ready = nullptr;
+  int* keep = nullptr;  // per problem: stays active after this iteration (k_update_xp)
   double* tolv = nullptr;   // per-problem tolerance (device)
   unsigned* slots = nullptr;
   void* inner = nullptr;
