@@ -44,9 +44,20 @@ __global__ void __launch_bounds__(MM_Q * MAXC) k_modemix_fwd(
 #pragma unroll
   for (int ci = 0; ci < MAXC; ++ci) r[ci] = (active && ci < C) ? __ldg(Rrow + ci) : 0.f;
   const int nload = MM_Q * C;
+  // each thread's element of the next PF samples is loaded ahead, so the
+  // loop over samples does not wait on a load every iteration
+  constexpr int PF = 4;
+  float nxt[PF];
+#pragma unroll
+  for (int u = 0; u < PF; ++u)
+    nxt[u] = (t < nload && b0 + u < b1) ? x[((long long)(b0 + u) * nq + q0) * C + t] : 0.f;
   for (int b = b0; b < b1; ++b) {
     float (*xb)[MM_LD] = xs[b & 1];
-    if (t < nload) xb[t / C][t % C] = x[((long long)b * nq + q0) * C + t];
+    if (t < nload) xb[t / C][t % C] = nxt[0];
+#pragma unroll
+    for (int u = 0; u + 1 < PF; ++u) nxt[u] = nxt[u + 1];
+    nxt[PF - 1] =
+        (t < nload && b + PF < b1) ? x[((long long)(b + PF) * nq + q0) * C + t] : 0.f;
     __syncthreads();
     if (active) {
       const float4* xv = reinterpret_cast<const float4*>(xb[ql]);
