@@ -66,6 +66,15 @@ constexpr int KB = 32;                     // FP32 elements per K block (128 B)
 constexpr int MT_MAX = 128;                // operator rows per tile (MMA N)
 constexpr int NTHREADS = 448;  // 14 warps
 constexpr uint32_t XBYTES = TILE_P * KB * 4;  // 16 KB
+// K elements per block of the 16-bit operator paths (split BF16, scaled split
+// FP16): 64 (two 128-byte FP32 input rows, one 128-byte operator row; 64 KB
+// stages, three of them), except for the field-multiply epilogue: its two
+// field boxes per epilogue warp leave room for only two such stages, and with
+// 32-element blocks (one input row, a 64-byte operator row under the 64-byte
+// swizzle; 32 KB stages) five fit.  Measured on the variable-coefficient
+// passes: the field pass 74.5 -> 66.3 us with 32, every other pass slower
+// with 32 (more handshakes per unit of work).
+__host__ __device__ constexpr int b16_ke(int epi) { return epi == JFG_EPI_MUL_FIELD ? 32 : 64; }
 constexpr unsigned long long WAIT_NS = 2000000000ull;  // 2 s budget per wait
 
 constexpr int GMAX = 40;  // groups per launch of the grouped kernel
@@ -221,6 +230,17 @@ __device__ __forceinline__ uint64_t sdesc(uint32_t saddr) {
   return d;
 }
 
+// The same for 64-byte rows (64-byte swizzle): 8-row groups 512 B apart.
+__device__ __forceinline__ uint64_t sdesc64(uint32_t saddr) {
+  uint64_t d = 0;
+  d |= (uint64_t)((saddr & 0x3FFFFu) >> 4);  // start address
+  d |= (uint64_t)1 << 16;                     // leading byte offset (unused, swizzled K-major)
+  d |= (uint64_t)(512 >> 4) << 32;            // stride byte offset
+  d |= (uint64_t)1 << 46;                     // descriptor version
+  d |= (uint64_t)4 << 61;                     // SWIZZLE_64B
+  return d;
+}
+
 // Instruction descriptor: kind::tf32, D = F32, A = B = TF32, both K-major.
 __host__ __device__ constexpr uint32_t idesc_tf32(int M, int N) {
   return (1u << 4) | (2u << 7) | (2u << 10) | ((uint32_t)(N >> 3) << 17) |
@@ -373,8 +393,11 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   constexpr bool H16 = PREC == 2;
   // K elements per block: 32 TF32 (one 128-byte row) or 64 BF16 (one 128-byte
   // operator row; the FP32 input block then takes two TMA boxes)
-  constexpr int KE = B16 ? 64 : KB;
-  constexpr uint32_t XB = B16 ? 2 * XBYTES : XBYTES;
+  constexpr int KE = B16 ? b16_ke(EPI) : KB;
+  constexpr uint32_t XB = B16 ? (uint32_t)(KE / KB) * XBYTES : XBYTES;
+  constexpr uint32_t OROW = B16 ? 2u * KE : 128u;  // bytes per operator row of a stage
+  // TMEM columns per stage of operand A (hi then lo)
+  constexpr uint32_t A_SLOT = B16 ? (uint32_t)KE : 2u * KB;
   extern __shared__ uint8_t smem_raw[];
   __shared__ long long tb[G + 1];
   __shared__ int nbs[G];
@@ -384,7 +407,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   const int S = L.stages;
   const bool ta = B16 || L.tmem_a != 0;
   const bool res = B16 && L.op_res != 0;
-  const uint32_t omax = (uint32_t)L.mt_max * 128;  // Mtile rows of 128 B (hi or lo)
+  const uint32_t omax = (uint32_t)L.mt_max * OROW;  // Mtile operator rows (hi or lo)
   const uint32_t xbuf = ta ? XB : 2 * XBYTES;  // X block (+ its lo part when in SMEM)
   const uint32_t stage_bytes = res ? xbuf : xbuf + 2 * omax;
   const uint32_t acc_stride = ta ? ACC_STRIDE_TA : 256;
@@ -523,7 +546,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       if (res) {
         // the operator chunk of this CTA's slot, once: every K block, hi and lo
         const TcGroup& q = L.g[0];
-        const uint32_t obytes = (uint32_t)q.Mtile * 128;
+        const uint32_t obytes = (uint32_t)q.Mtile * OROW;
         const int os = q.seg_op_map ? r_s : 0;
         mbar_expect_tx(opfull, (uint32_t)r_nkb * 2 * obytes);
         for (int kb = 0; kb < r_nkb; ++kb) {
@@ -537,7 +560,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         const int cs = q.seg_in_map ? s : 0;
         const int cb = (q.bat_in_map && b > 0) ? b : 0;
         const int os = q.seg_op_map ? s : 0;
-        const uint32_t obytes = (uint32_t)q.Mtile * 128;
+        const uint32_t obytes = (uint32_t)q.Mtile * OROW;
         const int nkb = nkb_of(gi);
         for (int kb = 0; kb < nkb; ++kb, ++g) {
           const int st = (int)(g % S);
@@ -548,7 +571,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           }
           mbar_expect_tx(&full[st], res ? XB : XB + 2 * obytes);
           tma_load_4d(Xh(st), &L.maps[gi][0], &full[st], kb * KE, pt * TILE_P, cs, cb);
-          if (B16)
+          if (B16 && KE > KB)
             tma_load_4d(Xh(st) + XBYTES, &L.maps[gi][0], &full[st], kb * KE + KB,
                         pt * TILE_P, cs, cb);
           if (!res) {
@@ -596,16 +619,19 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           const uint32_t oh = smem_u32(res ? OhR(kb) : Oh(st));
           const uint32_t ol = smem_u32(res ? OlR(kb) : Ol(st));
           if (B16) {
-            const uint32_t ah = tmem + (uint32_t)(A_COL0 + 64 * st), al = ah + 32;
+            const uint32_t ah = tmem + (uint32_t)A_COL0 + A_SLOT * (uint32_t)st,
+                           al = ah + A_SLOT / 2;
 #pragma unroll
-            for (int kk = 0; kk < 4; ++kk) {
+            for (int kk = 0; kk < KE / 16; ++kk) {
               const uint32_t off = kk * 32;  // 16 BF16 = 32 B of B per MMA, 8 A columns
-              mma_b16_ta(acc, ah + 8 * kk, sdesc(oh + off), idesc, (kb | kk) ? 1u : 0u);
-              mma_b16_ta(acc, ah + 8 * kk, sdesc(ol + off), idesc, 1u);
-              mma_b16_ta(acc, al + 8 * kk, sdesc(oh + off), idesc, 1u);
+              const uint64_t bh = KE == 64 ? sdesc(oh + off) : sdesc64(oh + off);
+              const uint64_t bl = KE == 64 ? sdesc(ol + off) : sdesc64(ol + off);
+              mma_b16_ta(acc, ah + 8 * kk, bh, idesc, (kb | kk) ? 1u : 0u);
+              mma_b16_ta(acc, ah + 8 * kk, bl, idesc, 1u);
+              mma_b16_ta(acc, al + 8 * kk, bh, idesc, 1u);
             }
           } else if (ta) {
-            const uint32_t ah = tmem + (uint32_t)(A_COL0 + 64 * st), al = ah + 32;
+            const uint32_t ah = tmem + (uint32_t)A_COL0 + A_SLOT * (uint32_t)st, al = ah + 32;
 #pragma unroll
             for (int kk = 0; kk < KB / 8; ++kk) {
               const uint32_t off = kk * 32;  // 8 TF32 = 32 B of B per MMA, 8 A columns
@@ -659,9 +685,9 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           // 32-element half at a time (16 hi and 16 lo columns) keeps the
           // live registers low
           const uint32_t tbase = tmem + ((uint32_t)(32 * (warp & 3)) << 16) +
-                                 (uint32_t)(A_COL0 + 64 * st);
+                                 (uint32_t)A_COL0 + A_SLOT * (uint32_t)st;
 #pragma unroll
-          for (int half = 0; half < 2; ++half) {
+          for (int half = 0; half < KE / KB; ++half) {
             uint32_t h[16], l[16];
             const float4* xr = (const float4*)(Xh(st) + half * XBYTES + row * 128);
 #pragma unroll
@@ -676,7 +702,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
               l[2 * c + 1] = pack_f16x2(a2 - f1.x, a3 - f1.y);
             }
             tmem_st16(tbase + 16 * half, h);
-            tmem_st16(tbase + 32 + 16 * half, l);
+            tmem_st16(tbase + A_SLOT / 2 + 16 * half, l);
           }
           asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
           asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -685,9 +711,9 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           // packed in pairs (lower k in the lower half) into 32 TMEM columns
           // each, one 32-element half (16 + 16 columns) at a time
           const uint32_t tbase = tmem + ((uint32_t)(32 * (warp & 3)) << 16) +
-                                 (uint32_t)(A_COL0 + 64 * st);
+                                 (uint32_t)A_COL0 + A_SLOT * (uint32_t)st;
 #pragma unroll
-          for (int half = 0; half < 2; ++half) {
+          for (int half = 0; half < KE / KB; ++half) {
             uint32_t h[16], l[16];
             const float4* xr = (const float4*)(Xh(st) + half * XBYTES + row * 128);
 #pragma unroll
@@ -702,7 +728,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
                                          v.w - __uint_as_float(h1 & 0xFFFF0000u));
             }
             tmem_st16(tbase + 16 * half, h);
-            tmem_st16(tbase + 32 + 16 * half, l);
+            tmem_st16(tbase + A_SLOT / 2 + 16 * half, l);
           }
           asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
           asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -721,7 +747,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             }
           }
           const uint32_t tbase = tmem + ((uint32_t)(32 * (warp & 3)) << 16) +
-                                 (uint32_t)(A_COL0 + 64 * st);
+                                 (uint32_t)A_COL0 + A_SLOT * (uint32_t)st;
           tmem_st32(tbase, h);
           tmem_st32(tbase + 32, l);
           asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
@@ -993,14 +1019,14 @@ EncodeTiledFn encode_fn() {
 
 int make_map(CUtensorMap* map, const void* base, int rank, const cuuint64_t* dims,
              const cuuint64_t* strides_bytes, const cuuint32_t* box,
-             CUtensorMapDataType dt = CU_TENSOR_MAP_DATA_TYPE_FLOAT32) {
+             CUtensorMapDataType dt = CU_TENSOR_MAP_DATA_TYPE_FLOAT32,
+             CUtensorMapSwizzle sw = CU_TENSOR_MAP_SWIZZLE_128B) {
   EncodeTiledFn fn = encode_fn();
   if (!fn) return JFG_ERR_UNSUPPORTED;
   cuuint32_t estr[5] = {1, 1, 1, 1, 1};
   CUresult r = fn(map, dt, (cuuint32_t)rank, (void*)base, dims,
-                  strides_bytes, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE,
-                  CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
-                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+                  strides_bytes, box, estr, CU_TENSOR_MAP_INTERLEAVE_NONE, sw,
+                  CU_TENSOR_MAP_L2_PROMOTION_L2_256B, CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
   return r == CUDA_SUCCESS ? JFG_OK : JFG_ERR_ARG;
 }
 
@@ -1078,12 +1104,16 @@ int fill_group(const jfg_contract_desc& d, const void* op_hi, const void* op_lo,
                           (cuuint64_t)(q.seg_op_map ? d.nseg : 1)};
     cuuint64_t str[2] = {(cuuint64_t)d.op_ld * eb,
                          (cuuint64_t)(q.seg_op_map ? d.op_seg : d.op_ld * d.M) * eb};
-    cuuint32_t box[3] = {(cuuint32_t)(128 / eb), (cuuint32_t)q.Mtile, 1};
+    // one operator row of a stage per box row: 128 B (TF32) or 64 B (16-bit)
+    const int orow = b16 ? 2 * b16_ke(d.epilogue) : 128;
+    cuuint32_t box[3] = {(cuuint32_t)(orow / eb), (cuuint32_t)q.Mtile, 1};
     const CUtensorMapDataType dt = prec == 2   ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16
                                    : prec == 1 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16
                                                : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
-    JFG_TRY(make_map(&maps[1], op_hi, 3, dims, str, box, dt));
-    JFG_TRY(make_map(&maps[2], op_lo, 3, dims, str, box, dt));
+    const CUtensorMapSwizzle sw =
+        orow == 64 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_128B;
+    JFG_TRY(make_map(&maps[1], op_hi, 3, dims, str, box, dt, sw));
+    JFG_TRY(make_map(&maps[2], op_lo, 3, dims, str, box, dt, sw));
   }
   // output through TMA stores when its rows are 16-byte aligned and every
   // 32-column group of a tile is full (else plain coalesced stores)
@@ -1203,14 +1233,18 @@ int launch_groups(int ng, const jfg_contract_desc* const* ds, const void* const*
     const TcGroup& q = L.g[0];
     const int mch = (q.d.M + q.Mtile - 1) / q.Mtile;
     nslots = q.d.nseg * mch;
-    res_bytes = (size_t)((q.d.K + 63) / 64) * 2 * (size_t)q.Mtile * 128;
+    res_bytes = (size_t)((q.d.K + b16_ke(epi) - 1) / b16_ke(epi)) * 2 * (size_t)q.Mtile * 2 *
+                b16_ke(epi);
     const long long per_slot = (long long)((q.d.P + TILE_P - 1) / TILE_P) * q.d.batch;
     const size_t room = (size_t)SMEM_MAX - 1024 - 64 * 8;
     res = nslots <= ctas && (sched == 2 || per_slot * nslots >= 2LL * ctas) &&
-          res_bytes + 2 * (2 * (size_t)XBYTES) <= room;
+          res_bytes + 2 * (size_t)(b16_ke(epi) / KB) * XBYTES <= room;
   }
-  const size_t stage = res ? 2 * (size_t)XBYTES
-                           : (b16 ? 2 : ta ? 1 : 2) * (size_t)XBYTES + 2 * (size_t)mt_max * 128;
+  const int ke16 = b16_ke(epi);
+  const size_t xstage = (size_t)(ke16 / KB) * XBYTES;  // FP32 input of a 16-bit stage
+  const size_t stage = res ? xstage
+                           : b16 ? xstage + 2 * (size_t)mt_max * 2 * ke16
+                                 : (ta ? 1 : 2) * (size_t)XBYTES + 2 * (size_t)mt_max * 128;
   // field-multiply launches stage both of a warp's boxes of a tile (the
   // field of each fetched ahead), when two pipeline stages still fit
   int nbuf = ostage ? 1 : 0;
@@ -1228,7 +1262,9 @@ int launch_groups(int ng, const jfg_contract_desc* const* ds, const void* const*
     L.g[0].tma_store = 0;
     stages = (int)(((size_t)SMEM_MAX - fixed) / stage);
   }
-  if (stages > (ta ? 4 : 6)) stages = ta ? 4 : 6;
+  // operand A in TMEM: 256 accumulator columns plus one A slot per stage
+  const int amax = ta ? 256 / (b16 ? ke16 : 2 * KB) : 6;
+  if (stages > amax) stages = amax;
   if (cfg.stages >= 2 && cfg.stages < stages) stages = cfg.stages;
   if (stages < 2) return JFG_ERR_UNSUPPORTED;
   L.stages = stages;
@@ -1349,8 +1385,9 @@ int tune_single(int prec, const jfg_contract_desc& d, const void* oh, const void
             if ((prec != 0 && ta == 0) || (prec == 0 && sched == 2)) continue;
             // the operator-stationary schedule only where the chunk fits beside
             // two input stages (else the launch would stream anyway)
-            if (sched == 2 && (size_t)((d.K + 63) / 64) * 2 * (mt ? mt : 128) * 128 +
-                                      4 * (size_t)XBYTES >
+            if (sched == 2 && (size_t)((d.K + b16_ke(d.epilogue) - 1) / b16_ke(d.epilogue)) *
+                                          2 * (mt ? mt : 128) * 2 * b16_ke(d.epilogue) +
+                                      2 * (size_t)(b16_ke(d.epilogue) / KB) * XBYTES >
                                   (size_t)SMEM_MAX - 1024 - 64 * 8)
               continue;
             jfg_tc_config c = tc_default_config();
