@@ -9,7 +9,8 @@ N(0,1) prod_i (1+k_i)^-2), solved by ``MixedVarCoefSolver``.  Fields are moved
 to the network's Legendre-Gauss grid by spectral truncation; the forcing and
 the solution are scaled by the forcing's RMS (the problem is linear in f).
 
-    python -m jaxfun_gb300.sno.train --train 20000 --test 1000 --epochs 8 --out ckpt.npz
+    python -m jaxfun_gb300.sno.train --train 20000 --test 1000 --epochs 80 --out ckpt.npz
+      (the committed 2-D weights: 80 epochs, test relative L2 0.42 %)
     python -m jaxfun_gb300.sno.train --ndim 3 --N 128 --n 32 --modes 16 --width 32 ...
 """
 
