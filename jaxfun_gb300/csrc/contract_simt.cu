@@ -96,7 +96,7 @@ __global__ void __launch_bounds__(NT)
   T* outS = out + (long long)b * d.out_batch + (long long)s * d.out_seg;
   const T alpha = T(d.alpha);
   const T beta = T(d.beta);
-  if (EPI == EPI_EXP_WEIGHT) {
+  if constexpr (EPI == EPI_EXP_WEIGHT) {
     // kappa = exp(scale (v - shift)), kw = kappa wm[m] wp[p] (FP64, optional
     // FP32 copy at the field strides); kappa itself into aux when given
     const T sh = d.c0 ? ((const T*)d.c0)[b] : T(0);
@@ -120,9 +120,7 @@ __global__ void __launch_bounds__(NT)
         if (a32) a32[(long long)m * d.field_ld + p] = (float)v;
       }
     }
-    return;
-  }
-  if (EPI == EPI_MOMENTS) {
+  } else if constexpr (EPI == EPI_MOMENTS) {
     // out = alpha v, and this tile's count, mean and sum of squared
     // deviations (two passes over the registers) at part[b][tile][3]
     __shared__ double red[NT / 32];
@@ -165,34 +163,34 @@ __global__ void __launch_bounds__(NT)
       pt[1] = mu;
       pt[2] = m2;
     }
-    return;
-  }
+  } else {
 #pragma unroll
-  for (int i = 0; i < R; ++i) {
-    const int m = m0 + ty * R + i;
-    if (m >= d.M) continue;
-    T denom_m = T(0), c0 = T(0), c1 = T(1);
-    if (EPI == JFG_EPI_DIV_EIG) {
-      denom_m = ((const T*)d.lam_m)[m];
-      c0 = d.c0 ? ((const T*)d.c0)[b] : T(0);
-      c1 = d.c1 ? ((const T*)d.c1)[b] : T(1);
-    }
-#pragma unroll
-    for (int j = 0; j < R; ++j) {
-      const int p = p0 + tx * R + j;
-      if (p >= d.P) continue;
-      T v = acc[i][j];
-      if (EPI == JFG_EPI_MUL_FIELD) {
-        const T* f = (const T*)d.field;
-        v *= f[(long long)b * d.field_batch + (long long)s * d.field_seg +
-               (long long)m * d.field_ld + p];
-      } else if (EPI == JFG_EPI_DIV_EIG) {
-        v = v / (c0 + c1 * (denom_m + ((const T*)d.lam_p)[p]));
+    for (int i = 0; i < R; ++i) {
+      const int m = m0 + ty * R + i;
+      if (m >= d.M) continue;
+      T denom_m = T(0), c0 = T(0), c1 = T(1);
+      if (EPI == JFG_EPI_DIV_EIG) {
+        denom_m = ((const T*)d.lam_m)[m];
+        c0 = d.c0 ? ((const T*)d.c0)[b] : T(0);
+        c1 = d.c1 ? ((const T*)d.c1)[b] : T(1);
       }
-      T* o = outS + (long long)m * d.out_ld + p;
-      v = alpha * v;
-      if (beta != T(0)) v += beta * *o;
-      *o = v;
+#pragma unroll
+      for (int j = 0; j < R; ++j) {
+        const int p = p0 + tx * R + j;
+        if (p >= d.P) continue;
+        T v = acc[i][j];
+        if (EPI == JFG_EPI_MUL_FIELD) {
+          const T* f = (const T*)d.field;
+          v *= f[(long long)b * d.field_batch + (long long)s * d.field_seg +
+                 (long long)m * d.field_ld + p];
+        } else if (EPI == JFG_EPI_DIV_EIG) {
+          v = v / (c0 + c1 * (denom_m + ((const T*)d.lam_p)[p]));
+        }
+        T* o = outS + (long long)m * d.out_ld + p;
+        v = alpha * v;
+        if (beta != T(0)) v += beta * *o;
+        *o = v;
+      }
     }
   }
 }

@@ -427,13 +427,14 @@ __global__ void k_field_moments(long long per, const double* __restrict__ g,
 }
 
 // kappa = exp(scale[b] (g - shift[b])) and kw = kappa * prod_ax w[i_ax] (FP64,
-// plus an FP32 copy) in one pass over the grid
+// plus an FP32 copy) in one pass over the grid.  g may be kw or kappa (in
+// place: each element is read by the thread that then overwrites it), so
+// those three are not restrict-qualified.
 __global__ void k_exp_weighted_field(int ndim, int nq, long long per, long long total,
-                                     const double* __restrict__ g,
-                                     const double* __restrict__ scale,
+                                     const double* g, const double* __restrict__ scale,
                                      const double* __restrict__ shift,
-                                     const double* __restrict__ w, double* __restrict__ kappa,
-                                     double* __restrict__ kw, float* __restrict__ kw32) {
+                                     const double* __restrict__ w, double* kappa, double* kw,
+                                     float* __restrict__ kw32) {
   for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < total;
        i += (long long)gridDim.x * blockDim.x) {
     const long long b = i / per;
