@@ -57,13 +57,14 @@ __global__ void k_pad_scale(int ndim, int n, int nq, long long Npad, long long N
                      : (int)blockIdx.y;
   if (b < 0) return;
   const double sc = scale[b];
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < Npad;
-       i += (long long)gridDim.x * blockDim.x) {
-    long long r = i, src = 0, mul = 1;
+  // per-problem indices fit 32 bits (the launchers check Npad < 2^31): the
+  // digit loop divides in 32-bit arithmetic
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < (int)Npad; i += gridDim.x * blockDim.x) {
+    int r = i, src = 0, mul = 1;
     bool inside = true;
     for (int a = 0; a < ndim; ++a) {
-      const int c = (int)(r % nq);
-      r /= nq;
+      const int q = r / nq, c = r - q * nq;
+      r = q;
       if (c >= n) inside = false;
       src += c * mul;
       mul *= n;
@@ -83,12 +84,11 @@ __global__ void k_unpad_axpy(int ndim, int n, int nq, long long Npad, long long 
   if (b < 0) return;
   const double sc = sign * s[b];
   if (sc == 0.0) return;
-  for (long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x; i < Nun;
-       i += (long long)gridDim.x * blockDim.x) {
-    long long r = i, src = 0, mul = 1;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < (int)Nun; i += gridDim.x * blockDim.x) {
+    int r = i, src = 0, mul = 1;
     for (int a = 0; a < ndim; ++a) {
-      const int c = (int)(r % n);
-      r /= n;
+      const int q = r / n, c = r - q * n;
+      r = q;
       src += c * mul;
       mul *= nq;
     }
@@ -402,6 +402,7 @@ int launch_pad_scale(int ndim, int n, int nq, int batch, const double* in, const
                      float* out, cudaStream_t st) {
   long long Nun = 1, Npad = 1;
   for (int i = 0; i < ndim; ++i) Nun *= n, Npad *= nq;
+  if (Npad > 2147483647LL) return JFG_ERR_ARG;
   k_pad_scale<<<dim3(blocks_for(Npad, 256), batch), 256, 0, st>>>(ndim, n, nq, Npad, Nun, in,
                                                                     scale, out);
   JFG_LAUNCHED();
@@ -412,6 +413,7 @@ int launch_unpad_axpy(int ndim, int n, int nq, int batch, const float* d, const 
                       double* x, double sign, cudaStream_t st) {
   long long Nun = 1, Npad = 1;
   for (int i = 0; i < ndim; ++i) Nun *= n, Npad *= nq;
+  if (Npad > 2147483647LL) return JFG_ERR_ARG;
   k_unpad_axpy<<<dim3(blocks_for(Nun, 256), batch), 256, 0, st>>>(ndim, n, nq, Npad, Nun, d, s,
                                                                     x, sign);
   JFG_LAUNCHED();
@@ -534,6 +536,7 @@ extern "C" int jfg_pcg_varcoef_mixed_guess(const jfg_mixed_plan* plan, const dou
     return JFG_ERR_ARG;
   const int ndim = P.ndim, n = P.n, nq = P.nq, batch = P.batch;
   const MixedLayout Lo = layout(ndim, n, nq, batch);
+  if (Lo.Npad > 2147483647LL) return JFG_ERR_ARG;  // per-problem indices are 32-bit
   if (!work || work_bytes < Lo.total) return JFG_ERR_WORKSPACE;
   cudaStream_t st = (cudaStream_t)stream;
   char* w = (char*)work;
@@ -679,7 +682,9 @@ extern "C" int jfg_pcg_varcoef_mixed_guess(const jfg_mixed_plan* plan, const dou
     k_sub_from64_list<<<ugrid, 256, 0, st>>>(rhs, r64, Lo.Nun, rdf, ctrl + 1, batch);
     JFG_LAUNCHED();
     // updated residuals r -= ||r|| A32 d (the apply's scratch is the inner
-    // solve's pass scratch, free between chunks)
+    // solve's pass scratch, free between chunks).  FP32 on the CUDA cores:
+    // the scaled split-FP16 tensor-core apply here measured a larger answer
+    // error (1.6e-10 against 1e-10 at inner tolerance 1e-5).
     if (fp32_ok) {
       JFG_TRY(varcoef_apply<float>(Engine::F32, ndim, nq, nq, batch,
                                    OpRef<float>{P.ops32, nullptr}, P.kw32, d32, r32, c.inner,
