@@ -167,16 +167,23 @@ class SNO:
                                               _lib.stream_handle()), "colsum")
 
     # ------------------------------------------------------------------ passes
-    def set_input(self, x_cl: torch.Tensor):
-        """x_cl: (Bt*P, 16) BF16 input channels (rows = (sample, pixel))."""
+    def set_input(self, x_cl: torch.Tensor, train: bool = True):
+        """x_cl: (Bt*P, 16) BF16 input channels (rows = (sample, pixel)).  The
+        channel-first copy is kept only for training (the lift's weight
+        gradient)."""
         Bt = x_cl.shape[0] // self.P
         self._ensure(Bt)
         self.X_cl.copy_(x_cl)
-        self.X_cf.copy_(x_cl.t())
+        if train:
+            self.X_cf.copy_(x_cl.t())
         return Bt
 
-    def forward(self, Bt: int) -> torch.Tensor:
-        """Forward pass on self.X_cl / X_cf; returns pred (Bt*P, 16) FP32 (col 0)."""
+    def forward(self, Bt: int, train: bool = True) -> torch.Tensor:
+        """Forward pass on self.X_cl / X_cf; returns pred (Bt*P, 16) FP32 (col 0).
+        With train=False (inference) the GEMM epilogues skip what only the
+        backward pass reads: the FP32 pre-activations and the channel-first
+        copies of the last spectral layer's output and of the projection's
+        hidden layer."""
         C_, P, NM, L = self.cfg.width, self.P, self.NM, self.cfg.layers
         R = Bt * P
         L_ = _lib.lib()
@@ -198,11 +205,13 @@ class SNO:
             last = l == L - 1
             self._gemm(self.U_cl[l], self.wbf[f"W{l}"], R, C_, C_, C_, C_,
                        add=self.S, ld_add=C_, bias=self.params[f"b{l}"],
-                       act=0 if last else 1, pre=None if last else self.Zpre[l], ld_pre=C_,
-                       dbf=self.U_cl[l + 1], ld_dbf=C_, dtbf=self.U_cf[l + 1], ld_dtbf=R)
+                       act=0 if last else 1,
+                       pre=None if (last or not train) else self.Zpre[l], ld_pre=C_,
+                       dbf=self.U_cl[l + 1], ld_dbf=C_,
+                       dtbf=self.U_cf[l + 1] if (train or not last) else None, ld_dtbf=R)
         self._gemm(self.U_cl[L], self.wbf["W_p1"], R, C_, C_, C_, C_, bias=self.params["b_p1"],
-                   act=1, pre=self.Q1pre, ld_pre=C_, dbf=self.Q1_cl, ld_dbf=C_,
-                   dtbf=self.Q1_cf, ld_dtbf=R)
+                   act=1, pre=self.Q1pre if train else None, ld_pre=C_, dbf=self.Q1_cl,
+                   ld_dbf=C_, dtbf=self.Q1_cf if train else None, ld_dtbf=R)
         self._gemm(self.Q1_cl, self.wbf["W_p2"], R, COUT, C_, C_, C_, bias=self.params["b_p2"],
                    d32=self.pred, ld_d32=COUT)
         return self.pred

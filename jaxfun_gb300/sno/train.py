@@ -201,8 +201,8 @@ def predict(model: SNO, X: torch.Tensor, Bt: int | None = None) -> torch.Tensor:
     out = torch.empty((nsamp, P), dtype=torch.float32, device="cuda")
     for i in range(0, nsamp, Bt):
         B = min(Bt, nsamp - i)
-        model.set_input(X[i * P:(i + B) * P])
-        pred = model.forward(B)
+        model.set_input(X[i * P:(i + B) * P], train=False)
+        pred = model.forward(B, train=False)
         out[i:i + B] = pred[:, 0].reshape(B, P)
     n = model.cfg.n
     return out.reshape((nsamp,) + (n,) * model.cfg.ndim)

@@ -179,8 +179,9 @@ def test_flat_schedule_outer_budget_exhausted():
     assert e.value.status == _lib.JFG_ERR_NOT_CONVERGED
 
 
+@pytest.mark.parametrize("ndim,N,batch", [(2, 48, 5), (3, 16, 3)])
 @pytest.mark.parametrize("sched", ["sync", "flat"])
-def test_whole_solve_graph_matches_host_loop(sched):
+def test_whole_solve_graph_matches_host_loop(sched, ndim, N, batch):
     """On a stream that can be captured the whole refinement loop is one CUDA
     graph (a conditional WHILE node around an IF/ELSE choice of outer step or
     inner chunk).  It gives bit-identical answers and iteration counts to the
@@ -192,14 +193,13 @@ def test_whole_solve_graph_matches_host_loop(sched):
 
     from jaxfun_gb300 import _lib
 
-    N, batch = 48, 5
     V = FunctionSpace(N, Legendre, bcs=DIRICHLET)
-    T = TensorProduct(V, V)
-    rng = np.random.default_rng(29)
-    kap = np.exp(rng.standard_normal((batch, N, N)))
+    T = TensorProduct(*([V] * ndim))
+    rng = np.random.default_rng(29 + ndim)
+    kap = np.exp(rng.standard_normal((batch,) + (N,) * ndim))
     A = VarCoefMatrix(T, kap)
     S = MixedVarCoefSolver(A, schedule=sched)
-    bs = [rng.standard_normal((batch, N - 2, N - 2)) for _ in range(2)]
+    bs = [rng.standard_normal((batch,) + (N - 2,) * ndim) for _ in range(2)]
     for b in bs:
         b[2] = 0.0
     x0 = 1e-3 * rng.standard_normal(bs[0].shape)
