@@ -571,16 +571,18 @@ typedef struct {
   const uint16_t* E_lo16;
   const uint16_t* W_hi16;
   const uint16_t* W_lo16;
-  int apply_f16;         /* 1 (2-D only): the inner operator passes run as scaled
-                            split FP16 (jfg_split_f16_rows_host of the packed padded
+  int apply_f16;         /* 1 (nq % 8 == 0): the inner operator passes run as scaled
+                            split FP16 (jfg_split_f16_rows_nd_host of the packed padded
                             operators, rows scaled by powers of two; the inputs of
                             each pass scaled per problem from a recorded max |x|):
                             the accuracy of split TF32 at the BF16 rate.  0: split
                             TF32 (ops_hi, ops_lo)                                   */
   const uint16_t* ops_hi16;  /* FP16 hi of the row-scaled packed padded operators   */
   const uint16_t* ops_lo16;  /* FP16 lo                                             */
-  const float* ops_inv16;    /* inverse row scales, jfg_varcoef_f16_rows(n, nq) of them:
-                                [B;D] 2nq | D, B 2nq | B^T, D^T 2n | [D^T|B^T] n     */
+  const float* ops_inv16;    /* inverse row scales, jfg_varcoef_f16_rows_nd(ndim, nq, nq)
+                                of them; 2-D: [B;D] 2nq | D, B 2nq | B^T, D^T 2n |
+                                [D^T|B^T] n; 3-D: [B;D] 2nq | D, B, B 3nq |
+                                B^T, B^T, D^T 3n                                     */
   int fused_dots;        /* inner PCG scalars from the contraction epilogues instead of
                             separate dot kernels: bit 0 p.Ap = sum kappa w |grad p|^2 in
                             the operator's field pass; bit 1 r.M^-1 r = sum (E r)^2 / D
@@ -603,6 +605,12 @@ size_t jfg_varcoef_f16_rows(int n, int nq);
  * scales (jfg_varcoef_f16_rows(n, nq) floats).  Host arrays. */
 void jfg_split_f16_rows_host(int n, int nq, const double* ops, uint16_t* hi, uint16_t* lo,
                              float* inv);
+/* The same for the 2-D or 3-D packed operators (jfg_varcoef_pack_ops_host(ndim,
+ * n, nq)); jfg_varcoef_f16_rows_nd gives the number of rows (2-D 4 nq + 3 n,
+ * 3-D 5 nq + 3 n). */
+size_t jfg_varcoef_f16_rows_nd(int ndim, int n, int nq);
+void jfg_split_f16_rows_nd_host(int ndim, int n, int nq, const double* ops, uint16_t* hi,
+                                uint16_t* lo, float* inv);
 
 size_t jfg_pcg_mixed_workspace_size(int ndim, int n, int nq, int batch);
 int jfg_pcg_varcoef_mixed(const jfg_mixed_plan* plan, const double* rhs, double* x, int use_x0,

@@ -136,6 +136,8 @@ SIGNATURES = {
     "jfg_varcoef_ops_count": (_sz, [_i, _i, _i]),
     "jfg_varcoef_f16_rows": (_sz, [_i, _i]),
     "jfg_split_f16_rows_host": (None, [_i, _i, _vp, _vp, _vp, _vp]),
+    "jfg_varcoef_f16_rows_nd": (_sz, [_i, _i, _i]),
+    "jfg_split_f16_rows_nd_host": (None, [_i, _i, _i, _vp, _vp, _vp, _vp]),
     "jfg_split_f16_rowscaled_host": (None, [_sz, _sz, _vp, _vp, _vp, _vp]),
     "jfg_contract_tc_f16x3": (_i, [C.POINTER(ContractDesc), _vp, _vp, _vp, C.c_longlong, _vp, _vp,
                                    _vp, _vp, _vp]),

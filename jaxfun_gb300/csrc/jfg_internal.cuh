@@ -69,8 +69,11 @@ enum class Engine { F64, F32, TC, DF, TB, TH };
 // apply's input (slot 0) and the inputs of its passes 2-4 (slots 1-3).
 struct H16Ops {
   const float* op_inv = nullptr;
-  unsigned* slots = nullptr;
+  unsigned* slots = nullptr;  // [H16_SLOTS][batch]: max |x| of each pass's input
 };
+// per-problem max slots of a scaled split-FP16 operator apply (the 3-D one
+// chains six)
+constexpr int H16_SLOTS = 6;
 
 // Fused dot product of a field-multiply or eigenvalue-divide pass: the
 // epilogue writes, per problem b, partials part[b * DOT_NBMAX + i], i < *nb,
@@ -203,6 +206,9 @@ int varcoef_apply(Engine e, int ndim, int n, int nq, int batch, OpRef<T> ops, co
                   const DotOut* dot = nullptr);
 // number of inverse row scales of the 2-D packed operators (TH engine)
 inline long long varcoef_h16_rows(int n, int nq) { return 4LL * nq + 3LL * n; }
+inline long long varcoef_h16_rows_nd(int ndim, int n, int nq) {
+  return ndim == 3 ? 5LL * nq + 3LL * n : varcoef_h16_rows(n, nq);
+}
 
 // Read and clear the device status word of the BF16 GEMM kernel.
 int gemm_status_take(int* status);

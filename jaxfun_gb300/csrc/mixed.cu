@@ -463,8 +463,7 @@ extern "C" int jfg_pcg_mixed_autotune(const jfg_mixed_plan* plan, void* work, si
   if ((P.ndim != 2 && P.ndim != 3) || P.n < 1 || P.nq < P.n || P.batch < 1 || !P.ops_hi ||
       !P.ops_lo || !P.kw32 || !P.E_hi || !P.E_lo || !P.W_hi || !P.W_lo || !P.lam ||
       (P.precond_bf16 && (!P.E_hi16 || !P.E_lo16 || !P.W_hi16 || !P.W_lo16)) ||
-      (P.apply_f16 && (P.ndim != 2 || (P.nq & 7) || !P.ops_hi16 || !P.ops_lo16 ||
-                       !P.ops_inv16)))
+      (P.apply_f16 && ((P.nq & 7) || !P.ops_hi16 || !P.ops_lo16 || !P.ops_inv16)))
     return JFG_ERR_ARG;
   const int ndim = P.ndim, nq = P.nq, batch = P.batch;
   const MixedLayout Lo = layout(ndim, P.n, nq, batch);
@@ -475,7 +474,7 @@ extern "C" int jfg_pcg_mixed_autotune(const jfg_mixed_plan* plan, void* work, si
   float* d32 = (float*)(w + Lo.vec32);
   char* wsin = w + 2 * Lo.vec32 + Lo.ws64;
   unsigned* slots = (unsigned*)wsin;
-  const size_t sb = align_up((size_t)4 * batch * sizeof(unsigned), 256);
+  const size_t sb = align_up((size_t)H16_SLOTS * batch * sizeof(unsigned), 256);
   void* inner = wsin + sb;
   const size_t inner_bytes = Lo.wsin - sb;
   JFG_CUDA_TRY(cudaMemsetAsync(r32, 0, Lo.vec32, st));
@@ -530,8 +529,7 @@ extern "C" int jfg_pcg_varcoef_mixed_guess(const jfg_mixed_plan* plan, const dou
       (P.precond_bf16 != 0 && P.precond_bf16 != 1) ||
       (P.precond_bf16 && (!P.E_hi16 || !P.E_lo16 || !P.W_hi16 || !P.W_lo16)) ||
       (P.apply_f16 != 0 && P.apply_f16 != 1) ||
-      (P.apply_f16 && (P.ndim != 2 || (P.nq & 7) || !P.ops_hi16 || !P.ops_lo16 ||
-                       !P.ops_inv16)) ||
+      (P.apply_f16 && ((P.nq & 7) || !P.ops_hi16 || !P.ops_lo16 || !P.ops_inv16)) ||
       (P.schedule != 0 && P.schedule != 1))
     return JFG_ERR_ARG;
   const int ndim = P.ndim, n = P.n, nq = P.nq, batch = P.batch;

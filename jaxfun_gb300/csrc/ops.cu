@@ -239,8 +239,7 @@ int varcoef_apply(Engine e, int ndim, int n, int nq, int batch, OpRef<T> ops, co
     JFG_TRY(split_pairs_f64((const double*)u, (float2*)bufB, nu, st));
     u1 = bufB;
   }
-  if (e == Engine::TH && (ndim != 2 || !h16 || !h16->op_inv || !h16->slots))
-    return JFG_ERR_ARG;
+  if (e == Engine::TH && (!h16 || !h16->op_inv || !h16->slots)) return JFG_ERR_ARG;
   if (ndim == 2) {
     // 1: T[b][r][j] = sum_l [B;D][r][l] U[b][j][l]            (M=2nq, P=n, K=n)
     jfg_contract_desc d1 = make_desc(batch, 2 * nq, n, n, act);
@@ -323,6 +322,69 @@ int varcoef_apply(Engine e, int ndim, int n, int nq, int batch, OpRef<T> ops, co
   const OpRef<T> BD = ops;                   // [B;D]  (2nq x n)
   const OpRef<T> Q3 = ops.offset(2 * nn);    // D, B, B
   const OpRef<T> Q4 = ops.offset(5 * nn);    // B^T, B^T, D^T
+  if constexpr (std::is_same<T, float>::value) {
+    if (e == Engine::TH) {
+      // Scaled split FP16: the passes below on the FP16 (hi, lo) operators.
+      // Pass t reads its input's max from slot t and records its output's
+      // max in slot t+1; a split output (bufB of passes 2a/2b, H2a and H2b
+      // of pass 5) shares one slot, a bound over all of it.  Inverse row
+      // scales: [B;D] 2nq | D,B,B 3nq | B^T,B^T,D^T 3n.
+      const uint16_t* oh = (const uint16_t*)ops.hi;
+      const uint16_t* ol = (const uint16_t*)ops.lo;
+      const float* inv = h16->op_inv;
+      unsigned* sl = h16->slots;
+      const long long Bs = batch;
+      auto hp = [&](const jfg_contract_desc& d, long long op_off, long long inv_off,
+                    long long inv_seg, const float* in, float* out, int sin, int sout) -> int {
+        return contract_tc_h16(d, oh + op_off, ol + op_off, inv + inv_off, inv_seg, sl + sin * Bs,
+                               sout >= 0 ? sl + sout * Bs : nullptr, in, out, st);
+      };
+      const long long iq3 = 2LL * nq, iq4 = 5LL * nq;  // inverse-scale blocks
+      jfg_contract_desc h1 = make_desc(batch, 2 * nq, (int)n2, n, act);
+      JFG_TRY(hp(h1, 0, 0, 0, u, bufA, 0, 1));
+      jfg_contract_desc h2 = make_desc(batch, 2 * nq, (int)nn, n, act);
+      h2.in_batch = 2 * nq * n2;
+      h2.out_batch = 3 * q2 * n;
+      JFG_TRY(hp(h2, 0, 0, 0, bufA, bufB, 1, 2));
+      jfg_contract_desc h2b = h2;
+      h2b.M = nq;
+      JFG_TRY(hp(h2b, 0, 0, 0, bufA + nq * n2, bufB + 2 * q2 * n, 1, 2));
+      jfg_contract_desc h3 = make_desc(batch, nq, (int)q2, n, act);
+      h3.nseg = 3;
+      h3.op_seg = nn;
+      h3.in_seg = q2 * n;
+      h3.in_batch = 3 * q2 * n;
+      h3.out_seg = q2 * nq;
+      h3.out_batch = 3 * q2 * nq;
+      h3.epilogue = JFG_EPI_MUL_FIELD;
+      h3.field = kw;
+      h3.field_ld = q2;
+      h3.field_seg = 0;
+      h3.field_batch = q2 * nq;
+      JFG_TRY(hp(h3, 2 * nn, iq3, nq, bufB, bufA, 2, 3));
+      jfg_contract_desc h4 = make_desc(batch, n, (int)q2, nq, act);
+      h4.nseg = 3;
+      h4.op_seg = nn;
+      h4.in_seg = q2 * nq;
+      h4.in_batch = 3 * q2 * nq;
+      h4.out_seg = q2 * n;
+      h4.out_batch = 3 * q2 * n;
+      JFG_TRY(hp(h4, 5 * nn, iq4, n, bufA, bufB, 3, 4));
+      float* G2a = bufA;
+      float* G2b = bufA + (size_t)batch * n2 * nq;
+      jfg_contract_desc h5 = make_desc(batch, n, (int)nn, nq, act);
+      h5.in_batch = 3 * q2 * n;
+      JFG_TRY(hp(h5, 5 * nn, iq4, 0, bufB, G2a, 4, 5));
+      JFG_TRY(hp(h5, 7 * nn, iq4 + 2LL * n, 0, bufB + q2 * n, G2b, 4, 5));
+      h5.beta = 1.0;
+      JFG_TRY(hp(h5, 5 * nn, iq4, 0, bufB + 2 * q2 * n, G2b, 4, 5));
+      jfg_contract_desc h6 = make_desc(batch, n, (int)n2, nq, act);
+      JFG_TRY(hp(h6, 7 * nn, iq4 + 2LL * n, 0, G2a, v, 5, -1));
+      h6.beta = 1.0;
+      JFG_TRY(hp(h6, 5 * nn, iq4, 0, G2b, v, 5, -1));
+      return JFG_OK;
+    }
+  }
   // 1: T1[b][(s2,q2)][(i0,i1)] = sum_i2 [B;D] U                 (M=2nq, P=n^2, K=n)
   jfg_contract_desc d1 = make_desc(batch, 2 * nq, (int)n2, n, act);
   JFG_TRY(pass(d1, BD, u1, bufA, dfp, dfp));
@@ -843,6 +905,12 @@ extern "C" size_t jfg_varcoef_f16_rows(int n, int nq) {
   return n < 1 || nq < 1 ? 0 : (size_t)jfg::varcoef_h16_rows(n, nq);
 }
 
+extern "C" size_t jfg_varcoef_f16_rows_nd(int ndim, int n, int nq) {
+  return (ndim != 2 && ndim != 3) || n < 1 || nq < 1
+             ? 0
+             : (size_t)jfg::varcoef_h16_rows_nd(ndim, n, nq);
+}
+
 extern "C" void jfg_split_f16_rowscaled_host(size_t rows, size_t cols, const double* src,
                                               uint16_t* hi, uint16_t* lo, float* inv) {
   for (size_t r = 0; r < rows; ++r) {
@@ -870,6 +938,26 @@ extern "C" void jfg_split_f16_rows_host(int n, int nq, const double* ops, uint16
                             {2 * nn, (size_t)2 * nq, (size_t)n},
                             {4 * nn, (size_t)2 * n, (size_t)nq},
                             {6 * nn, (size_t)n, (size_t)2 * nq}};
+  size_t r_out = 0;
+  for (const auto& bk : blk) {
+    jfg_split_f16_rowscaled_host(bk[1], bk[2], ops + bk[0], hi + bk[0], lo + bk[0],
+                                 inv + r_out);
+    r_out += bk[1];
+  }
+}
+
+extern "C" void jfg_split_f16_rows_nd_host(int ndim, int n, int nq, const double* ops,
+                                           uint16_t* hi, uint16_t* lo, float* inv) {
+  if (ndim != 3) {
+    jfg_split_f16_rows_host(n, nq, ops, hi, lo, inv);
+    return;
+  }
+  const size_t nn = (size_t)n * nq;
+  // 3-D: [B;D] 2nq rows of n, then D,B,B 3nq rows of n, then B^T,B^T,D^T 3n
+  // rows of nq
+  const size_t blk[3][3] = {{0, (size_t)2 * nq, (size_t)n},
+                            {2 * nn, (size_t)3 * nq, (size_t)n},
+                            {5 * nn, (size_t)3 * n, (size_t)nq}};
   size_t r_out = 0;
   for (const auto& bk : blk) {
     jfg_split_f16_rowscaled_host(bk[1], bk[2], ops + bk[0], hi + bk[0], lo + bk[0],

@@ -154,7 +154,7 @@ __device__ __forceinline__ bool al16(const void* ptr) {
 
 // r -= alpha q ; alpha = rz / (p.q) while active (x takes its alpha p in
 // k_update_xp, which reads p anyway)
-// slots (optional, [4][batch]): the scaled split-FP16 apply's max slots of
+// slots (optional, [H16_SLOTS][batch]): the scaled split-FP16 apply's max slots of
 // this problem are cleared here, after the apply read them and before the
 // p update and the next apply's passes record new maxima
 template <typename T>
@@ -172,7 +172,7 @@ __global__ void k_update_r(T* __restrict__ r, const T* __restrict__ q, long long
     s_act = is_active(rz, rz0[b], tolp[b]) ? 1 : 0;
     s_alpha = s_act ? rz / sum_part(pq_part, b, nb_pq) : T(0);
     if (s_act && slots && blockIdx.x == 0)
-      for (int k = 0; k < 4; ++k) slots[(long long)k * batch + b] = 0u;
+      for (int k = 0; k < H16_SLOTS; ++k) slots[(long long)k * batch + b] = 0u;
   }
   __syncthreads();
   if (!s_act) return;
@@ -379,7 +379,7 @@ __global__ void k_restart_scalars(unsigned* __restrict__ slots, int* __restrict_
     const int b = list ? list[j] : j;
     if (b < 0 || b >= batch) continue;
     if (slots)
-      for (int k = 0; k < 4; ++k) slots[(long long)k * batch + b] = 0u;
+      for (int k = 0; k < H16_SLOTS; ++k) slots[(long long)k * batch + b] = 0u;
     if (inner_it) inner_it[b] = 0;
   }
 }
@@ -552,7 +552,7 @@ size_t pcg_ws(int ndim, int n, int nq, int batch) {
   const size_t small = align_up((size_t)batch * sizeof(T), 256) +
                        5 * align_up((size_t)batch * sizeof(int), 256) + 256 +
                        align_up((size_t)batch * sizeof(double), 256) +
-                       align_up((size_t)4 * batch * sizeof(unsigned), 256);
+                       align_up((size_t)H16_SLOTS * batch * sizeof(unsigned), 256);
   size_t inner = varcoef_ws(ndim, n, nq, batch, sizeof(T));
   const size_t f = fd_ws(ndim, n, batch, sizeof(T));
   if (f > inner) inner = f;
@@ -610,13 +610,13 @@ int PcgCtx<T>::init(const PcgProblem<T>& problem, T* x_, void* work, size_t work
   keep = (int*)sm;
   sm += ib;
   slots = (unsigned*)sm;
-  sm += align_up((size_t)4 * batch * sizeof(unsigned), 256);
+  sm += align_up((size_t)H16_SLOTS * batch * sizeof(unsigned), 256);
   inner = sm;
   inner_bytes = work_bytes - (size_t)(sm - w);
   work_ptr = work;
   work_size = work_bytes;
   th = pb.engine == Engine::TH;
-  if (th && (ndim != 2 || !pb.ops_inv)) return JFG_ERR_ARG;
+  if (th && !pb.ops_inv) return JFG_ERR_ARG;
   h16.op_inv = pb.ops_inv;
   h16.slots = th ? slots : nullptr;
   // Fused dots (FP32 tensor-core engines): p.Ap from the operator's field

@@ -47,17 +47,17 @@ def split_bf16(a: np.ndarray) -> tuple[torch.Tensor, torch.Tensor]:
     return (as_device(hi.view(np.int16), torch.int16), as_device(lo.view(np.int16), torch.int16))
 
 
-def split_f16_rows(n: int, nq: int, ops: np.ndarray):
-    """2-D packed operators (FP64) -> FP16 (hi, lo) bit patterns as int16 device
-    tensors, each operator row scaled by a power of two, and the inverse row
-    scales (FP32 device tensor) for the scaled split-FP16 apply."""
+def split_f16_rows(n: int, nq: int, ops: np.ndarray, ndim: int = 2):
+    """2-D or 3-D packed operators (FP64) -> FP16 (hi, lo) bit patterns as int16
+    device tensors, each operator row scaled by a power of two, and the inverse
+    row scales (FP32 device tensor) for the scaled split-FP16 apply."""
     L = _lib.lib()
     a = np.ascontiguousarray(ops, dtype=np.float64)
     hi = np.empty(a.shape, dtype=np.uint16)
     lo = np.empty(a.shape, dtype=np.uint16)
-    inv = np.empty(L.jfg_varcoef_f16_rows(n, nq), dtype=np.float32)
-    L.jfg_split_f16_rows_host(n, nq, a.ctypes.data, hi.ctypes.data, lo.ctypes.data,
-                              inv.ctypes.data)
+    inv = np.empty(L.jfg_varcoef_f16_rows_nd(ndim, n, nq), dtype=np.float32)
+    L.jfg_split_f16_rows_nd_host(ndim, n, nq, a.ctypes.data, hi.ctypes.data, lo.ctypes.data,
+                                 inv.ctypes.data)
     return (as_device(hi.view(np.int16), torch.int16), as_device(lo.view(np.int16), torch.int16),
             as_device(inv, torch.float32))
 
@@ -83,7 +83,7 @@ class MixedVarCoefSolver:
 
     def __init__(self, A: VarCoefMatrix, M: TPMatricesLUFactors | None = None,
                  residual: str = "df64", fp32_updates: bool | None = None,
-                 precond: str = "bf16x3", apply: str = "f16x3", fused_dots: bool = True,
+                 precond: str = "bf16x3", apply: str | None = None, fused_dots: bool = True,
                  schedule: str = "sync"):
         """``residual``: arithmetic of the refinement residual r = b - A x,
         "df64" (double-FP32 on the FP32 units) or "f64" (FP64 FMAs).
@@ -95,10 +95,12 @@ class MixedVarCoefSolver:
         tolerates the BF16 pairs' ~2^-16 error (same iteration counts, ~7 %
         faster at N = 256).  Padded sizes with nq % 8 != 0 use split-TF32 (the
         BF16 rows would not be 16-byte multiples).
-        ``apply``: the inner operator passes as scaled split-"f16x3" (default
-        in 2-D: FP16 hi/lo pairs with power-of-two scales per operator row and
-        per problem, the accuracy of split TF32 at twice its MMA rate) or
-        split-"tf32"; 3-D and nq % 8 != 0 use split-TF32.
+        ``apply``: the inner operator passes as scaled split-"f16x3" (FP16
+        hi/lo pairs with power-of-two scales per operator row and per problem,
+        the accuracy of split TF32 at twice its MMA rate) or split-"tf32".
+        Default: "f16x3" in 2-D, "tf32" in 3-D (at 32 x 128^3 the FP16 passes
+        saved iterations but not time: 37.1 against 37.6 solves/s, and their
+        answer error was 3.2e-11 against 2.4e-12); nq % 8 != 0 uses split-TF32.
         ``fused_dots``: take the inner PCG's p.Ap and r.M^-1 r from the
         contraction epilogues (the field pass and the divide pass) instead of
         separate dot kernels; r.M^-1 r only for a symmetric factorisation.
@@ -114,6 +116,8 @@ class MixedVarCoefSolver:
             raise ValueError(f"schedule must be 'flat' or 'sync', not {schedule!r}")
         if precond not in ("tf32", "bf16x3"):
             raise ValueError(f"precond must be 'tf32' or 'bf16x3', not {precond!r}")
+        if apply is None:
+            apply = "f16x3" if A.ndim == 2 else "tf32"
         if apply not in ("tf32", "f16x3"):
             raise ValueError(f"apply must be 'tf32' or 'f16x3', not {apply!r}")
         if residual not in ("df64", "f64"):
@@ -127,9 +131,9 @@ class MixedVarCoefSolver:
         D = s0.backward_matrix(None, 1)
         ops_pad = pack_varcoef_ops(nd, _pad(B, nq, nq), _pad(D, nq, nq))
         self.ops_hi, self.ops_lo = split_tf32(ops_pad)
-        af = apply == "f16x3" and nd == 2 and nq % 8 == 0
+        af = apply == "f16x3" and nq % 8 == 0
         if af:
-            self.ops16 = split_f16_rows(nq, nq, ops_pad)
+            self.ops16 = split_f16_rows(nq, nq, ops_pad, nd)
         self.ops32 = as_device(ops_pad, torch.float32)
         self.kw32 = A.kw.to(torch.float32).contiguous()
         fac = fd_preconditioner(A.T) if M is None else M

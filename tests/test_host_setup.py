@@ -210,3 +210,42 @@ def test_f16_row_split_rounding_and_reconstruction():
                 + lo[r].view(np.float16).astype(np.float64)) * float(inv[r])
         assert np.abs(back - a[r]).max() <= 2.0 ** -22 * max(np.abs(a[r]).max(), 1e-300)
     assert inv[3] == 1.0
+
+
+def test_f16_packed_operator_split_2d_and_3d():
+    """The packed variable-coefficient operators split block by block into
+    row-scaled FP16 pairs: the row count (2-D 4 nq + 3 n, 3-D 5 nq + 3 n) and,
+    row by row in the blocks' order, the same scales and bits as the plain
+    row split of that block."""
+    import numpy as np
+
+    from jaxfun_gb300 import _lib
+
+    L = _lib.lib()
+    n = nq = 24
+    nn = n * nq
+    rng = np.random.default_rng(8)
+    for ndim, blocks in ((2, [(0, 2 * nq, n), (2 * nn, 2 * nq, n), (4 * nn, 2 * n, nq),
+                              (6 * nn, n, 2 * nq)]),
+                         (3, [(0, 2 * nq, n), (2 * nn, 3 * nq, n), (5 * nn, 3 * n, nq)])):
+        rows = L.jfg_varcoef_f16_rows_nd(ndim, n, nq)
+        assert rows == (4 * nq + 3 * n if ndim == 2 else 5 * nq + 3 * n)
+        ops = rng.standard_normal(8 * nn) * 10.0 ** rng.uniform(-3, 3, 8 * nn)
+        hi = np.zeros(8 * nn, np.uint16)
+        lo = np.zeros(8 * nn, np.uint16)
+        inv = np.zeros(rows, np.float32)
+        L.jfg_split_f16_rows_nd_host(ndim, n, nq, ops.ctypes.data, hi.ctypes.data,
+                                     lo.ctypes.data, inv.ctypes.data)
+        r0 = 0
+        for off, nr, ln in blocks:
+            blk = np.ascontiguousarray(ops[off: off + nr * ln])
+            h2 = np.zeros(nr * ln, np.uint16)
+            l2 = np.zeros(nr * ln, np.uint16)
+            i2 = np.zeros(nr, np.float32)
+            L.jfg_split_f16_rowscaled_host(nr, ln, blk.ctypes.data, h2.ctypes.data,
+                                           l2.ctypes.data, i2.ctypes.data)
+            assert np.array_equal(hi[off: off + nr * ln], h2)
+            assert np.array_equal(lo[off: off + nr * ln], l2)
+            assert np.array_equal(inv[r0: r0 + nr], i2)
+            r0 += nr
+        assert r0 == rows
