@@ -807,7 +807,7 @@ def run_varcoef3d(args):
     kap = torch.exp(g)
     b = T.scalar_product(To.backward(fh))
     A = VarCoefMatrix(T, kap)
-    S = MixedVarCoefSolver(A)
+    S = MixedVarCoefSolver(A, precond=args.precond)
     for _ in range(args.warmup):
         x, it_in, it_out = S.solve(b, tol=args.tol3d)
     torch.cuda.synchronize()
@@ -856,7 +856,8 @@ def run_varcoef3d(args):
             "mixed_solves_per_s": B / t, "mixed_inner_iterations_mean": float(it_in.mean()),
             "mixed_outer_iterations_mean": float(it_out.mean()), "mixed_max_rel_err": err,
             "fp64_pcg_solves_per_s": nf / t64, "fp64_pcg_iterations_mean": float(it64.mean()),
-            "fp64_pcg_max_rel_err": err64, "speedup": (B / t) / (nf / t64)}
+            "fp64_pcg_max_rel_err": err64, "speedup": (B / t) / (nf / t64),
+            "precond": S.precond}
     if learned is not None:
         xl = learned.pop("x")
         learned["max_rel_err"] = float(((xl[:nf] - xt).abs().amax(dim=(1, 2, 3))
@@ -906,7 +907,7 @@ def run_ours(args):
         fgrid = torch.as_tensor(f_h, device="cuda")
         A = VarCoefMatrix(T, kap)                 # FP64 operator (kw = kappa w (x) w)
         solver = MixedVarCoefSolver(A, fused_dots=not args.no_fused_dots,
-                                    schedule=args.schedule)
+                                    schedule=args.schedule, precond=args.precond)
         SP = torch.as_tensor(np.array(D.scalar_product_matrix()), device="cuda")
         rhs = torch.empty(B, n, n, dtype=torch.float64, device="cuda")
         x = torch.empty(B, n, n, dtype=torch.float64, device="cuda")
@@ -1218,8 +1219,11 @@ def run_ours(args):
         cfg = {"workload": "varcoef-poisson-2d-legendre-N256", "N": N, "batch": B,
                "path": ("learned guess (BF16 tcgen05 spectral neural operator) + "
                         if model is not None else "") +
-                       "mixed: tcgen05 PCG (scaled split-FP16 operator, split-BF16 "
-                       "preconditioner) + FP64 refinement",
+                       "mixed: tcgen05 PCG (scaled split-FP16 operator, " +
+                       {"bf16x3": "split-BF16", "bf16": "plain BF16",
+                        "tf32": "split-TF32"}[solver.precond] +
+                       " preconditioner) + FP64 refinement",
+               "precond": solver.precond,
                "tol_relres": args.tol, "inner_tol": args.inner_tol,
                "inner_iterations_mean": float(its_in.mean()),
                "outer_iterations_mean": float(its_out.mean()),
@@ -1292,6 +1296,9 @@ def main():
     ap.add_argument("--skip-cpu", action="store_true")
     ap.add_argument("--schedule", default="sync", choices=["flat", "sync"],
                     help="refinement steps per problem (flat) or for the whole batch (sync)")
+    ap.add_argument("--precond", default=None, choices=["bf16x3", "bf16", "tf32"],
+                    help="arithmetic of the inner preconditioner's passes (default: the "
+                         "solver's, plain BF16 in 2-D and split BF16 in 3-D)")
     ap.add_argument("--no-fused-dots", action="store_true",
                     help="inner PCG dots as separate kernels (not from the epilogues)")
     ap.add_argument("--no-autotune", action="store_true",

@@ -159,7 +159,11 @@ int jfg_contract_tc(const jfg_contract_desc* d, const float* op_hi, const float*
  * (jfg_split_bf16_host) and the FP32 input split into BF16 pairs in the
  * kernel: three BF16 MMAs (hi*hi + hi*lo + lo*hi, FP32 accumulate) per
  * product at twice the TF32 rate; ~2^-16 relative per product.  For the
- * HBM-bound batched transforms.  op_ld, op_seg % 8 == 0. */
+ * HBM-bound batched transforms.  op_ld, op_seg % 8 == 0.
+ * op_lo NULL: plain BF16, one MMA per product (hi*hi: operator hi and the
+ * input rounded to BF16, ~2^-8 relative; products exact in FP32), for the
+ * inner preconditioner's passes; beta 0 and no field epilogue then (else
+ * JFG_ERR_ARG). */
 int jfg_contract_tc_bf16x3(const jfg_contract_desc* d, const uint16_t* op_hi,
                            const uint16_t* op_lo, const float* in, float* out, void* stream);
 /* Split n FP64 values into BF16 hi (round to nearest even) and lo = x - hi
@@ -564,7 +568,8 @@ typedef struct {
                             (jfg_contract_df64 passes)                                */
   int precond_bf16;      /* 1: the inner preconditioner's FD passes use split-BF16
                             operators (E/W_hi16, _lo16: jfg_split_bf16_host of the
-                            padded factors), 0: split-TF32 (E/W_hi, _lo).  The
+                            padded factors), 2: plain BF16 (E/W_hi16 only; the
+                            _lo16 pointers unused), 0: split-TF32 (E/W_hi, _lo).  The
                             operator passes stay split-TF32: with split-BF16 they
                             stall the inner solve near its 1e-5 tolerance           */
   const uint16_t* E_hi16;

@@ -388,9 +388,12 @@ template <int EPI, bool BETA, int G, int PREC>
 __global__ void __launch_bounds__(NTHREADS, 1)
     k_contract_tc(const __grid_constant__ TcLaunch<G> L) {
   // PREC: 0 split TF32 (kind::tf32), 1 split BF16, 2 scaled split FP16 (both
-  // kind::f16: 16-bit operator pairs, 64-element K blocks)
+  // kind::f16: 16-bit operator pairs, 64-element K blocks), 3 plain BF16 (one
+  // product hi*hi, the operator's hi only: ~2^-8 relative per product)
   constexpr bool B16 = PREC != 0;
   constexpr bool H16 = PREC == 2;
+  constexpr bool B1 = PREC == 3;
+  constexpr uint32_t NOP = B1 ? 1u : 2u;  // operator pieces per stage (hi, lo)
   // K elements per block: 32 TF32 (one 128-byte row) or 64 BF16 (one 128-byte
   // operator row; the FP32 input block then takes two TMA boxes)
   constexpr int KE = B16 ? b16_ke(EPI) : KB;
@@ -406,10 +409,10 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   const int S = L.stages;
   const bool ta = B16 || L.tmem_a != 0;
-  const bool res = B16 && L.op_res != 0;
+  const bool res = B16 && !B1 && L.op_res != 0;
   const uint32_t omax = (uint32_t)L.mt_max * OROW;  // Mtile operator rows (hi or lo)
   const uint32_t xbuf = ta ? XB : 2 * XBYTES;  // X block (+ its lo part when in SMEM)
-  const uint32_t stage_bytes = res ? xbuf : xbuf + 2 * omax;
+  const uint32_t stage_bytes = res ? xbuf : xbuf + NOP * omax;
   const uint32_t acc_stride = ta ? ACC_STRIDE_TA : 256;
   // operator-stationary schedule: this CTA's operator slot and tile stride
   const int r_slot = res ? (int)(blockIdx.x % (unsigned)L.nslots) : 0;
@@ -569,14 +572,15 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             ok = false;
             break;
           }
-          mbar_expect_tx(&full[st], res ? XB : XB + 2 * obytes);
+          mbar_expect_tx(&full[st], res ? XB : XB + NOP * obytes);
           tma_load_4d(Xh(st), &L.maps[gi][0], &full[st], kb * KE, pt * TILE_P, cs, cb);
           if (B16 && KE > KB)
             tma_load_4d(Xh(st) + XBYTES, &L.maps[gi][0], &full[st], kb * KE + KB,
                         pt * TILE_P, cs, cb);
           if (!res) {
             tma_load_3d(Oh(st), &L.maps[gi][1], &full[st], kb * KE, mc * q.Mtile, os);
-            tma_load_3d(Ol(st), &L.maps[gi][2], &full[st], kb * KE, mc * q.Mtile, os);
+            if (!B1)
+              tma_load_3d(Ol(st), &L.maps[gi][2], &full[st], kb * KE, mc * q.Mtile, os);
           }
           issued = g + 1;
         }
@@ -627,8 +631,10 @@ __global__ void __launch_bounds__(NTHREADS, 1)
               const uint64_t bh = KE == 64 ? sdesc(oh + off) : sdesc64(oh + off);
               const uint64_t bl = KE == 64 ? sdesc(ol + off) : sdesc64(ol + off);
               mma_b16_ta(acc, ah + 8 * kk, bh, idesc, (kb | kk) ? 1u : 0u);
-              mma_b16_ta(acc, ah + 8 * kk, bl, idesc, 1u);
-              mma_b16_ta(acc, al + 8 * kk, bh, idesc, 1u);
+              if (!B1) {
+                mma_b16_ta(acc, ah + 8 * kk, bl, idesc, 1u);
+                mma_b16_ta(acc, al + 8 * kk, bh, idesc, 1u);
+              }
             }
           } else if (ta) {
             const uint32_t ah = tmem + (uint32_t)A_COL0 + A_SLOT * (uint32_t)st, al = ah + 32;
@@ -722,13 +728,15 @@ __global__ void __launch_bounds__(NTHREADS, 1)
               const uint32_t h0 = pack_bf16x2(v.x, v.y), h1 = pack_bf16x2(v.z, v.w);
               h[2 * c] = h0;
               h[2 * c + 1] = h1;
-              l[2 * c] = pack_bf16x2(v.x - __uint_as_float(h0 << 16),
-                                     v.y - __uint_as_float(h0 & 0xFFFF0000u));
-              l[2 * c + 1] = pack_bf16x2(v.z - __uint_as_float(h1 << 16),
-                                         v.w - __uint_as_float(h1 & 0xFFFF0000u));
+              if (!B1) {
+                l[2 * c] = pack_bf16x2(v.x - __uint_as_float(h0 << 16),
+                                       v.y - __uint_as_float(h0 & 0xFFFF0000u));
+                l[2 * c + 1] = pack_bf16x2(v.z - __uint_as_float(h1 << 16),
+                                           v.w - __uint_as_float(h1 & 0xFFFF0000u));
+              }
             }
             tmem_st16(tbase + 16 * half, h);
-            tmem_st16(tbase + A_SLOT / 2 + 16 * half, l);
+            if (!B1) tmem_st16(tbase + A_SLOT / 2 + 16 * half, l);
           }
           asm volatile("tcgen05.wait::st.sync.aligned;" ::: "memory");
           asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
@@ -1030,6 +1038,15 @@ int make_map(CUtensorMap* map, const void* base, int rank, const cuuint64_t* dim
   return r == CUDA_SUCCESS ? JFG_OK : JFG_ERR_ARG;
 }
 
+// the plain BF16 kernel exists for the epilogues of the fast diagonalisation
+template <int E>
+int set_attr_b1(int mx) {
+  if constexpr (E != JFG_EPI_MUL_FIELD)
+    JFG_CUDA_TRY(cudaFuncSetAttribute(k_contract_tc<E, false, 1, 3>,
+                                      cudaFuncAttributeMaxDynamicSharedMemorySize, mx));
+  return JFG_OK;
+}
+
 // Opt every kernel variant into the largest dynamic shared-memory size once
 // per device (before any stream capture can be active in the caller).
 int setup_kernel_attr() {
@@ -1046,7 +1063,8 @@ int setup_kernel_attr() {
                                     cudaFuncAttributeMaxDynamicSharedMemorySize, mx));     \
   if (G == 1)                                                                              \
   JFG_CUDA_TRY(cudaFuncSetAttribute(k_contract_tc<E, B, 1, 2>,                             \
-                                    cudaFuncAttributeMaxDynamicSharedMemorySize, mx))
+                                    cudaFuncAttributeMaxDynamicSharedMemorySize, mx));     \
+  if (G == 1 && !B) JFG_TRY(set_attr_b1<E>(mx))
 #define JFG_SET_ATTR_G(G)                   \
   JFG_SET_ATTR(JFG_EPI_NONE, false, G);     \
   JFG_SET_ATTR(JFG_EPI_NONE, true, G);      \
@@ -1065,16 +1083,17 @@ int setup_kernel_attr() {
 
 // Validate one group and fill its descriptor, tile height and tensor maps.
 // prec: 0 the operator is TF32 in FP32 words; 1 BF16 (hi, lo) and 2 FP16
-// (hi, lo), both with 64-element K blocks.
+// (hi, lo), both with 64-element K blocks; 3 BF16 hi only (op_lo unused).
 int fill_group(const jfg_contract_desc& d, const void* op_hi, const void* op_lo,
                const float* in, float* out, TcGroup& q, CUtensorMap* maps, int prec,
                int mt_cap) {
   const bool b16 = prec != 0;
   JFG_TRY(validate_desc(d));
-  if (!op_hi || !op_lo || !in || !out) return JFG_ERR_ARG;
+  const bool lo = prec != 3;
+  if (!op_hi || (lo && !op_lo) || !in || !out) return JFG_ERR_ARG;
   // TMA: 16-byte aligned bases and strides
   auto al16 = [](const void* p) { return ((uintptr_t)p & 15u) == 0; };
-  if (!al16(op_hi) || !al16(op_lo) || !al16(in)) return JFG_ERR_ARG;
+  if (!al16(op_hi) || (lo && !al16(op_lo)) || !al16(in)) return JFG_ERR_ARG;
   const int om = b16 ? 7 : 3;  // operator strides in elements: multiples of 16 bytes
   if ((d.op_ld & om) || (d.in_ld & 3) || (d.op_seg & om) || (d.in_seg & 3) || (d.in_batch & 3))
     return JFG_ERR_ARG;
@@ -1107,13 +1126,13 @@ int fill_group(const jfg_contract_desc& d, const void* op_hi, const void* op_lo,
     // one operator row of a stage per box row: 128 B (TF32) or 64 B (16-bit)
     const int orow = b16 ? 2 * b16_ke(d.epilogue) : 128;
     cuuint32_t box[3] = {(cuuint32_t)(orow / eb), (cuuint32_t)q.Mtile, 1};
-    const CUtensorMapDataType dt = prec == 2   ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16
-                                   : prec == 1 ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16
-                                               : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+    const CUtensorMapDataType dt = prec == 2 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT16
+                                   : b16     ? CU_TENSOR_MAP_DATA_TYPE_BFLOAT16
+                                             : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
     const CUtensorMapSwizzle sw =
         orow == 64 ? CU_TENSOR_MAP_SWIZZLE_64B : CU_TENSOR_MAP_SWIZZLE_128B;
     JFG_TRY(make_map(&maps[1], op_hi, 3, dims, str, box, dt, sw));
-    JFG_TRY(make_map(&maps[2], op_lo, 3, dims, str, box, dt, sw));
+    if (lo) JFG_TRY(make_map(&maps[2], op_lo, 3, dims, str, box, dt, sw));
   }
   // output through TMA stores when its rows are 16-byte aligned and every
   // 32-column group of a tile is full (else plain coalesced stores)
@@ -1148,6 +1167,13 @@ template <int E, bool BETA, int G>
 void launch_h16(dim3 grid, size_t smem, cudaStream_t st, const TcLaunch<G>& L) {
   if constexpr (G == 1) k_contract_tc<E, BETA, 1, 2><<<grid, NTHREADS, smem, st>>>(L);
 }
+// ... and so does the plain BF16 kernel (the fast diagonalisation's passes:
+// no beta, no field)
+template <int E, bool BETA, int G>
+void launch_b1(dim3 grid, size_t smem, cudaStream_t st, const TcLaunch<G>& L) {
+  if constexpr (G == 1 && !BETA && E != JFG_EPI_MUL_FIELD)
+    k_contract_tc<E, false, 1, 3><<<grid, NTHREADS, smem, st>>>(L);
+}
 
 // h16 (one group only): the scaled split-FP16 auxiliaries of that group.
 struct H16Aux {
@@ -1165,6 +1191,9 @@ int launch_groups(int ng, const jfg_contract_desc* const* ds, const void* const*
   if (dot && dot->nb) *dot->nb = 0;
   const bool b16 = prec != 0;
   if (prec == 2 && (G != 1 || ng != 1 || !h16 || !h16->op_inv)) return JFG_ERR_ARG;
+  if (prec == 3 && (G != 1 || ng != 1 || ds[0]->beta != 0.0 ||
+                    ds[0]->epilogue == JFG_EPI_MUL_FIELD))
+    return JFG_ERR_ARG;
   static_assert(sizeof(TcLaunch<G>) <= 32000, "kernel parameter block too large");
   TcLaunch<G> L;
   memset(&L, 0, sizeof(L));
@@ -1229,7 +1258,7 @@ int launch_groups(int ng, const jfg_contract_desc* const* ds, const void* const*
   int nslots = 0;
   size_t res_bytes = 0;
   const int sched = cfg.schedule == 1 ? 0 : cfg.schedule == 2 ? 2 : g_op_resident;
-  if (b16 && ng == 1 && sched) {
+  if (b16 && prec != 3 && ng == 1 && sched) {
     const TcGroup& q = L.g[0];
     const int mch = (q.d.M + q.Mtile - 1) / q.Mtile;
     nslots = q.d.nseg * mch;
@@ -1243,7 +1272,7 @@ int launch_groups(int ng, const jfg_contract_desc* const* ds, const void* const*
   const int ke16 = b16_ke(epi);
   const size_t xstage = (size_t)(ke16 / KB) * XBYTES;  // FP32 input of a 16-bit stage
   const size_t stage = res ? xstage
-                           : b16 ? xstage + 2 * (size_t)mt_max * 2 * ke16
+                           : b16 ? xstage + (prec == 3 ? 1 : 2) * (size_t)mt_max * 2 * ke16
                                  : (ta ? 1 : 2) * (size_t)XBYTES + 2 * (size_t)mt_max * 128;
   // field-multiply launches stage both of a warp's boxes of a tile (the
   // field of each fetched ahead), when two pipeline stages still fit
@@ -1302,6 +1331,8 @@ int launch_groups(int ng, const jfg_contract_desc* const* ds, const void* const*
         launch_h16<E, true, G>(grid, smem, st, L);                             \
       else                                                                     \
         launch_h16<E, false, G>(grid, smem, st, L);                            \
+    } else if (prec == 3) {                                                    \
+      launch_b1<E, false, G>(grid, smem, st, L);                               \
     } else if (b16) {                                                          \
       if (hb)                                                                  \
         k_contract_tc<E, true, G, 1><<<grid, NTHREADS, smem, st>>>(L);         \
@@ -1382,7 +1413,7 @@ int tune_single(int prec, const jfg_contract_desc& d, const void* oh, const void
       for (int sg : {0, 3, 2})
         for (int store : {1, 2})
           for (int mt : {0, 64}) {
-            if ((prec != 0 && ta == 0) || (prec == 0 && sched == 2)) continue;
+            if ((prec != 0 && ta == 0) || ((prec == 0 || prec == 3) && sched == 2)) continue;
             // the operator-stationary schedule only where the chunk fits beside
             // two input stages (else the launch would stream anyway)
             if (sched == 2 && (size_t)((d.K + b16_ke(d.epilogue) - 1) / b16_ke(d.epilogue)) *
@@ -1489,7 +1520,7 @@ int contract_tc_b16(const jfg_contract_desc& d, const uint16_t* op_hi, const uin
                     const float* in, float* out, cudaStream_t st, const DotOut* dot) {
   if (dot && dot->nb) *dot->nb = 0;
   if (d.batch == 0 || d.M == 0 || d.P == 0) return validate_desc(d);
-  return launch_single(1, d, op_hi, op_lo, in, out, nullptr, st, dot);
+  return launch_single(op_lo ? 1 : 3, d, op_hi, op_lo, in, out, nullptr, st, dot);
 }
 
 int contract_tc_h16(const jfg_contract_desc& d, const uint16_t* op_hi, const uint16_t* op_lo,

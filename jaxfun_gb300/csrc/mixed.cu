@@ -462,7 +462,9 @@ extern "C" int jfg_pcg_mixed_autotune(const jfg_mixed_plan* plan, void* work, si
   const jfg_mixed_plan& P = *plan;
   if ((P.ndim != 2 && P.ndim != 3) || P.n < 1 || P.nq < P.n || P.batch < 1 || !P.ops_hi ||
       !P.ops_lo || !P.kw32 || !P.E_hi || !P.E_lo || !P.W_hi || !P.W_lo || !P.lam ||
-      (P.precond_bf16 && (!P.E_hi16 || !P.E_lo16 || !P.W_hi16 || !P.W_lo16)) ||
+      (P.precond_bf16 != 0 && P.precond_bf16 != 1 && P.precond_bf16 != 2) ||
+      (P.precond_bf16 && (!P.E_hi16 || !P.W_hi16)) ||
+      (P.precond_bf16 == 1 && (!P.E_lo16 || !P.W_lo16)) ||
       (P.apply_f16 && ((P.nq & 7) || !P.ops_hi16 || !P.ops_lo16 || !P.ops_inv16)))
     return JFG_ERR_ARG;
   const int ndim = P.ndim, nq = P.nq, batch = P.batch;
@@ -486,10 +488,14 @@ extern "C" int jfg_pcg_mixed_autotune(const jfg_mixed_plan* plan, void* work, si
   const bool pbf = P.precond_bf16 != 0;
   const OpRef<float> ops = th ? OpRef<float>{(const float*)P.ops_hi16, (const float*)P.ops_lo16}
                               : OpRef<float>{P.ops_hi, P.ops_lo};
-  const OpRef<float> E = pbf ? OpRef<float>{(const float*)P.E_hi16, (const float*)P.E_lo16}
-                             : OpRef<float>{P.E_hi, P.E_lo};
-  const OpRef<float> W = pbf ? OpRef<float>{(const float*)P.W_hi16, (const float*)P.W_lo16}
-                             : OpRef<float>{P.W_hi, P.W_lo};
+  // plain BF16 (precond_bf16 2): no lo halves, one product per term
+  const bool p1 = P.precond_bf16 == 2;
+  const OpRef<float> E =
+      pbf ? OpRef<float>{(const float*)P.E_hi16, p1 ? nullptr : (const float*)P.E_lo16}
+          : OpRef<float>{P.E_hi, P.E_lo};
+  const OpRef<float> W =
+      pbf ? OpRef<float>{(const float*)P.W_hi16, p1 ? nullptr : (const float*)P.W_lo16}
+          : OpRef<float>{P.W_hi, P.W_lo};
   const int prev = single_autotune();
   set_single_autotune(1);
   int s = varcoef_apply<float>(th ? Engine::TH : Engine::TC, ndim, nq, nq, batch, ops, P.kw32,
@@ -526,8 +532,9 @@ extern "C" int jfg_pcg_varcoef_mixed_guess(const jfg_mixed_plan* plan, const dou
   if ((P.ndim != 2 && P.ndim != 3) || P.n < 1 || P.nq < P.n || P.batch < 1 || !P.ops64 ||
       !P.kw64 || !P.ops_hi || !P.ops_lo || !P.kw32 || !P.E_hi || !P.E_lo || !P.W_hi ||
       !P.W_lo || !P.lam || (P.residual != 0 && P.residual != 1) ||
-      (P.precond_bf16 != 0 && P.precond_bf16 != 1) ||
-      (P.precond_bf16 && (!P.E_hi16 || !P.E_lo16 || !P.W_hi16 || !P.W_lo16)) ||
+      (P.precond_bf16 != 0 && P.precond_bf16 != 1 && P.precond_bf16 != 2) ||
+      (P.precond_bf16 && (!P.E_hi16 || !P.W_hi16)) ||
+      (P.precond_bf16 == 1 && (!P.E_lo16 || !P.W_lo16)) ||
       (P.apply_f16 != 0 && P.apply_f16 != 1) ||
       (P.apply_f16 && ((P.nq & 7) || !P.ops_hi16 || !P.ops_lo16 || !P.ops_inv16)) ||
       (P.schedule != 0 && P.schedule != 1))
@@ -570,9 +577,11 @@ extern "C" int jfg_pcg_varcoef_mixed_guess(const jfg_mixed_plan* plan, const dou
   pb.ops_inv = P.apply_f16 ? P.ops_inv16 : nullptr;
   pb.fuse_dots = P.fused_dots & 3;
   pb.kw = P.kw32;
-  pb.E = pbf ? OpRef<float>{(const float*)P.E_hi16, (const float*)P.E_lo16}
+  // plain BF16 (precond_bf16 2): no lo halves, one product per term
+  const bool p1 = P.precond_bf16 == 2;
+  pb.E = pbf ? OpRef<float>{(const float*)P.E_hi16, p1 ? nullptr : (const float*)P.E_lo16}
              : OpRef<float>{P.E_hi, P.E_lo};
-  pb.W = pbf ? OpRef<float>{(const float*)P.W_hi16, (const float*)P.W_lo16}
+  pb.W = pbf ? OpRef<float>{(const float*)P.W_hi16, p1 ? nullptr : (const float*)P.W_lo16}
              : OpRef<float>{P.W_hi, P.W_lo};
   pb.lam = P.lam;
   pb.fd_scale = P.fd_scale;

@@ -83,18 +83,23 @@ class MixedVarCoefSolver:
 
     def __init__(self, A: VarCoefMatrix, M: TPMatricesLUFactors | None = None,
                  residual: str = "df64", fp32_updates: bool | None = None,
-                 precond: str = "bf16x3", apply: str | None = None, fused_dots: bool = True,
+                 precond: str | None = None, apply: str | None = None, fused_dots: bool = True,
                  schedule: str = "sync"):
         """``residual``: arithmetic of the refinement residual r = b - A x,
         "df64" (double-FP32 on the FP32 units) or "f64" (FP64 FMAs).
         ``fp32_updates``: once ||r|| <= 1e-4 ||b||, update r -= ||r|| A d in FP32
         instead of recomputing it (default: in 2-D only; in 3-D the operator's
         conditioning turns the FP32 update error into > 1e-10 solution error).
-        ``precond``: split-"bf16x3" (default) or split-"tf32" tensor-core passes
-        for the inner fast-diagonalisation preconditioner; the preconditioner
-        tolerates the BF16 pairs' ~2^-16 error (same iteration counts, ~7 %
-        faster at N = 256).  Padded sizes with nq % 8 != 0 use split-TF32 (the
-        BF16 rows would not be 16-byte multiples).
+        ``precond``: plain "bf16" (one BF16 product per term, ~2^-8 relative),
+        split-"bf16x3" (~2^-16) or split-"tf32" tensor-core passes for the
+        inner fast-diagonalisation preconditioner.  Default: "bf16" in 2-D,
+        "bf16x3" in 3-D.  The preconditioner tolerates the rounding: in the
+        oracle's PCG at N = 128 and 256 plain BF16 left every iteration count
+        unchanged, and on the benchmark's 128 problems at N = 256 it ran
+        90.42 inner iterations against 90.40 with split BF16, 5.5 % faster
+        (split BF16 was ~7 % faster than split TF32).  Padded sizes with
+        nq % 8 != 0 use split-TF32 (the BF16 rows would not be 16-byte
+        multiples).
         ``apply``: the inner operator passes as scaled split-"f16x3" (FP16
         hi/lo pairs with power-of-two scales per operator row and per problem,
         the accuracy of split TF32 at twice its MMA rate) or split-"tf32".
@@ -114,8 +119,10 @@ class MixedVarCoefSolver:
         step to step."""
         if schedule not in ("flat", "sync"):
             raise ValueError(f"schedule must be 'flat' or 'sync', not {schedule!r}")
-        if precond not in ("tf32", "bf16x3"):
-            raise ValueError(f"precond must be 'tf32' or 'bf16x3', not {precond!r}")
+        if precond is None:
+            precond = "bf16" if A.ndim == 2 else "bf16x3"
+        if precond not in ("tf32", "bf16x3", "bf16"):
+            raise ValueError(f"precond must be 'tf32', 'bf16x3' or 'bf16', not {precond!r}")
         if apply is None:
             apply = "f16x3" if A.ndim == 2 else "tf32"
         if apply not in ("tf32", "f16x3"):
@@ -140,7 +147,9 @@ class MixedVarCoefSolver:
         self.E_hi, self.E_lo = split_tf32(_pad(fac.E_host, nq, nq))
         self.W_hi, self.W_lo = split_tf32(_pad(fac.W_host, nq, nq))
         # BF16 operator rows must be 16-byte multiples (nq % 8 == 0) for TMA
-        pb = precond == "bf16x3" and nq % 8 == 0
+        pb = precond in ("bf16x3", "bf16") and nq % 8 == 0
+        p1 = pb and precond == "bf16"
+        self.precond = ("bf16" if p1 else "bf16x3") if pb else "tf32"  # as run
         if pb:
             self.E16 = split_bf16(_pad(fac.E_host, nq, nq))
             self.W16 = split_bf16(_pad(fac.W_host, nq, nq))
@@ -157,11 +166,11 @@ class MixedVarCoefSolver:
                               self.kw32.data_ptr(), self.E_hi.data_ptr(), self.E_lo.data_ptr(),
                               self.W_hi.data_ptr(), self.W_lo.data_ptr(), self.lam.data_ptr(),
                               None, self.ops32.data_ptr() if fp32_updates else None,
-                              1 if residual == "df64" else 0, 1 if pb else 0,
+                              1 if residual == "df64" else 0, (2 if p1 else 1) if pb else 0,
                               self.E16[0].data_ptr() if pb else None,
-                              self.E16[1].data_ptr() if pb else None,
+                              self.E16[1].data_ptr() if pb and not p1 else None,
                               self.W16[0].data_ptr() if pb else None,
-                              self.W16[1].data_ptr() if pb else None,
+                              self.W16[1].data_ptr() if pb and not p1 else None,
                               1 if af else 0,
                               self.ops16[0].data_ptr() if af else None,
                               self.ops16[1].data_ptr() if af else None,

@@ -26,7 +26,7 @@ def schedule(request):
 
 
 @pytest.mark.parametrize("apply", ["f16x3", "tf32"])
-@pytest.mark.parametrize("precond", ["bf16x3", "tf32"])
+@pytest.mark.parametrize("precond", ["bf16x3", "bf16", "tf32"])
 @pytest.mark.parametrize("ndim,N,batch", [(2, 32, 3), (2, 64, 2), (3, 16, 2)])
 def test_mixed_matches_fp64(ndim, N, batch, precond, apply, schedule):
     V = FunctionSpace(N, Legendre, bcs=DIRICHLET)
@@ -75,7 +75,9 @@ def test_mixed_with_initial_guess_and_converged_problem():
 
 def test_mixed_after_autotune():
     """The solver's autotune tunes every distinct tensor-core pass of its inner
-    solve; the solve with the tuned configurations still reaches 1e-10."""
+    solve (2-D defaults: scaled split-FP16 operator passes, p2, and plain BF16
+    preconditioner passes, p3); the solve with the tuned configurations still
+    reaches 1e-10."""
     N, batch = 64, 3
     V = FunctionSpace(N, Legendre, bcs=DIRICHLET)
     T = TensorProduct(V, V)
@@ -86,12 +88,37 @@ def test_mixed_after_autotune():
     S = MixedVarCoefSolver(A)
     tuned = S.autotune()
     sigs = [t["signature"] for t in tuned]
-    assert any(":p2:b3:" in s for s in sigs) and any(":p1:b3:" in s for s in sigs), sigs
+    assert any(":p2:b3:" in s for s in sigs) and any(":p3:b3:" in s for s in sigs), sigs
     xr, _ = pcg(A, b, tol=1e-14, maxiter=3000)
     x, _, _ = S.solve(b, tol=1e-12)
     xr, x = xr.cpu().numpy(), x.cpu().numpy()
     for i in range(batch):
         assert rel(x[i], xr[i]) < 1e-10
+
+
+def test_plain_bf16_preconditioner_keeps_iterations(schedule):
+    """The preconditioner's passes in plain BF16 (one product per term,
+    ~2^-8) against split BF16 (~2^-16), N = 128, 4 problems: the same answers
+    (<= 1e-10 vs a tight FP64 solve) and inner iteration counts within 3 %."""
+    N, batch = 128, 4
+    V = FunctionSpace(N, Legendre, bcs=DIRICHLET)
+    T = TensorProduct(V, V)
+    rng = np.random.default_rng(128)
+    kap = np.exp(0.5 * rng.standard_normal((batch, N, N)))
+    b = rng.standard_normal((batch, N - 2, N - 2))
+    A = VarCoefMatrix(T, kap)
+    xr, _ = pcg(A, b, tol=1e-14, maxiter=4000)
+    xr = xr.cpu().numpy()
+    its = {}
+    for precond in ("bf16x3", "bf16"):
+        S = MixedVarCoefSolver(A, precond=precond)
+        assert S.plan.precond_bf16 == (2 if precond == "bf16" else 1)
+        x, it_in, _ = S.solve(b, tol=1e-12)
+        x = x.cpu().numpy()
+        for i in range(batch):
+            assert rel(x[i], xr[i]) < 1e-10, (precond, i)
+        its[precond] = it_in.astype(float)
+    assert np.all(np.abs(its["bf16"] - its["bf16x3"]) <= 0.03 * its["bf16x3"] + 1), its
 
 
 @pytest.mark.parametrize("precond", ["bf16x3", "tf32"])
