@@ -218,7 +218,8 @@ def roofline_microbench(B: int, N: int, reps: int = 20, M: int | None = None,
     operator: M = 2N quadrature rows, P = K = N padded coefficients, B problems;
     M = N gives the preconditioner pass) -- with CUDA events on its launch
     stream.  prec "f16x3": scaled split FP16 (kind::f16, the inner solve's
-    operator passes); "tf32": split TF32 (kind::tf32).  field_pass: the
+    operator passes); "tf32": split TF32 (kind::tf32); "bf16" / "bf16x3":
+    plain / split BF16 (the preconditioner's passes, with M = N).  field_pass: the
     second operator pass instead (two segments of M = N rows, the kappa*w
     field multiplied in the epilogue).  Returns achieved numbers; FLOPs count
     each contraction once."""
@@ -260,6 +261,13 @@ def roofline_microbench(B: int, N: int, reps: int = 20, M: int | None = None,
         call = lambda: L.jfg_contract_tc_f16x3(  # noqa: E731
             d, t_hi.data_ptr(), t_lo.data_ptr(), t_inv.data_ptr(), M, in_max.data_ptr(),
             out_max.data_ptr(), x.data_ptr(), y.data_ptr(), s.cuda_stream)
+    elif prec in ("bf16", "bf16x3"):
+        from jaxfun_gb300.la.mixed import split_bf16
+
+        hi, lo = split_bf16(op)
+        lo_p = lo.data_ptr() if prec == "bf16x3" else None
+        call = lambda: L.jfg_contract_tc_bf16x3(d, hi.data_ptr(), lo_p,  # noqa: E731
+                                                x.data_ptr(), y.data_ptr(), s.cuda_stream)
     else:
         hi, lo = split_tf32(op)
         call = lambda: L.jfg_contract_tc(d, hi.data_ptr(), lo.data_ptr(),  # noqa: E731
@@ -278,7 +286,8 @@ def roofline_microbench(B: int, N: int, reps: int = 20, M: int | None = None,
     nbytes = 4.0 * B * S * P * (K + M) + (4.0 * B * M * P if field_pass else 0.0)
     return {"M": M, "P": P, "K": K, "S": S, "t": t, "flops": flops, "bytes": nbytes, "prec": prec,
             "tflops_alg": flops / t / 1e12,
-            "tflops_issued": 3 * flops / t / 1e12, "gbs": nbytes / t / 1e9}
+            "tflops_issued": (1 if prec == "bf16" else 3) * flops / t / 1e12,
+            "gbs": nbytes / t / 1e9}
 
 
 def other_kernel_microbench(which: str, B: int, reps: int = 3):
@@ -1315,13 +1324,15 @@ def main():
         ROOT, "jaxfun_gb300", "sno", "weights", "sno_varcoef2d_N256.npz"))
     ap.add_argument("--kernel-only", nargs="?", const="contract", default=None,
                     choices=["contract", "contract_tf32", "contract_field",
-                             "contract_field_tf32", "gemm", "fp64", "df64", "transform",
-                             "transform_tf32"],
+                             "contract_field_tf32", "precond", "precond_bf16x3", "gemm",
+                             "fp64", "df64", "transform", "transform_tf32"],
                     help="time one kernel and print its numbers (used for ncu captures): "
                          "contract = tcgen05 scaled split-FP16 contraction at the variable-"
                          "coefficient pass shape (M = 512, P = K = 256), B problems; "
                          "contract_tf32 = its split-TF32 variant; contract_field(_tf32) = "
                          "the second operator pass (2 segments, kappa*w field epilogue); "
+                         "precond(_bf16x3) = a plain (split) BF16 preconditioner pass "
+                         "(M = P = K = 256); "
                          "gemm = BF16 GEMM of the neural operator's spectral transform "
                          "(1024 x 64 x 4096 per sample, B samples); fp64 = FP64 CUDA-core "
                          "contraction at the variable-coefficient pass shape; df64 = the same "
@@ -1367,6 +1378,10 @@ def main():
                    **roofline_microbench(args.batch, N_GRID, reps=3, prec=prec,
                                          field_pass=args.kernel_only.startswith(
                                              "contract_field"))}
+        elif args.kernel_only in ("precond", "precond_bf16x3"):
+            prec = "bf16x3" if args.kernel_only.endswith("bf16x3") else "bf16"
+            out = {"kernel": "k_contract_tc",
+                   **roofline_microbench(args.batch, N_GRID, reps=3, M=N_GRID, prec=prec)}
         else:
             out = other_kernel_microbench(args.kernel_only, args.batch)
         print(json.dumps({"batch": args.batch, **out}), flush=True)
