@@ -497,37 +497,52 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   // resident operator chunk: K block kb of hi at 2 kb omax, lo right after it
   auto OhR = [&](int kb) { return smem + (size_t)kb * 2 * omax; };
   auto OlR = [&](int kb) { return smem + (size_t)kb * 2 * omax + omax; };
-  // b = problem index (-1: an out-of-range list entry, computed but not stored)
-  auto decode = [&](long long t, int& gi, int& pt, int& mc, int& b, int& s) {
+  // b = problem index (-1: an out-of-range list entry, computed but not stored);
+  // roles that do not use b (need_b false) skip its list load.  Tile indices
+  // below 2^32 take 32-bit division: the 64-bit one is a long software
+  // sequence, paid by every role at every tile.
+  auto decode = [&](long long t, int& gi, int& pt, int& mc, int& b, int& s, bool need_b) {
     gi = 0;
     while (gi + 1 < L.ngroups && t >= tb[gi + 1]) ++gi;
     const TcGroup& q = L.g[gi];
-    const int nptiles = (q.d.P + TILE_P - 1) / TILE_P;
-    const int mchunks = (q.d.M + q.Mtile - 1) / q.Mtile;
-    long long r = t - tb[gi];
+    const unsigned nptiles = (unsigned)((q.d.P + TILE_P - 1) / TILE_P);
+    const unsigned mchunks = (unsigned)((q.d.M + q.Mtile - 1) / q.Mtile);
+    const long long r = t - tb[gi];
     int bs;
-    if (q.mc_inner) {  // the CTAs that share an input tile run it at the same time
+    if (r <= 0xFFFFFFFFLL) {
+      unsigned ru = (unsigned)r;
+      if (q.mc_inner) {  // the CTAs that share an input tile run it at the same time
+        mc = (int)(ru % mchunks);
+        ru /= mchunks;
+        pt = (int)(ru % nptiles);
+        bs = (int)(ru / nptiles);
+      } else {           // the CTAs that share an operator chunk run it at the same time
+        pt = (int)(ru % nptiles);
+        ru /= nptiles;
+        mc = (int)(ru % mchunks);
+        bs = (int)(ru / mchunks);
+      }
+    } else if (q.mc_inner) {
       mc = (int)(r % mchunks);
-      r /= mchunks;
+      pt = (int)((r / mchunks) % nptiles);
+      bs = (int)(r / mchunks / nptiles);
+    } else {
       pt = (int)(r % nptiles);
-      bs = (int)(r / nptiles);
-    } else {           // the CTAs that share an operator chunk run it at the same time
-      pt = (int)(r % nptiles);
-      r /= nptiles;
-      mc = (int)(r % mchunks);
-      bs = (int)(r / mchunks);
+      mc = (int)((r / nptiles) % mchunks);
+      bs = (int)(r / nptiles / mchunks);
     }
     const int slot = bs / q.d.nseg;
     s = bs - slot * q.d.nseg;
-    b = active_problem(q.d.batch_list, nbs[gi], q.d.batch, slot);
+    b = need_b ? active_problem(q.d.batch_list, nbs[gi], q.d.batch, slot) : 0;
   };
   auto nkb_of = [&](int gi) { return (L.g[gi].d.K + KE - 1) / KE; };
   // tile li of this CTA (false past the last one)
-  auto tile_of = [&](long long li, int& gi, int& pt, int& mc, int& b, int& s) -> bool {
+  auto tile_of = [&](long long li, int& gi, int& pt, int& mc, int& b, int& s,
+                     bool need_b = true) -> bool {
     if (!res) {
       const long long t = (long long)blockIdx.x + li * (long long)gridDim.x;
       if (t >= ntiles) return false;
-      decode(t, gi, pt, mc, b, s);
+      decode(t, gi, pt, mc, b, s, need_b);
       return true;
     }
     const long long j = r_j0 + li * r_step;
@@ -535,7 +550,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     const TcGroup& q = L.g[0];
     gi = 0;
     pt = (int)(j % r_nptiles);
-    b = active_problem(q.d.batch_list, nbs[0], q.d.batch, (int)(j / r_nptiles));
+    b = need_b ? active_problem(q.d.batch_list, nbs[0], q.d.batch, (int)(j / r_nptiles)) : 0;
     s = r_s;
     mc = r_mc;
     return true;
@@ -558,6 +573,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         }
       }
       int gi, pt, mc, b, s;
+      int st = 0;       // stage of K block g (g % S, kept running: no division)
+      uint32_t ph = 0;  // (g / S) & 1
       for (long long li = 0; ok && tile_of(li, gi, pt, mc, b, s); ++li) {
         const TcGroup& q = L.g[gi];
         const int cs = q.seg_in_map ? s : 0;
@@ -566,9 +583,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         const uint32_t obytes = (uint32_t)q.Mtile * OROW;
         const int nkb = nkb_of(gi);
         for (int kb = 0; kb < nkb; ++kb, ++g) {
-          const int st = (int)(g % S);
-          const uint32_t u = (uint32_t)(g / S);
-          if (g >= S && !mbar_wait(&empty[st], (u & 1u) ^ 1u, budget)) {
+          if (g >= S && !mbar_wait(&empty[st], ph ^ 1u, budget)) {
             ok = false;
             break;
           }
@@ -583,6 +598,10 @@ __global__ void __launch_bounds__(NTHREADS, 1)
               tma_load_3d(Ol(st), &L.maps[gi][2], &full[st], kb * KE, mc * q.Mtile, os);
           }
           issued = g + 1;
+          if (++st == S) {
+            st = 0;
+            ph ^= 1u;
+          }
         }
       }
       // drain: the latest use of every stage (and the resident operator) must
@@ -599,7 +618,9 @@ __global__ void __launch_bounds__(NTHREADS, 1)
       bool ok = true, issued_any = false;
       if (res && !mbar_wait(opfull, 0, budget)) ok = false;
       int gi, pt, mc, b, s;
-      for (; ok && tile_of(li, gi, pt, mc, b, s); ++li) {
+      int st = 0;       // stage of K block g
+      uint32_t ph = 0;  // (g / S) & 1
+      for (; ok && tile_of(li, gi, pt, mc, b, s, false); ++li) {
         const uint32_t idesc = H16   ? idesc_f16(TILE_P, L.g[gi].Mtile)
                                : B16 ? idesc_b16(TILE_P, L.g[gi].Mtile)
                                      : idesc_tf32(TILE_P, L.g[gi].Mtile);
@@ -613,8 +634,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
         const uint32_t acc = tmem + (uint32_t)buf * acc_stride;
         for (int kb = 0; kb < nkb; ++kb, ++g) {
-          const int st = (int)(g % S);
-          if (!mbar_wait(&conv[st], (uint32_t)(g / S) & 1u, budget)) {
+          if (!mbar_wait(&conv[st], ph, budget)) {
             ok = false;
             break;
           }
@@ -656,6 +676,10 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             }
           }
           mma_commit(&empty[st]);
+          if (++st == S) {
+            st = 0;
+            ph ^= 1u;
+          }
         }
         if (ok) mma_commit(&tfull[buf]);
       }
@@ -673,16 +697,16 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     // its 32 values from the 128-byte-swizzled tile and stores hi / lo into
     // its TMEM lane with tcgen05.st.
     const int row = 32 * (warp & 3) + lane;
-    long long g = 0;
     bool ok = true;
     int gi, pt, mc, b, s;
-    for (long long li = 0; ok && tile_of(li, gi, pt, mc, b, s); ++li) {
+    int st = 0;       // stage of the current K block
+    uint32_t ph = 0;  // its use count parity
+    for (long long li = 0; ok && tile_of(li, gi, pt, mc, b, s, H16); ++li) {
       const int nkb = nkb_of(gi);
       float xsc = 1.f, xinv = 1.f;
       if (H16) h16_scale(L.g[gi].in_max, b, xsc, xinv);
-      for (int kb = 0; kb < nkb; ++kb, ++g) {
-        const int st = (int)(g % S);
-        if (!mbar_wait(&full[st], (uint32_t)(g / S) & 1u, budget)) {
+      for (int kb = 0; kb < nkb; ++kb) {
+        if (!mbar_wait(&full[st], ph, budget)) {
           ok = false;
           break;
         }
@@ -775,6 +799,10 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         }
         __syncwarp();
         if (lane == 0) mbar_arrive(&conv[st]);
+        if (++st == S) {
+          st = 0;
+          ph ^= 1u;
+        }
       }
     }
   } else {
