@@ -100,10 +100,10 @@ __global__ void __launch_bounds__(NTH, 1)
   if (warp == 0) {
     if (lane == 0 && nkb > 0) {
       int issued = 0;
+      int st = 0;       // i % S, kept running (no division per K block)
+      uint32_t ph = 0;  // (i / S) & 1
       for (int i = 0; i < nkb; ++i) {
-        const int st = i % S;
-        const uint32_t u = (uint32_t)(i / S);
-        if (i >= S && !tc::mbar_wait(&empty[st], (u & 1u) ^ 1u, &g_gemm_status)) break;
+        if (i >= S && !tc::mbar_wait(&empty[st], ph ^ 1u, &g_gemm_status)) break;
         uint8_t* sa = smem + (size_t)st * stage_bytes;
         tc::mbar_expect_tx(&full[st], stage_bytes);
         const int ab = prm.a_bat ? b0 : 0, bb = prm.b_bat ? b0 : 0;
@@ -119,6 +119,10 @@ __global__ void __launch_bounds__(NTH, 1)
             tc::tma_load_3d(sbj, &tmB, &full[st], (kb0 + i) * KBE, 0, bb + j);
         }
         issued = i + 1;
+        if (++st == S) {
+          st = 0;
+          ph ^= 1u;
+        }
       }
       for (int i = (issued > S ? issued - S : 0); i < issued; ++i)
         tc::mbar_wait(&full[i % S], (uint32_t)(i / S) & 1u, &g_gemm_status);
@@ -127,9 +131,10 @@ __global__ void __launch_bounds__(NTH, 1)
     if (lane == 0 && nkb > 0) {
       const uint32_t idesc = tc::idesc_bf16(TM, NB * Nt);
       bool ok = true;
+      int st = 0;       // i % S
+      uint32_t ph = 0;  // (i / S) & 1
       for (int i = 0; i < nkb; ++i) {
-        const int st = i % S;
-        if (!tc::mbar_wait(&full[st], (uint32_t)(i / S) & 1u, &g_gemm_status)) {
+        if (!tc::mbar_wait(&full[st], ph, &g_gemm_status)) {
           ok = false;
           break;
         }
@@ -143,6 +148,10 @@ __global__ void __launch_bounds__(NTH, 1)
                        (i | kk) ? 1u : 0u);
         }
         tc::mma_commit(&empty[st]);
+        if (++st == S) {
+          st = 0;
+          ph ^= 1u;
+        }
       }
       if (ok) tc::mma_commit(accum);
     }
