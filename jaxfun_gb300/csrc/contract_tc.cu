@@ -312,16 +312,22 @@ __host__ __device__ constexpr uint32_t idesc_f16(int M, int N) {
 // relative to the maximum and nothing overflows.  Zero, non-finite or
 // missing bounds give scale 1; the exponent is clamped to [2^-126, 2^126]
 // so the inverse is exact as well.
-__device__ __forceinline__ void h16_scale(const unsigned* in_max, int b, float& sc, float& inv) {
+__device__ __forceinline__ void h16_scale_bits(unsigned bits, float& sc, float& inv) {
   sc = inv = 1.f;
-  if (!in_max || b < 0) return;
-  const unsigned bits = __ldg(in_max + b) & 0x7FFFFFFFu;
+  bits &= 0x7FFFFFFFu;
   const int e = (int)(bits >> 23);
   if (bits == 0 || e == 0xFF) return;
   int eb = 268 - e;  // biased exponent of 2^(15 - E), max |x| < 2^E, E = e - 126
   eb = eb < 1 ? 1 : (eb > 253 ? 253 : eb);
   sc = __uint_as_float((unsigned)eb << 23);
   inv = __uint_as_float((unsigned)(254 - eb) << 23);
+}
+// the recorded bound of problem b (0: none, scale 1)
+__device__ __forceinline__ unsigned h16_bits(const unsigned* in_max, int b) {
+  return (in_max && b >= 0) ? __ldg(in_max + b) : 0u;
+}
+__device__ __forceinline__ void h16_scale(const unsigned* in_max, int b, float& sc, float& inv) {
+  h16_scale_bits(h16_bits(in_max, b), sc, inv);
 }
 
 // Store 32 consecutive 32-bit columns of this thread's TMEM lane.
@@ -406,6 +412,10 @@ __global__ void __launch_bounds__(NTHREADS, 1)
   __shared__ int nbs[G];
   __shared__ unsigned long long s_budget;
   __shared__ int s_hold;
+  // scaled split FP16: the input bound of each stage's problem, written by the
+  // producer with the stage's loads (it reads the list and the bound well
+  // ahead), read by the split warps after the stage's full barrier
+  __shared__ unsigned s_xbits[16];
   uint8_t* smem = (uint8_t*)(((uintptr_t)smem_raw + 1023) & ~(uintptr_t)1023);
   const int S = L.stages;
   const bool ta = B16 || L.tmem_a != 0;
@@ -582,11 +592,13 @@ __global__ void __launch_bounds__(NTHREADS, 1)
         const int os = q.seg_op_map ? s : 0;
         const uint32_t obytes = (uint32_t)q.Mtile * OROW;
         const int nkb = nkb_of(gi);
+        const unsigned xbits = H16 ? h16_bits(q.in_max, b) : 0u;
         for (int kb = 0; kb < nkb; ++kb, ++g) {
           if (g >= S && !mbar_wait(&empty[st], ph ^ 1u, budget)) {
             ok = false;
             break;
           }
+          if (H16) s_xbits[st] = xbits;
           mbar_expect_tx(&full[st], res ? XB : XB + NOP * obytes);
           tma_load_4d(Xh(st), &L.maps[gi][0], &full[st], kb * KE, pt * TILE_P, cs, cb);
           if (B16 && KE > KB)
@@ -701,15 +713,15 @@ __global__ void __launch_bounds__(NTHREADS, 1)
     int gi, pt, mc, b, s;
     int st = 0;       // stage of the current K block
     uint32_t ph = 0;  // its use count parity
-    for (long long li = 0; ok && tile_of(li, gi, pt, mc, b, s, H16); ++li) {
+    for (long long li = 0; ok && tile_of(li, gi, pt, mc, b, s, false); ++li) {
       const int nkb = nkb_of(gi);
       float xsc = 1.f, xinv = 1.f;
-      if (H16) h16_scale(L.g[gi].in_max, b, xsc, xinv);
       for (int kb = 0; kb < nkb; ++kb) {
         if (!mbar_wait(&full[st], ph, budget)) {
           ok = false;
           break;
         }
+        if (H16 && kb == 0) h16_scale_bits(s_xbits[st], xsc, xinv);
         if (H16) {
           // 64 FP32 of this row, scaled by 2^k, -> FP16 hi / lo pairs; one
           // 32-element half at a time (16 hi and 16 lo columns) keeps the
@@ -1321,7 +1333,7 @@ int launch_groups(int ng, const jfg_contract_desc* const* ds, const void* const*
   }
   // operand A in TMEM: 256 accumulator columns plus one A slot per stage
   const int amax = ta ? 256 / (b16 ? ke16 : 2 * KB) : 6;
-  if (stages > amax) stages = amax;
+  if (stages > amax) stages = amax;  // <= 8: the kernel's per-stage tables hold 16
   if (cfg.stages >= 2 && cfg.stages < stages) stages = cfg.stages;
   if (stages < 2) return JFG_ERR_UNSUPPORTED;
   L.stages = stages;
