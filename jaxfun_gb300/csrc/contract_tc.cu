@@ -895,10 +895,17 @@ __global__ void __launch_bounds__(NTHREADS, 1)
           if (EPI == JFG_EPI_MUL_FIELD && !tfld)
             v = ok ? __ldg(fld + (long long)m * d.field_ld + p) : 0.f;
           if (EPI == JFG_EPI_DIV_EIG) v = ok ? __ldg(lam_m + m) : 1.f;
-          if (H16 && EPI != JFG_EPI_DIV_EIG) v *= ok ? __ldg(oinv + m) * xinv : 0.f;
+          if (H16 && EPI != JFG_EPI_DIV_EIG) {
+            // the row's inverse scale alone: the problem's (a power of two,
+            // xs) is applied where aux is used, so these loads stay in flight
+            // while the block before is processed
+            const float oi = ok ? __ldg(oinv + m) : 0.f;
+            v = (EPI == JFG_EPI_MUL_FIELD && !tfld) ? v * oi : oi;
+          }
           a[j] = v;
         }
       };
+      const float xs = (H16 && EPI != JFG_EPI_DIV_EIG) ? xinv : 1.f;
       float aux[16], nxt[16];
       if (cb_of(0) < ncb) {
         load_aux(cb_of(0), aux);
@@ -961,7 +968,8 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             // a = the contraction before the epilogue factor (operator and
             // input scales applied), for the fused dot sum(a * out)
             float a = r;
-            if (EPI != JFG_EPI_NONE || H16) r *= (EPI == JFG_EPI_DIV_EIG) ? 1.f : (pin ? aux[j] : 0.f);
+            if (EPI != JFG_EPI_NONE || H16)
+              r *= (EPI == JFG_EPI_DIV_EIG) ? 1.f : (pin ? aux[j] * xs : 0.f);
             if (tfld) a = r;  // aux held only the scales; the field comes next
             if (tfld) r *= cbox[(16 * (k & 1) + j) * 32 + lane];
             if (H16 && EPI == JFG_EPI_DIV_EIG) r *= pin ? osc[j] : 0.f;
@@ -989,7 +997,7 @@ __global__ void __launch_bounds__(NTHREADS, 1)
             if (m < d.M) {
               float r = v[j];
               float a = r;  // (split FP16 with the field in aux fuses no dot)
-              if (EPI != JFG_EPI_NONE || H16) r *= (EPI == JFG_EPI_DIV_EIG) ? 1.f : aux[j];
+              if (EPI != JFG_EPI_NONE || H16) r *= (EPI == JFG_EPI_DIV_EIG) ? 1.f : aux[j] * xs;
               if (H16 && EPI == JFG_EPI_DIV_EIG) r *= osc[j];
               if (EPI == JFG_EPI_DIV_EIG) {
                 a = r;
